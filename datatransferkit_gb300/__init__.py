@@ -1,0 +1,14 @@
+"""GB300-native moving-least-squares point-cloud transfer (DataTransferKit MLS path).
+
+The compute path is ``libdtk_gb300.so`` (hand-written sm_103a CUDA behind the
+C ABI of ``include/dtk_gb300.h``); this package is its host-side mirror of
+DataTransferKit's operator API.  There is no CPU fallback.
+"""
+from .operators import (FP64, MIXED, Buhmann, Constant, Linear, MovingLeastSquaresOperator,
+                        MultivariatePolynomialBasis, PointCloudOperator, Quadratic, Wendland, Wu,
+                        knn_search, svd_pinv)
+from ._capi import DTKError, InvalidArgument, Unsupported
+
+__all__ = ["MovingLeastSquaresOperator", "PointCloudOperator", "MultivariatePolynomialBasis",
+           "Constant", "Linear", "Quadratic", "Wendland", "Wu", "Buhmann", "FP64", "MIXED",
+           "knn_search", "svd_pinv", "DTKError", "InvalidArgument", "Unsupported"]

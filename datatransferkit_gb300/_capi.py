@@ -1,0 +1,109 @@
+"""ctypes binding of ``libdtk_gb300.so`` (the C ABI in ``include/dtk_gb300.h``).
+
+The library is built in-tree by ``datatransferkit_gb300.build`` (or
+``__graft_entry__.build()``).  There is no fallback: if the library is
+missing, loading raises, and every operator call fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "libdtk_gb300.so"
+
+# dtk_status
+DTK_OK = 0
+STATUS_NAMES = {0: "DTK_OK", 1: "DTK_ERR_INVALID_ARG", 2: "DTK_ERR_UNSUPPORTED",
+                3: "DTK_ERR_CUDA", 4: "DTK_ERR_OOM", 5: "DTK_ERR_TIMEOUT", 6: "DTK_ERR_INTERNAL"}
+
+# Every function declared in include/dtk_gb300.h.
+EXPORTED = [
+    "dtk_mls_default_options", "dtk_mls_create", "dtk_mls_apply", "dtk_mls_apply_adjoint",
+    "dtk_mls_get_csr", "dtk_mls_get_sizes", "dtk_mls_underdetermined_count",
+    "dtk_mls_get_stage_times", "dtk_mls_get_rotation_count", "dtk_mls_destroy",
+    "dtk_knn_search", "dtk_svd_pinv", "dtk_mls_batch_create", "dtk_mls_batch_apply",
+    "dtk_mls_batch_get_csr", "dtk_mls_batch_destroy", "dtk_last_error", "dtk_status_string",
+]
+
+
+class Options(C.Structure):
+    _fields_ = [("rbf", C.c_int32), ("basis", C.c_int32), ("k", C.c_int32),
+                ("precision", C.c_int32), ("radius", C.c_double), ("comm_size", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class DTKError(RuntimeError):
+    """A dtk_status other than DTK_OK (mirrors DataTransferKitException)."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        self.status_name = STATUS_NAMES.get(status, str(status))
+        super().__init__(f"{self.status_name}: {message}")
+
+
+class InvalidArgument(DTKError, ValueError):
+    pass
+
+
+class Unsupported(DTKError, NotImplementedError):
+    pass
+
+
+_lib = None
+_vp = C.c_void_p
+_i64 = C.c_int64
+
+
+def _declare(L):
+    L.dtk_mls_default_options.argtypes = [C.POINTER(Options)]
+    L.dtk_mls_default_options.restype = None
+    L.dtk_mls_create.argtypes = [C.POINTER(Options), _vp, _i64, _i64, _i64, _vp, _i64, _i64, _i64,
+                                 _vp, C.POINTER(_vp)]
+    L.dtk_mls_apply.argtypes = [_vp, _vp, _i64, _vp, _i64, _vp]
+    L.dtk_mls_apply_adjoint.argtypes = [_vp, _vp, _i64, _vp, _vp, _vp, _vp]
+    L.dtk_mls_get_csr.argtypes = [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp),
+                                  C.POINTER(_i64), C.POINTER(C.c_int32)]
+    L.dtk_mls_get_sizes.argtypes = [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)]
+    L.dtk_mls_underdetermined_count.argtypes = [_vp, C.POINTER(_i64)]
+    L.dtk_mls_get_stage_times.argtypes = [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.dtk_mls_get_rotation_count.argtypes = [_vp, C.POINTER(_i64)]
+    L.dtk_mls_destroy.argtypes = [_vp]
+    L.dtk_knn_search.argtypes = [_vp, _i64, _i64, _i64, _vp, _i64, _i64, _i64, C.c_int32, _vp, _vp, _vp]
+    L.dtk_svd_pinv.argtypes = [C.c_int32, _i64, _vp, _vp, C.POINTER(_i64), _vp]
+    L.dtk_mls_batch_create.argtypes = [C.c_int32, C.POINTER(Options), C.POINTER(_i64), _vp,
+                                       C.POINTER(_i64), _vp, _vp, C.POINTER(_vp)]
+    L.dtk_mls_batch_apply.argtypes = [_vp, _vp, _vp, C.c_int32, _vp]
+    L.dtk_mls_batch_get_csr.argtypes = L.dtk_mls_get_csr.argtypes
+    L.dtk_mls_batch_destroy.argtypes = [_vp]
+    L.dtk_last_error.restype = C.c_char_p
+    L.dtk_last_error.argtypes = []
+    L.dtk_status_string.restype = C.c_char_p
+    L.dtk_status_string.argtypes = [C.c_int]
+    for name in EXPORTED:
+        if name not in ("dtk_last_error", "dtk_status_string", "dtk_mls_default_options"):
+            getattr(L, name).restype = C.c_int
+
+
+def lib():
+    """The loaded library; raises if it was not built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(
+                f"{LIB_PATH} is missing: build the CUDA library first "
+                "(python -c 'import __graft_entry__ as g; g.build()'); there is no CPU fallback")
+        L = C.CDLL(str(LIB_PATH))
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != DTK_OK:
+        msg = lib().dtk_last_error().decode(errors="replace")
+        if status == 1:
+            raise InvalidArgument(status, msg)
+        if status == 2:
+            raise Unsupported(status, msg)
+        raise DTKError(status, msg)

@@ -1,0 +1,168 @@
+// MLS apply: CSR gather-SpMV (sm_103a).
+//
+// Replaces MovingLeastSquaresOperator::apply
+// (packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:188-208):
+// the single-rank fetch (a gather of source values into per-neighbour
+// order, DTK_DetailsNearestNeighborOperatorImpl.hpp:152-192), computeTargetValues
+// (DTK_DetailsMovingLeastSquaresOperatorImpl.hpp:49-70) and the deep_copy fuse
+// into one kernel that reads idx/coeff once and writes each target once.
+//
+// Rows of equal length R with R % 4 == 0 and R/4 a power of two (kNN rows,
+// e.g. R = 32) use R/4 lanes per row with 128-bit loads: int4 of indices and
+// two double2 (FP64 form) or one float4 (mixed form) of coefficients, then a
+// shuffle reduction.  Other rows use S lanes per row (S a power of two chosen
+// from the mean row length) with coalesced scalar loads.  Source values are
+// gathered through the read-only path; at 8M sources they are 64 MB and stay
+// resident in the 129 MB L2 while the CSR streams from HBM.
+#include "dtk_common.cuh"
+
+#include <algorithm>
+
+namespace dtk
+{
+namespace
+{
+
+constexpr unsigned FULL = 0xffffffffu;
+
+template <int L>
+__device__ __forceinline__ double group_sum( double v )
+{
+#pragma unroll
+    for ( int o = L / 2; o > 0; o >>= 1 )
+        v += __shfl_xor_sync( FULL, v, o );
+    return v;
+}
+
+// L lanes per row, each lane 4 consecutive entries.
+template <int L, bool F32>
+__global__ void __launch_bounds__( 256 )
+    k_apply_vec( int64_t n_tgt, int32_t const *__restrict__ idx,
+                 void const *__restrict__ coeff, double const *__restrict__ values,
+                 double *__restrict__ target )
+{
+    constexpr int R = 4 * L;
+    int64_t const gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t const row = gt / L;
+    int const sub = (int)( gt % L );
+    double acc = 0.0;
+    if ( row < n_tgt )
+    {
+        int64_t const e = row * R + 4 * sub;
+        int4 const ix = __ldcs( reinterpret_cast<int4 const *>( idx + e ) );
+        if constexpr ( F32 )
+        {
+            float4 const c = __ldcs( reinterpret_cast<float4 const *>( static_cast<float const *>( coeff ) + e ) );
+            acc = (double)c.x * __ldg( values + ix.x ) + (double)c.y * __ldg( values + ix.y ) +
+                  (double)c.z * __ldg( values + ix.z ) + (double)c.w * __ldg( values + ix.w );
+        }
+        else
+        {
+            double const *cp = static_cast<double const *>( coeff ) + e;
+            double2 const c0 = __ldcs( reinterpret_cast<double2 const *>( cp ) );
+            double2 const c1 = __ldcs( reinterpret_cast<double2 const *>( cp + 2 ) );
+            acc = c0.x * __ldg( values + ix.x ) + c0.y * __ldg( values + ix.y ) +
+                  c1.x * __ldg( values + ix.z ) + c1.y * __ldg( values + ix.w );
+        }
+    }
+    acc = group_sum<L>( acc );
+    if ( row < n_tgt && sub == 0 )
+        target[row] = acc;
+}
+
+// S lanes per row, strided scalar loads.
+template <int S, bool F32>
+__global__ void __launch_bounds__( 256 )
+    k_apply_csr( int64_t n_tgt, int32_t const *__restrict__ offset,
+                 int32_t const *__restrict__ idx, void const *__restrict__ coeff,
+                 double const *__restrict__ values, double *__restrict__ target )
+{
+    int64_t const gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t const row = gt / S;
+    int const sub = (int)( gt % S );
+    double acc = 0.0;
+    if ( row < n_tgt )
+    {
+        int const b = offset[row], e = offset[row + 1];
+        for ( int j = b + sub; j < e; j += S )
+        {
+            double const c = F32 ? (double)static_cast<float const *>( coeff )[j]
+                                 : static_cast<double const *>( coeff )[j];
+            acc += c * __ldg( values + idx[j] );
+        }
+    }
+    acc = group_sum<S>( acc );
+    if ( row < n_tgt && sub == 0 )
+        target[row] = acc;
+}
+
+template <bool F32>
+void launch_vec( int L, int64_t n_tgt, int32_t const *idx, void const *coeff,
+                 double const *values, double *target, cudaStream_t s )
+{
+    int64_t const threads = n_tgt * L;
+    unsigned const blocks = (unsigned)( ( threads + 255 ) / 256 );
+    switch ( L )
+    {
+    case 1: k_apply_vec<1, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
+    case 2: k_apply_vec<2, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
+    case 4: k_apply_vec<4, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
+    case 8: k_apply_vec<8, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
+    case 16: k_apply_vec<16, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
+    default: k_apply_vec<32, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
+    }
+    check_launch( "k_apply_vec" );
+}
+
+template <bool F32>
+void launch_csr( int S, int64_t n_tgt, int32_t const *offset, int32_t const *idx,
+                 void const *coeff, double const *values, double *target, cudaStream_t s )
+{
+    int64_t const threads = n_tgt * S;
+    unsigned const blocks = (unsigned)( ( threads + 255 ) / 256 );
+    switch ( S )
+    {
+    case 1: k_apply_csr<1, F32><<<blocks, 256, 0, s>>>( n_tgt, offset, idx, coeff, values, target ); break;
+    case 2: k_apply_csr<2, F32><<<blocks, 256, 0, s>>>( n_tgt, offset, idx, coeff, values, target ); break;
+    case 4: k_apply_csr<4, F32><<<blocks, 256, 0, s>>>( n_tgt, offset, idx, coeff, values, target ); break;
+    case 8: k_apply_csr<8, F32><<<blocks, 256, 0, s>>>( n_tgt, offset, idx, coeff, values, target ); break;
+    case 16: k_apply_csr<16, F32><<<blocks, 256, 0, s>>>( n_tgt, offset, idx, coeff, values, target ); break;
+    default: k_apply_csr<32, F32><<<blocks, 256, 0, s>>>( n_tgt, offset, idx, coeff, values, target ); break;
+    }
+    check_launch( "k_apply_csr" );
+}
+
+bool is_pow2( int v ) { return v > 0 && ( v & ( v - 1 ) ) == 0; }
+
+} // namespace
+
+// uniform_row > 0: every row has that length (offset[i] = i * uniform_row);
+// otherwise mean_row picks the lanes per row.
+void apply_csr( int64_t n_tgt, int32_t const *offset, int32_t const *idx, double const *coeff64,
+                float const *coeff32, int uniform_row, int mean_row, double const *values,
+                double *target, cudaStream_t s )
+{
+    if ( n_tgt == 0 )
+        return;
+    bool const f32 = coeff32 != nullptr;
+    void const *coeff = f32 ? (void const *)coeff32 : (void const *)coeff64;
+    if ( uniform_row > 0 && uniform_row % 4 == 0 && is_pow2( uniform_row / 4 ) &&
+         uniform_row / 4 <= 32 )
+    {
+        if ( f32 )
+            launch_vec<true>( uniform_row / 4, n_tgt, idx, coeff, values, target, s );
+        else
+            launch_vec<false>( uniform_row / 4, n_tgt, idx, coeff, values, target, s );
+        return;
+    }
+    int const len = uniform_row > 0 ? uniform_row : mean_row;
+    int S = 1;
+    while ( S < 32 && S * 2 <= len )
+        S *= 2;
+    if ( f32 )
+        launch_csr<true>( S, n_tgt, offset, idx, coeff, values, target, s );
+    else
+        launch_csr<false>( S, n_tgt, offset, idx, coeff, values, target, s );
+}
+
+} // namespace dtk

@@ -1,0 +1,446 @@
+// C ABI of the GB300 MLS transfer (declared in include/dtk_gb300.h).
+//
+// The handle mirrors the data members of
+// DataTransferKit::MovingLeastSquaresOperator
+// (packages/Meshfree/src/DTK_MovingLeastSquaresOperator_decl.hpp:56-62):
+// the CSR offset, the source indices and the coefficients, plus the source
+// count.  The reference's `_ranks` array is absent: on one rank every rank is
+// 0 and the fetch is a local gather fused into apply.
+#include "dtk_common.cuh"
+
+#include <cmath>
+#include <memory>
+#include <new>
+#include <string>
+
+namespace dtk
+{
+
+namespace
+{
+thread_local std::string g_error;
+}
+
+void set_error( std::string const &msg ) { g_error = msg; }
+
+template <class F>
+dtk_status guarded( F &&f )
+{
+    try
+    {
+        f();
+        return DTK_OK;
+    }
+    catch ( Error const &e )
+    {
+        set_error( e.msg );
+        return e.status;
+    }
+    catch ( std::bad_alloc const & )
+    {
+        set_error( "host allocation failed" );
+        return DTK_ERR_OOM;
+    }
+    catch ( std::exception const &e )
+    {
+        set_error( e.what() );
+        return DTK_ERR_INTERNAL;
+    }
+}
+
+__global__ void k_fill_uniform_offsets( int32_t *offset, int64_t n_tgt, int row )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i <= n_tgt )
+        offset[i] = (int32_t)( i * row );
+}
+
+__global__ void k_narrow_offsets( int64_t const *in, int32_t *out, int64_t n )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i <= n )
+        out[i] = (int32_t)in[i];
+}
+
+__global__ void k_pack_points( PointsView p, double *out )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i < p.n )
+    {
+        out[3 * i + 0] = p( i, 0 );
+        out[3 * i + 1] = p( i, 1 );
+        out[3 * i + 2] = p( i, 2 );
+    }
+}
+
+void validate_points( double const *p, int64_t n, int64_t ps, int64_t ds, char const *what )
+{
+    DTK_REQUIRE_OR_THROW( n >= 0, std::string( what ) + " count is negative" );
+    DTK_REQUIRE_OR_THROW( n == 0 || p != nullptr, std::string( what ) + " pointer is null" );
+    DTK_REQUIRE_OR_THROW( n <= INT32_MAX, std::string( what ) + " count exceeds int32 indices" );
+    DTK_REQUIRE_OR_THROW( n == 0 || ( ps != 0 || n == 1 ) && ds != 0,
+                          std::string( what ) + " strides are zero" );
+}
+
+struct Geometry
+{
+    dtk_mls_options opts;
+    int m = 0, k = 0, row = 0;
+    bool radius_mode = false;
+};
+
+Geometry check_options( dtk_mls_options const *o )
+{
+    DTK_REQUIRE_OR_THROW( o != nullptr, "options pointer is null" );
+    if ( o->comm_size != 1 )
+        throw Error{DTK_ERR_UNSUPPORTED,
+                    "only a single-rank communicator (MPI_COMM_SELF) is supported"};
+    DTK_REQUIRE_OR_THROW( o->rbf >= DTK_WENDLAND0 && o->rbf <= DTK_BUHMANN4, "unknown rbf" );
+    DTK_REQUIRE_OR_THROW( o->basis >= DTK_CONSTANT3 && o->basis <= DTK_QUADRATIC3,
+                          "unknown polynomial basis" );
+    DTK_REQUIRE_OR_THROW( o->precision == DTK_FP64 || o->precision == DTK_MIXED,
+                          "unknown precision form" );
+    DTK_REQUIRE_OR_THROW( o->k >= 0, "k is negative" );
+    DTK_REQUIRE_OR_THROW( std::isfinite( o->radius ) && o->radius >= 0.0,
+                          "radius must be finite and >= 0" );
+    Geometry g;
+    g.opts = *o;
+    g.m = basis_size( o->basis );
+    g.radius_mode = o->radius > 0.0;
+    g.k = o->k ? o->k : g.m;
+    if ( !g.radius_mode && g.k > 32 )
+        throw Error{DTK_ERR_UNSUPPORTED, "kNN search supports k <= 32"};
+    return g;
+}
+
+} // namespace dtk
+
+struct dtk_mls_s
+{
+    dtk_mls_options opts;
+    int64_t n_src = 0, n_tgt = 0, nnz = 0;
+    int m = 0;
+    int uniform_row = 0; // > 0 for kNN rows
+    int mean_row = 0;
+    dtk::DeviceBuffer<int32_t> offset, idx;
+    dtk::DeviceBuffer<double> coeff64;
+    dtk::DeviceBuffer<float> coeff32;
+    dtk::DeviceBuffer<uint32_t> order; // Morton order of targets
+    dtk::DeviceBuffer<double> src_copy, tgt_copy; // packed n x 3 (adjoint)
+    dtk::DeviceBuffer<int32_t> t_offset, t_entry, entry_row;
+    int64_t underdetermined = 0;
+    int64_t rotations = 0;
+    float search_ms = 0.f, setup_ms = 0.f;
+};
+
+using namespace dtk;
+
+extern "C" {
+
+void dtk_mls_default_options( dtk_mls_options *o )
+{
+    if ( !o )
+        return;
+    o->rbf = DTK_WENDLAND0;
+    o->basis = DTK_LINEAR3;
+    o->k = 0;
+    o->precision = DTK_FP64;
+    o->radius = 0.0;
+    o->comm_size = 1;
+    o->reserved = 0;
+}
+
+const char *dtk_last_error( void ) { return g_error.c_str(); }
+
+const char *dtk_status_string( dtk_status s )
+{
+    switch ( s )
+    {
+    case DTK_OK: return "DTK_OK";
+    case DTK_ERR_INVALID_ARG: return "DTK_ERR_INVALID_ARG";
+    case DTK_ERR_UNSUPPORTED: return "DTK_ERR_UNSUPPORTED";
+    case DTK_ERR_CUDA: return "DTK_ERR_CUDA";
+    case DTK_ERR_OOM: return "DTK_ERR_OOM";
+    case DTK_ERR_TIMEOUT: return "DTK_ERR_TIMEOUT";
+    case DTK_ERR_INTERNAL: return "DTK_ERR_INTERNAL";
+    }
+    return "unknown dtk_status";
+}
+
+dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64_t n_src,
+                           int64_t src_pt_stride, int64_t src_dim_stride, const double *tgt,
+                           int64_t n_tgt, int64_t tgt_pt_stride, int64_t tgt_dim_stride,
+                           dtk_stream_t stream_, dtk_mls_handle *out )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( out != nullptr, "output handle pointer is null" );
+        *out = nullptr;
+        Geometry const g = check_options( opts );
+        validate_points( src, n_src, src_pt_stride, src_dim_stride, "source points" );
+        validate_points( tgt, n_tgt, tgt_pt_stride, tgt_dim_stride, "target points" );
+        // DTK_CHECK( !search_tree.empty() ), DTK_MovingLeastSquaresOperator_def.hpp:116
+        DTK_REQUIRE_OR_THROW( n_src > 0, "the source point cloud is empty" );
+        cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        auto h = new dtk_mls_s();
+        std::unique_ptr<dtk_mls_s> guard( h );
+        h->opts = *opts;
+        h->n_src = n_src;
+        h->n_tgt = n_tgt;
+        h->m = g.m;
+        PointsView const sv{src, n_src, src_pt_stride, src_dim_stride};
+        PointsView const tv{tgt, n_tgt, tgt_pt_stride, tgt_dim_stride};
+
+        cudaEvent_t ev[3];
+        for ( auto &e : ev )
+            DTK_CUDA_OR_THROW( cudaEventCreate( &e ) );
+        struct EvGuard
+        {
+            cudaEvent_t *e;
+            ~EvGuard()
+            {
+                for ( int i = 0; i < 3; ++i )
+                    cudaEventDestroy( e[i] );
+            }
+        } evg{ev};
+        DeviceBuffer<unsigned> status( 1, s );
+        DeviceBuffer<unsigned long long> counters( 2, s );
+        DTK_CUDA_OR_THROW( cudaMemsetAsync( status.get(), 0, sizeof( unsigned ), s ) );
+        DTK_CUDA_OR_THROW( cudaMemsetAsync( counters.get(), 0, 2 * sizeof( unsigned long long ), s ) );
+        DTK_CUDA_OR_THROW( cudaEventRecord( ev[0], s ) );
+
+        // --- search (ArborX tree + query, def.hpp:114-129) ---
+        Lbvh tree;
+        build_lbvh( sv, tree, status.get(), s );
+        sort_queries( tree, tv, h->order, s );
+        h->offset.allocate( n_tgt + 1, s );
+        if ( !g.radius_mode )
+        {
+            int const row = (int)std::min<int64_t>( g.k, n_src );
+            DTK_REQUIRE_OR_THROW( n_tgt * (int64_t)row <= INT32_MAX,
+                                  "n_targets * k exceeds int32 CSR offsets" );
+            h->uniform_row = row;
+            h->mean_row = row;
+            h->nnz = n_tgt * (int64_t)row;
+            k_fill_uniform_offsets<<<(unsigned)( ( n_tgt + 256 ) / 256 ), 256, 0, s>>>(
+                h->offset.get(), n_tgt, row );
+            check_launch( "k_fill_uniform_offsets" );
+            h->idx.allocate( std::max<int64_t>( 1, h->nnz ), s );
+            knn_query( tree, tv, h->order.get(), g.k, h->idx.get(), status.get(), s );
+        }
+        else
+        {
+            DeviceBuffer<int64_t> counts( std::max<int64_t>( 1, n_tgt ), s ),
+                offs( n_tgt + 1, s );
+            radius_count( tree, tv, h->order.get(), g.opts.radius, counts.get(), status.get(), s );
+            exclusive_scan_i64( counts.get(), offs.get(), n_tgt, s );
+            int64_t total = 0;
+            DTK_CUDA_OR_THROW( cudaMemcpyAsync( &total, offs.get() + n_tgt, sizeof( int64_t ),
+                                                cudaMemcpyDeviceToHost, s ) );
+            DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+            DTK_REQUIRE_OR_THROW( total <= INT32_MAX, "neighbour count exceeds int32 CSR offsets" );
+            h->nnz = total;
+            h->mean_row = n_tgt ? (int)( ( total + n_tgt - 1 ) / n_tgt ) : 0;
+            k_narrow_offsets<<<(unsigned)( ( n_tgt + 256 ) / 256 ), 256, 0, s>>>( offs.get(),
+                                                                                  h->offset.get(), n_tgt );
+            check_launch( "k_narrow_offsets" );
+            h->idx.allocate( std::max<int64_t>( 1, total ), s );
+            radius_fill( tree, tv, h->order.get(), g.opts.radius, h->offset.get(), h->idx.get(),
+                         status.get(), s );
+        }
+        DTK_CUDA_OR_THROW( cudaEventRecord( ev[1], s ) );
+
+        // --- setup numerics (def.hpp:136-185) ---
+        SetupArgs a{};
+        a.src = sv;
+        a.tgt = tv;
+        a.offset = h->offset.get();
+        a.idx = h->idx.get();
+        a.order = h->order.get();
+        a.n_tgt = n_tgt;
+        a.rbf = g.opts.rbf;
+        a.basis = g.opts.basis;
+        a.rows_sorted = !g.radius_mode;
+        a.underdetermined = counters.get();
+        a.rotations = counters.get() + 1;
+        a.status = status.get();
+        if ( g.opts.precision == DTK_FP64 )
+        {
+            h->coeff64.allocate( std::max<int64_t>( 1, h->nnz ), s );
+            a.coeff64 = h->coeff64.get();
+            setup_fp64( a, s );
+        }
+        else
+        {
+            h->coeff32.allocate( std::max<int64_t>( 1, h->nnz ), s );
+            a.coeff32 = h->coeff32.get();
+            setup_mixed( a, s );
+        }
+        DTK_CUDA_OR_THROW( cudaEventRecord( ev[2], s ) );
+
+        unsigned st = 0;
+        unsigned long long cnt[2] = {0, 0};
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, status.get(), sizeof( unsigned ),
+                                            cudaMemcpyDeviceToHost, s ) );
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( cnt, counters.get(), sizeof( cnt ),
+                                            cudaMemcpyDeviceToHost, s ) );
+        // Release the tree and scratch before returning (stream ordered).
+        tree = Lbvh();
+        DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+        if ( st & DEV_TIMEOUT )
+            throw Error{DTK_ERR_TIMEOUT, "a Jacobi iteration hit its iteration cap"};
+        if ( st )
+            throw Error{DTK_ERR_INTERNAL, "search traversal reported an internal error"};
+        h->underdetermined = (int64_t)cnt[0];
+        h->rotations = (int64_t)cnt[1];
+        DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->search_ms, ev[0], ev[1] ) );
+        DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->setup_ms, ev[1], ev[2] ) );
+        *out = guard.release();
+    } );
+}
+
+dtk_status dtk_mls_apply( dtk_mls_handle h, const double *source_values, int64_t n_source_values,
+                          double *target_values, int64_t n_target_values, dtk_stream_t stream_ )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
+        // DTK_REQUIRE at DTK_MovingLeastSquaresOperator_def.hpp:196-197
+        DTK_REQUIRE_OR_THROW( n_source_values == h->n_src,
+                              "source_values.extent(0) == n_source_points" );
+        DTK_REQUIRE_OR_THROW( n_target_values == h->n_tgt,
+                              "target_values.extent(0) == n_target_points" );
+        DTK_REQUIRE_OR_THROW( h->n_src == 0 || source_values != nullptr, "source_values is null" );
+        DTK_REQUIRE_OR_THROW( h->n_tgt == 0 || target_values != nullptr, "target_values is null" );
+        cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        apply_csr( h->n_tgt, h->offset.get(), h->idx.get(), h->coeff64.get(), h->coeff32.get(),
+                   h->uniform_row, h->mean_row, source_values, target_values, s );
+    } );
+}
+
+dtk_status dtk_mls_get_csr( dtk_mls_handle h, const int32_t **offset, const int32_t **indices,
+                            const void **coeff, int64_t *nnz, int32_t *coeff_is_fp32 )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
+        if ( offset )
+            *offset = h->offset.get();
+        if ( indices )
+            *indices = h->idx.get();
+        bool const f32 = h->coeff32.get() != nullptr;
+        if ( coeff )
+            *coeff = f32 ? (const void *)h->coeff32.get() : (const void *)h->coeff64.get();
+        if ( nnz )
+            *nnz = h->nnz;
+        if ( coeff_is_fp32 )
+            *coeff_is_fp32 = f32 ? 1 : 0;
+    } );
+}
+
+dtk_status dtk_mls_get_sizes( dtk_mls_handle h, int64_t *n_src, int64_t *n_tgt, int64_t *nnz )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
+        if ( n_src )
+            *n_src = h->n_src;
+        if ( n_tgt )
+            *n_tgt = h->n_tgt;
+        if ( nnz )
+            *nnz = h->nnz;
+    } );
+}
+
+dtk_status dtk_mls_underdetermined_count( dtk_mls_handle h, int64_t *count )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( h != nullptr && count != nullptr, "null argument" );
+        *count = h->underdetermined;
+    } );
+}
+
+dtk_status dtk_mls_get_stage_times( dtk_mls_handle h, float *search_ms, float *setup_ms )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
+        if ( search_ms )
+            *search_ms = h->search_ms;
+        if ( setup_ms )
+            *setup_ms = h->setup_ms;
+    } );
+}
+
+dtk_status dtk_mls_get_rotation_count( dtk_mls_handle h, int64_t *rotations )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( h != nullptr && rotations != nullptr, "null argument" );
+        *rotations = h->rotations;
+    } );
+}
+
+dtk_status dtk_mls_destroy( dtk_mls_handle h )
+{
+    return guarded( [&] { delete h; } );
+}
+
+dtk_status dtk_knn_search( const double *src, int64_t n_src, int64_t src_pt_stride,
+                           int64_t src_dim_stride, const double *tgt, int64_t n_tgt,
+                           int64_t tgt_pt_stride, int64_t tgt_dim_stride, int32_t k,
+                           int32_t *offset, int32_t *indices, dtk_stream_t stream_ )
+{
+    return guarded( [&] {
+        validate_points( src, n_src, src_pt_stride, src_dim_stride, "source points" );
+        validate_points( tgt, n_tgt, tgt_pt_stride, tgt_dim_stride, "target points" );
+        DTK_REQUIRE_OR_THROW( n_src > 0, "the source point cloud is empty" );
+        DTK_REQUIRE_OR_THROW( k >= 0, "k is negative" );
+        if ( k > 32 )
+            throw Error{DTK_ERR_UNSUPPORTED, "kNN search supports k <= 32"};
+        DTK_REQUIRE_OR_THROW( offset != nullptr, "offset is null" );
+        int const row = (int)std::min<int64_t>( k, n_src );
+        DTK_REQUIRE_OR_THROW( n_tgt * (int64_t)row <= INT32_MAX, "n_targets * k exceeds int32" );
+        DTK_REQUIRE_OR_THROW( n_tgt * (int64_t)row == 0 || indices != nullptr, "indices is null" );
+        cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        PointsView const sv{src, n_src, src_pt_stride, src_dim_stride};
+        PointsView const tv{tgt, n_tgt, tgt_pt_stride, tgt_dim_stride};
+        DeviceBuffer<unsigned> status( 1, s );
+        DTK_CUDA_OR_THROW( cudaMemsetAsync( status.get(), 0, sizeof( unsigned ), s ) );
+        k_fill_uniform_offsets<<<(unsigned)( ( n_tgt + 256 ) / 256 ), 256, 0, s>>>( offset, n_tgt, row );
+        check_launch( "k_fill_uniform_offsets" );
+        Lbvh tree;
+        build_lbvh( sv, tree, status.get(), s );
+        DeviceBuffer<uint32_t> order;
+        sort_queries( tree, tv, order, s );
+        knn_query( tree, tv, order.get(), k, indices, status.get(), s );
+        unsigned st = 0;
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, status.get(), sizeof( unsigned ),
+                                            cudaMemcpyDeviceToHost, s ) );
+        tree = Lbvh();
+        DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+        if ( st )
+            throw Error{DTK_ERR_INTERNAL, "search traversal reported an internal error"};
+    } );
+}
+
+dtk_status dtk_svd_pinv( int32_t n, int64_t count, const double *a, double *pinv,
+                         int64_t *underdetermined, dtk_stream_t stream_ )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( n >= 1 && n <= 64, "matrix size must be in [1, 64]" );
+        DTK_REQUIRE_OR_THROW( count >= 0, "count is negative" );
+        DTK_REQUIRE_OR_THROW( count == 0 || ( a && pinv ), "null matrix pointer" );
+        cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        DeviceBuffer<unsigned> status( 1, s );
+        DeviceBuffer<unsigned long long> under( 1, s );
+        DTK_CUDA_OR_THROW( cudaMemsetAsync( status.get(), 0, sizeof( unsigned ), s ) );
+        DTK_CUDA_OR_THROW( cudaMemsetAsync( under.get(), 0, sizeof( unsigned long long ), s ) );
+        svd_pinv_batched( n, count, a, pinv, under.get(), status.get(), s );
+        unsigned st = 0;
+        unsigned long long u = 0;
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, status.get(), sizeof( st ), cudaMemcpyDeviceToHost, s ) );
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( &u, under.get(), sizeof( u ), cudaMemcpyDeviceToHost, s ) );
+        DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+        if ( st & DEV_TIMEOUT )
+            throw Error{DTK_ERR_TIMEOUT, "a Jacobi iteration hit its iteration cap"};
+        if ( underdetermined )
+            *underdetermined = (int64_t)u;
+    } );
+}
+
+} // extern "C"

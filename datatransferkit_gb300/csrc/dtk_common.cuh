@@ -1,0 +1,347 @@
+// Shared internals of the GB300 MLS transfer library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cstdint>
+#include <string>
+
+#include "../../include/dtk_gb300.h"
+
+namespace dtk
+{
+
+// ---------------------------------------------------------------------------
+// Host-side error plumbing: every C-ABI entry point returns a dtk_status and
+// records a message for dtk_last_error().
+// ---------------------------------------------------------------------------
+void set_error( std::string const &msg );
+
+struct Error
+{
+    dtk_status status;
+    std::string msg;
+};
+
+#define DTK_CUDA_OR_THROW( expr )                                              \
+    do                                                                         \
+    {                                                                          \
+        cudaError_t e__ = ( expr );                                            \
+        if ( e__ != cudaSuccess )                                              \
+            throw ::dtk::Error{e__ == cudaErrorMemoryAllocation                \
+                                   ? DTK_ERR_OOM                               \
+                                   : DTK_ERR_CUDA,                             \
+                               std::string( #expr ) + ": " +                   \
+                                   cudaGetErrorString( e__ )};                 \
+    } while ( 0 )
+
+#define DTK_REQUIRE_OR_THROW( cond, msg )                                      \
+    do                                                                         \
+    {                                                                          \
+        if ( !( cond ) )                                                       \
+            throw ::dtk::Error{DTK_ERR_INVALID_ARG,                            \
+                               std::string( "DTK_REQUIRE( " #cond " ): " ) +   \
+                                   ( msg )};                                   \
+    } while ( 0 )
+
+// Stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync).
+template <class T>
+struct DeviceBuffer
+{
+    T *ptr = nullptr;
+    size_t n = 0;
+    cudaStream_t stream = nullptr;
+
+    DeviceBuffer() = default;
+    DeviceBuffer( size_t count, cudaStream_t s ) { allocate( count, s ); }
+    DeviceBuffer( DeviceBuffer const & ) = delete;
+    DeviceBuffer &operator=( DeviceBuffer const & ) = delete;
+    DeviceBuffer( DeviceBuffer &&o ) noexcept { *this = std::move( o ); }
+    DeviceBuffer &operator=( DeviceBuffer &&o ) noexcept
+    {
+        release();
+        ptr = o.ptr;
+        n = o.n;
+        stream = o.stream;
+        o.ptr = nullptr;
+        o.n = 0;
+        return *this;
+    }
+    ~DeviceBuffer() { release(); }
+
+    void allocate( size_t count, cudaStream_t s )
+    {
+        release();
+        stream = s;
+        n = count;
+        if ( count )
+            DTK_CUDA_OR_THROW( cudaMallocAsync( (void **)&ptr, count * sizeof( T ), s ) );
+    }
+    void release()
+    {
+        if ( ptr )
+            cudaFreeAsync( ptr, stream );
+        ptr = nullptr;
+        n = 0;
+    }
+    T *get() const { return ptr; }
+};
+
+// Launch-error check after a kernel launch.
+inline void check_launch( char const *what )
+{
+    cudaError_t e = cudaGetLastError();
+    if ( e != cudaSuccess )
+        throw Error{DTK_ERR_CUDA, std::string( what ) + ": " + cudaGetErrorString( e )};
+}
+
+inline int num_sms()
+{
+    static int sms = 0;
+    if ( !sms )
+    {
+        int dev = 0;
+        cudaGetDevice( &dev );
+        cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev );
+        if ( sms <= 0 )
+            sms = 152;
+    }
+    return sms;
+}
+
+inline int basis_size( int basis )
+{
+    return basis == DTK_CONSTANT3 ? 1 : basis == DTK_LINEAR3 ? 4 : basis == DTK_QUADRATIC3 ? 10 : -1;
+}
+
+// Device status word bits (set by bounded device loops).
+enum : unsigned
+{
+    DEV_TIMEOUT = 1u,
+    DEV_STACK_OVERFLOW = 2u,
+    DEV_BAD_INDEX = 4u
+};
+
+// ---------------------------------------------------------------------------
+// Device math shared by the kernels.
+// ---------------------------------------------------------------------------
+
+// Squared distance with the contract's association and separately rounded
+// operations: (dx*dx + dy*dy) + dz*dz, dx = s.x - t.x.
+__device__ __forceinline__ double dist2_rn( double sx, double sy, double sz,
+                                            double tx, double ty, double tz )
+{
+    double const dx = __dsub_rn( sx, tx );
+    double const dy = __dsub_rn( sy, ty );
+    double const dz = __dsub_rn( sz, tz );
+    return __dadd_rn( __dadd_rn( __dmul_rn( dx, dx ), __dmul_rn( dy, dy ) ),
+                      __dmul_rn( dz, dz ) );
+}
+
+// Compactly supported RBFs on the scaled argument x = distance / radius
+// (DTK_CompactlySupportedRadialBasisFunctions.hpp:45-147).
+template <class T>
+__device__ __forceinline__ T rbf_eval( int rbf, T x )
+{
+    T const y = T( 1 ) - x;
+    switch ( rbf )
+    {
+    case DTK_WENDLAND0:
+        return y * y;
+    case DTK_WENDLAND2:
+        return y * y * y * y * ( T( 4 ) * x + T( 1 ) );
+    case DTK_WENDLAND4:
+        return y * y * y * y * y * y * ( T( 35 ) * x * x + T( 18 ) * x + T( 3 ) );
+    case DTK_WENDLAND6:
+        return y * y * y * y * y * y * y * y *
+               ( T( 32 ) * x * x * x + T( 25 ) * x * x + T( 8 ) * x + T( 1 ) );
+    case DTK_WU2:
+        return y * y * y * y * ( T( 3 ) * x * x * x + T( 12 ) * x * x + T( 16 ) * x + T( 4 ) );
+    case DTK_WU4:
+        return y * y * y * y * y * y *
+               ( T( 5 ) * x * x * x * x * x + T( 30 ) * x * x * x * x +
+                 T( 72 ) * x * x * x + T( 82 ) * x * x + T( 36 ) * x + T( 6 ) );
+    case DTK_BUHMANN2:
+        return T( 2 ) * x * x * x * x * log( x ) - T( 7.0 / 2.0 ) * x * x * x * x +
+               T( 16 / 3.0 ) * x * x * x - T( 2 ) * x * x + T( 1.0 / 6.0 );
+    case DTK_BUHMANN3:
+        return x * x * x * x * x * x * x * x - T( 84.0 / 5.0 ) * x * x * x * x * x * x +
+               T( 1024.0 / 5.0 ) * x * x * x * x * sqrt( x ) -
+               T( 378 ) * x * x * x * x + T( 1024.0 / 5.0 ) * x * x * x * sqrt( x ) -
+               T( 84.0 / 5.0 ) * x * x + T( 1 );
+    default: // DTK_BUHMANN4
+        return T( 99.0 / 35.0 ) * x * x * x * x * x * x * x * x -
+               T( 132 ) * x * x * x * x * x * x +
+               T( 9216.0 / 35.0 ) * x * x * x * x * x * sqrt( x ) -
+               T( 11264.0 / 35.0 ) * x * x * x * x * sqrt( x ) +
+               T( 198 ) * x * x * x * x - T( 396.0 / 5.0 ) * x * x + T( 1 );
+    }
+}
+
+// d rbf / dx (hand-derived; used by the adjoint).
+__device__ __forceinline__ double rbf_deriv( int rbf, double x )
+{
+    double const y = 1.0 - x;
+    switch ( rbf )
+    {
+    case DTK_WENDLAND0:
+        return -2.0 * y;
+    case DTK_WENDLAND2:
+        return -20.0 * x * y * y * y;
+    case DTK_WENDLAND4:
+        return -56.0 * x * ( 5.0 * x + 1.0 ) * y * y * y * y * y;
+    case DTK_WENDLAND6:
+        return -22.0 * x * ( 16.0 * x * x + 7.0 * x + 1.0 ) * y * y * y * y * y * y * y;
+    case DTK_WU2:
+        return -7.0 * x * ( 3.0 * x * x + 9.0 * x + 8.0 ) * y * y * y;
+    case DTK_WU4:
+        return -11.0 * x * ( 5.0 * x * x * x * x + 25.0 * x * x * x + 48.0 * x * x + 40.0 * x + 8.0 ) *
+               y * y * y * y * y;
+    case DTK_BUHMANN2:
+        return x > 0.0 ? 8.0 * x * x * x * log( x ) - 12.0 * x * x * x + 16.0 * x * x - 4.0 * x : 0.0;
+    case DTK_BUHMANN3:
+    {
+        double const r = sqrt( x );
+        double const x2 = x * x, x3 = x2 * x, x5 = x3 * x2, x7 = x5 * x2;
+        return 8.0 * x7 - 504.0 / 5.0 * x5 + 4608.0 / 5.0 * x3 * r - 1512.0 * x3 +
+               3584.0 / 5.0 * x2 * r - 168.0 / 5.0 * x;
+    }
+    default:
+    {
+        double const r = sqrt( x );
+        double const x2 = x * x, x3 = x2 * x, x4 = x2 * x2, x5 = x4 * x, x7 = x5 * x2;
+        return 792.0 / 35.0 * x7 - 792.0 * x5 + 50688.0 / 35.0 * x4 * r -
+               50688.0 / 35.0 * x3 * r + 792.0 * x3 - 792.0 / 5.0 * x;
+    }
+    }
+}
+
+// Polynomial basis in 3-D, order 1, x, y, z, x^2, xy, xz, y^2, yz, z^2
+// (DTK_MultivariatePolynomialBasis.hpp:249-276).
+template <int M, class T>
+__device__ __forceinline__ void basis_eval( T x, T y, T z, T *p )
+{
+    p[0] = T( 1 );
+    if constexpr ( M >= 4 )
+    {
+        p[1] = x;
+        p[2] = y;
+        p[3] = z;
+    }
+    if constexpr ( M == 10 )
+    {
+        p[4] = x * x;
+        p[5] = x * y;
+        p[6] = x * z;
+        p[7] = y * y;
+        p[8] = y * z;
+        p[9] = z * z;
+    }
+}
+
+// Strided point access: element (i, d) at base[i*ps + d*ds].
+struct PointsView
+{
+    double const *base;
+    int64_t n, ps, ds;
+    __host__ __device__ double operator()( int64_t i, int d ) const
+    {
+        return base[i * ps + d * ds];
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Internal library API shared between translation units.
+// ---------------------------------------------------------------------------
+
+// Device-wide exclusive scan of n int64 counts (out may alias nothing);
+// out has n+1 entries, out[n] = total.  Returns nothing; total is on device.
+void exclusive_scan_i64( int64_t const *in, int64_t *out, int64_t n, cudaStream_t s );
+
+// Stable LSD radix sort of (keys, values) pairs by the low `bits` bits of
+// the keys.  Buffers are swapped internally; the result ends in keys/values.
+void radix_sort_pairs( uint32_t *keys, uint32_t *values, int64_t n, int bits,
+                       cudaStream_t s );
+
+// Linear BVH over source points with 32-point leaf buckets.
+struct Lbvh
+{
+    int64_t n = 0;        // points
+    int64_t n_leaves = 0; // ceil(n / 32)
+    double lo[3], hi[3];  // scene bounds (host copy)
+    DeviceBuffer<double> sx, sy, sz;  // Morton-sorted coordinates
+    DeviceBuffer<uint32_t> codes;     // sorted Morton codes
+    DeviceBuffer<uint32_t> perm;      // sorted position -> original index
+    DeviceBuffer<float4> nodes;       // 4 float4 per internal node
+    DeviceBuffer<float4> root_box;    // box of the whole tree (2 float4)
+    DeviceBuffer<double> scene;       // device copy of lo/hi (6 doubles)
+};
+
+void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s );
+
+// Morton order of query points (sorted query ids) using the tree's scene box.
+void sort_queries( Lbvh const &tree, PointsView tgt, DeviceBuffer<uint32_t> &order,
+                   cudaStream_t s );
+
+// kNN: writes idx rows (ascending (d2, index)); offset must be pre-filled.
+void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
+                int32_t *idx, unsigned *status, cudaStream_t s );
+
+// Radius: count pass (counts[n_tgt]) and fill pass given offsets.
+void radius_count( Lbvh const &tree, PointsView tgt, uint32_t const *order, double r,
+                   int64_t *counts, unsigned *status, cudaStream_t s );
+void radius_fill( Lbvh const &tree, PointsView tgt, uint32_t const *order, double r,
+                  int32_t const *offset, int32_t *idx, unsigned *status, cudaStream_t s );
+
+// Setup (coefficients) kernels.
+struct SetupArgs
+{
+    PointsView src, tgt;
+    int32_t const *offset;
+    int32_t const *idx;
+    uint32_t const *order; // target processing order (may be null)
+    int64_t n_tgt;
+    int rbf, basis;
+    bool rows_sorted;     // rows ascending by distance (kNN)
+    double *coeff64;      // FP64 form output
+    float *coeff32;       // mixed form output
+    unsigned long long *underdetermined;
+    unsigned long long *rotations;
+    unsigned *status;
+};
+void setup_fp64( SetupArgs const &a, cudaStream_t s );
+void setup_mixed( SetupArgs const &a, cudaStream_t s );
+
+// Batched SVD pseudo-inverse (general n <= 64), DTK SVDFunctor semantics.
+void svd_pinv_batched( int n, int64_t count, double const *a, double *pinv,
+                       unsigned long long *underdetermined, unsigned *status,
+                       cudaStream_t s );
+
+// Apply kernels.
+void apply_csr( int64_t n_tgt, int32_t const *offset, int32_t const *idx,
+                double const *coeff64, float const *coeff32, int uniform_row, int mean_row,
+                double const *values, double *target, cudaStream_t s );
+
+// Adjoint kernels.
+struct AdjointArgs
+{
+    int64_t n_src, n_tgt;
+    int32_t const *offset, *idx;
+    double const *coeff64;
+    float const *coeff32;
+    double const *cot;
+    double *grad_values;
+    // transpose CSR (source -> entries), built on demand
+    int32_t const *t_offset, *t_entry;
+    int32_t const *entry_row;
+};
+void build_transpose( int64_t n_src, int64_t n_tgt, int64_t nnz, int32_t const *offset,
+                      int32_t const *idx, DeviceBuffer<int32_t> &t_offset,
+                      DeviceBuffer<int32_t> &t_entry, DeviceBuffer<int32_t> &entry_row,
+                      cudaStream_t s );
+void apply_transpose( AdjointArgs const &a, cudaStream_t s );
+void coord_grad( SetupArgs const &a, double const *values, double const *cot,
+                 double *grad_xyz, cudaStream_t s );
+
+} // namespace dtk

@@ -1,0 +1,819 @@
+// Linear BVH and warp-cooperative kNN / radius search (sm_103a).
+//
+// Replaces the ArborX tree and query the MLS constructor runs
+// (packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:114-129).
+//
+// Build: scene box -> 30-bit Morton codes -> stable radix sort (codes, ids)
+// -> Morton-sorted FP64 coordinates (SoA) -> leaf buckets of 32 consecutive
+// points -> Karras (2012) binary radix tree over the leaf keys (first code of
+// each leaf, ties broken by leaf index) -> bottom-up refit with atomic flags.
+// Boxes are FP32, rounded outward, stored as both children's boxes inside
+// the parent (64 B per internal node), so one node fetch tests two children.
+//
+// Query: one warp per target, targets in Morton order.  kNN keeps the k best
+// (d2, index) keys distributed one per lane (sorted across lanes).  The
+// initial bound comes from the 32 Morton-sorted sources around the target's
+// code (a valid upper bound on the k-th distance); traversal is near-first
+// with a per-warp shared-memory stack; a box is pruned only when its FP32
+// round-down lower bound exceeds the round-up bound with a 2^-20 relative
+// margin, so no point whose FP64 distance could tie or beat the bound is
+// skipped.  Distances of points are exact FP64 with separately rounded
+// operations: (dx*dx + dy*dy) + dz*dz.  Keys compare as integers (d2 >= 0,
+// so its IEEE bits are monotone), lexicographic with the source index.
+#include "dtk_common.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace dtk
+{
+namespace
+{
+
+constexpr int LEAF = 32;
+constexpr int STACK = 64;
+constexpr int Q_WARPS = 4; // warps per block in the query kernels
+constexpr unsigned FULL = 0xffffffffu;
+constexpr unsigned long long KEY_INF = 0xffffffffffffffffull;
+
+__device__ __forceinline__ uint32_t expand10( uint32_t v )
+{
+    v &= 0x3ffu;
+    v = ( v | ( v << 16 ) ) & 0x030000FFu;
+    v = ( v | ( v << 8 ) ) & 0x0300F00Fu;
+    v = ( v | ( v << 4 ) ) & 0x030C30C3u;
+    v = ( v | ( v << 2 ) ) & 0x09249249u;
+    return v;
+}
+
+__device__ __forceinline__ uint32_t quantize( double c, double lo, double scale )
+{
+    double const u = ( c - lo ) * scale;
+    if ( !( u > 0.0 ) )
+        return 0u;
+    if ( u >= 1023.0 )
+        return 1023u;
+    return (uint32_t)u;
+}
+
+__device__ __forceinline__ uint32_t morton3( double x, double y, double z,
+                                             double const *scene )
+{
+    // scene: lo[3], scale[3] (1024 / extent, or 0 for a flat axis)
+    return ( expand10( quantize( x, scene[0], scene[3] ) ) << 2 ) |
+           ( expand10( quantize( y, scene[1], scene[4] ) ) << 1 ) |
+           expand10( quantize( z, scene[2], scene[5] ) );
+}
+
+// ---------------------------------------------------------------------------
+// Scene bounds (two-stage reduction).  Min/max of doubles through an
+// order-preserving integer map, so the reduction stays off the FP64 pipe.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long ord_of( double v )
+{
+    unsigned long long b = (unsigned long long)__double_as_longlong( v );
+    return ( b >> 63 ) ? ~b : ( b | 0x8000000000000000ull );
+}
+__device__ __forceinline__ double double_of( unsigned long long o )
+{
+    unsigned long long b = ( o >> 63 ) ? ( o & 0x7fffffffffffffffull ) : ~o;
+    return __longlong_as_double( (long long)b );
+}
+
+constexpr int BND_THREADS = 256;
+
+__global__ void __launch_bounds__( BND_THREADS )
+    k_bounds_partial( PointsView p, unsigned long long *partial )
+{
+    unsigned long long mn[3] = {KEY_INF, KEY_INF, KEY_INF}, mx[3] = {0, 0, 0};
+    for ( int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < p.n;
+          i += (int64_t)gridDim.x * blockDim.x )
+        for ( int d = 0; d < 3; ++d )
+        {
+            unsigned long long const o = ord_of( p( i, d ) );
+            mn[d] = min( mn[d], o );
+            mx[d] = max( mx[d], o );
+        }
+    __shared__ unsigned long long s[6][BND_THREADS / 32];
+    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for ( int d = 0; d < 3; ++d )
+    {
+        for ( int o = 16; o; o >>= 1 )
+        {
+            mn[d] = min( mn[d], __shfl_xor_sync( FULL, mn[d], o ) );
+            mx[d] = max( mx[d], __shfl_xor_sync( FULL, mx[d], o ) );
+        }
+        if ( lane == 0 )
+        {
+            s[d][warp] = mn[d];
+            s[3 + d][warp] = mx[d];
+        }
+    }
+    __syncthreads();
+    if ( threadIdx.x < 6 )
+    {
+        unsigned long long v = s[threadIdx.x][0];
+        for ( int w = 1; w < BND_THREADS / 32; ++w )
+            v = threadIdx.x < 3 ? min( v, s[threadIdx.x][w] ) : max( v, s[threadIdx.x][w] );
+        partial[blockIdx.x * 6 + threadIdx.x] = v;
+    }
+}
+
+// scene[0..2] = lo, scene[3..5] = 1024/extent (0 when flat), scene[6..8] = hi
+__global__ void k_bounds_final( unsigned long long const *partial, int nblocks,
+                                double *scene )
+{
+    if ( threadIdx.x < 3 )
+    {
+        int const d = threadIdx.x;
+        unsigned long long mn = KEY_INF, mx = 0;
+        for ( int b = 0; b < nblocks; ++b )
+        {
+            mn = min( mn, partial[b * 6 + d] );
+            mx = max( mx, partial[b * 6 + 3 + d] );
+        }
+        double const lo = double_of( mn ), hi = double_of( mx );
+        double const e = hi - lo;
+        scene[d] = lo;
+        scene[3 + d] = e > 0.0 ? 1024.0 / e : 0.0;
+        scene[6 + d] = hi;
+    }
+}
+
+__global__ void k_morton( PointsView p, double const *scene, uint32_t *codes,
+                          uint32_t *ids )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i < p.n )
+    {
+        codes[i] = morton3( p( i, 0 ), p( i, 1 ), p( i, 2 ), scene );
+        ids[i] = (uint32_t)i;
+    }
+}
+
+__global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double *sx,
+                                 double *sy, double *sz )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i < p.n )
+    {
+        int64_t const o = perm[i];
+        sx[i] = p( o, 0 );
+        sy[i] = p( o, 1 );
+        sz[i] = p( o, 2 );
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Karras hierarchy over leaf keys.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int delta( uint32_t const *codes, int64_t nl, int64_t i,
+                                      int64_t j )
+{
+    if ( j < 0 || j >= nl )
+        return -1;
+    uint32_t const ki = codes[i * LEAF], kj = codes[j * LEAF];
+    if ( ki != kj )
+        return __clz( ki ^ kj );
+    // equal leaf keys: ranks by leaf index, always above any 32-bit key prefix
+    return 32 + __clzll( (unsigned long long)( i ^ j ) );
+}
+
+__global__ void k_karras( uint32_t const *codes, int64_t nl, int *left, int *right,
+                          int *parent_node, int *parent_leaf )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i >= nl - 1 )
+        return;
+    int const d = ( delta( codes, nl, i, i + 1 ) - delta( codes, nl, i, i - 1 ) ) >= 0 ? 1 : -1;
+    int const dmin = delta( codes, nl, i, i - d );
+    int64_t lmax = 2;
+    while ( delta( codes, nl, i, i + lmax * d ) > dmin )
+        lmax <<= 1;
+    int64_t l = 0;
+    for ( int64_t t = lmax >> 1; t >= 1; t >>= 1 )
+        if ( delta( codes, nl, i, i + ( l + t ) * d ) > dmin )
+            l += t;
+    int64_t const j = i + l * d;
+    int const dnode = delta( codes, nl, i, j );
+    int64_t s = 0;
+    int64_t t = l;
+    do
+    {
+        t = ( t + 1 ) >> 1;
+        if ( delta( codes, nl, i, i + ( s + t ) * d ) > dnode )
+            s += t;
+    } while ( t > 1 );
+    int64_t const gamma = i + s * d + min( d, 0 );
+    int64_t const lo = min( i, j ), hi = max( i, j );
+    int lc, rc;
+    if ( lo == gamma )
+    {
+        lc = ~(int)gamma;
+        parent_leaf[gamma] = (int)i;
+    }
+    else
+    {
+        lc = (int)gamma;
+        parent_node[gamma] = (int)i;
+    }
+    if ( hi == gamma + 1 )
+    {
+        rc = ~(int)( gamma + 1 );
+        parent_leaf[gamma + 1] = (int)i;
+    }
+    else
+    {
+        rc = (int)( gamma + 1 );
+        parent_node[gamma + 1] = (int)i;
+    }
+    left[i] = lc;
+    right[i] = rc;
+}
+
+struct Box
+{
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ void store_child_box( float4 *nodes, int parent, bool is_left,
+                                                 Box const &b )
+{
+    float *n = reinterpret_cast<float *>( nodes + 4 * (int64_t)parent );
+    int const o = is_left ? 0 : 6;
+#pragma unroll
+    for ( int d = 0; d < 3; ++d )
+    {
+        __stcg( n + o + d, b.lo[d] );
+        __stcg( n + o + 3 + d, b.hi[d] );
+    }
+}
+
+__device__ __forceinline__ Box load_child_box( float4 const *nodes, int parent, bool is_left )
+{
+    float const *n = reinterpret_cast<float const *>( nodes + 4 * (int64_t)parent );
+    int const o = is_left ? 0 : 6;
+    Box b;
+#pragma unroll
+    for ( int d = 0; d < 3; ++d )
+    {
+        b.lo[d] = __ldcg( n + o + d );
+        b.hi[d] = __ldcg( n + o + 3 + d );
+    }
+    return b;
+}
+
+// One thread per leaf: leaf box, then walk up; the second child to arrive at
+// a node computes its box and continues.
+__global__ void k_refit( double const *sx, double const *sy, double const *sz, int64_t n,
+                         int64_t nl, int const *left, int const *right,
+                         int const *parent_node, int const *parent_leaf, float4 *nodes,
+                         unsigned *flags, float4 *root_box, unsigned *status )
+{
+    int64_t const leaf = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( leaf >= nl )
+        return;
+    double lo[3] = {sx[leaf * LEAF], sy[leaf * LEAF], sz[leaf * LEAF]};
+    double hi[3] = {lo[0], lo[1], lo[2]};
+    int64_t const end = min( n, ( leaf + 1 ) * (int64_t)LEAF );
+    for ( int64_t p = leaf * LEAF + 1; p < end; ++p )
+    {
+        double const c[3] = {sx[p], sy[p], sz[p]};
+#pragma unroll
+        for ( int d = 0; d < 3; ++d )
+        {
+            lo[d] = fmin( lo[d], c[d] );
+            hi[d] = fmax( hi[d], c[d] );
+        }
+    }
+    Box b;
+#pragma unroll
+    for ( int d = 0; d < 3; ++d )
+    {
+        b.lo[d] = __double2float_rd( lo[d] );
+        b.hi[d] = __double2float_ru( hi[d] );
+    }
+    if ( nl == 1 )
+    {
+        root_box[0] = make_float4( b.lo[0], b.lo[1], b.lo[2], b.hi[0] );
+        root_box[1] = make_float4( b.hi[1], b.hi[2], 0.f, 0.f );
+        return;
+    }
+    int node = parent_leaf[leaf];
+    int child = ~(int)leaf;
+    // A radix tree over nl leaves is at most nl - 1 levels deep; the cap only
+    // turns a malformed tree into a reported error instead of a hang.
+    for ( int64_t guard = 0; guard < nl; ++guard )
+    {
+        store_child_box( nodes, node, left[node] == child, b );
+        __threadfence();
+        unsigned const prev = atomicAdd( &flags[node], 1u );
+        if ( prev == 0 )
+            return; // sibling not done yet; it will continue upwards
+        __threadfence();
+        Box const a = load_child_box( nodes, node, true );
+        Box const c = load_child_box( nodes, node, false );
+#pragma unroll
+        for ( int d = 0; d < 3; ++d )
+        {
+            b.lo[d] = fminf( a.lo[d], c.lo[d] );
+            b.hi[d] = fmaxf( a.hi[d], c.hi[d] );
+        }
+        if ( node == 0 )
+        {
+            root_box[0] = make_float4( b.lo[0], b.lo[1], b.lo[2], b.hi[0] );
+            root_box[1] = make_float4( b.hi[1], b.hi[2], 0.f, 0.f );
+            return;
+        }
+        child = node;
+        node = parent_node[node];
+        if ( node < 0 || node >= nl - 1 )
+            break;
+    }
+    atomicOr( status, DEV_BAD_INDEX ); // malformed tree
+}
+
+__global__ void k_pack_children( int64_t n_internal, int const *left, int const *right,
+                                 float4 *nodes )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i < n_internal )
+        nodes[4 * i + 3] = make_float4( __int_as_float( left[i] ), __int_as_float( right[i] ),
+                                        0.f, 0.f );
+}
+
+// ---------------------------------------------------------------------------
+// Queries
+// ---------------------------------------------------------------------------
+struct TreeView
+{
+    double const *sx, *sy, *sz;
+    uint32_t const *codes, *perm;
+    float4 const *nodes;
+    double const *scene;
+    int64_t n, nl;
+};
+
+// FP32 lower bound of the squared distance between any point of [lo, hi]
+// and any point of the query interval [qlo, qhi] (round-down arithmetic).
+__device__ __forceinline__ float box_lb( float const *lo, float const *hi,
+                                         float const *qlo, float const *qhi )
+{
+    float acc = 0.f;
+#pragma unroll
+    for ( int d = 0; d < 3; ++d )
+    {
+        float g = fmaxf( 0.f, fmaxf( __fsub_rd( lo[d], qhi[d] ), __fsub_rd( qlo[d], hi[d] ) ) );
+        acc = __fadd_rd( acc, __fmul_rd( g, g ) );
+    }
+    return acc;
+}
+
+// Upper FP32 threshold for pruning against an FP64 bound (2^-20 margin).
+__device__ __forceinline__ float prune_threshold( double bound_d2 )
+{
+    if ( !( bound_d2 < 1e300 ) )
+        return __int_as_float( 0x7f800000 ); // +inf: prune nothing
+    float const f = __double2float_ru( bound_d2 );
+    return __fmul_ru( f, 1.0f + 9.5367431640625e-07f );
+}
+
+__device__ __forceinline__ bool key_less( unsigned long long ad, int ai,
+                                          unsigned long long bd, int bi )
+{
+    return ad < bd || ( ad == bd && ai < bi );
+}
+
+// 32-ary lower_bound of `code` in the sorted codes (warp-uniform result).
+__device__ __forceinline__ int64_t warp_lower_bound( uint32_t const *codes, int64_t n,
+                                                     uint32_t code, int lane )
+{
+    int64_t lo = 0, hi = n;
+    while ( hi - lo > 32 )
+    {
+        int64_t const step = ( hi - lo + 31 ) / 32;
+        int64_t const p = lo + lane * step;
+        bool const pred = p < hi && __ldg( codes + p ) < code;
+        unsigned const b = __ballot_sync( FULL, pred );
+        int const cnt = __popc( b );
+        int64_t const nlo = cnt ? lo + ( cnt - 1 ) * step + 1 : lo;
+        int64_t const nhi = ( cnt < 32 && lo + cnt * step < hi ) ? lo + cnt * step : hi;
+        lo = nlo;
+        hi = nhi;
+    }
+    bool const pred = lo + lane < hi && __ldg( codes + lo + lane ) < code;
+    return lo + __popc( __ballot_sync( FULL, pred ) );
+}
+
+__device__ __forceinline__ void load_node( float4 const *nodes, int node, float *l_lo,
+                                           float *l_hi, float *r_lo, float *r_hi, int &lc,
+                                           int &rc )
+{
+    float4 const a = __ldg( nodes + 4 * (int64_t)node );
+    float4 const b = __ldg( nodes + 4 * (int64_t)node + 1 );
+    float4 const c = __ldg( nodes + 4 * (int64_t)node + 2 );
+    float4 const e = __ldg( nodes + 4 * (int64_t)node + 3 );
+    l_lo[0] = a.x;
+    l_lo[1] = a.y;
+    l_lo[2] = a.z;
+    l_hi[0] = a.w;
+    l_hi[1] = b.x;
+    l_hi[2] = b.y;
+    r_lo[0] = b.z;
+    r_lo[1] = b.w;
+    r_lo[2] = c.x;
+    r_hi[0] = c.y;
+    r_hi[1] = c.z;
+    r_hi[2] = c.w;
+    lc = __float_as_int( e.x );
+    rc = __float_as_int( e.y );
+}
+
+__global__ void __launch_bounds__( Q_WARPS * 32 )
+    k_knn( TreeView tr, PointsView tgt, uint32_t const *order, int k, int row,
+           int32_t *idx_out, unsigned *status )
+{
+    __shared__ int s_stack[Q_WARPS][STACK];
+    __shared__ float s_lb[Q_WARPS][STACK];
+    int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    int64_t const w = blockIdx.x * (int64_t)Q_WARPS + wib;
+    if ( w >= tgt.n )
+        return;
+    int64_t const qi = order ? (int64_t)order[w] : w;
+    double const tx = tgt( qi, 0 ), ty = tgt( qi, 1 ), tz = tgt( qi, 2 );
+    float const qlo[3] = {__double2float_rd( tx ), __double2float_rd( ty ), __double2float_rd( tz )};
+    float const qhi[3] = {__double2float_ru( tx ), __double2float_ru( ty ), __double2float_ru( tz )};
+
+    // Initial candidates: the 32 Morton-sorted sources around the target.
+    uint32_t const code = morton3( tx, ty, tz, tr.scene );
+    int64_t const pos = warp_lower_bound( tr.codes, tr.n, code, lane );
+    int64_t const W = tr.n < 32 ? tr.n : (int64_t)32;
+    int64_t s0 = pos - 16;
+    if ( s0 > tr.n - W )
+        s0 = tr.n - W;
+    if ( s0 < 0 )
+        s0 = 0;
+    unsigned long long kd = KEY_INF;
+    int ki = 0x7fffffff;
+    if ( lane < W )
+    {
+        int64_t const p = s0 + lane;
+        kd = (unsigned long long)__double_as_longlong(
+            dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), tx, ty, tz ) );
+        ki = (int)__ldg( tr.perm + p );
+    }
+    // Bitonic sort of the 32 keys across lanes (ascending).
+#pragma unroll
+    for ( int size = 2; size <= 32; size <<= 1 )
+#pragma unroll
+        for ( int stride = size >> 1; stride > 0; stride >>= 1 )
+        {
+            unsigned long long const od = __shfl_xor_sync( FULL, kd, stride );
+            int const oi = __shfl_xor_sync( FULL, ki, stride );
+            bool const up = ( lane & size ) == 0 || size == 32;
+            bool const lower = ( lane & stride ) == 0;
+            bool const mine_less = key_less( kd, ki, od, oi );
+            bool const take = ( lower == up ) ? !mine_less : mine_less;
+            if ( take )
+            {
+                kd = od;
+                ki = oi;
+            }
+        }
+    if ( lane >= k )
+    {
+        kd = KEY_INF;
+        ki = 0x7fffffff;
+    }
+    unsigned long long bd = __shfl_sync( FULL, kd, k - 1 );
+    int bi = __shfl_sync( FULL, ki, k - 1 );
+    float bound_f = prune_threshold( __longlong_as_double( (long long)bd ) );
+
+    auto process_leaf = [&]( int leaf ) {
+        int64_t const p = (int64_t)leaf * LEAF + lane;
+        bool const in_window = p >= s0 && p < s0 + W;
+        unsigned long long cd = KEY_INF;
+        int ci = 0x7fffffff;
+        if ( p < tr.n && !in_window )
+        {
+            cd = (unsigned long long)__double_as_longlong(
+                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), tx, ty, tz ) );
+            ci = (int)__ldg( tr.perm + p );
+        }
+        unsigned cand = __ballot_sync( FULL, key_less( cd, ci, bd, bi ) );
+        while ( cand )
+        {
+            int const src_lane = __ffs( cand ) - 1;
+            cand &= cand - 1;
+            unsigned long long const nd = __shfl_sync( FULL, cd, src_lane );
+            int const ni = __shfl_sync( FULL, ci, src_lane );
+            if ( !key_less( nd, ni, bd, bi ) )
+                continue;
+            unsigned const gt = __ballot_sync( FULL, key_less( nd, ni, kd, ki ) );
+            int const at = __ffs( gt ) - 1;
+            unsigned long long const ud = __shfl_up_sync( FULL, kd, 1 );
+            int const ui = __shfl_up_sync( FULL, ki, 1 );
+            if ( lane > at )
+            {
+                kd = ud;
+                ki = ui;
+            }
+            else if ( lane == at )
+            {
+                kd = nd;
+                ki = ni;
+            }
+            bd = __shfl_sync( FULL, kd, k - 1 );
+            bi = __shfl_sync( FULL, ki, k - 1 );
+        }
+        bound_f = prune_threshold( __longlong_as_double( (long long)bd ) );
+    };
+
+    if ( tr.nl == 1 )
+    {
+        process_leaf( 0 );
+    }
+    else
+    {
+        // Near-first depth-first traversal; the farther child goes on the
+        // stack with its lower bound and is re-tested when popped.
+        int sp = 0;
+        int node = 0;
+        // every internal node is entered at most once
+        for ( int64_t guard = 0;; ++guard )
+        {
+            if ( guard >= tr.nl )
+            {
+                if ( lane == 0 )
+                    atomicOr( status, DEV_TIMEOUT );
+                break;
+            }
+            float l_lo[3], l_hi[3], r_lo[3], r_hi[3];
+            int lc, rc;
+            load_node( tr.nodes, node, l_lo, l_hi, r_lo, r_hi, lc, rc );
+            float const lbl = box_lb( l_lo, l_hi, qlo, qhi );
+            float const lbr = box_lb( r_lo, r_hi, qlo, qhi );
+            bool const near_left = lbl <= lbr;
+            int const c_near = near_left ? lc : rc, c_far = near_left ? rc : lc;
+            float const lb_near = near_left ? lbl : lbr, lb_far = near_left ? lbr : lbl;
+            int next = -1;
+            if ( lb_far <= bound_f )
+            {
+                if ( sp < STACK )
+                {
+                    if ( lane == 0 )
+                    {
+                        s_stack[wib][sp] = c_far;
+                        s_lb[wib][sp] = lb_far;
+                    }
+                    ++sp;
+                }
+                else if ( lane == 0 )
+                    atomicOr( status, DEV_STACK_OVERFLOW );
+            }
+            if ( lb_near <= bound_f )
+            {
+                if ( c_near < 0 )
+                    process_leaf( ~c_near );
+                else
+                    next = c_near;
+            }
+            __syncwarp();
+            while ( next < 0 && sp > 0 )
+            {
+                --sp;
+                int const cand = s_stack[wib][sp];
+                float const lb = s_lb[wib][sp];
+                __syncwarp();
+                if ( lb > bound_f )
+                    continue;
+                if ( cand < 0 )
+                    process_leaf( ~cand );
+                else
+                    next = cand;
+            }
+            if ( next < 0 )
+                break;
+            node = next;
+        }
+    }
+    if ( lane < row )
+        idx_out[qi * (int64_t)row + lane] = ki;
+}
+
+// Radius traversal shared by the count and fill passes.  FILL=false counts
+// hits into counts[qi]; FILL=true writes them at offset[qi] in traversal
+// order (Morton order of the sources, lane order inside a leaf).
+template <bool FILL>
+__global__ void __launch_bounds__( Q_WARPS * 32 )
+    k_radius( TreeView tr, PointsView tgt, uint32_t const *order, double r,
+              int64_t *counts, int32_t const *offset, int32_t *idx_out, unsigned *status )
+{
+    __shared__ int s_stack[Q_WARPS][STACK];
+    int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    int64_t const w = blockIdx.x * (int64_t)Q_WARPS + wib;
+    if ( w >= tgt.n )
+        return;
+    int64_t const qi = order ? (int64_t)order[w] : w;
+    double const tx = tgt( qi, 0 ), ty = tgt( qi, 1 ), tz = tgt( qi, 2 );
+    float const qlo[3] = {__double2float_rd( tx ), __double2float_rd( ty ), __double2float_rd( tz )};
+    float const qhi[3] = {__double2float_ru( tx ), __double2float_ru( ty ), __double2float_ru( tz )};
+    float const bound_f = prune_threshold( __dmul_ru( r, r ) );
+    int64_t cnt = 0;
+    int64_t out = FILL ? offset[qi] : 0;
+    int64_t const out_end = FILL ? offset[qi + 1] : 0;
+
+    auto process_leaf = [&]( int leaf ) {
+        int64_t const p = (int64_t)leaf * LEAF + lane;
+        bool hit = false;
+        if ( p < tr.n )
+        {
+            double const d2 = dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ),
+                                        tx, ty, tz );
+            hit = __dsqrt_rn( d2 ) <= r;
+        }
+        unsigned const b = __ballot_sync( FULL, hit );
+        if ( FILL && hit )
+        {
+            int64_t const o = out + __popc( b & ( ( 1u << lane ) - 1u ) );
+            if ( o < out_end )
+                idx_out[o] = (int32_t)__ldg( tr.perm + p );
+            else
+                atomicOr( status, DEV_BAD_INDEX );
+        }
+        out += __popc( b );
+        cnt += __popc( b );
+    };
+
+    if ( tr.nl == 1 )
+    {
+        process_leaf( 0 );
+    }
+    else
+    {
+        int sp = 0;
+        int node = 0;
+        // every internal node is entered at most once
+        for ( int64_t guard = 0;; ++guard )
+        {
+            if ( guard >= tr.nl )
+            {
+                if ( lane == 0 )
+                    atomicOr( status, DEV_TIMEOUT );
+                break;
+            }
+            float l_lo[3], l_hi[3], r_lo[3], r_hi[3];
+            int lc, rc;
+            load_node( tr.nodes, node, l_lo, l_hi, r_lo, r_hi, lc, rc );
+            bool const hl = box_lb( l_lo, l_hi, qlo, qhi ) <= bound_f;
+            bool const hr = box_lb( r_lo, r_hi, qlo, qhi ) <= bound_f;
+            int next = -1;
+            if ( hl )
+            {
+                if ( lc < 0 )
+                    process_leaf( ~lc );
+                else
+                    next = lc;
+            }
+            if ( hr )
+            {
+                if ( rc < 0 )
+                    process_leaf( ~rc );
+                else if ( next < 0 )
+                    next = rc;
+                else if ( sp < STACK )
+                {
+                    if ( lane == 0 )
+                        s_stack[wib][sp] = rc;
+                    ++sp;
+                }
+                else if ( lane == 0 )
+                    atomicOr( status, DEV_STACK_OVERFLOW );
+            }
+            __syncwarp();
+            if ( next < 0 )
+            {
+                if ( sp == 0 )
+                    break;
+                --sp;
+                next = s_stack[wib][sp];
+                __syncwarp();
+            }
+            node = next;
+        }
+    }
+    if ( !FILL && lane == 0 )
+        counts[qi] = cnt;
+    if ( FILL && lane == 0 && out != out_end )
+        atomicOr( status, DEV_BAD_INDEX );
+}
+
+TreeView view_of( Lbvh const &t )
+{
+    return TreeView{t.sx.get(), t.sy.get(), t.sz.get(), t.codes.get(), t.perm.get(),
+                    t.nodes.get(), t.scene.get(), t.n, t.n_leaves};
+}
+
+unsigned blocks_for( int64_t n, int threads )
+{
+    return (unsigned)std::max<int64_t>( 1, ( n + threads - 1 ) / threads );
+}
+
+} // namespace
+
+void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s )
+{
+    int64_t const n = src.n;
+    tree.n = n;
+    tree.n_leaves = ( n + LEAF - 1 ) / LEAF;
+    int64_t const nl = tree.n_leaves;
+    tree.scene.allocate( 9, s );
+    int const nb = std::max( 1, std::min<int>( 4 * num_sms(), (int)( ( n + BND_THREADS - 1 ) / BND_THREADS ) ) );
+    DeviceBuffer<unsigned long long> partial( 6 * nb, s );
+    k_bounds_partial<<<nb, BND_THREADS, 0, s>>>( src, partial.get() );
+    check_launch( "k_bounds_partial" );
+    k_bounds_final<<<1, 32, 0, s>>>( partial.get(), nb, tree.scene.get() );
+    check_launch( "k_bounds_final" );
+
+    tree.codes.allocate( n, s );
+    tree.perm.allocate( n, s );
+    k_morton<<<blocks_for( n, 256 ), 256, 0, s>>>( src, tree.scene.get(), tree.codes.get(),
+                                                     tree.perm.get() );
+    check_launch( "k_morton" );
+    radix_sort_pairs( tree.codes.get(), tree.perm.get(), n, 30, s );
+
+    tree.sx.allocate( n, s );
+    tree.sy.allocate( n, s );
+    tree.sz.allocate( n, s );
+    k_gather_sorted<<<blocks_for( n, 256 ), 256, 0, s>>>( src, tree.perm.get(), tree.sx.get(),
+                                                            tree.sy.get(), tree.sz.get() );
+    check_launch( "k_gather_sorted" );
+
+    int64_t const ni = std::max<int64_t>( 0, nl - 1 );
+    tree.nodes.allocate( 4 * std::max<int64_t>( 1, ni ), s );
+    tree.root_box.allocate( 2, s );
+    DeviceBuffer<int> left( std::max<int64_t>( 1, ni ), s ), right( std::max<int64_t>( 1, ni ), s ),
+        parent_node( std::max<int64_t>( 1, ni ), s ), parent_leaf( nl, s );
+    DeviceBuffer<unsigned> flags( std::max<int64_t>( 1, ni ), s );
+    DTK_CUDA_OR_THROW( cudaMemsetAsync( flags.get(), 0, flags.n * sizeof( unsigned ), s ) );
+    if ( ni > 0 )
+    {
+        k_karras<<<blocks_for( ni, 256 ), 256, 0, s>>>( tree.codes.get(), nl, left.get(), right.get(),
+                                                          parent_node.get(), parent_leaf.get() );
+        check_launch( "k_karras" );
+        k_pack_children<<<blocks_for( ni, 256 ), 256, 0, s>>>( ni, left.get(), right.get(),
+                                                                 tree.nodes.get() );
+        check_launch( "k_pack_children" );
+    }
+    k_refit<<<blocks_for( nl, 128 ), 128, 0, s>>>( tree.sx.get(), tree.sy.get(), tree.sz.get(), n, nl,
+                                                     left.get(), right.get(), parent_node.get(),
+                                                     parent_leaf.get(), tree.nodes.get(), flags.get(),
+                                                     tree.root_box.get(), status );
+    check_launch( "k_refit" );
+}
+
+void sort_queries( Lbvh const &tree, PointsView tgt, DeviceBuffer<uint32_t> &order,
+                   cudaStream_t s )
+{
+    int64_t const n = tgt.n;
+    order.allocate( std::max<int64_t>( 1, n ), s );
+    if ( n == 0 )
+        return;
+    DeviceBuffer<uint32_t> codes( n, s );
+    k_morton<<<blocks_for( n, 256 ), 256, 0, s>>>( tgt, tree.scene.get(), codes.get(), order.get() );
+    check_launch( "k_morton(targets)" );
+    radix_sort_pairs( codes.get(), order.get(), n, 30, s );
+}
+
+void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k, int32_t *idx,
+                unsigned *status, cudaStream_t s )
+{
+    if ( tgt.n == 0 || tree.n == 0 || k == 0 )
+        return;
+    int const row = (int)std::min<int64_t>( k, tree.n );
+    k_knn<<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, k, row,
+                                                                  idx, status );
+    check_launch( "k_knn" );
+}
+
+void radius_count( Lbvh const &tree, PointsView tgt, uint32_t const *order, double r,
+                   int64_t *counts, unsigned *status, cudaStream_t s )
+{
+    if ( tgt.n == 0 )
+        return;
+    k_radius<false><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
+        view_of( tree ), tgt, order, r, counts, nullptr, nullptr, status );
+    check_launch( "k_radius(count)" );
+}
+
+void radius_fill( Lbvh const &tree, PointsView tgt, uint32_t const *order, double r,
+                  int32_t const *offset, int32_t *idx, unsigned *status, cudaStream_t s )
+{
+    if ( tgt.n == 0 )
+        return;
+    k_radius<true><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
+        view_of( tree ), tgt, order, r, nullptr, offset, idx, status );
+    check_launch( "k_radius(fill)" );
+}
+
+} // namespace dtk

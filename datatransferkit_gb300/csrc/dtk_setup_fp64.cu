@@ -1,0 +1,468 @@
+// Fused MLS setup, FP64 form (sm_103a).
+//
+// One thread per target (targets in Morton order) runs every stage of the
+// reference constructor after the search, fused, with nothing but the
+// coefficients written to HBM:
+//   gather + transformSourceCoordinates  Impl.hpp:72-99
+//   computeVandermonde                   Impl.hpp:171-190
+//   computeRadius (1.1 * max(10 eps, max |x|))   Impl.hpp:101-138
+//   computeWeights                       Impl.hpp:143-169
+//   computeMoments (symmetric, registers)        Impl.hpp:213-258
+//   invertMoments -> SVDFunctor          SVDImpl.hpp:197-302
+//   computePolynomialCoefficients        Impl.hpp:293-336
+// (Impl.hpp = packages/Meshfree/src/DTK_DetailsMovingLeastSquaresOperatorImpl.hpp,
+//  SVDImpl.hpp = packages/Meshfree/src/DTK_DetailsSVDImpl.hpp)
+//
+// The pseudo-inverse keeps DTK's algorithm exactly: two-sided Jacobi with the
+// largest off-diagonal pivot (first in row-major order on ties), p<q swap,
+// the explicit 2x2 SVD (atan2 half angles, copysign correction, the sr sign
+// rule), the absolute DBL_EPSILON stop on the off-diagonal Frobenius norm and
+// the absolute DBL_EPSILON truncation.  Its results carry a deterministic
+// deviation from the exact pseudo-inverse at fine point spacing (the stop is
+// absolute on unscaled moments), so matching the reference to 1e-12 needs the
+// same pivots, rotations and stops, not merely any accurate pseudo-inverse.
+//
+// Thread-per-target, not warp-per-target: GB300's FP64 pipe issues one warp
+// instruction per 64 cycles per SM sub-partition, so every FP64 instruction
+// must carry 32 useful lanes; the 2x2 SVD is scalar work.  Iteration counts
+// are tight (about 114 +- 13 for the quadratic basis), so divergence costs
+// little.  E (m x m), U (m x m) and column 0 of V live in shared memory,
+// interleaved by thread so that dynamic (p, q) accesses are conflict-free.
+// The argmax runs on the integer pipe over the IEEE bits of |E_ij|.
+#include "dtk_common.cuh"
+
+#include <algorithm>
+
+namespace dtk
+{
+namespace
+{
+
+constexpr int SETUP_BLOCK = 32;
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ void svd_2x2( double a, double b, double c, double d, double &cl,
+                                         double &sl, double &cr, double &sr )
+{
+    // A A^T and A^T A in the element order of SVDImpl.hpp:109-117,123-126
+    double const p00 = a * a + b * b, p01 = a * c + b * d, p10 = c * a + d * b,
+                 p11 = c * c + d * d;
+    double const q00 = a * a + c * c, q01 = a * b + c * d, q10 = b * a + d * c,
+                 q11 = b * b + d * d;
+    double sphi, cphi, sth, cth;
+    sincos( 0.5 * atan2( p01 + p10, p00 - p11 ), &sphi, &cphi );
+    sincos( 0.5 * atan2( q01 + q10, q00 - q11 ), &sth, &cth );
+    // S = U^T A W diagonal signs (SVDImpl.hpp:149-159)
+    double const aw00 = a * cth + b * sth, aw01 = a * -sth + b * cth;
+    double const aw10 = c * cth + d * sth, aw11 = c * -sth + d * cth;
+    double const s00 = cphi * aw00 + sphi * aw10;
+    double const s11 = -sphi * aw01 + cphi * aw11;
+    double const c0 = copysign( 1.0, s00 ), c1 = copysign( 1.0, s11 );
+    // V = W diag(c0, c1); sr sign rule of SVDImpl.hpp:260-263
+    double const v00 = cth * c0, v01 = -sth * c1, v10 = sth * c0;
+    cl = cphi;
+    sl = -sphi;
+    cr = v00;
+    int const g01 = ( v01 > 0 ) - ( v01 < 0 ), g10 = ( v10 > 0 ) - ( v10 < 0 );
+    sr = ( g01 == g10 ) ? -v01 : v01;
+}
+
+// |x| as an ordered integer (non-negative doubles order like their bits).
+__device__ __forceinline__ long long abs_bits( double x )
+{
+    return __double_as_longlong( x ) & 0x7fffffffffffffffll;
+}
+
+template <int M>
+struct Smem
+{
+    double *E, *U, *V0;
+    int t;
+    __device__ double &e( int i, int j ) const { return E[( i * M + j ) * SETUP_BLOCK + t]; }
+    __device__ double &u( int i, int j ) const { return U[( i * M + j ) * SETUP_BLOCK + t]; }
+    __device__ double &v( int i ) const { return V0[i * SETUP_BLOCK + t]; }
+};
+
+// Runs DTK's Jacobi on the thread's E; on return row0 holds row 0 of the
+// pseudo-inverse.  Returns 1 if a singular value was truncated.
+template <int M>
+__device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, unsigned cap,
+                            unsigned *status )
+{
+    double const tol = DBL_EPSILON;
+    unsigned it = 0;
+    while ( true )
+    {
+        // Fused scan: off-diagonal Frobenius norm and first largest |E_ij|.
+        double acc0 = 0.0, acc1 = 0.0;
+        long long best = -1;
+        int p = 0, q = 1;
+#pragma unroll
+        for ( int i = 0; i < M; ++i )
+#pragma unroll
+            for ( int j = 0; j < M; ++j )
+            {
+                if ( i == j )
+                    continue;
+                double const x = s.e( i, j );
+                if ( ( i * M + j ) & 1 )
+                    acc1 = fma( x, x, acc1 );
+                else
+                    acc0 = fma( x, x, acc0 );
+                long long const ab = abs_bits( x );
+                if ( ab > best )
+                {
+                    best = ab;
+                    p = i;
+                    q = j;
+                }
+            }
+        double const norm = sqrt( acc0 + acc1 );
+        if ( !( norm > tol ) )
+            break;
+        if ( ++it > cap )
+        {
+            atomicOr( status, DEV_TIMEOUT );
+            break;
+        }
+        if ( p > q )
+        {
+            int const tmp = p;
+            p = q;
+            q = tmp;
+        }
+        double cl, sl, cr, sr;
+        svd_2x2( s.e( p, p ), s.e( p, q ), s.e( q, p ), s.e( q, q ), cl, sl, cr, sr );
+        // givens_left(E, cl, sl, p, q)
+#pragma unroll
+        for ( int j = 0; j < M; ++j )
+        {
+            double const a = s.e( p, j ), b = s.e( q, j );
+            s.e( p, j ) = cl * a - sl * b;
+            s.e( q, j ) = sl * a + cl * b;
+        }
+        // givens_right(E, cr, sr, p, q)
+#pragma unroll
+        for ( int j = 0; j < M; ++j )
+        {
+            double const a = s.e( j, p ), b = s.e( j, q );
+            s.e( j, p ) = cr * a - sr * b;
+            s.e( j, q ) = sr * a + cr * b;
+        }
+        // givens_right(U, cl, sl, p, q)
+#pragma unroll
+        for ( int j = 0; j < M; ++j )
+        {
+            double const a = s.u( j, p ), b = s.u( j, q );
+            s.u( j, p ) = cl * a - sl * b;
+            s.u( j, q ) = sl * a + cl * b;
+        }
+        // givens_left(V, cr, sr, p, q), column 0 only
+        {
+            double const a = s.v( p ), b = s.v( q );
+            s.v( p ) = cr * a - sr * b;
+            s.v( q ) = sr * a + cr * b;
+        }
+    }
+    iters += it;
+    // pinv(0, j) = sum_k V(k,0) U(j,k) / E(k,k) over |E(k,k)| >= DBL_EPSILON
+    int dropped = 0;
+    double w[M];
+#pragma unroll
+    for ( int k = 0; k < M; ++k )
+    {
+        double const ek = s.e( k, k );
+        if ( fabs( ek ) >= tol )
+            w[k] = s.v( k ) / ek;
+        else
+        {
+            w[k] = 0.0;
+            dropped = 1;
+        }
+    }
+#pragma unroll
+    for ( int j = 0; j < M; ++j )
+    {
+        double v = 0.0;
+#pragma unroll
+        for ( int k = 0; k < M; ++k )
+            v = fma( s.u( j, k ), w[k], v );
+        row0[j] = v;
+    }
+    return dropped;
+}
+
+template <int M>
+__global__ void __launch_bounds__( SETUP_BLOCK )
+    k_setup_fp64( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
+                  uint32_t const *order, int64_t n_tgt, int rbf, bool rows_sorted,
+                  double *coeff, unsigned long long *under_count,
+                  unsigned long long *rot_count, unsigned *status )
+{
+    extern __shared__ double smem[];
+    Smem<M> s{smem, smem + M * M * SETUP_BLOCK, smem + 2 * M * M * SETUP_BLOCK, (int)threadIdx.x};
+    int64_t const g = blockIdx.x * (int64_t)SETUP_BLOCK + threadIdx.x;
+    unsigned iters = 0;
+    int dropped = 0;
+    if ( g < n_tgt )
+    {
+        int64_t const i = order ? (int64_t)order[g] : g;
+        int64_t const b = offset[i];
+        int len = offset[i + 1] - (int)b;
+        for ( int j = 0; j < len; ++j )
+            if ( (uint32_t)idx[b + j] >= (uint64_t)src.n )
+            {
+                atomicOr( status, DEV_BAD_INDEX );
+                len = 0;
+            }
+        double const tx = tgt( i, 0 ), ty = tgt( i, 1 ), tz = tgt( i, 2 );
+
+        // computeRadius: the largest neighbour distance (last entry when the
+        // row is sorted by distance).
+        double d2max = 0.0;
+        for ( int j = rows_sorted ? max( 0, len - 1 ) : 0; j < len; ++j )
+        {
+            int64_t const sj = idx[b + j];
+            d2max = fmax( d2max, dist2_rn( src( sj, 0 ), src( sj, 1 ), src( sj, 2 ), tx, ty, tz ) );
+        }
+        double distance = 10. * DBL_EPSILON;
+        double const dmax = __dsqrt_rn( d2max );
+        if ( dmax > distance )
+            distance = dmax;
+        double const radius = 1.1 * distance;
+
+        // computeMoments (upper triangle, registers)
+        double A[M * ( M + 1 ) / 2];
+#pragma unroll
+        for ( int a = 0; a < M * ( M + 1 ) / 2; ++a )
+            A[a] = 0.0;
+        for ( int j = 0; j < len; ++j )
+        {
+            int64_t const sj = idx[b + j];
+            double const x = __dsub_rn( src( sj, 0 ), tx ), y = __dsub_rn( src( sj, 1 ), ty ),
+                         z = __dsub_rn( src( sj, 2 ), tz );
+            double P[M];
+            basis_eval<M>( x, y, z, P );
+            double const dist =
+                __dsqrt_rn( __dadd_rn( __dadd_rn( __dmul_rn( x, x ), __dmul_rn( y, y ) ), __dmul_rn( z, z ) ) );
+            double const phi = rbf_eval<double>( rbf, dist / radius );
+            int o = 0;
+#pragma unroll
+            for ( int a = 0; a < M; ++a )
+            {
+                double const pa = P[a] * phi;
+#pragma unroll
+                for ( int c = a; c < M; ++c, ++o )
+                    A[o] = fma( pa, P[c], A[o] );
+            }
+        }
+        {
+            int o = 0;
+#pragma unroll
+            for ( int a = 0; a < M; ++a )
+#pragma unroll
+                for ( int c = a; c < M; ++c )
+                {
+                    s.e( a, c ) = A[o];
+                    s.e( c, a ) = A[o];
+                    ++o;
+                }
+#pragma unroll
+            for ( int a = 0; a < M; ++a )
+            {
+#pragma unroll
+                for ( int c = 0; c < M; ++c )
+                    s.u( a, c ) = ( a == c ) ? 1.0 : 0.0;
+                s.v( a ) = a == 0 ? 1.0 : 0.0;
+            }
+        }
+        double row0[M];
+        dropped = jacobi_row0<M>( s, row0, iters, 200u * M * M + 2000u, status );
+
+        // computePolynomialCoefficients: c_k = phi_k * (row0 . P_k)
+        for ( int j = 0; j < len; ++j )
+        {
+            int64_t const sj = idx[b + j];
+            double const x = __dsub_rn( src( sj, 0 ), tx ), y = __dsub_rn( src( sj, 1 ), ty ),
+                         z = __dsub_rn( src( sj, 2 ), tz );
+            double P[M];
+            basis_eval<M>( x, y, z, P );
+            double const dist =
+                __dsqrt_rn( __dadd_rn( __dadd_rn( __dmul_rn( x, x ), __dmul_rn( y, y ) ), __dmul_rn( z, z ) ) );
+            double const phi = rbf_eval<double>( rbf, dist / radius );
+            double acc = 0.0;
+#pragma unroll
+            for ( int a = 0; a < M; ++a )
+                acc = fma( row0[a], P[a], acc );
+            coeff[b + j] = acc * phi;
+        }
+    }
+    // warp totals -> one atomic each
+    unsigned long long it64 = iters, dr64 = dropped;
+    for ( int o = 16; o; o >>= 1 )
+    {
+        it64 += __shfl_xor_sync( FULL, it64, o );
+        dr64 += __shfl_xor_sync( FULL, dr64, o );
+    }
+    if ( threadIdx.x == 0 )
+    {
+        if ( it64 )
+            atomicAdd( rot_count, it64 );
+        if ( dr64 )
+            atomicAdd( under_count, dr64 );
+    }
+}
+
+// General-n SVDFunctor (one thread per matrix, E/U/V in a global work area):
+// the batched pseudo-inverse kernel of DTK_DetailsSVDImpl.hpp:197-302.
+__global__ void k_svd_general( int n, int64_t count, double const *a, double *pinv,
+                               double *work, unsigned long long *under, unsigned *status )
+{
+    int64_t const mid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( mid >= count )
+        return;
+    int64_t const nn = (int64_t)n * n;
+    double *E = work + 3 * nn * mid, *U = E + nn, *V = U + nn;
+    double const *A = a + nn * mid;
+    for ( int64_t i = 0; i < nn; ++i )
+        E[i] = A[i];
+    for ( int i = 0; i < n; ++i )
+        for ( int j = 0; j < n; ++j )
+        {
+            U[i * n + j] = i == j ? 1.0 : 0.0;
+            V[i * n + j] = i == j ? 1.0 : 0.0;
+        }
+    double const tol = DBL_EPSILON;
+    unsigned long long const cap = 200ull * nn + 2000ull;
+    unsigned long long it = 0;
+    while ( true )
+    {
+        double acc = 0.0;
+        long long best = -1;
+        int p = 0, q = 1;
+        for ( int i = 0; i < n; ++i )
+            for ( int j = 0; j < n; ++j )
+            {
+                if ( i == j )
+                    continue;
+                double const x = E[i * n + j];
+                acc = fma( x, x, acc );
+                long long const ab = abs_bits( x );
+                if ( ab > best )
+                {
+                    best = ab;
+                    p = i;
+                    q = j;
+                }
+            }
+        if ( !( sqrt( acc ) > tol ) || n < 2 )
+            break;
+        if ( ++it > cap )
+        {
+            atomicOr( status, DEV_TIMEOUT );
+            break;
+        }
+        if ( p > q )
+        {
+            int const t = p;
+            p = q;
+            q = t;
+        }
+        double cl, sl, cr, sr;
+        svd_2x2( E[p * n + p], E[p * n + q], E[q * n + p], E[q * n + q], cl, sl, cr, sr );
+        for ( int j = 0; j < n; ++j )
+        {
+            double const x = E[p * n + j], y = E[q * n + j];
+            E[p * n + j] = cl * x - sl * y;
+            E[q * n + j] = sl * x + cl * y;
+        }
+        for ( int j = 0; j < n; ++j )
+        {
+            double const x = E[j * n + p], y = E[j * n + q];
+            E[j * n + p] = cr * x - sr * y;
+            E[j * n + q] = sr * x + cr * y;
+        }
+        for ( int j = 0; j < n; ++j )
+        {
+            double const x = U[j * n + p], y = U[j * n + q];
+            U[j * n + p] = cl * x - sl * y;
+            U[j * n + q] = sl * x + cl * y;
+        }
+        for ( int j = 0; j < n; ++j )
+        {
+            double const x = V[p * n + j], y = V[q * n + j];
+            V[p * n + j] = cr * x - sr * y;
+            V[q * n + j] = sr * x + cr * y;
+        }
+    }
+    int dropped = 0;
+    double *out = pinv + nn * mid;
+    for ( int i = 0; i < n; ++i )
+        for ( int j = 0; j < n; ++j )
+        {
+            double v = 0.0;
+            for ( int k = 0; k < n; ++k )
+            {
+                double const ek = E[k * n + k];
+                if ( fabs( ek ) >= tol )
+                    v += V[k * n + i] * U[j * n + k] / ek;
+                else
+                    dropped = 1;
+            }
+            out[i * n + j] = v;
+        }
+    if ( dropped )
+        atomicAdd( under, 1ull );
+}
+
+template <int M>
+void launch_fp64( SetupArgs const &a, cudaStream_t s )
+{
+    size_t const smem = ( 2 * M * M + M ) * SETUP_BLOCK * sizeof( double );
+    static bool configured = false;
+    if ( !configured )
+    {
+        DTK_CUDA_OR_THROW( cudaFuncSetAttribute( k_setup_fp64<M>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem ) );
+        configured = true;
+    }
+    unsigned const blocks = (unsigned)( ( a.n_tgt + SETUP_BLOCK - 1 ) / SETUP_BLOCK );
+    k_setup_fp64<M><<<blocks, SETUP_BLOCK, smem, s>>>( a.src, a.tgt, a.offset, a.idx, a.order,
+                                                        a.n_tgt, a.rbf, a.rows_sorted, a.coeff64,
+                                                        a.underdetermined, a.rotations, a.status );
+    check_launch( "k_setup_fp64" );
+}
+
+} // namespace
+
+void setup_fp64( SetupArgs const &a, cudaStream_t s )
+{
+    if ( a.n_tgt == 0 )
+        return;
+    switch ( a.basis )
+    {
+    case DTK_CONSTANT3:
+        launch_fp64<1>( a, s );
+        break;
+    case DTK_LINEAR3:
+        launch_fp64<4>( a, s );
+        break;
+    default:
+        launch_fp64<10>( a, s );
+        break;
+    }
+}
+
+void svd_pinv_batched( int n, int64_t count, double const *a, double *pinv,
+                       unsigned long long *underdetermined, unsigned *status, cudaStream_t s )
+{
+    if ( count == 0 )
+        return;
+    DeviceBuffer<double> work( 3 * (size_t)n * n * count, s );
+    unsigned const blocks = (unsigned)( ( count + 63 ) / 64 );
+    k_svd_general<<<blocks, 64, 0, s>>>( n, count, a, pinv, work.get(), underdetermined, status );
+    check_launch( "k_svd_general" );
+}
+
+} // namespace dtk

@@ -1,0 +1,293 @@
+"""Host-side mirror of DataTransferKit's MLS operator API over the C ABI.
+
+Mirrors (paths inside the DataTransferKit project):
+  PointCloudOperator<DeviceType>            packages/Meshfree/src/DTK_PointCloudOperator.hpp:24-37
+  MovingLeastSquaresOperator<Device, RBF, Basis>
+        constructor (setup) / apply          DTK_MovingLeastSquaresOperator_decl.hpp:36-63
+  Wendland<k>, Wu<k>, Buhmann<k>             DTK_CompactlySupportedRadialBasisFunctions.hpp:42-147
+  MultivariatePolynomialBasis<Basis, DIM>    DTK_MultivariatePolynomialBasis.hpp:178-238
+
+Arrays are CUDA tensors (device memory, the analogue of Kokkos Views in a
+CUDA memory space): points float64 of shape (n, 3) with any strides
+(LayoutRight or LayoutLeft), values float64 of shape (n,).  Precondition
+failures raise ``InvalidArgument`` (DTK_REQUIRE -> DataTransferKitException).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _capi
+from ._capi import Options, check, lib
+
+
+# ---------------------------------------------------------------------------
+# Template-parameter types
+# ---------------------------------------------------------------------------
+class _RBF:
+    family = ""
+    orders = ()
+    _ids = {}
+
+    def __init__(self, k: int):
+        if k not in self.orders:
+            raise ValueError(f"{type(self).__name__}<{k}> does not exist (orders {self.orders})")
+        self.k = k
+        self.id = self._ids[k]
+
+    def __repr__(self):
+        return f"{type(self).__name__}<{self.k}>"
+
+    def __eq__(self, other):
+        return isinstance(other, _RBF) and other.id == self.id
+
+    def __hash__(self):
+        return hash(self.id)
+
+
+class Wendland(_RBF):
+    orders = (0, 2, 4, 6)
+    _ids = {0: 0, 2: 1, 4: 2, 6: 3}
+
+
+class Wu(_RBF):
+    orders = (2, 4)
+    _ids = {2: 4, 4: 5}
+
+
+class Buhmann(_RBF):
+    orders = (2, 3, 4)
+    _ids = {2: 6, 3: 7, 4: 8}
+
+
+class Constant:
+    pass
+
+
+class Linear:
+    pass
+
+
+class Quadratic:
+    pass
+
+
+class MultivariatePolynomialBasis:
+    """Basis<Constant|Linear|Quadratic, DIM>; the MLS operator needs DIM = 3."""
+
+    _sizes = {(Constant, 3): 1, (Linear, 3): 4, (Quadratic, 3): 10,
+              (Constant, 2): 1, (Linear, 2): 3, (Quadratic, 2): 6}
+    _ids = {Constant: 0, Linear: 1, Quadratic: 2}
+
+    def __init__(self, kind, dim: int = 3):
+        if (kind, dim) not in self._sizes:
+            raise ValueError("unknown polynomial basis")
+        self.kind = kind
+        self.dim = dim
+        self.size = self._sizes[(kind, dim)]
+        self.id = self._ids[kind]
+
+    def __repr__(self):
+        return f"MultivariatePolynomialBasis<{self.kind.__name__}, {self.dim}>"
+
+
+FP64 = 0
+MIXED = 1
+_PRECISIONS = {"fp64": FP64, "mixed": MIXED, FP64: FP64, MIXED: MIXED}
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, torch.cuda.Stream):
+        return stream.cuda_stream
+    return int(stream)
+
+
+def _check_points(p: torch.Tensor, what: str) -> torch.Tensor:
+    if not isinstance(p, torch.Tensor) or not p.is_cuda:
+        raise _capi.InvalidArgument(1, f"{what} must be a CUDA tensor")
+    if p.dtype != torch.float64:
+        raise _capi.InvalidArgument(1, f"{what} must be float64 (Coordinate = double)")
+    if p.dim() != 2:
+        raise _capi.InvalidArgument(1, f"{what} must be rank 2")
+    return p
+
+
+def _comm_size(comm) -> int:
+    if comm is None:
+        return 1
+    for attr in ("Get_size", "size"):
+        f = getattr(comm, attr, None)
+        if callable(f):
+            return int(f())
+    if isinstance(comm, int):
+        return comm
+    return 1
+
+
+class PointCloudOperator:
+    """Base class of the meshfree operators (virtual apply)."""
+
+    def apply(self, source_values: torch.Tensor, target_values: torch.Tensor) -> None:
+        raise NotImplementedError
+
+
+class MovingLeastSquaresOperator(PointCloudOperator):
+    """Moving least squares transfer between point clouds (one rank).
+
+    ``MovingLeastSquaresOperator(comm, source_points, target_points,
+    rbf=Wendland(0), basis=MultivariatePolynomialBasis(Linear, 3))`` builds the
+    operator (search, weights, moments, pseudo-inverse, coefficients) on the
+    GPU; ``apply(source_values, target_values)`` writes every target value.
+    Extensions beyond the reference: ``k`` (neighbours, default the basis
+    size as in the reference), ``radius`` (radius search instead of kNN) and
+    ``precision`` ("fp64" = the reference algorithm, "mixed").
+    """
+
+    def __init__(self, comm, source_points, target_points, rbf=None, basis=None, *,
+                 k: int | None = None, radius: float | None = None, precision="fp64",
+                 stream=None):
+        self.polynomial_basis = basis or MultivariatePolynomialBasis(Linear, 3)
+        self.radial_basis_function = rbf or Wendland(0)
+        src = _check_points(source_points, "source_points")
+        tgt = _check_points(target_points, "target_points")
+        # DTK_REQUIRE(source dim == target dim), DTK_REQUIRE(dim == 3):
+        # DTK_MovingLeastSquaresOperator_def.hpp:106-109
+        if src.shape[1] != tgt.shape[1]:
+            raise _capi.InvalidArgument(1, "source_points.extent(1) == target_points.extent(1)")
+        if src.shape[1] != 3 or self.polynomial_basis.dim != 3:
+            raise _capi.InvalidArgument(1, "source_points.extent(1) == 3")
+        o = Options()
+        lib().dtk_mls_default_options(C.byref(o))
+        o.rbf = self.radial_basis_function.id
+        o.basis = self.polynomial_basis.id
+        o.k = 0 if k is None else int(k)
+        o.radius = 0.0 if radius is None else float(radius)
+        o.precision = _PRECISIONS[precision]
+        o.comm_size = _comm_size(comm)
+        self.options = o
+        self._h = C.c_void_p()
+        self._stream = stream
+        check(lib().dtk_mls_create(C.byref(o), src.data_ptr(), src.shape[0], src.stride(0),
+                                   src.stride(1), tgt.data_ptr(), tgt.shape[0], tgt.stride(0),
+                                   tgt.stride(1), _stream(stream), C.byref(self._h)))
+        self.n_source_points = int(src.shape[0])
+        self.n_target_points = int(tgt.shape[0])
+
+    # -- reference API ------------------------------------------------------
+    def apply(self, source_values: torch.Tensor, target_values: torch.Tensor, stream=None) -> None:
+        for t, what in ((source_values, "source_values"), (target_values, "target_values")):
+            if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float64:
+                raise _capi.InvalidArgument(1, f"{what} must be a float64 CUDA tensor")
+            if t.dim() != 1 or (t.numel() > 1 and t.stride(0) != 1):
+                raise _capi.InvalidArgument(1, f"{what} must be rank 1 and contiguous")
+        check(lib().dtk_mls_apply(self._h, source_values.data_ptr(), source_values.shape[0],
+                                  target_values.data_ptr(), target_values.shape[0],
+                                  _stream(stream if stream is not None else self._stream)))
+
+    # -- extensions ------------------------------------------------------------
+    def apply_adjoint(self, cot: torch.Tensor, source_values: torch.Tensor | None = None,
+                      coords: bool = False, stream=None):
+        """(dL/d source_values, dL/d source coordinates or None) for dL/d target = cot."""
+        gv = torch.empty(self.n_source_points, dtype=torch.float64, device=cot.device)
+        gc = torch.empty((self.n_source_points, 3), dtype=torch.float64, device=cot.device) if coords else None
+        check(lib().dtk_mls_apply_adjoint(
+            self._h, cot.data_ptr(), cot.shape[0],
+            source_values.data_ptr() if source_values is not None else None,
+            gv.data_ptr(), gc.data_ptr() if gc is not None else None,
+            _stream(stream if stream is not None else self._stream)))
+        return gv, gc
+
+    def csr(self):
+        """(offset, indices, coefficients) device tensors (copies)."""
+        off, idx, coeff = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        nnz, f32 = C.c_int64(), C.c_int32()
+        check(lib().dtk_mls_get_csr(self._h, C.byref(off), C.byref(idx), C.byref(coeff),
+                                    C.byref(nnz), C.byref(f32)))
+        torch.cuda.synchronize()
+        n = nnz.value
+        o = _from_device(off.value, self.n_target_points + 1, torch.int32)
+        i = _from_device(idx.value, n, torch.int32)
+        c = _from_device(coeff.value, n, torch.float32 if f32.value else torch.float64)
+        return o, i, c
+
+    @property
+    def nnz(self) -> int:
+        n = C.c_int64()
+        check(lib().dtk_mls_get_sizes(self._h, None, None, C.byref(n)))
+        return n.value
+
+    @property
+    def underdetermined(self) -> int:
+        n = C.c_int64()
+        check(lib().dtk_mls_underdetermined_count(self._h, C.byref(n)))
+        return n.value
+
+    @property
+    def rotations(self) -> int:
+        n = C.c_int64()
+        check(lib().dtk_mls_get_rotation_count(self._h, C.byref(n)))
+        return n.value
+
+    @property
+    def stage_times_ms(self):
+        a, b = C.c_float(), C.c_float()
+        check(lib().dtk_mls_get_stage_times(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().dtk_mls_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _DeviceArray:
+    """Exposes a raw device pointer through __cuda_array_interface__."""
+
+    def __init__(self, ptr: int, n: int, typestr: str):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr,
+                                         "data": (ptr, True), "version": 3, "strides": None}
+
+
+_TYPESTR = {torch.int32: "<i4", torch.float32: "<f4", torch.float64: "<f8"}
+
+
+def _from_device(ptr: int, n: int, dtype) -> torch.Tensor:
+    """Copy of n elements at a device pointer owned by the library."""
+    if n == 0 or not ptr:
+        return torch.empty(0, dtype=dtype, device="cuda")
+    view = torch.as_tensor(_DeviceArray(ptr, n, _TYPESTR[dtype]), device="cuda")
+    return view.clone()
+
+
+def knn_search(source_points: torch.Tensor, target_points: torch.Tensor, k: int, stream=None):
+    """(offset, indices) of the k nearest sources per target by (d2, index)."""
+    src = _check_points(source_points, "source_points")
+    tgt = _check_points(target_points, "target_points")
+    row = min(int(k), src.shape[0])
+    offset = torch.empty(tgt.shape[0] + 1, dtype=torch.int32, device=tgt.device)
+    idx = torch.empty(max(1, tgt.shape[0] * row), dtype=torch.int32, device=tgt.device)
+    check(lib().dtk_knn_search(src.data_ptr(), src.shape[0], src.stride(0), src.stride(1),
+                               tgt.data_ptr(), tgt.shape[0], tgt.stride(0), tgt.stride(1),
+                               int(k), offset.data_ptr(), idx.data_ptr(), _stream(stream)))
+    return offset, idx[: tgt.shape[0] * row]
+
+
+def svd_pinv(matrices: torch.Tensor, stream=None):
+    """Batched DTK Jacobi pseudo-inverse of (count, n, n) float64 CUDA matrices."""
+    a = matrices.contiguous()
+    if a.dtype != torch.float64 or not a.is_cuda or a.dim() != 3 or a.shape[1] != a.shape[2]:
+        raise _capi.InvalidArgument(1, "matrices must be a (count, n, n) float64 CUDA tensor")
+    out = torch.empty_like(a)
+    under = C.c_int64()
+    check(lib().dtk_svd_pinv(a.shape[1], a.shape[0], a.data_ptr(), out.data_ptr(),
+                             C.byref(under), _stream(stream)))
+    return out, under.value

@@ -1,0 +1,198 @@
+/*
+ * dtk_gb300.h -- C ABI of the GB300-native moving-least-squares (MLS)
+ * point-cloud transfer of DataTransferKit, on one rank.
+ *
+ * Plain C: pointers, sizes and POD structs only.  Every function returns a
+ * dtk_status; none throws.  All data pointers are DEVICE pointers unless
+ * stated otherwise; the caller owns every input and output buffer, the
+ * handle owns the operator's CSR product (offset, indices, coefficients).
+ * Calls on one handle are ordered on the stream they are given and are not
+ * re-entrant.  `stream` is a cudaStream_t (NULL = legacy default stream).
+ *
+ * Reference interface replaced (paths inside the DataTransferKit project):
+ *   DataTransferKit::MovingLeastSquaresOperator<DeviceType, RBF, Basis>
+ *     packages/Meshfree/src/DTK_MovingLeastSquaresOperator_decl.hpp:36-63
+ *   its constructor (setup: search, weights, moments, pseudo-inverse,
+ *   coefficients)  DTK_MovingLeastSquaresOperator_def.hpp:91-186
+ *   apply(source_values, target_values)
+ *                   DTK_MovingLeastSquaresOperator_def.hpp:188-208
+ */
+#ifndef DTK_GB300_H
+#define DTK_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct dtk_mls_s *dtk_mls_handle;
+typedef struct CUstream_st *dtk_stream_t; /* == cudaStream_t */
+
+typedef enum
+{
+    DTK_OK = 0,
+    DTK_ERR_INVALID_ARG = 1, /* a DTK_REQUIRE precondition failed */
+    DTK_ERR_UNSUPPORTED = 2, /* e.g. comm_size > 1, dimension != 3 */
+    DTK_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+    DTK_ERR_OOM = 4,         /* device allocation failed */
+    DTK_ERR_TIMEOUT = 5,     /* a bounded device loop hit its cap */
+    DTK_ERR_INTERNAL = 6
+} dtk_status;
+
+/* Compactly supported RBFs: DTK_CompactlySupportedRadialBasisFunctions.hpp:42-147 */
+typedef enum
+{
+    DTK_WENDLAND0 = 0,
+    DTK_WENDLAND2 = 1,
+    DTK_WENDLAND4 = 2,
+    DTK_WENDLAND6 = 3,
+    DTK_WU2 = 4,
+    DTK_WU4 = 5,
+    DTK_BUHMANN2 = 6,
+    DTK_BUHMANN3 = 7,
+    DTK_BUHMANN4 = 8
+} dtk_rbf;
+
+/* MultivariatePolynomialBasis<., 3>: DTK_MultivariatePolynomialBasis.hpp:249-276 */
+typedef enum
+{
+    DTK_CONSTANT3 = 0, /* m = 1  */
+    DTK_LINEAR3 = 1,   /* m = 4  */
+    DTK_QUADRATIC3 = 2 /* m = 10 */
+} dtk_basis;
+
+typedef enum
+{
+    /* The reference algorithm in FP64: unscaled relative coordinates,
+     * two-sided largest-pivot Jacobi with DTK's absolute DBL_EPSILON stop and
+     * truncation (DTK_DetailsSVDImpl.hpp:197-302). */
+    DTK_FP64 = 0,
+    /* Centring and scaling by the support radius, FP32 basis / weights /
+     * moment assembly and FP32 coefficients for apply; the Jacobi rotations
+     * and the pseudo-inverse truncation in FP64. */
+    DTK_MIXED = 1
+} dtk_precision;
+
+typedef struct
+{
+    int32_t rbf;       /* dtk_rbf; reference default Wendland<0> */
+    int32_t basis;     /* dtk_basis; reference default Linear3 */
+    int32_t k;         /* neighbours per target; 0 = basis size (reference) */
+    int32_t precision; /* dtk_precision */
+    double radius;     /* > 0: radius search instead of kNN (extension) */
+    int32_t comm_size; /* ranks of the communicator; must be 1 */
+    int32_t reserved;
+} dtk_mls_options;
+
+/* Options of MovingLeastSquaresOperator<Device> with its template defaults:
+ * Wendland<0>, Linear3, k = basis size, FP64, comm_size 1. */
+void dtk_mls_default_options(dtk_mls_options *opts);
+
+/* Setup.  Replaces the constructor, DTK_MovingLeastSquaresOperator_def.hpp:91-186.
+ * src / tgt: n x 3 coordinates, element (i, d) at ptr[i*pt_stride + d*dim_stride]
+ * (doubles; LayoutRight: (3, 1); LayoutLeft: (1, n)).  Preconditions as the
+ * reference: dimension 3 (implied), n_src > 0 (DTK_CHECK(!tree.empty())).
+ * Returns when the product is complete (the reference fences). */
+dtk_status dtk_mls_create(const dtk_mls_options *opts, const double *src,
+                          int64_t n_src, int64_t src_pt_stride,
+                          int64_t src_dim_stride, const double *tgt,
+                          int64_t n_tgt, int64_t tgt_pt_stride,
+                          int64_t tgt_dim_stride, dtk_stream_t stream,
+                          dtk_mls_handle *out);
+
+/* apply: target_values[i] = sum_j coeff_j * source_values[idx_j].
+ * Replaces MovingLeastSquaresOperator::apply, DTK_MovingLeastSquaresOperator_def.hpp:188-208,
+ * with its preconditions n_source_values == n_src and n_target_values ==
+ * n_tgt (DTK_REQUIRE at :196-197).  Writes every target value; enqueued on
+ * `stream`, asynchronous. */
+dtk_status dtk_mls_apply(dtk_mls_handle h, const double *source_values,
+                         int64_t n_source_values, double *target_values,
+                         int64_t n_target_values, dtk_stream_t stream);
+
+/* Adjoint of apply and of the setup (extension; the reference has none).
+ * grad_values[s] = sum over entries j with idx_j == s of coeff_j * cot[row(j)]
+ * (deterministic transpose gather, overwrites n_src values).  When
+ * grad_coords is non-NULL it receives dL/d(source coordinates) as an n_src x 3
+ * row-major array (overwritten), through the weights, the support radius and
+ * the pseudo-inverse, recomputed per target with connectivity fixed; that
+ * part needs `source_values` (the field the forward apply used). */
+dtk_status dtk_mls_apply_adjoint(dtk_mls_handle h, const double *cot,
+                                 int64_t n_cot, const double *source_values,
+                                 double *grad_values, double *grad_coords,
+                                 dtk_stream_t stream);
+
+/* Read-only view of the CSR product for parity checks.  coeff points to
+ * doubles (FP64 form) or floats (mixed form, *coeff_is_fp32 = 1). */
+dtk_status dtk_mls_get_csr(dtk_mls_handle h, const int32_t **offset,
+                           const int32_t **indices, const void **coeff,
+                           int64_t *nnz, int32_t *coeff_is_fp32);
+
+/* Sizes of the operator. */
+dtk_status dtk_mls_get_sizes(dtk_mls_handle h, int64_t *n_src, int64_t *n_tgt,
+                             int64_t *nnz);
+
+/* Number of targets whose moment matrix was rank-deficient (the value the
+ * reference returns from invertMoments, DTK_DetailsMovingLeastSquaresOperatorImpl.hpp:263-291). */
+dtk_status dtk_mls_underdetermined_count(dtk_mls_handle h, int64_t *count);
+
+/* Device-side timings of the last create (milliseconds): search, setup. */
+dtk_status dtk_mls_get_stage_times(dtk_mls_handle h, float *search_ms,
+                                   float *setup_ms);
+
+/* Number of Jacobi rotations the last create performed (FP64 flop counts). */
+dtk_status dtk_mls_get_rotation_count(dtk_mls_handle h, int64_t *rotations);
+
+dtk_status dtk_mls_destroy(dtk_mls_handle h);
+
+/* ---- search only (the ArborX query the constructor runs,
+ *      DTK_MovingLeastSquaresOperator_def.hpp:114-129) ----
+ * kNN: row i = the min(k, n_src) nearest sources by (d2, index), ascending,
+ * d2 = (dx*dx + dy*dy) + dz*dz in FP64 with separately rounded operations.
+ * offset must hold n_tgt+1 and indices n_tgt*min(k, n_src) entries. */
+dtk_status dtk_knn_search(const double *src, int64_t n_src,
+                          int64_t src_pt_stride, int64_t src_dim_stride,
+                          const double *tgt, int64_t n_tgt,
+                          int64_t tgt_pt_stride, int64_t tgt_dim_stride,
+                          int32_t k, int32_t *offset, int32_t *indices,
+                          dtk_stream_t stream);
+
+/* ---- batched pseudo-inverse (the SVDFunctor kernel, DTK_DetailsSVDImpl.hpp:39-309) ----
+ * count row-major n x n matrices -> their pseudo-inverses with DTK's
+ * absolute DBL_EPSILON tolerances; *underdetermined (host) receives the
+ * number of matrices with a dropped singular value.  n <= 64. */
+dtk_status dtk_svd_pinv(int32_t n, int64_t count, const double *a,
+                        double *pinv, int64_t *underdetermined,
+                        dtk_stream_t stream);
+
+/* ---- batched uneven transfers (extension) ----
+ * n_problems independent operators in one schedule.  Problem p uses
+ * sources [src_offsets[p], src_offsets[p+1]) and targets
+ * [tgt_offsets[p], tgt_offsets[p+1]) of the packed row-major n x 3 arrays,
+ * and options opts[p] (HOST arrays: src_offsets, tgt_offsets, opts).
+ * The batch's CSR product is one global CSR over all targets with global
+ * source indices. */
+typedef struct dtk_mls_batch_s *dtk_mls_batch_handle;
+dtk_status dtk_mls_batch_create(int32_t n_problems, const dtk_mls_options *opts,
+                                const int64_t *src_offsets, const double *src,
+                                const int64_t *tgt_offsets, const double *tgt,
+                                dtk_stream_t stream, dtk_mls_batch_handle *out);
+/* All problems' apply in one launch: values/targets are packed like the
+ * points.  When use_graph != 0 the launch sequence is captured once into a
+ * CUDA graph and replayed. */
+dtk_status dtk_mls_batch_apply(dtk_mls_batch_handle h, const double *src_values,
+                               double *tgt_values, int32_t use_graph,
+                               dtk_stream_t stream);
+dtk_status dtk_mls_batch_get_csr(dtk_mls_batch_handle h, const int32_t **offset,
+                                 const int32_t **indices, const void **coeff,
+                                 int64_t *nnz, int32_t *coeff_is_fp32);
+dtk_status dtk_mls_batch_destroy(dtk_mls_batch_handle h);
+
+/* Last error message of the calling host thread (never NULL). */
+const char *dtk_last_error(void);
+const char *dtk_status_string(dtk_status s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

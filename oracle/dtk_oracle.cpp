@@ -1,0 +1,979 @@
+// CPU oracle for the MLS transfer path -- TEST INFRASTRUCTURE ONLY.
+//
+// This file is the checker for the GPU product and the timed CPU baseline of
+// the benchmark; the product never links or loads it.  It restates the
+// reference algorithm in FP64 with OpenMP over targets (the reference's
+// Kokkos RangePolicy(0, n_targets) structure).  Built with -ffp-contract=off
+// so that every product and sum is rounded separately on every host.
+//
+// Reference files restated (paths inside the DataTransferKit project):
+//   packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:91-208
+//   packages/Meshfree/src/DTK_DetailsMovingLeastSquaresOperatorImpl.hpp:49-336
+//   packages/Meshfree/src/DTK_DetailsSVDImpl.hpp:29-302
+//   packages/Meshfree/src/DTK_CompactlySupportedRadialBasisFunctions.hpp:22-147
+//   packages/Meshfree/src/DTK_MultivariatePolynomialBasis.hpp:249-304
+#include "dtk_oracle.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <utility>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace
+{
+
+// ---------------------------------------------------------------------------
+// Radial basis functions, evaluated as rbf(x) on the already-scaled argument
+// x = distance / radius.  Same factor order as
+// DTK_CompactlySupportedRadialBasisFunctions.hpp:45-147 (left-to-right
+// products), so results round identically.
+// ---------------------------------------------------------------------------
+enum
+{
+    WENDLAND0 = 0,
+    WENDLAND2,
+    WENDLAND4,
+    WENDLAND6,
+    WU2,
+    WU4,
+    BUHMANN2,
+    BUHMANN3,
+    BUHMANN4,
+    N_RBF
+};
+
+inline double rbf_eval( int rbf, double x )
+{
+    double const y = 1.0 - x;
+    switch ( rbf )
+    {
+    case WENDLAND0:
+        return y * y;
+    case WENDLAND2:
+        return y * y * y * y * ( 4.0 * x + 1.0 );
+    case WENDLAND4:
+        return y * y * y * y * y * y * ( 35.0 * x * x + 18.0 * x + 3.0 );
+    case WENDLAND6:
+        return y * y * y * y * y * y * y * y *
+               ( 32.0 * x * x * x + 25.0 * x * x + 8.0 * x + 1.0 );
+    case WU2:
+        return y * y * y * y * ( 3.0 * x * x * x + 12.0 * x * x + 16.0 * x + 4.0 );
+    case WU4:
+        return y * y * y * y * y * y *
+               ( 5.0 * x * x * x * x * x + 30.0 * x * x * x * x +
+                 72.0 * x * x * x + 82.0 * x * x + 36.0 * x + 6.0 );
+    case BUHMANN2:
+        return 2.0 * x * x * x * x * std::log( x ) - 7.0 / 2.0 * x * x * x * x +
+               16 / 3.0 * x * x * x - 2 * x * x + 1.0 / 6.0;
+    case BUHMANN3:
+        return x * x * x * x * x * x * x * x - 84.0 / 5.0 * x * x * x * x * x * x +
+               1024.0 / 5.0 * x * x * x * x * std::sqrt( x ) -
+               378.0 * x * x * x * x + 1024.0 / 5.0 * x * x * x * std::sqrt( x ) -
+               84.0 / 5.0 * x * x + 1.0;
+    case BUHMANN4:
+        return 99.0 / 35.0 * x * x * x * x * x * x * x * x -
+               132.0 * x * x * x * x * x * x +
+               9216.0 / 35.0 * x * x * x * x * x * std::sqrt( x ) -
+               11264.0 / 35.0 * x * x * x * x * std::sqrt( x ) +
+               198.0 * x * x * x * x - 396.0 / 5.0 * x * x + 1.0;
+    }
+    return std::numeric_limits<double>::quiet_NaN();
+}
+
+// d rbf / dx, derived by hand from the formulas above (not in the reference,
+// which has no adjoint).
+inline double rbf_deriv( int rbf, double x )
+{
+    double const y = 1.0 - x;
+    switch ( rbf )
+    {
+    case WENDLAND0:
+        return -2.0 * y;
+    case WENDLAND2:
+        return -20.0 * x * y * y * y;
+    case WENDLAND4:
+        return -56.0 * x * ( 5.0 * x + 1.0 ) * y * y * y * y * y;
+    case WENDLAND6:
+        return -22.0 * x * ( 16.0 * x * x + 7.0 * x + 1.0 ) * y * y * y * y * y *
+               y * y;
+    case WU2:
+        return -7.0 * x * ( 3.0 * x * x + 9.0 * x + 8.0 ) * y * y * y;
+    case WU4:
+        return -11.0 * x *
+               ( 5.0 * x * x * x * x + 25.0 * x * x * x + 48.0 * x * x +
+                 40.0 * x + 8.0 ) *
+               y * y * y * y * y;
+    case BUHMANN2:
+        return x > 0.0 ? 8.0 * x * x * x * std::log( x ) - 12.0 * x * x * x +
+                             16.0 * x * x - 4.0 * x
+                       : 0.0;
+    case BUHMANN3:
+    {
+        double const r = std::sqrt( x );
+        return 8.0 * std::pow( x, 7 ) - 504.0 / 5.0 * std::pow( x, 5 ) +
+               4608.0 / 5.0 * x * x * x * r - 1512.0 * x * x * x +
+               3584.0 / 5.0 * x * x * r - 168.0 / 5.0 * x;
+    }
+    case BUHMANN4:
+    {
+        double const r = std::sqrt( x );
+        return 792.0 / 35.0 * std::pow( x, 7 ) - 792.0 * std::pow( x, 5 ) +
+               50688.0 / 35.0 * x * x * x * x * r -
+               50688.0 / 35.0 * x * x * x * r + 792.0 * x * x * x -
+               792.0 / 5.0 * x;
+    }
+    }
+    return std::numeric_limits<double>::quiet_NaN();
+}
+
+// ---------------------------------------------------------------------------
+// Polynomial bases in 3-D: DTK_MultivariatePolynomialBasis.hpp:249-276.
+// basis id 0 = Constant (m=1), 1 = Linear (m=4), 2 = Quadratic (m=10).
+// ---------------------------------------------------------------------------
+inline int basis_size( int basis )
+{
+    return basis == 0 ? 1 : basis == 1 ? 4 : basis == 2 ? 10 : -1;
+}
+
+inline void basis_eval( int basis, double const *p, double *out )
+{
+    out[0] = 1.;
+    if ( basis >= 1 )
+    {
+        out[1] = p[0];
+        out[2] = p[1];
+        out[3] = p[2];
+    }
+    if ( basis == 2 )
+    {
+        out[4] = p[0] * p[0];
+        out[5] = p[0] * p[1];
+        out[6] = p[0] * p[2];
+        out[7] = p[1] * p[1];
+        out[8] = p[1] * p[2];
+        out[9] = p[2] * p[2];
+    }
+}
+
+// Jacobian of the basis: jac[c*3 + d] = d basis_c / d p_d.
+inline void basis_jacobian( int basis, double const *p, double *jac )
+{
+    int const m = basis_size( basis );
+    for ( int i = 0; i < 3 * m; ++i )
+        jac[i] = 0.0;
+    if ( basis >= 1 )
+    {
+        jac[1 * 3 + 0] = 1.0;
+        jac[2 * 3 + 1] = 1.0;
+        jac[3 * 3 + 2] = 1.0;
+    }
+    if ( basis == 2 )
+    {
+        jac[4 * 3 + 0] = 2.0 * p[0];
+        jac[5 * 3 + 0] = p[1];
+        jac[5 * 3 + 1] = p[0];
+        jac[6 * 3 + 0] = p[2];
+        jac[6 * 3 + 2] = p[0];
+        jac[7 * 3 + 1] = 2.0 * p[1];
+        jac[8 * 3 + 1] = p[2];
+        jac[8 * 3 + 2] = p[1];
+        jac[9 * 3 + 2] = 2.0 * p[2];
+    }
+}
+
+// Squared distance with the contract's association; -ffp-contract=off keeps
+// the products and sums separately rounded.
+inline double dist2( double const *s, double const *t )
+{
+    double const dx = s[0] - t[0];
+    double const dy = s[1] - t[1];
+    double const dz = s[2] - t[2];
+    return ( dx * dx + dy * dy ) + dz * dz;
+}
+
+// ---------------------------------------------------------------------------
+// Two-sided Jacobi pseudo-inverse, restating DTK_DetailsSVDImpl.hpp:65-302:
+// largest off-diagonal pivot, p<q swap, explicit 2x2 SVD via atan2, absolute
+// DBL_EPSILON stop on the off-diagonal Frobenius norm and on |E_kk|.
+// Matrices are n x n row-major in a per-thread workspace.
+// ---------------------------------------------------------------------------
+struct Jacobi
+{
+    int n = 0;
+    std::vector<double> E, U, V;
+
+    void resize( int n_ )
+    {
+        n = n_;
+        E.assign( n * n, 0. );
+        U.assign( n * n, 0. );
+        V.assign( n * n, 0. );
+    }
+
+    // M(i,:) and M(k,:) rotated: DTK_DetailsSVDImpl.hpp:65-77
+    void rot_rows( std::vector<double> &M, double c, double s, int i, int k )
+    {
+        for ( int j = 0; j < n; ++j )
+        {
+            double const a = M[i * n + j];
+            double const b = M[k * n + j];
+            M[i * n + j] = c * a - s * b;
+            M[k * n + j] = s * a + c * b;
+        }
+    }
+    // M(:,i) and M(:,k) rotated: DTK_DetailsSVDImpl.hpp:79-91
+    void rot_cols( std::vector<double> &M, double c, double s, int i, int k )
+    {
+        for ( int j = 0; j < n; ++j )
+        {
+            double const a = M[j * n + i];
+            double const b = M[j * n + k];
+            M[j * n + i] = c * a - s * b;
+            M[j * n + k] = s * a + c * b;
+        }
+    }
+
+    double offdiag_norm() const
+    {
+        double acc = 0.0;
+        for ( int i = 0; i < n; ++i )
+            for ( int j = 0; j < n; ++j )
+                acc += ( i != j ) ? E[i * n + j] * E[i * n + j] : 0;
+        return std::sqrt( acc );
+    }
+
+    // Left rotation (cl, sl) and right rotation (cr, sr) that diagonalise the
+    // 2x2 block [[a, b], [c, d]]: DTK_DetailsSVDImpl.hpp:119-162,260-263.
+    static void two_by_two( double a, double b, double c, double d, double &cl,
+                            double &sl, double &cr, double &sr )
+    {
+        // A A^T and A^T A, element order as mult_2x2 forms them.
+        double const p00 = a * a + b * b;
+        double const p01 = a * c + b * d;
+        double const p10 = c * a + d * b;
+        double const p11 = c * c + d * d;
+        double const q00 = a * a + c * c;
+        double const q01 = a * b + c * d;
+        double const q10 = b * a + d * c;
+        double const q11 = b * b + d * d;
+        double const phi = 0.5 * std::atan2( p01 + p10, p00 - p11 );
+        double const cphi = std::cos( phi );
+        double const sphi = std::sin( phi );
+        double const theta = 0.5 * std::atan2( q01 + q10, q00 - q11 );
+        double const cth = std::cos( theta );
+        double const sth = std::sin( theta );
+        // S = U^T A W with U = [[cphi,-sphi],[sphi,cphi]],
+        // W = [[cth,-sth],[sth,cth]]; only the diagonal signs are used.
+        double const aw00 = a * cth + b * sth;
+        double const aw01 = a * -sth + b * cth;
+        double const aw10 = c * cth + d * sth;
+        double const aw11 = c * -sth + d * cth;
+        double const s00 = cphi * aw00 + sphi * aw10;
+        double const s11 = -sphi * aw01 + cphi * aw11;
+        double const c0 = std::copysign( 1., s00 );
+        double const c1 = std::copysign( 1., s11 );
+        // V = W diag(c0, c1)
+        double const v00 = cth * c0 + -sth * 0.0;
+        double const v01 = cth * 0.0 + -sth * c1;
+        double const v10 = sth * c0 + cth * 0.0;
+        cl = cphi;
+        sl = -sphi;
+        cr = v00;
+        int const sg01 = ( v01 > 0 ) - ( v01 < 0 );
+        int const sg10 = ( v10 > 0 ) - ( v10 < 0 );
+        sr = ( sg01 == sg10 ) ? -v01 : v01;
+    }
+
+    // Runs the sweep loop on E (already loaded).  U = V = I on entry.
+    void run()
+    {
+        double const tol = DBL_EPSILON;
+        double norm = offdiag_norm();
+        // The reference loop has no cap; this one only guards the test suite
+        // against a pathological input and is never reached in practice.
+        long guard = 0;
+        while ( norm > tol && guard++ < 1000000 )
+        {
+            int p = -1, q = -1;
+            double best = -1;
+            for ( int i = 0; i < n; ++i )
+                for ( int j = 0; j < n; ++j )
+                    if ( i != j && std::abs( E[i * n + j] ) > best )
+                    {
+                        p = i;
+                        q = j;
+                        best = std::abs( E[i * n + j] );
+                    }
+            if ( p > q )
+                std::swap( p, q );
+            double cl, sl, cr, sr;
+            two_by_two( E[p * n + p], E[p * n + q], E[q * n + p], E[q * n + q],
+                        cl, sl, cr, sr );
+            rot_rows( E, cl, sl, p, q );
+            rot_cols( E, cr, sr, p, q );
+            rot_cols( U, cl, sl, p, q );
+            rot_rows( V, cr, sr, p, q );
+            norm = offdiag_norm();
+        }
+    }
+
+    void load( double const *a )
+    {
+        for ( int i = 0; i < n * n; ++i )
+            E[i] = a[i];
+        for ( int i = 0; i < n; ++i )
+            for ( int j = 0; j < n; ++j )
+            {
+                U[i * n + j] = ( i == j ? 1.0 : 0.0 );
+                V[i * n + j] = ( i == j ? 1.0 : 0.0 );
+            }
+    }
+
+    // pinv(i,j) = sum_k V(k,i) U(j,k) / E(k,k) over |E(k,k)| >= DBL_EPSILON.
+    // Returns 1 if some singular value was dropped.  rows < n computes only
+    // the leading rows (the MLS path needs row 0 only; same arithmetic).
+    int pinv_rows( double *out, int rows ) const
+    {
+        int dropped = 0;
+        for ( int i = 0; i < rows; ++i )
+            for ( int j = 0; j < n; ++j )
+            {
+                double value = 0;
+                for ( int k = 0; k < n; ++k )
+                {
+                    if ( std::abs( E[k * n + k] ) >= DBL_EPSILON )
+                        value += V[k * n + i] * U[j * n + k] / E[k * n + k];
+                    else
+                        dropped = 1;
+                }
+                out[i * n + j] = value;
+            }
+        return dropped;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Uniform grid index for exact kNN / radius search on the CPU.
+// ---------------------------------------------------------------------------
+struct Grid
+{
+    double lo[3], h[3], inv_h[3], slack;
+    int n[3];
+    std::vector<int64_t> start;
+    std::vector<int32_t> ids;
+    std::vector<double> xyz;
+
+    int cell_coord( double v, int d ) const
+    {
+        double f = std::floor( ( v - lo[d] ) * inv_h[d] );
+        if ( !( f >= 0. ) )
+            return 0;
+        if ( f > n[d] - 1 )
+            return n[d] - 1;
+        return (int)f;
+    }
+
+    void build( double const *src, int64_t n_src, double per_cell )
+    {
+        double hi[3];
+        for ( int d = 0; d < 3; ++d )
+        {
+            lo[d] = std::numeric_limits<double>::infinity();
+            hi[d] = -std::numeric_limits<double>::infinity();
+        }
+        for ( int64_t i = 0; i < n_src; ++i )
+            for ( int d = 0; d < 3; ++d )
+            {
+                lo[d] = std::min( lo[d], src[3 * i + d] );
+                hi[d] = std::max( hi[d], src[3 * i + d] );
+            }
+        double vol = 1.0, scale = 0.0;
+        int active = 0;
+        for ( int d = 0; d < 3; ++d )
+        {
+            double const e = hi[d] - lo[d];
+            scale = std::max( scale, std::abs( lo[d] ) + e );
+            if ( e > 0 )
+            {
+                vol *= e;
+                ++active;
+            }
+        }
+        double const cells = std::max( 1.0, (double)n_src / per_cell );
+        double const hc = active ? std::pow( vol / cells, 1.0 / active ) : 1.0;
+        int64_t total = 1;
+        for ( int d = 0; d < 3; ++d )
+        {
+            double const e = hi[d] - lo[d];
+            if ( e > 0 )
+            {
+                n[d] = (int)std::min( 1024.0, std::max( 1.0, std::ceil( e / hc ) ) );
+                h[d] = e / n[d];
+            }
+            else
+            {
+                n[d] = 1;
+                h[d] = 1.0;
+            }
+            inv_h[d] = 1.0 / h[d];
+            total *= n[d];
+        }
+        slack = 1e-12 * ( scale + 1.0 );
+        start.assign( total + 1, 0 );
+        std::vector<int64_t> cell( n_src );
+        for ( int64_t i = 0; i < n_src; ++i )
+        {
+            int64_t c = cell_coord( src[3 * i + 0], 0 ) +
+                        (int64_t)n[0] * ( cell_coord( src[3 * i + 1], 1 ) +
+                                          (int64_t)n[1] * cell_coord( src[3 * i + 2], 2 ) );
+            cell[i] = c;
+            start[c + 1]++;
+        }
+        for ( int64_t c = 0; c < total; ++c )
+            start[c + 1] += start[c];
+        std::vector<int64_t> fill( start.begin(), start.end() - 1 );
+        ids.resize( n_src );
+        xyz.resize( 3 * n_src );
+        for ( int64_t i = 0; i < n_src; ++i )
+        {
+            int64_t const pos = fill[cell[i]]++;
+            ids[pos] = (int32_t)i;
+            for ( int d = 0; d < 3; ++d )
+                xyz[3 * pos + d] = src[3 * i + d];
+        }
+    }
+
+    template <typename F>
+    void visit_cell( int cx, int cy, int cz, F &&f ) const
+    {
+        int64_t const c = cx + (int64_t)n[0] * ( cy + (int64_t)n[1] * cz );
+        for ( int64_t p = start[c]; p < start[c + 1]; ++p )
+            f( ids[p], &xyz[3 * p] );
+    }
+};
+
+using Cand = std::pair<double, int32_t>; // (d2, index), lexicographic
+
+void knn_one( Grid const &g, double const *t, int k, std::vector<Cand> &heap )
+{
+    heap.clear();
+    int ct[3];
+    for ( int d = 0; d < 3; ++d )
+        ct[d] = g.cell_coord( t[d], d );
+    auto consider = [&]( int32_t id, double const *s ) {
+        Cand const c( dist2( s, t ), id );
+        if ( (int)heap.size() < k )
+        {
+            heap.push_back( c );
+            std::push_heap( heap.begin(), heap.end() );
+        }
+        else if ( c < heap.front() )
+        {
+            std::pop_heap( heap.begin(), heap.end() );
+            heap.back() = c;
+            std::push_heap( heap.begin(), heap.end() );
+        }
+    };
+    for ( int s = 0;; ++s )
+    {
+        int lo[3], hi[3];
+        for ( int d = 0; d < 3; ++d )
+        {
+            lo[d] = std::max( 0, ct[d] - s );
+            hi[d] = std::min( g.n[d] - 1, ct[d] + s );
+        }
+        for ( int cz = lo[2]; cz <= hi[2]; ++cz )
+            for ( int cy = lo[1]; cy <= hi[1]; ++cy )
+            {
+                bool const face = std::abs( cz - ct[2] ) == s || std::abs( cy - ct[1] ) == s;
+                if ( face )
+                {
+                    for ( int cx = lo[0]; cx <= hi[0]; ++cx )
+                        g.visit_cell( cx, cy, cz, consider );
+                }
+                else
+                {
+                    if ( ct[0] - s >= 0 )
+                        g.visit_cell( ct[0] - s, cy, cz, consider );
+                    if ( s > 0 && ct[0] + s < g.n[0] )
+                        g.visit_cell( ct[0] + s, cy, cz, consider );
+                }
+            }
+        // Lower bound on the distance of any source outside the searched block.
+        double gap = std::numeric_limits<double>::infinity();
+        bool all = true;
+        for ( int d = 0; d < 3; ++d )
+        {
+            if ( lo[d] > 0 )
+            {
+                all = false;
+                gap = std::min( gap, t[d] - ( g.lo[d] + lo[d] * g.h[d] ) );
+            }
+            if ( hi[d] < g.n[d] - 1 )
+            {
+                all = false;
+                gap = std::min( gap, ( g.lo[d] + ( hi[d] + 1 ) * g.h[d] ) - t[d] );
+            }
+        }
+        if ( all )
+            break;
+        double const ge = gap - g.slack;
+        if ( (int)heap.size() == k && ge > 0 && heap.front().first < ge * ge )
+            break;
+    }
+    std::sort( heap.begin(), heap.end() );
+}
+
+template <typename F>
+void radius_visit( Grid const &g, double const *t, double r, F &&f )
+{
+    int lo[3], hi[3];
+    for ( int d = 0; d < 3; ++d )
+    {
+        lo[d] = std::max( 0, g.cell_coord( t[d] - r, d ) - 1 );
+        hi[d] = std::min( g.n[d] - 1, g.cell_coord( t[d] + r, d ) + 1 );
+    }
+    for ( int cz = lo[2]; cz <= hi[2]; ++cz )
+        for ( int cy = lo[1]; cy <= hi[1]; ++cy )
+            for ( int cx = lo[0]; cx <= hi[0]; ++cx )
+                g.visit_cell( cx, cy, cz, [&]( int32_t id, double const *s ) {
+                    double const d2 = dist2( s, t );
+                    if ( std::sqrt( d2 ) <= r )
+                        f( id, d2 );
+                } );
+}
+
+struct RowScratch
+{
+    std::vector<double> x, P, phi, dist, A, jac;
+    Jacobi jac_solver;
+};
+
+// Stages of MovingLeastSquaresOperator setup for one target row, in the
+// reference order (DTK_MovingLeastSquaresOperator_def.hpp:133-185).
+// Returns the rank-deficiency flag; fills coeff[0..len) and row0[0..m).
+int mls_row( double const *src, double const *t, int32_t const *idx, int len,
+             int rbf, int basis, RowScratch &w, double *coeff, double *radius_out,
+             double *row0 )
+{
+    int const m = basis_size( basis );
+    w.x.resize( 3 * len );
+    w.P.resize( (size_t)m * len );
+    w.phi.resize( len );
+    w.dist.resize( len );
+    w.A.resize( m * m );
+    // fetch + transformSourceCoordinates: Impl.hpp:72-99
+    for ( int j = 0; j < len; ++j )
+        for ( int d = 0; d < 3; ++d )
+            w.x[3 * j + d] = src[3 * (int64_t)idx[j] + d] - t[d];
+    // computeVandermonde: Impl.hpp:171-190
+    for ( int j = 0; j < len; ++j )
+        basis_eval( basis, &w.x[3 * j], &w.P[(size_t)m * j] );
+    // computeRadius: Impl.hpp:101-138 (distance to the origin)
+    double distance = 10. * DBL_EPSILON;
+    for ( int j = 0; j < len; ++j )
+    {
+        double const *p = &w.x[3 * j];
+        double const nd = std::sqrt( ( p[0] * p[0] + p[1] * p[1] ) + p[2] * p[2] );
+        w.dist[j] = nd;
+        if ( nd > distance )
+            distance = nd;
+    }
+    double const radius = 1.1 * distance;
+    if ( radius_out )
+        *radius_out = radius;
+    // computeWeights: Impl.hpp:143-169
+    for ( int j = 0; j < len; ++j )
+        w.phi[j] = rbf_eval( rbf, w.dist[j] / radius );
+    // computeMoments: Impl.hpp:213-258 (full m x m, l-order)
+    for ( int a = 0; a < m; ++a )
+        for ( int b = 0; b < m; ++b )
+        {
+            double tmp = 0.;
+            for ( int l = 0; l < len; ++l )
+                tmp += w.P[(size_t)l * m + a] * w.phi[l] * w.P[(size_t)l * m + b];
+            w.A[a * m + b] = tmp;
+        }
+    // invertMoments: Impl.hpp:263-291 -> SVDImpl.hpp:197-302 (row 0 only)
+    if ( w.jac_solver.n != m )
+        w.jac_solver.resize( m );
+    w.jac_solver.load( w.A.data() );
+    w.jac_solver.run();
+    double inv0[16];
+    int const dropped = w.jac_solver.pinv_rows( inv0, 1 );
+    if ( row0 )
+        for ( int j = 0; j < m; ++j )
+            row0[j] = inv0[j];
+    // computePolynomialCoefficients: Impl.hpp:293-336
+    for ( int k = 0; k < len; ++k )
+    {
+        double c = 0.;
+        for ( int j = 0; j < m; ++j )
+            c += inv0[j] * w.P[(size_t)k * m + j] * w.phi[k];
+        coeff[k] = c;
+    }
+    return dropped;
+}
+
+bool bad_points( double const *p, int64_t n ) { return n < 0 || ( n > 0 && !p ); }
+
+} // namespace
+
+extern "C" {
+
+int dtk_oracle_max_threads( void )
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void dtk_oracle_set_threads( int n )
+{
+#ifdef _OPENMP
+    if ( n > 0 )
+        omp_set_num_threads( n );
+#else
+    (void)n;
+#endif
+}
+
+int dtk_oracle_knn( double const *src, int64_t n_src, double const *tgt,
+                    int64_t n_tgt, int k, int32_t *offset, int32_t *idx,
+                    double *d2 )
+{
+    if ( bad_points( src, n_src ) || bad_points( tgt, n_tgt ) || k < 0 || !offset ||
+         n_src > INT32_MAX )
+        return -1;
+    int64_t const row = std::min<int64_t>( k, n_src );
+    if ( n_tgt * row > INT32_MAX )
+        return -1;
+    for ( int64_t i = 0; i <= n_tgt; ++i )
+        offset[i] = (int32_t)( i * row );
+    if ( row == 0 || n_tgt == 0 )
+        return 0;
+    Grid g;
+    g.build( src, n_src, std::max( 2.0, row / 4.0 ) );
+#pragma omp parallel
+    {
+        std::vector<Cand> heap;
+#pragma omp for schedule( dynamic, 256 )
+        for ( int64_t i = 0; i < n_tgt; ++i )
+        {
+            knn_one( g, tgt + 3 * i, (int)row, heap );
+            for ( int64_t j = 0; j < row; ++j )
+            {
+                idx[i * row + j] = heap[j].second;
+                if ( d2 )
+                    d2[i * row + j] = heap[j].first;
+            }
+        }
+    }
+    return 0;
+}
+
+int dtk_oracle_knn_brute( double const *src, int64_t n_src, double const *tgt,
+                          int64_t n_tgt, int k, int32_t *offset, int32_t *idx,
+                          double *d2 )
+{
+    if ( bad_points( src, n_src ) || bad_points( tgt, n_tgt ) || k < 0 || !offset )
+        return -1;
+    int64_t const row = std::min<int64_t>( k, n_src );
+    for ( int64_t i = 0; i <= n_tgt; ++i )
+        offset[i] = (int32_t)( i * row );
+#pragma omp parallel
+    {
+        std::vector<Cand> all( n_src );
+#pragma omp for schedule( dynamic, 16 )
+        for ( int64_t i = 0; i < n_tgt; ++i )
+        {
+            for ( int64_t s = 0; s < n_src; ++s )
+                all[s] = Cand( dist2( src + 3 * s, tgt + 3 * i ), (int32_t)s );
+            std::partial_sort( all.begin(), all.begin() + row, all.end() );
+            for ( int64_t j = 0; j < row; ++j )
+            {
+                idx[i * row + j] = all[j].second;
+                if ( d2 )
+                    d2[i * row + j] = all[j].first;
+            }
+        }
+    }
+    return 0;
+}
+
+int64_t dtk_oracle_radius_count( double const *src, int64_t n_src,
+                                 double const *tgt, int64_t n_tgt, double r,
+                                 int32_t *offset )
+{
+    if ( bad_points( src, n_src ) || bad_points( tgt, n_tgt ) || !offset ||
+         !( r >= 0 ) )
+        return -1;
+    offset[0] = 0;
+    if ( n_src == 0 )
+    {
+        for ( int64_t i = 0; i <= n_tgt; ++i )
+            offset[i] = 0;
+        return 0;
+    }
+    Grid g;
+    g.build( src, n_src, 2.0 );
+    std::vector<int64_t> cnt( n_tgt );
+#pragma omp parallel for schedule( dynamic, 256 )
+    for ( int64_t i = 0; i < n_tgt; ++i )
+    {
+        int64_t c = 0;
+        radius_visit( g, tgt + 3 * i, r, [&]( int32_t, double ) { ++c; } );
+        cnt[i] = c;
+    }
+    int64_t acc = 0;
+    for ( int64_t i = 0; i < n_tgt; ++i )
+    {
+        acc += cnt[i];
+        if ( acc > INT32_MAX )
+            return -1;
+        offset[i + 1] = (int32_t)acc;
+    }
+    return acc;
+}
+
+int dtk_oracle_radius_fill( double const *src, int64_t n_src, double const *tgt,
+                            int64_t n_tgt, double r, int32_t const *offset,
+                            int32_t *idx, double *d2 )
+{
+    if ( bad_points( src, n_src ) || bad_points( tgt, n_tgt ) || !offset )
+        return -1;
+    if ( n_src == 0 )
+        return 0;
+    Grid g;
+    g.build( src, n_src, 2.0 );
+#pragma omp parallel
+    {
+        std::vector<Cand> row;
+#pragma omp for schedule( dynamic, 256 )
+        for ( int64_t i = 0; i < n_tgt; ++i )
+        {
+            row.clear();
+            radius_visit( g, tgt + 3 * i, r,
+                          [&]( int32_t id, double dd ) { row.emplace_back( dd, id ); } );
+            std::sort( row.begin(), row.end() );
+            int64_t const o = offset[i];
+            for ( size_t j = 0; j < row.size() && o + (int64_t)j < offset[i + 1]; ++j )
+            {
+                idx[o + j] = row[j].second;
+                if ( d2 )
+                    d2[o + j] = row[j].first;
+            }
+        }
+    }
+    return 0;
+}
+
+int64_t dtk_oracle_mls_coefficients( double const *src, double const *tgt,
+                                     int64_t n_tgt, int32_t const *offset,
+                                     int32_t const *idx, int rbf, int basis,
+                                     double *coeff, double *radius, double *row0 )
+{
+    int const m = basis_size( basis );
+    if ( m < 0 || rbf < 0 || rbf >= N_RBF || n_tgt < 0 || !offset )
+        return -1;
+    int64_t under = 0;
+#pragma omp parallel reduction( + : under )
+    {
+        RowScratch w;
+#pragma omp for schedule( dynamic, 64 )
+        for ( int64_t i = 0; i < n_tgt; ++i )
+        {
+            int const b = offset[i];
+            int const len = offset[i + 1] - b;
+            under += mls_row( src, tgt + 3 * i, idx + b, len, rbf, basis, w,
+                              coeff + b, radius ? radius + i : nullptr,
+                              row0 ? row0 + i * m : nullptr );
+        }
+    }
+    return under;
+}
+
+int dtk_oracle_apply( int64_t n_tgt, int32_t const *offset, int32_t const *idx,
+                      double const *coeff, double const *values, double *target )
+{
+    if ( n_tgt < 0 || !offset )
+        return -1;
+#pragma omp parallel for schedule( static, 1024 )
+    for ( int64_t i = 0; i < n_tgt; ++i )
+    {
+        double acc = 0.;
+        for ( int j = offset[i]; j < offset[i + 1]; ++j )
+            acc += coeff[j] * values[idx[j]];
+        target[i] = acc;
+    }
+    return 0;
+}
+
+int dtk_oracle_apply_transpose( int64_t n_tgt, int64_t n_src,
+                                int32_t const *offset, int32_t const *idx,
+                                double const *coeff, double const *cot,
+                                double *grad )
+{
+    if ( n_tgt < 0 || n_src < 0 || !offset )
+        return -1;
+    for ( int64_t s = 0; s < n_src; ++s )
+        grad[s] = 0.;
+    for ( int64_t i = 0; i < n_tgt; ++i )
+        for ( int j = offset[i]; j < offset[i + 1]; ++j )
+            grad[idx[j]] += coeff[j] * cot[i];
+    return 0;
+}
+
+// Adjoint of the setup with connectivity fixed.  For one row, with
+// x_j = s_j - t, rho_j = |x_j|, R = 1.1 max(10 eps, max rho), phi_j =
+// rbf(rho_j / R), A = sum phi P P^T, a = A^+ e0, z = A^+ b,
+// b = sum phi_j v_j P_j, y = a.b:
+//   dy/dx_j = phi_j J_j^T (e_j a - alpha_j z) + (g_j / R) u_j
+//             - [j == farthest] 1.1 (sum_l g_l rho_l) / R^2 u_j
+// with alpha_j = a.P_j, e_j = v_j - P_j.z, g_j = alpha_j e_j rbf'(rho_j/R),
+// u_j = x_j / rho_j.  The farthest entry is the last one of largest rho.
+int dtk_oracle_coord_grad( double const *src, int64_t n_src, double const *tgt,
+                           int64_t n_tgt, int32_t const *offset,
+                           int32_t const *idx, int rbf, int basis,
+                           double const *values, double const *cot,
+                           double *grad_xyz )
+{
+    int const m = basis_size( basis );
+    if ( m < 0 || rbf < 0 || rbf >= N_RBF || n_tgt < 0 || n_src < 0 || !offset )
+        return -1;
+    int const nth = dtk_oracle_max_threads();
+    std::vector<std::vector<double>> partial( nth );
+#pragma omp parallel
+    {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        std::vector<double> &acc = partial[tid];
+        acc.assign( 3 * n_src, 0.0 );
+        RowScratch w;
+        std::vector<double> pinv, jac( 30 ), zc, alpha, e;
+#pragma omp for schedule( dynamic, 64 )
+        for ( int64_t i = 0; i < n_tgt; ++i )
+        {
+            int const b0 = offset[i];
+            int const len = offset[i + 1] - b0;
+            if ( len == 0 || cot[i] == 0.0 )
+                continue;
+            double const *t = tgt + 3 * i;
+            std::vector<double> coeff( len );
+            double radius;
+            mls_row( src, t, idx + b0, len, rbf, basis, w, coeff.data(), &radius,
+                     nullptr );
+            // full pseudo-inverse for z = A^+ b
+            pinv.resize( m * m );
+            w.jac_solver.pinv_rows( pinv.data(), m );
+            std::vector<double> bvec( m, 0.0 );
+            for ( int j = 0; j < len; ++j )
+                for ( int c = 0; c < m; ++c )
+                    bvec[c] += w.phi[j] * values[idx[b0 + j]] * w.P[(size_t)j * m + c];
+            zc.assign( m, 0.0 );
+            for ( int r = 0; r < m; ++r )
+                for ( int c = 0; c < m; ++c )
+                    zc[r] += pinv[r * m + c] * bvec[c];
+            double const *a = pinv.data(); // row 0
+            int far = 0;
+            for ( int j = 0; j < len; ++j )
+                if ( w.dist[j] >= w.dist[far] )
+                    far = j;
+            double sum_g_rho = 0.0;
+            std::vector<double> g( len );
+            alpha.assign( len, 0.0 );
+            e.assign( len, 0.0 );
+            for ( int j = 0; j < len; ++j )
+            {
+                double al = 0.0, pz = 0.0;
+                for ( int c = 0; c < m; ++c )
+                {
+                    al += a[c] * w.P[(size_t)j * m + c];
+                    pz += w.P[(size_t)j * m + c] * zc[c];
+                }
+                alpha[j] = al;
+                e[j] = values[idx[b0 + j]] - pz;
+                g[j] = al * e[j] * rbf_deriv( rbf, w.dist[j] / radius );
+                sum_g_rho += g[j] * w.dist[j];
+            }
+            bool const radius_live = w.dist[far] > 10. * DBL_EPSILON;
+            for ( int j = 0; j < len; ++j )
+            {
+                double gx[3] = {0, 0, 0};
+                basis_jacobian( basis, &w.x[3 * j], jac.data() );
+                for ( int c = 0; c < m; ++c )
+                {
+                    double const wc = w.phi[j] * ( e[j] * a[c] - alpha[j] * zc[c] );
+                    for ( int d = 0; d < 3; ++d )
+                        gx[d] += wc * jac[c * 3 + d];
+                }
+                double const rho = w.dist[j];
+                if ( rho > 0.0 )
+                {
+                    double coef = g[j] / radius;
+                    if ( j == far && radius_live )
+                        coef -= 1.1 * sum_g_rho / ( radius * radius );
+                    for ( int d = 0; d < 3; ++d )
+                        gx[d] += coef * w.x[3 * j + d] / rho;
+                }
+                int64_t const s = idx[b0 + j];
+                for ( int d = 0; d < 3; ++d )
+                    acc[3 * s + d] += cot[i] * gx[d];
+            }
+        }
+    }
+    for ( int th = 0; th < nth; ++th )
+        if ( !partial[th].empty() )
+            for ( int64_t q = 0; q < 3 * n_src; ++q )
+                grad_xyz[q] += partial[th][q];
+    return 0;
+}
+
+int64_t dtk_oracle_svd_pinv( int n, int64_t count, double const *a, double *pinv )
+{
+    if ( n <= 0 || count < 0 )
+        return -1;
+    int64_t under = 0;
+#pragma omp parallel reduction( + : under )
+    {
+        Jacobi J;
+        J.resize( n );
+#pragma omp for schedule( dynamic, 1 )
+        for ( int64_t i = 0; i < count; ++i )
+        {
+            J.load( a + i * n * n );
+            J.run();
+            under += J.pinv_rows( pinv + i * n * n, n );
+        }
+    }
+    return under;
+}
+
+void dtk_oracle_rbf( int rbf, double const *x, int64_t n, double *out )
+{
+    for ( int64_t i = 0; i < n; ++i )
+        out[i] = rbf_eval( rbf, x[i] );
+}
+
+int dtk_oracle_basis_size( int basis ) { return basis_size( basis ); }
+
+void dtk_oracle_basis( int basis, double const *pts, int64_t n, double *out )
+{
+    int const m = basis_size( basis );
+    for ( int64_t i = 0; i < n; ++i )
+        basis_eval( basis, pts + 3 * i, out + i * m );
+}
+
+} // extern "C"
