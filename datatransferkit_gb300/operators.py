@@ -254,7 +254,7 @@ class _DeviceArray:
 
     def __init__(self, ptr: int, n: int, typestr: str):
         self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr,
-                                         "data": (ptr, True), "version": 3, "strides": None}
+                                         "data": (ptr, False), "version": 3, "strides": None}
 
 
 _TYPESTR = {torch.int32: "<i4", torch.float32: "<f4", torch.float64: "<f8"}

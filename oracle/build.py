@@ -3,6 +3,9 @@
 * ``_build/libdtk_oracle.so``: the FP64 restatement (dtk_oracle.cpp), g++
   -O3 -fopenmp -ffp-contract=off.  Built on every machine (here and on the
   GPU host) by ``__graft_entry__.build()``.
+* ``_build/libdtk_oracle_contract.so``: the same restatement built with
+  multiply-add contraction, to measure the rounding spread of the reference
+  algorithm (the parity tolerance of the FP64 form is derived from it).
 * ``_ref/libdtk_ref.so``: the reference's own MLS numerics headers compiled
   where they lie in the DataTransferKit tree against the project-written API
   shim in ``ref_shim/`` plus ``ref_driver.cpp``.  Built only when the
@@ -15,6 +18,7 @@ and aarch64 hosts.
 from __future__ import annotations
 
 import os
+import platform
 import subprocess
 import sys
 from pathlib import Path
@@ -23,6 +27,7 @@ HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
 ORACLE_SO = BUILD / "libdtk_oracle.so"
+ORACLE_CONTRACT_SO = BUILD / "libdtk_oracle_contract.so"
 REF_SO = REF_OUT / "libdtk_ref.so"
 
 COMMON = ["-O3", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
@@ -40,13 +45,26 @@ def _stale(out: Path, deps) -> bool:
     return any(Path(d).stat().st_mtime > t for d in deps)
 
 
-def build_oracle(force: bool = False) -> Path:
+def _contract_flags():
+    # Same sources with multiply-add contraction on: the build that a compiler
+    # for another backend (an FMA-contracting GPU or Arm build) would make.
+    # The distance between the two builds measures how far the reference
+    # algorithm itself moves under equally valid roundings.
+    flags = ["-ffp-contract=fast"]
+    if platform.machine() in ("x86_64", "AMD64"):
+        flags.append("-mfma")
+    return flags
+
+
+def build_oracle(force: bool = False, contract: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
+    out = ORACLE_CONTRACT_SO if contract else ORACLE_SO
     deps = [HERE / "dtk_oracle.cpp", HERE / "dtk_oracle.h"]
-    if force or _stale(ORACLE_SO, deps):
-        cmd = ["g++", *COMMON, str(HERE / "dtk_oracle.cpp"), "-o", str(ORACLE_SO)]
+    if force or _stale(out, deps):
+        flags = [f for f in COMMON if f != "-ffp-contract=off"] + _contract_flags() if contract else COMMON
+        cmd = ["g++", *flags, str(HERE / "dtk_oracle.cpp"), "-o", str(out)]
         subprocess.run(cmd, check=True)
-    return ORACLE_SO
+    return out
 
 
 def build_ref(force: bool = False) -> Path | None:
@@ -66,4 +84,5 @@ def build_ref(force: bool = False) -> Path | None:
 
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
+    print(build_oracle(force="--force" in sys.argv, contract=True))
     print(build_ref(force="--force" in sys.argv))

@@ -13,6 +13,7 @@ import numpy as np
 from . import build as _build
 
 _lib = None
+_lib_contract = None
 
 RBF_IDS = {"wendland0": 0, "wendland2": 1, "wendland4": 2, "wendland6": 3,
            "wu2": 4, "wu4": 5, "buhmann2": 6, "buhmann3": 7, "buhmann4": 8}
@@ -22,29 +23,36 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
 
 
-def lib():
-    global _lib
+def lib(contract: bool = False):
+    """The oracle library; contract=True gives its multiply-add-contracted build."""
+    global _lib, _lib_contract
+    if contract:
+        if _lib_contract is None:
+            _lib_contract = _declare(C.CDLL(str(_build.build_oracle(contract=True))))
+        return _lib_contract
     if _lib is None:
-        so = _build.build_oracle()
-        L = C.CDLL(str(so))
-        L.dtk_oracle_knn.argtypes = [_dp, C.c_int64, _dp, C.c_int64, C.c_int, _ip, _ip, _dp]
-        L.dtk_oracle_knn_brute.argtypes = L.dtk_oracle_knn.argtypes
-        L.dtk_oracle_radius_count.argtypes = [_dp, C.c_int64, _dp, C.c_int64, C.c_double, _ip]
-        L.dtk_oracle_radius_count.restype = C.c_int64
-        L.dtk_oracle_radius_fill.argtypes = [_dp, C.c_int64, _dp, C.c_int64, C.c_double, _ip, _ip, _dp]
-        L.dtk_oracle_mls_coefficients.argtypes = [_dp, _dp, C.c_int64, _ip, _ip, C.c_int, C.c_int, _dp, _dp, _dp]
-        L.dtk_oracle_mls_coefficients.restype = C.c_int64
-        L.dtk_oracle_apply.argtypes = [C.c_int64, _ip, _ip, _dp, _dp, _dp]
-        L.dtk_oracle_apply_transpose.argtypes = [C.c_int64, C.c_int64, _ip, _ip, _dp, _dp, _dp]
-        L.dtk_oracle_coord_grad.argtypes = [_dp, C.c_int64, _dp, C.c_int64, _ip, _ip, C.c_int, C.c_int, _dp, _dp, _dp]
-        L.dtk_oracle_svd_pinv.argtypes = [C.c_int, C.c_int64, _dp, _dp]
-        L.dtk_oracle_svd_pinv.restype = C.c_int64
-        L.dtk_oracle_rbf.argtypes = [C.c_int, _dp, C.c_int64, _dp]
-        L.dtk_oracle_basis.argtypes = [C.c_int, _dp, C.c_int64, _dp]
-        L.dtk_oracle_max_threads.restype = C.c_int
-        L.dtk_oracle_set_threads.argtypes = [C.c_int]
-        _lib = L
+        _lib = _declare(C.CDLL(str(_build.build_oracle())))
     return _lib
+
+
+def _declare(L):
+    L.dtk_oracle_knn.argtypes = [_dp, C.c_int64, _dp, C.c_int64, C.c_int, _ip, _ip, _dp]
+    L.dtk_oracle_knn_brute.argtypes = L.dtk_oracle_knn.argtypes
+    L.dtk_oracle_radius_count.argtypes = [_dp, C.c_int64, _dp, C.c_int64, C.c_double, _ip]
+    L.dtk_oracle_radius_count.restype = C.c_int64
+    L.dtk_oracle_radius_fill.argtypes = [_dp, C.c_int64, _dp, C.c_int64, C.c_double, _ip, _ip, _dp]
+    L.dtk_oracle_mls_coefficients.argtypes = [_dp, _dp, C.c_int64, _ip, _ip, C.c_int, C.c_int, _dp, _dp, _dp]
+    L.dtk_oracle_mls_coefficients.restype = C.c_int64
+    L.dtk_oracle_apply.argtypes = [C.c_int64, _ip, _ip, _dp, _dp, _dp]
+    L.dtk_oracle_apply_transpose.argtypes = [C.c_int64, C.c_int64, _ip, _ip, _dp, _dp, _dp]
+    L.dtk_oracle_coord_grad.argtypes = [_dp, C.c_int64, _dp, C.c_int64, _ip, _ip, C.c_int, C.c_int, _dp, _dp, _dp]
+    L.dtk_oracle_svd_pinv.argtypes = [C.c_int, C.c_int64, _dp, _dp]
+    L.dtk_oracle_svd_pinv.restype = C.c_int64
+    L.dtk_oracle_rbf.argtypes = [C.c_int, _dp, C.c_int64, _dp]
+    L.dtk_oracle_basis.argtypes = [C.c_int, _dp, C.c_int64, _dp]
+    L.dtk_oracle_max_threads.restype = C.c_int
+    L.dtk_oracle_set_threads.argtypes = [C.c_int]
+    return L
 
 
 def _d(a):
@@ -98,7 +106,7 @@ def radius(src, tgt, r):
     return offset, idx, d2
 
 
-def mls_coefficients(src, tgt, offset, idx, rbf, basis, want_row0=False):
+def mls_coefficients(src, tgt, offset, idx, rbf, basis, want_row0=False, contract=False):
     """(coeff, radius, row0|None, n_underdetermined) for given connectivity."""
     src, tgt = _pts(src), _pts(tgt)
     offset = np.ascontiguousarray(offset, np.int32)
@@ -107,7 +115,7 @@ def mls_coefficients(src, tgt, offset, idx, rbf, basis, want_row0=False):
     coeff = np.zeros(int(offset[-1]), np.float64)
     rad = np.zeros(len(tgt), np.float64)
     row0 = np.zeros(len(tgt) * m, np.float64) if want_row0 else None
-    under = lib().dtk_oracle_mls_coefficients(_d(src), _d(tgt), len(tgt), _i(offset), _i(idx),
+    under = lib(contract).dtk_oracle_mls_coefficients(_d(src), _d(tgt), len(tgt), _i(offset), _i(idx),
                                               int(rbf), int(basis), _d(coeff), _d(rad), _d(row0))
     if under < 0:
         raise ValueError("oracle setup rejected its arguments")
@@ -181,3 +189,25 @@ def mls_transfer(src, tgt, values, rbf_id, basis_id, k=None, r=None):
     out = apply(offset, idx, coeff, values)
     return dict(offset=offset, idx=idx, d2=d2, coeff=coeff, radius=rad,
                 underdetermined=under, target=out)
+
+
+def rounding_spread(src, tgt, offset, idx, rbf, basis, values, coeff=None):
+    """How far the reference algorithm moves under another valid rounding.
+
+    Returns (coefficient spread, target spread): the largest per-row
+    max|c - c'| / max|c| and the relative L2 distance of the transferred
+    values between the oracle and its multiply-add-contracted build.
+    """
+    if coeff is None:
+        coeff = mls_coefficients(src, tgt, offset, idx, rbf, basis)[0]
+    c2 = mls_coefficients(src, tgt, offset, idx, rbf, basis, contract=True)[0]
+    worst = 0.0
+    offset = np.asarray(offset)
+    for i in range(len(offset) - 1):
+        a, b = c2[offset[i]:offset[i + 1]], coeff[offset[i]:offset[i + 1]]
+        if len(b):
+            worst = max(worst, float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)))
+    y = apply(offset, idx, coeff, values)
+    y2 = apply(offset, idx, c2, values)
+    ny = np.linalg.norm(y)
+    return worst, float(np.linalg.norm(y2 - y) / (ny if ny > 0 else 1.0))
