@@ -1,0 +1,412 @@
+"""MLS setup+apply throughput on GB300 (DataTransferKit MovingLeastSquaresOperator path).
+
+Workload (default, "mixed_8m"): 8,000,000 sources and 8,000,000 targets
+U[0,1]^3 (seeds 6, 7), Quadratic3 basis, Wendland<4>, k = 32 -- the
+configuration the headline metric is quoted on.  One step = one operator
+setup (search, weights, moments, pseudo-inverse, coefficients) plus one
+apply over all targets.  ``value`` is targets/s of the mixed FP32/FP64 form
+with inputs resident in HBM; the plain FP64 form (the reference algorithm) is
+timed on the same inputs and reported beside it, with the relative L2 error
+of both against the FP64 CPU oracle on a sample of targets.  ``e2e`` is the
+same metric through the public API with host buffers: the H2D copies of the
+points and the source field from pinned memory and the D2H copy of the
+target field are inside the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU (torchrun, one process per GPU): targets shard across ranks
+(each rank its own 8M-target shard, seeds 7 + rank) with the sources
+replicated; no data-path collective ("scaling": "weak").  Timing takes the
+max over ranks.  ``--impl reference`` times the CPU restatement of the
+reference algorithm (the oracle, all host threads) on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "MLS setup+apply targets/s on 1 GB300: mixed vs FP64 form at ≤1e-6 rel L2 err"
+UNIT = "targets/s"
+WORKLOADS = {
+    # name: (n_src, n_tgt, src_seed, tgt_seed, rbf, basis, k)
+    "mixed_8m": (8_000_000, 8_000_000, 6, 7, 2, 2, 32),
+    "fp64_2m": (2_000_000, None, 3, 4, 1, 2, 32),  # 126^3 jittered-grid targets
+}
+RBF_NAMES = {1: "Wendland<2>", 2: "Wendland<4>"}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="mixed_8m", choices=sorted(WORKLOADS))
+    ap.add_argument("--sample", type=int, default=20000, help="targets in the CPU/oracle sample")
+    return ap.parse_args()
+
+
+def make_inputs(name, rank=0):
+    from datatransferkit_gb300 import synthetic as syn
+    n_src, n_tgt, s_seed, t_seed, rbf, basis, k = WORKLOADS[name]
+    src = syn.uniform_points(n_src, s_seed)
+    tgt = syn.jittered_grid(126, t_seed + rank) if n_tgt is None else syn.uniform_points(n_tgt, t_seed + rank)
+    return src, tgt, rbf, basis, k
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.rows = []
+        self.proc = None
+        self.device_index = device_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device_index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 8:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        smax = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for name, v in zip(names, r[4:8]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic FLOP counts (FP64) of the setup kernels
+# ---------------------------------------------------------------------------
+def fp64_form_flops(n_tgt, k, m, rotations):
+    """Reference algorithm: per rotation the off-diagonal norm scan 2m(m-1),
+    the 2x2 SVD ~30 (transcendentals counted once), the E row/column, U column
+    and V column-0 rotations 3*(6m) + 6; per target-neighbour the gather,
+    distance, weight, basis and symmetric moments ~ 30 + m + m(m+1), and the
+    coefficients ~ 30 + 2m; per target row 0 of the pseudo-inverse 2m^2 + m."""
+    per_rot = 2 * m * (m - 1) + 30 + 18 * m + 6
+    per_nb = (30 + m + m * (m + 1)) + (30 + 2 * m)
+    return rotations * per_rot + n_tgt * k * per_nb + n_tgt * (2 * m * m + m)
+
+
+def mixed_form_flops(n_tgt, k, m, rotations64):
+    """Mixed form, FP64 part only: per target the centring/scaling
+    2 passes x k x 6, B = V32^T A V32 (2 m^3 + m^2 (m+1)), row 0 (2 m^2 + m),
+    the radius ~10; per FP64 rotation 12 m + 16."""
+    per_rot = 12 * m + 16
+    per_tgt = 2 * k * 6 + 2 * m ** 3 + m * m * (m + 1) + 2 * m * m + m + 10
+    return rotations64 * per_rot + n_tgt * per_tgt
+
+
+def measure_fp64_peak(torch, dev):
+    """cuBLAS DGEMM rate (the FP64 analogue of the measured bf16 peak)."""
+    n = 4096
+    a = torch.rand(n, n, dtype=torch.float64, device=dev)
+    b = torch.rand(n, n, dtype=torch.float64, device=dev)
+    best = 0.0
+    for _ in range(4):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    del a, b
+    return best
+
+
+def read_profile_traffic():
+    """dram bytes per launch of the setup kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "setup_mixed_traffic.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("bytes_per_target="):
+            return float(line.split("=", 1)[1])
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle timing (bounded sample)
+# ---------------------------------------------------------------------------
+def cpu_oracle_run(src, tgt, vals, rbf, basis, k, sample):
+    from oracle import cpu
+    threads = cpu.max_threads()
+    sub = tgt[:sample]
+    t0 = time.perf_counter()
+    cpu.knn(src, tgt[:1], k)  # index build alone
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    off, idx, _ = cpu.knn(src, sub, k)
+    coeff, _, _, _ = cpu.mls_coefficients(src, sub, off, idx, rbf, basis)
+    y = cpu.apply(off, idx, coeff, vals)
+    t_total = time.perf_counter() - t0
+    per_target = max(t_total - t_build, 1e-9) / len(sub)
+    n_full = len(tgt)
+    value = n_full / (t_build + n_full * per_target)
+    return dict(value=value, threads=threads, t_build=t_build, t_sample=t_total, y=y,
+                sample=len(sub))
+
+
+# ---------------------------------------------------------------------------
+# reference arm
+# ---------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from datatransferkit_gb300 import synthetic as syn
+    src, tgt, rbf, basis, k = make_inputs(args.workload)
+    vals = syn.smooth_field(src)
+    times, last = [], None
+    for it in range(args.warmup + args.steps):
+        r = cpu_oracle_run(src, tgt, vals, rbf, basis, k, args.sample)
+        if it >= args.warmup:
+            times.append(r["value"])
+        last = r
+    value = float(np.median(times))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": len(tgt) / value * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded U[0,1]^3 clouds)",
+        "config": {"workload": args.workload, "n_sources": len(src), "n_targets": len(tgt),
+                   "basis": "Quadratic3", "rbf": RBF_NAMES[rbf], "k": k},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": last["threads"], "kind": "port",
+                         "sample": (f"full {len(src)}-source grid index build + {last['sample']} "
+                                    f"of {len(tgt)} targets (kNN, setup, apply), extrapolated "
+                                    "to the full target set")},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import datatransferkit_gb300 as dtk
+    from datatransferkit_gb300 import synthetic as syn
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    src, tgt, rbf, basis_id, k = make_inputs(args.workload, rank)
+    vals = syn.smooth_field(src)
+    front = syn.front_field(src)
+    RBF = {1: dtk.Wendland(2), 2: dtk.Wendland(4)}[rbf]
+    BASIS = {1: dtk.MultivariatePolynomialBasis(dtk.Linear, 3),
+             2: dtk.MultivariatePolynomialBasis(dtk.Quadratic, 3)}[basis_id]
+    m = BASIS.size
+    n_tgt = len(tgt)
+
+    s_d = torch.from_numpy(src).to(dev)
+    t_d = torch.from_numpy(tgt).to(dev)
+    v_d = torch.from_numpy(vals).to(dev)
+    out = torch.empty(n_tgt, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def step(precision, record):
+        op = dtk.MovingLeastSquaresOperator(None, s_d, t_d, RBF, BASIS, k=k, precision=precision)
+        op.apply(v_d, out)
+        if record is not None:
+            record.append((op.stage_times_ms, op.rotations, op.rotations_fp32, op.nnz))
+        return op
+
+    def timed(precision, steps, warmup):
+        for _ in range(warmup):
+            step(precision, None)
+        rec = []
+        barrier()
+        launches0 = dtk.kernel_launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(dev.index) as clk:
+            e0.record(stream)
+            for _ in range(steps):
+                step(precision, rec)
+            e1.record(stream)
+            barrier()
+        launches = (dtk.kernel_launch_count() - launches0) // steps
+        ms = max_over_ranks(e0.elapsed_time(e1) / steps)
+        return ms, rec, clk.summary(), launches
+
+    # -- headline: mixed form, inputs resident ---------------------------------
+    ms_mixed, rec_mixed, clocks, launches = timed("mixed", args.steps, args.warmup)
+    # -- FP64 form on the same inputs -------------------------------------------
+    ms_fp64, rec_fp64, clocks64, _ = timed("fp64", max(2, args.steps // 2), 1)
+
+    # -- accuracy vs the FP64 oracle on a sample of targets ----------------------
+    acc = {}
+    cpu = None
+    if rank == 0:
+        cpu = cpu_oracle_run(src, tgt, vals, rbf, basis_id, k, args.sample)
+    for name, field in (("smooth", vals), ("front", front)):
+        f_d = torch.from_numpy(field).to(dev)
+        res = {}
+        for prec in ("mixed", "fp64"):
+            op = dtk.MovingLeastSquaresOperator(None, s_d, t_d, RBF, BASIS, k=k, precision=prec)
+            op.apply(f_d, out)
+            res[prec] = out[: args.sample].cpu().numpy()
+            if prec == "fp64":
+                off, idx, _ = op.csr()
+        if rank == 0:
+            from oracle import cpu as ocpu
+            sub = tgt[: args.sample]
+            o_off, o_idx, _ = ocpu.knn(src, sub, k)
+            same = np.array_equal(idx[: len(o_idx)].cpu().numpy(), o_idx)
+            coeff, _, _, _ = ocpu.mls_coefficients(src, sub, o_off, o_idx, rbf, basis_id)
+            y_ref = ocpu.apply(o_off, o_idx, coeff, field)
+            nrm = np.linalg.norm(y_ref)
+            acc[name] = {prec: float(np.linalg.norm(res[prec] - y_ref) / nrm) for prec in res}
+            acc["neighbours_bit_exact"] = bool(same)
+
+    # -- e2e through the public API with host buffers -----------------------------
+    src_h = torch.from_numpy(src).pin_memory()
+    tgt_h = torch.from_numpy(tgt).pin_memory()
+    val_h = torch.from_numpy(vals).pin_memory()
+    out_h = torch.empty(n_tgt, dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        s = src_h.to(dev, non_blocking=True)
+        t = tgt_h.to(dev, non_blocking=True)
+        v = val_h.to(dev, non_blocking=True)
+        o = torch.empty(n_tgt, dtype=torch.float64, device=dev)
+        op = dtk.MovingLeastSquaresOperator(None, s, t, RBF, BASIS, k=k, precision="mixed")
+        op.apply(v, o)
+        out_h.copy_(o, non_blocking=True)
+
+    for _ in range(max(1, args.warmup - 1)):
+        e2e_step()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    ms_e2e = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+
+    if rank != 0:
+        return
+    # -- roofline of the dominant kernel (the mixed setup kernel) ----------------
+    setup_ms = float(np.mean([r[0][1] for r in rec_mixed]))
+    search_ms = float(np.mean([r[0][0] for r in rec_mixed]))
+    rot64 = float(np.mean([r[1] for r in rec_mixed]))
+    flops = mixed_form_flops(n_tgt, k, m, rot64)
+    achieved = flops / (setup_ms / 1e3) / 1e12
+    peak = measure_fp64_peak(torch, dev)
+    traffic_pt = read_profile_traffic()
+    setup64_ms = float(np.mean([r[0][1] for r in rec_fp64]))
+    rot_fp64_form = float(np.mean([r[1] for r in rec_fp64]))
+    flops64 = fp64_form_flops(n_tgt, k, m, rot_fp64_form)
+    total_targets = n_tgt * world
+    value = total_targets / (ms_mixed / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded U[0,1]^3 clouds)",
+        "config": {"workload": args.workload, "n_sources": len(src), "n_targets_per_gpu": n_tgt,
+                   "basis": "Quadratic3", "rbf": RBF_NAMES[rbf], "k": k, "form": "mixed",
+                   "l2_flush": "inputs larger than L2 (192 MB coordinates per cloud)"},
+        "fp64_form": {"value": total_targets / (ms_fp64 / 1e3), "ms_per_step": ms_fp64,
+                      "setup_ms": setup64_ms,
+                      "setup_fp64_tflops": flops64 / (setup64_ms / 1e3) / 1e12},
+        "mixed_over_fp64": ms_fp64 / ms_mixed,
+        "accuracy_vs_fp64_oracle": acc,
+        "stages_ms": {"search": search_ms, "setup": setup_ms,
+                      "apply": ms_mixed - search_ms - setup_ms},
+        "roofline": {"bound": "fp64", "kernel": "k_setup_mixed<10>",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "peak_source": "measured cuBLAS DGEMM 4096^3 in this run",
+                     "traffic": (traffic_pt * n_tgt) if traffic_pt else None},
+        "e2e": {"value": total_targets / (ms_e2e / 1e3), "unit": UNIT,
+                "h2d_bytes_per_step": int(src_h.numel() * 8 + tgt_h.numel() * 8 + val_h.numel() * 8),
+                "d2h_bytes_per_step": int(out_h.numel() * 8)},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = {
+            "value": cpu["value"], "unit": UNIT, "cores": cpu["threads"], "kind": "port",
+            "sample": (f"full {len(src)}-source grid index build + {cpu['sample']} of {n_tgt} "
+                       "targets (kNN, FP64 setup, apply), extrapolated to the full target set")}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -6,9 +6,9 @@ DataTransferKit's operator API.  There is no CPU fallback.
 """
 from .operators import (FP64, MIXED, Buhmann, Constant, Linear, MovingLeastSquaresOperator,
                         MultivariatePolynomialBasis, PointCloudOperator, Quadratic, Wendland, Wu,
-                        knn_search, svd_pinv)
+                        kernel_launch_count, knn_search, svd_pinv)
 from ._capi import DTKError, InvalidArgument, Unsupported
 
 __all__ = ["MovingLeastSquaresOperator", "PointCloudOperator", "MultivariatePolynomialBasis",
            "Constant", "Linear", "Quadratic", "Wendland", "Wu", "Buhmann", "FP64", "MIXED",
-           "knn_search", "svd_pinv", "DTKError", "InvalidArgument", "Unsupported"]
+           "knn_search", "svd_pinv", "kernel_launch_count", "DTKError", "InvalidArgument", "Unsupported"]

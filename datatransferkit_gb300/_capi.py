@@ -24,6 +24,7 @@ EXPORTED = [
     "dtk_mls_get_stage_times", "dtk_mls_get_rotation_count", "dtk_mls_destroy",
     "dtk_knn_search", "dtk_svd_pinv", "dtk_mls_batch_create", "dtk_mls_batch_apply",
     "dtk_mls_batch_get_csr", "dtk_mls_batch_destroy", "dtk_last_error", "dtk_status_string",
+    "dtk_kernel_launch_count",
 ]
 
 
@@ -67,7 +68,8 @@ def _declare(L):
     L.dtk_mls_get_sizes.argtypes = [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)]
     L.dtk_mls_underdetermined_count.argtypes = [_vp, C.POINTER(_i64)]
     L.dtk_mls_get_stage_times.argtypes = [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
-    L.dtk_mls_get_rotation_count.argtypes = [_vp, C.POINTER(_i64)]
+    L.dtk_mls_get_rotation_count.argtypes = [_vp, C.POINTER(_i64), C.POINTER(_i64)]
+    L.dtk_kernel_launch_count.argtypes = []
     L.dtk_mls_destroy.argtypes = [_vp]
     L.dtk_knn_search.argtypes = [_vp, _i64, _i64, _i64, _vp, _i64, _i64, _i64, C.c_int32, _vp, _vp, _vp]
     L.dtk_svd_pinv.argtypes = [C.c_int32, _i64, _vp, _vp, C.POINTER(_i64), _vp]
@@ -83,6 +85,7 @@ def _declare(L):
     for name in EXPORTED:
         if name not in ("dtk_last_error", "dtk_status_string", "dtk_mls_default_options"):
             getattr(L, name).restype = C.c_int
+    L.dtk_kernel_launch_count.restype = _i64
 
 
 def lib():

@@ -23,6 +23,12 @@ thread_local std::string g_error;
 
 void set_error( std::string const &msg ) { g_error = msg; }
 
+long long &launch_counter()
+{
+    static long long n = 0;
+    return n;
+}
+
 template <class F>
 dtk_status guarded( F &&f )
 {
@@ -129,7 +135,7 @@ struct dtk_mls_s
     dtk::DeviceBuffer<double> src_copy, tgt_copy; // packed n x 3 (adjoint)
     dtk::DeviceBuffer<int32_t> t_offset, t_entry, entry_row;
     int64_t underdetermined = 0;
-    int64_t rotations = 0;
+    int64_t rotations = 0, rotations32 = 0;
     float search_ms = 0.f, setup_ms = 0.f;
 };
 
@@ -203,9 +209,9 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
             }
         } evg{ev};
         DeviceBuffer<unsigned> status( 1, s );
-        DeviceBuffer<unsigned long long> counters( 2, s );
+        DeviceBuffer<unsigned long long> counters( 3, s );
         DTK_CUDA_OR_THROW( cudaMemsetAsync( status.get(), 0, sizeof( unsigned ), s ) );
-        DTK_CUDA_OR_THROW( cudaMemsetAsync( counters.get(), 0, 2 * sizeof( unsigned long long ), s ) );
+        DTK_CUDA_OR_THROW( cudaMemsetAsync( counters.get(), 0, 3 * sizeof( unsigned long long ), s ) );
         DTK_CUDA_OR_THROW( cudaEventRecord( ev[0], s ) );
 
         // --- search (ArborX tree + query, def.hpp:114-129) ---
@@ -262,6 +268,7 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
         a.rows_sorted = !g.radius_mode;
         a.underdetermined = counters.get();
         a.rotations = counters.get() + 1;
+        a.rotations32 = counters.get() + 2;
         a.status = status.get();
         if ( g.opts.precision == DTK_FP64 )
         {
@@ -278,7 +285,7 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
         DTK_CUDA_OR_THROW( cudaEventRecord( ev[2], s ) );
 
         unsigned st = 0;
-        unsigned long long cnt[2] = {0, 0};
+        unsigned long long cnt[3] = {0, 0, 0};
         DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, status.get(), sizeof( unsigned ),
                                             cudaMemcpyDeviceToHost, s ) );
         DTK_CUDA_OR_THROW( cudaMemcpyAsync( cnt, counters.get(), sizeof( cnt ),
@@ -292,6 +299,7 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
             throw Error{DTK_ERR_INTERNAL, "search traversal reported an internal error"};
         h->underdetermined = (int64_t)cnt[0];
         h->rotations = (int64_t)cnt[1];
+        h->rotations32 = (int64_t)cnt[2];
         DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->search_ms, ev[0], ev[1] ) );
         DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->setup_ms, ev[1], ev[2] ) );
         *out = guard.release();
@@ -367,13 +375,19 @@ dtk_status dtk_mls_get_stage_times( dtk_mls_handle h, float *search_ms, float *s
     } );
 }
 
-dtk_status dtk_mls_get_rotation_count( dtk_mls_handle h, int64_t *rotations )
+dtk_status dtk_mls_get_rotation_count( dtk_mls_handle h, int64_t *rotations,
+                                       int64_t *rotations_fp32 )
 {
     return guarded( [&] {
-        DTK_REQUIRE_OR_THROW( h != nullptr && rotations != nullptr, "null argument" );
-        *rotations = h->rotations;
+        DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
+        if ( rotations )
+            *rotations = h->rotations;
+        if ( rotations_fp32 )
+            *rotations_fp32 = h->rotations32;
     } );
 }
+
+int64_t dtk_kernel_launch_count( void ) { return launch_counter(); }
 
 dtk_status dtk_mls_destroy( dtk_mls_handle h )
 {

@@ -88,9 +88,13 @@ struct DeviceBuffer
     T *get() const { return ptr; }
 };
 
-// Launch-error check after a kernel launch.
+// Running count of this library's kernel launches (diagnostics).
+long long &launch_counter();
+
+// Launch-error check after a kernel launch (also counts the launch).
 inline void check_launch( char const *what )
 {
+    ++launch_counter();
     cudaError_t e = cudaGetLastError();
     if ( e != cudaSuccess )
         throw Error{DTK_ERR_CUDA, std::string( what ) + ": " + cudaGetErrorString( e )};
@@ -307,7 +311,8 @@ struct SetupArgs
     double *coeff64;      // FP64 form output
     float *coeff32;       // mixed form output
     unsigned long long *underdetermined;
-    unsigned long long *rotations;
+    unsigned long long *rotations;     // FP64 Jacobi rotations
+    unsigned long long *rotations32;   // FP32 Jacobi rotations (mixed form)
     unsigned *status;
 };
 void setup_fp64( SetupArgs const &a, cudaStream_t s );

@@ -1,14 +1,6 @@
 // Entry points whose kernels are not built yet: they report DTK_ERR_UNSUPPORTED.
 #include "dtk_common.cuh"
 
-namespace dtk
-{
-void setup_mixed( SetupArgs const &, cudaStream_t )
-{
-    throw Error{DTK_ERR_UNSUPPORTED, "the mixed precision form is not built yet"};
-}
-} // namespace dtk
-
 extern "C" {
 dtk_status dtk_mls_apply_adjoint( dtk_mls_handle, const double *, int64_t, const double *, double *,
                                   double *, dtk_stream_t )

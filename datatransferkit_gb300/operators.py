@@ -227,8 +227,16 @@ class MovingLeastSquaresOperator(PointCloudOperator):
 
     @property
     def rotations(self) -> int:
+        """FP64 Jacobi rotations performed by the setup."""
         n = C.c_int64()
-        check(lib().dtk_mls_get_rotation_count(self._h, C.byref(n)))
+        check(lib().dtk_mls_get_rotation_count(self._h, C.byref(n), None))
+        return n.value
+
+    @property
+    def rotations_fp32(self) -> int:
+        """FP32 Jacobi rotations performed by the setup (mixed form)."""
+        n = C.c_int64()
+        check(lib().dtk_mls_get_rotation_count(self._h, None, C.byref(n)))
         return n.value
 
     @property
@@ -266,6 +274,11 @@ def _from_device(ptr: int, n: int, dtype) -> torch.Tensor:
         return torch.empty(0, dtype=dtype, device="cuda")
     view = torch.as_tensor(_DeviceArray(ptr, n, _TYPESTR[dtype]), device="cuda")
     return view.clone()
+
+
+def kernel_launch_count() -> int:
+    """Kernels the library has launched so far in this process."""
+    return int(lib().dtk_kernel_launch_count())
 
 
 def knn_search(source_points: torch.Tensor, target_points: torch.Tensor, k: int, stream=None):

@@ -140,8 +140,14 @@ dtk_status dtk_mls_underdetermined_count(dtk_mls_handle h, int64_t *count);
 dtk_status dtk_mls_get_stage_times(dtk_mls_handle h, float *search_ms,
                                    float *setup_ms);
 
-/* Number of Jacobi rotations the last create performed (FP64 flop counts). */
-dtk_status dtk_mls_get_rotation_count(dtk_mls_handle h, int64_t *rotations);
+/* Jacobi rotations the create performed, in FP64 and (mixed form) in FP32;
+ * the basis of the FLOP counts in the benchmark.  Either pointer may be NULL. */
+dtk_status dtk_mls_get_rotation_count(dtk_mls_handle h, int64_t *rotations,
+                                      int64_t *rotations_fp32);
+
+/* Running count of the kernels this library has launched in the process
+ * (diagnostics; not a reference interface). */
+int64_t dtk_kernel_launch_count(void);
 
 dtk_status dtk_mls_destroy(dtk_mls_handle h);
 

@@ -1,0 +1,132 @@
+"""Mixed FP32/FP64 form against the FP64 oracle.
+
+Tolerance: relative L2 error of the transferred field <= 1e-6 against the
+FP64 oracle (the reference algorithm) on the benchmark neighbourhoods
+(k = 20/32, quadratic basis), for a smooth field and for a tanh front of
+width 0.01.  Neighbour sets are the same bit-exact search as the FP64 form.
+The reference's known-answer layouts check polynomial reproduction with the
+mixed form's FP32 resolution (1e-5 relative).
+"""
+import numpy as np
+import pytest
+import torch
+
+import datatransferkit_gb300 as dtk
+from datatransferkit_gb300 import synthetic as syn
+from oracle import cpu
+
+pytestmark = pytest.mark.gpu
+MIXED_TOL = 1e-6
+Q = dtk.MultivariatePolynomialBasis(dtk.Quadratic, 3)
+L = dtk.MultivariatePolynomialBasis(dtk.Linear, 3)
+C = dtk.MultivariatePolynomialBasis(dtk.Constant, 3)
+RBF = [dtk.Wendland(0), dtk.Wendland(2), dtk.Wendland(4), dtk.Wendland(6), dtk.Wu(2), dtk.Wu(4),
+       dtk.Buhmann(2), dtk.Buhmann(3), dtk.Buhmann(4)]
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def transfer(src, tgt, vals, rbf, basis, k=None, radius=None, precision="mixed"):
+    op = dtk.MovingLeastSquaresOperator(None, dev(src), dev(tgt), rbf, basis, k=k, radius=radius,
+                                        precision=precision)
+    out = torch.full((len(tgt),), np.nan, dtype=torch.float64, device="cuda")
+    op.apply(dev(vals), out)
+    return out.cpu().numpy(), op
+
+
+def rel_l2(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("field", ["smooth", "front"])
+@pytest.mark.parametrize("density,rbf_id,k", [(8_000_000, 2, 32), (2_000_000, 1, 32),
+                                              (2_000_000, 1, 20)])
+def test_mixed_at_benchmark_density(field, density, rbf_id, k):
+    side = 0.1
+    n = int(density * side ** 3)
+    src = 0.45 + syn.uniform_points(n, 100 + k) * side
+    tgt = 0.47 + syn.uniform_points(3000, 200 + k) * 0.06
+    f = syn.smooth_field if field == "smooth" else syn.front_field
+    vals = f(src)
+    y, op = transfer(src, tgt, vals, RBF[rbf_id], Q, k=k)
+    ref = cpu.mls_transfer(src, tgt, vals, rbf_id, 2, k=k)
+    _, idx, _ = op.csr()
+    assert np.array_equal(idx.cpu().numpy(), ref["idx"])
+    err = rel_l2(y, ref["target"])
+    assert err <= MIXED_TOL, err
+    assert op.underdetermined == 0
+
+
+def test_mixed_uniform_unit_cube():
+    src = syn.uniform_points(200000, 6)
+    tgt = syn.uniform_points(20000, 7)
+    for f in (syn.smooth_field, syn.front_field):
+        vals = f(src)
+        y, _ = transfer(src, tgt, vals, RBF[2], Q, k=32)
+        ref = cpu.mls_transfer(src, tgt, vals, 2, 2, k=32)
+        assert rel_l2(y, ref["target"]) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("rbf_id", range(9))
+def test_mixed_all_rbfs_quadratic_k32(rbf_id):
+    src = syn.uniform_points(30000, 10 + rbf_id)
+    tgt = syn.uniform_points(5000, 30 + rbf_id)
+    vals = syn.smooth_field(src)
+    y, _ = transfer(src, tgt, vals, RBF[rbf_id], Q, k=32)
+    ref = cpu.mls_transfer(src, tgt, vals, rbf_id, 2, k=32)
+    assert rel_l2(y, ref["target"]) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("basis,basis_id,k", [(L, 1, 8), (L, 1, 16), (C, 0, 4)])
+def test_mixed_linear_and_constant(basis, basis_id, k):
+    src = syn.uniform_points(30000, 50)
+    tgt = syn.uniform_points(5000, 51)
+    vals = syn.smooth_field(src)
+    y, _ = transfer(src, tgt, vals, RBF[1], basis, k=k)
+    ref = cpu.mls_transfer(src, tgt, vals, 1, basis_id, k=k)
+    assert rel_l2(y, ref["target"]) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("basis_id", [0, 1, 2])
+def test_mixed_polynomial_reproduction(basis_id):
+    basis = [C, L, Q][basis_id]
+    f = syn.polynomial_of_basis(basis.size)
+    src = syn.grid_points((40, 40, 1), (0.0, 0.0, 0.0))
+    tgt = syn.grid_points((1, 1, 1), (19.0, 19.0, 0.0))
+    y, _ = transfer(src, tgt, f(src), RBF[0], basis)
+    np.testing.assert_allclose(y, f(tgt), rtol=1e-5)
+    src = syn.grid_points((40, 1, 1), (0.0, 0.0, 0.0))
+    tgt = syn.grid_points((39, 1, 1), (0.5, 0.0, 0.0))
+    y, op = transfer(src, tgt, f(src), RBF[0], basis)
+    np.testing.assert_allclose(y, f(tgt), rtol=1e-5)
+    if basis_id:
+        assert op.underdetermined == len(tgt)  # y and z columns vanish on a line
+    src = syn.uniform_points(20000, 3)
+    tgt = syn.uniform_points(2000, 4)
+    y, _ = transfer(src, tgt, f(src), RBF[2], basis, k=32)
+    np.testing.assert_allclose(y, f(tgt), rtol=1e-5, atol=1e-5)
+
+
+def test_mixed_radius_mode():
+    src = syn.gaussian_mixture(20000, 80)
+    tgt = syn.uniform_points(4000, 81)
+    vals = syn.smooth_field(src)
+    y, op = transfer(src, tgt, vals, RBF[1], Q, radius=0.05)
+    ref = cpu.mls_transfer(src, tgt, vals, 1, 2, r=0.05)
+    off, _, _ = op.csr()
+    assert np.array_equal(off.cpu().numpy(), ref["offset"])
+    rows = np.diff(ref["offset"])
+    well = rows >= 20  # rows with enough neighbours for a quadratic fit
+    assert rel_l2(y[well], ref["target"][well]) <= MIXED_TOL
+    assert np.all(np.isfinite(y))
+
+
+def test_mixed_coefficients_are_fp32():
+    src = syn.uniform_points(5000, 1)
+    tgt = syn.uniform_points(100, 2)
+    _, op = transfer(src, tgt, syn.smooth_field(src), RBF[2], Q, k=32)
+    _, _, coeff = op.csr()
+    assert coeff.dtype == torch.float32
+    assert op.rotations > 0 and op.rotations_fp32 > 0
