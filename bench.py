@@ -42,6 +42,7 @@ WORKLOADS = {
     # name: (n_src, n_tgt, src_seed, tgt_seed, rbf, basis, k)
     "mixed_8m": (8_000_000, 8_000_000, 6, 7, 2, 2, 32),
     "fp64_2m": (2_000_000, None, 3, 4, 1, 2, 32),  # 126^3 jittered-grid targets
+    "mixed_1m": (1_000_000, 1_000_000, 6, 7, 2, 2, 32),  # profiling size (ncu captures)
 }
 RBF_NAMES = {1: "Wendland<2>", 2: "Wendland<4>"}
 
@@ -54,6 +55,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="mixed_8m", choices=sorted(WORKLOADS))
     ap.add_argument("--sample", type=int, default=20000, help="targets in the CPU/oracle sample")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run only the timed steps of both forms (for profiler captures)")
     return ap.parse_args()
 
 
@@ -135,11 +138,13 @@ def fp64_form_flops(n_tgt, k, m, rotations):
 
 
 def mixed_form_flops(n_tgt, k, m, rotations64):
-    """Mixed form, FP64 part only: per target the centring/scaling
-    2 passes x k x 6, B = V32^T A V32 (2 m^3 + m^2 (m+1)), row 0 (2 m^2 + m),
-    the radius ~10; per FP64 rotation 12 m + 16."""
+    """Mixed form, FP64 part only.  Per target: the centring/scaling in three
+    passes 3 x k x 6; B = V32^T A V32, 2 m^3 + m^2 (m+1); row 0, 2 m^2; the
+    refinement residual k (4m + 7) and its solve 4 m^2 + m; the coefficient
+    dot products k (2m + 7); the radius ~10.  Per FP64 rotation 12 m + 16."""
     per_rot = 12 * m + 16
-    per_tgt = 2 * k * 6 + 2 * m ** 3 + m * m * (m + 1) + 2 * m * m + m + 10
+    per_tgt = (3 * k * 6 + 2 * m ** 3 + m * m * (m + 1) + 2 * m * m + k * (4 * m + 7)
+               + 4 * m * m + m + k * (2 * m + 7) + 10)
     return rotations64 * per_rot + n_tgt * per_tgt
 
 
@@ -176,22 +181,34 @@ def read_profile_traffic():
 # CPU oracle timing (bounded sample)
 # ---------------------------------------------------------------------------
 def cpu_oracle_run(src, tgt, vals, rbf, basis, k, sample):
+    """Time the FP64 CPU oracle (all host threads) on a sample of the targets.
+
+    The index build over all sources is timed on its own (warm, best of two),
+    the per-target work (kNN query, setup, apply) on `sample` targets; the
+    returned value extrapolates to the full target set:
+    n_targets / (t_build + n_targets * t_per_target).
+    """
     from oracle import cpu
     threads = cpu.max_threads()
     sub = tgt[:sample]
-    t0 = time.perf_counter()
-    cpu.knn(src, tgt[:1], k)  # index build alone
-    t_build = time.perf_counter() - t0
+    cpu.knn(src[:1000], tgt[:10], k)  # load and warm the library
+    t_build = float("inf")
+    for _ in range(2):
+        t0 = time.perf_counter()
+        cpu.knn(src, tgt[:1], k)
+        t_build = min(t_build, time.perf_counter() - t0)
     t0 = time.perf_counter()
     off, idx, _ = cpu.knn(src, sub, k)
+    t_knn = time.perf_counter() - t0
+    t0 = time.perf_counter()
     coeff, _, _, _ = cpu.mls_coefficients(src, sub, off, idx, rbf, basis)
     y = cpu.apply(off, idx, coeff, vals)
-    t_total = time.perf_counter() - t0
-    per_target = max(t_total - t_build, 1e-9) / len(sub)
+    t_setup = time.perf_counter() - t0
+    per_target = (max(t_knn - t_build, 0.0) + t_setup) / len(sub)
     n_full = len(tgt)
     value = n_full / (t_build + n_full * per_target)
-    return dict(value=value, threads=threads, t_build=t_build, t_sample=t_total, y=y,
-                sample=len(sub))
+    return dict(value=value, threads=threads, t_build=t_build, t_knn=t_knn, t_setup=t_setup,
+                y=y, sample=len(sub))
 
 
 # ---------------------------------------------------------------------------
@@ -291,6 +308,11 @@ def run_ours(args, rank, world, local_rank):
     ms_mixed, rec_mixed, clocks, launches = timed("mixed", args.steps, args.warmup)
     # -- FP64 form on the same inputs -------------------------------------------
     ms_fp64, rec_fp64, clocks64, _ = timed("fp64", max(2, args.steps // 2), 1)
+    if args.profile_only:
+        if rank == 0:
+            print(json.dumps({"profile_only": True, "ms_mixed": ms_mixed, "ms_fp64": ms_fp64,
+                              "workload": args.workload}), flush=True)
+        return
 
     # -- accuracy vs the FP64 oracle on a sample of targets ----------------------
     acc = {}

@@ -17,14 +17,18 @@
 //     lambda_max is dropped (the scaled moments are well conditioned, cond
 //     ~1e3-1e4 at the benchmark densities, so only geometric rank deficiency
 //     falls below it);
-//   * coefficients c_j = phi_j (row0^ . P(x^_j)) in FP32, stored in FP32.
-// Row 0 of the pseudo-inverse is assembled without forming it:
-//   row0^ = W L^+ W^T e0 = sum_k W_0k W_:k / lambda_k.
+//   * one FP64 iterative-refinement step of row 0 of the pseudo-inverse
+//     against the exact residual e0 - sum_j phi_j P_j (P_j . a) (the basis
+//     of FP32 coordinates is exact in FP64), which removes the FP32
+//     assembly error (the step contracts it by ~cond(A^) * 2^-24);
+//   * coefficients c_j = phi_j (P(x^_j) . a), stored in FP32.
+// Row 0 of the pseudo-inverse is applied without forming it:
+//   A^+ v = W L^+ W^T v.
 // GB300 issues one FP64 warp instruction per 64 cycles per SM sub-partition,
 // so all Jacobi state lives in shared memory (thread-interleaved, 1640 B per
 // thread at M = 10: four warps per SM, one per sub-partition) and the FP64
-// work is what sets the time: ~9k FP64 operations per target against ~57k for
-// the FP64 form's reference Jacobi.
+// work is what sets the time: ~11k FP64 operations per target against ~57k
+// for the FP64 form's reference Jacobi.
 #include "dtk_common.cuh"
 
 namespace dtk
@@ -239,46 +243,92 @@ __global__ void __launch_bounds__( MB )
                 break;
         }
 
-        // truncation relative to the scaled spectrum; row0^ = W L^+ W^T e0
+        // truncation relative to the scaled spectrum: keep 1/lambda_k (or 0)
+        // on the diagonal of B for the pseudo-inverse A^+ = W L^+ W^T
         double lmax = 0.0;
         for ( int k = 0; k < M; ++k )
             lmax = fmax( lmax, fabs( B( ut<M>( k, k ) ) ) );
         double const cut = lmax * 9.5367431640625e-07; // 2^-20
-        double row0d[M];
-#pragma unroll
-        for ( int a = 0; a < M; ++a )
-            row0d[a] = 0.0;
         for ( int k = 0; k < M; ++k )
         {
             double const lk = B( ut<M>( k, k ) );
             if ( fabs( lk ) > cut && lk != 0.0 )
-            {
-                double const gk = W( 0, k ) / lk;
-#pragma unroll
-                for ( int a = 0; a < M; ++a )
-                    row0d[a] = fma( W( a, k ), gk, row0d[a] );
-            }
+                B( ut<M>( k, k ) ) = 1.0 / lk;
             else
+            {
+                B( ut<M>( k, k ) ) = 0.0;
                 dropped = 1;
+            }
         }
-        float row0[M];
+        // y += A^+ v (FP64), one eigen-direction at a time
+        auto pinv_add = [&]( double const *v, double *y ) {
+            for ( int k = 0; k < M; ++k )
+            {
+                double acc = 0.0;
 #pragma unroll
-        for ( int a = 0; a < M; ++a )
-            row0[a] = (float)row0d[a];
+                for ( int r = 0; r < M; ++r )
+                    acc = fma( W( r, k ), v[r], acc );
+                acc *= B( ut<M>( k, k ) );
+#pragma unroll
+                for ( int r = 0; r < M; ++r )
+                    y[r] = fma( W( r, k ), acc, y[r] );
+            }
+        };
+        double a[M];
+#pragma unroll
+        for ( int r = 0; r < M; ++r )
+            a[r] = 0.0;
+        for ( int k = 0; k < M; ++k )
+        {
+            double const g = W( 0, k ) * B( ut<M>( k, k ) );
+#pragma unroll
+            for ( int r = 0; r < M; ++r )
+                a[r] = fma( W( r, k ), g, a[r] );
+        }
 
-        // coefficients (FP32)
+        // One FP64 refinement step of row 0: the FP32 moments carry
+        // ~cond * 6e-8 relative error; the residual r = e0 - sum_j phi_j
+        // P_j (P_j . a) is exact up to FP64 rounding (P of the FP32
+        // coordinates is exact in FP64, phi_j is the FP32 weight), and
+        // a += A32^+ r contracts the error by ~cond(A^) * 2^-24.
+        {
+            double r[M];
+#pragma unroll
+            for ( int q = 0; q < M; ++q )
+                r[q] = q == 0 ? 1.0 : 0.0;
+            for ( int j = 0; j < len; ++j )
+            {
+                float x, y, z;
+                scaled( j, x, y, z );
+                double P[M];
+                basis_eval<M, double>( (double)x, (double)y, (double)z, P );
+                double const phi = (double)rbf_eval<float>( rbf, sqrtf( x * x + y * y + z * z ) );
+                double dot = 0.0;
+#pragma unroll
+                for ( int q = 0; q < M; ++q )
+                    dot = fma( P[q], a[q], dot );
+                double const w = phi * dot;
+#pragma unroll
+                for ( int q = 0; q < M; ++q )
+                    r[q] = fma( -w, P[q], r[q] );
+            }
+            pinv_add( r, a );
+        }
+
+        // coefficients c_j = phi_j (P_j . a): FP64 dot of exact FP64 basis
+        // values of the FP32 coordinates, stored in FP32
         for ( int j = 0; j < len; ++j )
         {
             float x, y, z;
             scaled( j, x, y, z );
-            float P[M];
-            basis_eval<M, float>( x, y, z, P );
+            double P[M];
+            basis_eval<M, double>( (double)x, (double)y, (double)z, P );
             float const phi = rbf_eval<float>( rbf, sqrtf( x * x + y * y + z * z ) );
-            float acc = 0.f;
+            double dot = 0.0;
 #pragma unroll
-            for ( int a = 0; a < M; ++a )
-                acc = fmaf( row0[a], P[a], acc );
-            coeff[b + j] = acc * phi;
+            for ( int q = 0; q < M; ++q )
+                dot = fma( P[q], a[q], dot );
+            coeff[b + j] = (float)( dot * (double)phi );
         }
     }
     unsigned long long it64 = rotations, it32 = rotations32, dr64 = dropped;
