@@ -275,11 +275,12 @@ struct Lbvh
     int64_t n_leaves = 0; // ceil(n / 32)
     double lo[3], hi[3];  // scene bounds (host copy)
     DeviceBuffer<double> sx, sy, sz;  // Morton-sorted coordinates
+    DeviceBuffer<float> fx, fy, fz;   // the same, centred on the scene box, FP32
     DeviceBuffer<uint32_t> codes;     // sorted Morton codes
     DeviceBuffer<uint32_t> perm;      // sorted position -> original index
     DeviceBuffer<float4> nodes;       // 4 float4 per internal node
     DeviceBuffer<float4> root_box;    // box of the whole tree (2 float4)
-    DeviceBuffer<double> scene;       // device copy of lo/hi (6 doubles)
+    DeviceBuffer<double> scene;       // lo[3], Morton scale[3], hi[3], centre[3], bound S
 };
 
 void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s );

@@ -119,10 +119,12 @@ __global__ void __launch_bounds__( BND_THREADS )
     }
 }
 
-// scene[0..2] = lo, scene[3..5] = 1024/extent (0 when flat), scene[6..8] = hi
+// scene[0..2] = lo, scene[3..5] = 1024/extent (0 when flat), scene[6..8] = hi,
+// scene[9..11] = centre c, scene[12] = S >= max_i,d |p_id - c_d| (with slack)
 __global__ void k_bounds_final( unsigned long long const *partial, int nblocks,
                                 double *scene )
 {
+    __shared__ double half[3];
     if ( threadIdx.x < 3 )
     {
         int const d = threadIdx.x;
@@ -137,7 +139,13 @@ __global__ void k_bounds_final( unsigned long long const *partial, int nblocks,
         scene[d] = lo;
         scene[3 + d] = e > 0.0 ? 1024.0 / e : 0.0;
         scene[6 + d] = hi;
+        double const c = 0.5 * lo + 0.5 * hi;
+        scene[9 + d] = c;
+        half[d] = fmax( hi - c, c - lo );
     }
+    __syncthreads();
+    if ( threadIdx.x == 0 )
+        scene[12] = fmax( half[0], fmax( half[1], half[2] ) ) * ( 1.0 + 1e-6 ) + 1e-300;
 }
 
 __global__ void k_morton( PointsView p, double const *scene, uint32_t *codes,
@@ -151,16 +159,21 @@ __global__ void k_morton( PointsView p, double const *scene, uint32_t *codes,
     }
 }
 
-__global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double *sx,
-                                 double *sy, double *sz )
+__global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double const *scene,
+                                 double *sx, double *sy, double *sz, float *fx, float *fy,
+                                 float *fz )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i < p.n )
     {
         int64_t const o = perm[i];
-        sx[i] = p( o, 0 );
-        sy[i] = p( o, 1 );
-        sz[i] = p( o, 2 );
+        double const x = p( o, 0 ), y = p( o, 1 ), z = p( o, 2 );
+        sx[i] = x;
+        sy[i] = y;
+        sz[i] = z;
+        fx[i] = (float)( x - scene[9] );
+        fy[i] = (float)( y - scene[10] );
+        fz[i] = (float)( z - scene[11] );
     }
 }
 
@@ -265,8 +278,9 @@ __device__ __forceinline__ Box load_child_box( float4 const *nodes, int parent, 
 
 // One thread per leaf: leaf box, then walk up; the second child to arrive at
 // a node computes its box and continues.
-__global__ void k_refit( double const *sx, double const *sy, double const *sz, int64_t n,
-                         int64_t nl, int const *left, int const *right,
+__global__ void k_refit( double const *sx, double const *sy, double const *sz,
+                         double const *scene, int64_t n, int64_t nl, int const *left,
+                         int const *right,
                          int const *parent_node, int const *parent_leaf, float4 *nodes,
                          unsigned *flags, float4 *root_box, unsigned *status )
 {
@@ -286,12 +300,14 @@ __global__ void k_refit( double const *sx, double const *sy, double const *sz, i
             hi[d] = fmax( hi[d], c[d] );
         }
     }
+    // centred FP32 box, rounded outward and widened by one FP32 ulp so that
+    // it contains the exact centred coordinates despite the FP64 subtraction
     Box b;
 #pragma unroll
     for ( int d = 0; d < 3; ++d )
     {
-        b.lo[d] = __double2float_rd( lo[d] );
-        b.hi[d] = __double2float_ru( hi[d] );
+        b.lo[d] = nextafterf( __double2float_rd( lo[d] - scene[9 + d] ), -INFINITY );
+        b.hi[d] = nextafterf( __double2float_ru( hi[d] - scene[9 + d] ), INFINITY );
     }
     if ( nl == 1 )
     {
@@ -348,6 +364,7 @@ __global__ void k_pack_children( int64_t n_internal, int const *left, int const 
 struct TreeView
 {
     double const *sx, *sy, *sz;
+    float const *fx, *fy, *fz;
     uint32_t const *codes, *perm;
     float4 const *nodes;
     double const *scene;
@@ -370,11 +387,11 @@ __device__ __forceinline__ float box_lb( float const *lo, float const *hi,
 }
 
 // Upper FP32 threshold for pruning against an FP64 bound (2^-20 margin).
-__device__ __forceinline__ float prune_threshold( double bound_d2 )
+__device__ __forceinline__ float prune_threshold( unsigned long long bound_bits )
 {
-    if ( !( bound_d2 < 1e300 ) )
-        return __int_as_float( 0x7f800000 ); // +inf: prune nothing
-    float const f = __double2float_ru( bound_d2 );
+    if ( bound_bits >= 0x7ff0000000000000ull )
+        return __int_as_float( 0x7f800000 ); // +inf (list not full): prune nothing
+    float const f = __double2float_ru( __longlong_as_double( (long long)bound_bits ) );
     return __fmul_ru( f, 1.0f + 9.5367431640625e-07f );
 }
 
@@ -429,23 +446,72 @@ __device__ __forceinline__ void load_node( float4 const *nodes, int node, float 
     rc = __float_as_int( e.y );
 }
 
+// The query in the centred frame: an FP32 interval [qlo, qhi] certain to
+// contain t - c, its FP32 rounding tf, and the per-axis error bound E of an
+// FP32 coordinate difference: |fl(pf - tf) - (p - t)| <= E for every source
+// (E = 2^-22 (S + T), twice the 2u(|p - c| + |t - c|) bound).
+struct Query
+{
+    double tx, ty, tz;
+    float qlo[3], qhi[3], tf[3];
+    float err;
+};
+
+__device__ __forceinline__ Query make_query( TreeView const &tr, PointsView const &tgt,
+                                             int64_t qi )
+{
+    Query q;
+    q.tx = tgt( qi, 0 );
+    q.ty = tgt( qi, 1 );
+    q.tz = tgt( qi, 2 );
+    double const tc[3] = {q.tx - tr.scene[9], q.ty - tr.scene[10], q.tz - tr.scene[11]};
+    float tmax = 0.f;
+#pragma unroll
+    for ( int d = 0; d < 3; ++d )
+    {
+        q.qlo[d] = nextafterf( __double2float_rd( tc[d] ), -INFINITY );
+        q.qhi[d] = nextafterf( __double2float_ru( tc[d] ), INFINITY );
+        q.tf[d] = (float)tc[d];
+        tmax = fmaxf( tmax, fmaxf( fabsf( q.qlo[d] ), fabsf( q.qhi[d] ) ) );
+    }
+    q.err = ( (float)tr.scene[12] + tmax ) * 2.384185791015625e-07f; // 2^-22
+    return q;
+}
+
+// FP32 bounds lo <= d2(p, t) <= hi for sorted source p (centred FP32 copy).
+__device__ __forceinline__ void d2_bounds( TreeView const &tr, Query const &q, int64_t p,
+                                           float &lo, float &hi )
+{
+    float const dx = __ldg( tr.fx + p ) - q.tf[0];
+    float const dy = __ldg( tr.fy + p ) - q.tf[1];
+    float const dz = __ldg( tr.fz + p ) - q.tf[2];
+    float const d2 = fmaf( dz, dz, fmaf( dy, dy, dx * dx ) );
+    float const spread = q.err * ( 4.f * ( fabsf( dx ) + fabsf( dy ) + fabsf( dz ) ) + 3.f * q.err ) +
+                         d2 * 9.5367431640625e-07f;
+    lo = d2 - spread;
+    hi = d2 + spread;
+}
+
+constexpr int QUEUE = 64;
+
 __global__ void __launch_bounds__( Q_WARPS * 32 )
     k_knn( TreeView tr, PointsView tgt, uint32_t const *order, int k, int row,
            int32_t *idx_out, unsigned *status )
 {
     __shared__ int s_stack[Q_WARPS][STACK];
     __shared__ float s_lb[Q_WARPS][STACK];
+    __shared__ int s_queue[Q_WARPS][QUEUE];
     int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     int64_t const w = blockIdx.x * (int64_t)Q_WARPS + wib;
     if ( w >= tgt.n )
         return;
     int64_t const qi = order ? (int64_t)order[w] : w;
-    double const tx = tgt( qi, 0 ), ty = tgt( qi, 1 ), tz = tgt( qi, 2 );
-    float const qlo[3] = {__double2float_rd( tx ), __double2float_rd( ty ), __double2float_rd( tz )};
-    float const qhi[3] = {__double2float_ru( tx ), __double2float_ru( ty ), __double2float_ru( tz )};
+    Query const q = make_query( tr, tgt, qi );
+    unsigned const lt_mask = ( 1u << lane ) - 1u;
 
-    // Initial candidates: the 32 Morton-sorted sources around the target.
-    uint32_t const code = morton3( tx, ty, tz, tr.scene );
+    // Initial candidates: the 32 Morton-sorted sources around the target,
+    // with exact keys.
+    uint32_t const code = morton3( q.tx, q.ty, q.tz, tr.scene );
     int64_t const pos = warp_lower_bound( tr.codes, tr.n, code, lane );
     int64_t const W = tr.n < 32 ? tr.n : (int64_t)32;
     int64_t s0 = pos - 16;
@@ -459,7 +525,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     {
         int64_t const p = s0 + lane;
         kd = (unsigned long long)__double_as_longlong(
-            dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), tx, ty, tz ) );
+            dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), q.tx, q.ty, q.tz ) );
         ki = (int)__ldg( tr.perm + p );
     }
     // Bitonic sort of the 32 keys across lanes (ascending).
@@ -487,17 +553,19 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     }
     unsigned long long bd = __shfl_sync( FULL, kd, k - 1 );
     int bi = __shfl_sync( FULL, ki, k - 1 );
-    float bound_f = prune_threshold( __longlong_as_double( (long long)bd ) );
+    float bound_f = prune_threshold( bd );
+    int qn = 0; // queued survivors (warp-uniform)
 
-    auto process_leaf = [&]( int leaf ) {
-        int64_t const p = (int64_t)leaf * LEAF + lane;
-        bool const in_window = p >= s0 && p < s0 + W;
+    // Exact FP64 keys for up to 32 queued sources, inserted into the list.
+    auto flush = [&]( int count ) {
+        int const p = lane < count ? s_queue[wib][lane] : -1;
+        __syncwarp();
         unsigned long long cd = KEY_INF;
         int ci = 0x7fffffff;
-        if ( p < tr.n && !in_window )
+        if ( p >= 0 )
         {
             cd = (unsigned long long)__double_as_longlong(
-                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), tx, ty, tz ) );
+                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), q.tx, q.ty, q.tz ) );
             ci = (int)__ldg( tr.perm + p );
         }
         unsigned cand = __ballot_sync( FULL, key_less( cd, ci, bd, bi ) );
@@ -526,7 +594,35 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
             bd = __shfl_sync( FULL, kd, k - 1 );
             bi = __shfl_sync( FULL, ki, k - 1 );
         }
-        bound_f = prune_threshold( __longlong_as_double( (long long)bd ) );
+        bound_f = prune_threshold( bd );
+        // move the remaining queue entries to the front
+        int const rest = qn - count;
+        int const v = lane < rest ? s_queue[wib][count + lane] : 0;
+        __syncwarp();
+        if ( lane < rest )
+            s_queue[wib][lane] = v;
+        __syncwarp();
+        qn = rest;
+    };
+
+    // FP32 screen of a leaf: a source whose FP32 lower bound exceeds the
+    // bound cannot beat or tie it; the others queue for exact keys.
+    auto process_leaf = [&]( int leaf ) {
+        int64_t const p = (int64_t)leaf * LEAF + lane;
+        bool surv = false;
+        if ( p < tr.n && !( p >= s0 && p < s0 + W ) )
+        {
+            float lo, hi;
+            d2_bounds( tr, q, p, lo, hi );
+            surv = lo <= bound_f;
+        }
+        unsigned const m = __ballot_sync( FULL, surv );
+        if ( surv )
+            s_queue[wib][qn + __popc( m & lt_mask )] = (int)p;
+        __syncwarp();
+        qn += __popc( m );
+        if ( qn >= 32 )
+            flush( 32 );
     };
 
     if ( tr.nl == 1 )
@@ -551,8 +647,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
             float l_lo[3], l_hi[3], r_lo[3], r_hi[3];
             int lc, rc;
             load_node( tr.nodes, node, l_lo, l_hi, r_lo, r_hi, lc, rc );
-            float const lbl = box_lb( l_lo, l_hi, qlo, qhi );
-            float const lbr = box_lb( r_lo, r_hi, qlo, qhi );
+            float const lbl = box_lb( l_lo, l_hi, q.qlo, q.qhi );
+            float const lbr = box_lb( r_lo, r_hi, q.qlo, q.qhi );
             bool const near_left = lbl <= lbr;
             int const c_near = near_left ? lc : rc, c_far = near_left ? rc : lc;
             float const lb_near = near_left ? lbl : lbr, lb_far = near_left ? lbr : lbl;
@@ -597,13 +693,18 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
             node = next;
         }
     }
+    if ( qn > 0 )
+        flush( qn );
     if ( lane < row )
         idx_out[qi * (int64_t)row + lane] = ki;
 }
 
 // Radius traversal shared by the count and fill passes.  FILL=false counts
 // hits into counts[qi]; FILL=true writes them at offset[qi] in traversal
-// order (Morton order of the sources, lane order inside a leaf).
+// order (Morton order of the sources, lane order inside a leaf).  A source
+// is a hit iff sqrt(d2) <= r with the exact FP64 d2; the FP32 bounds decide
+// every source whose bound interval lies clear of r^2 (2^-20 margins), and
+// only the rest pay for an FP64 distance.
 template <bool FILL>
 __global__ void __launch_bounds__( Q_WARPS * 32 )
     k_radius( TreeView tr, PointsView tgt, uint32_t const *order, double r,
@@ -615,21 +716,28 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     if ( w >= tgt.n )
         return;
     int64_t const qi = order ? (int64_t)order[w] : w;
-    double const tx = tgt( qi, 0 ), ty = tgt( qi, 1 ), tz = tgt( qi, 2 );
-    float const qlo[3] = {__double2float_rd( tx ), __double2float_rd( ty ), __double2float_rd( tz )};
-    float const qhi[3] = {__double2float_ru( tx ), __double2float_ru( ty ), __double2float_ru( tz )};
-    float const bound_f = prune_threshold( __dmul_ru( r, r ) );
+    Query const q = make_query( tr, tgt, qi );
+    double const r2 = __dmul_ru( r, r );
+    float const bound_f = prune_threshold( (unsigned long long)__double_as_longlong( r2 ) );
+    float const in_f = __fmul_rd( __double2float_rd( __dmul_rd( r, r ) ), 1.0f - 9.5367431640625e-07f );
     int64_t cnt = 0;
     int64_t out = FILL ? offset[qi] : 0;
     int64_t const out_end = FILL ? offset[qi + 1] : 0;
 
     auto process_leaf = [&]( int leaf ) {
         int64_t const p = (int64_t)leaf * LEAF + lane;
-        bool hit = false;
+        bool hit = false, unsure = false;
         if ( p < tr.n )
         {
+            float lo, hi;
+            d2_bounds( tr, q, p, lo, hi );
+            hit = hi < in_f;                  // certainly inside
+            unsure = !hit && !( lo > bound_f ); // neither certainly in nor out
+        }
+        if ( __any_sync( FULL, unsure ) && unsure )
+        {
             double const d2 = dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ),
-                                        tx, ty, tz );
+                                        q.tx, q.ty, q.tz );
             hit = __dsqrt_rn( d2 ) <= r;
         }
         unsigned const b = __ballot_sync( FULL, hit );
@@ -665,8 +773,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
             float l_lo[3], l_hi[3], r_lo[3], r_hi[3];
             int lc, rc;
             load_node( tr.nodes, node, l_lo, l_hi, r_lo, r_hi, lc, rc );
-            bool const hl = box_lb( l_lo, l_hi, qlo, qhi ) <= bound_f;
-            bool const hr = box_lb( r_lo, r_hi, qlo, qhi ) <= bound_f;
+            bool const hl = box_lb( l_lo, l_hi, q.qlo, q.qhi ) <= bound_f;
+            bool const hr = box_lb( r_lo, r_hi, q.qlo, q.qhi ) <= bound_f;
             int next = -1;
             if ( hl )
             {
@@ -710,8 +818,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
 
 TreeView view_of( Lbvh const &t )
 {
-    return TreeView{t.sx.get(), t.sy.get(), t.sz.get(), t.codes.get(), t.perm.get(),
-                    t.nodes.get(), t.scene.get(), t.n, t.n_leaves};
+    return TreeView{t.sx.get(), t.sy.get(), t.sz.get(), t.fx.get(), t.fy.get(), t.fz.get(),
+                    t.codes.get(), t.perm.get(), t.nodes.get(), t.scene.get(), t.n, t.n_leaves};
 }
 
 unsigned blocks_for( int64_t n, int threads )
@@ -727,7 +835,7 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s )
     tree.n = n;
     tree.n_leaves = ( n + LEAF - 1 ) / LEAF;
     int64_t const nl = tree.n_leaves;
-    tree.scene.allocate( 9, s );
+    tree.scene.allocate( 13, s );
     int const nb = std::max( 1, std::min<int>( 4 * num_sms(), (int)( ( n + BND_THREADS - 1 ) / BND_THREADS ) ) );
     DeviceBuffer<unsigned long long> partial( 6 * nb, s );
     k_bounds_partial<<<nb, BND_THREADS, 0, s>>>( src, partial.get() );
@@ -745,8 +853,12 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s )
     tree.sx.allocate( n, s );
     tree.sy.allocate( n, s );
     tree.sz.allocate( n, s );
-    k_gather_sorted<<<blocks_for( n, 256 ), 256, 0, s>>>( src, tree.perm.get(), tree.sx.get(),
-                                                            tree.sy.get(), tree.sz.get() );
+    tree.fx.allocate( n, s );
+    tree.fy.allocate( n, s );
+    tree.fz.allocate( n, s );
+    k_gather_sorted<<<blocks_for( n, 256 ), 256, 0, s>>>( src, tree.perm.get(), tree.scene.get(),
+                                                            tree.sx.get(), tree.sy.get(), tree.sz.get(),
+                                                            tree.fx.get(), tree.fy.get(), tree.fz.get() );
     check_launch( "k_gather_sorted" );
 
     int64_t const ni = std::max<int64_t>( 0, nl - 1 );
@@ -765,7 +877,8 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s )
                                                                  tree.nodes.get() );
         check_launch( "k_pack_children" );
     }
-    k_refit<<<blocks_for( nl, 128 ), 128, 0, s>>>( tree.sx.get(), tree.sy.get(), tree.sz.get(), n, nl,
+    k_refit<<<blocks_for( nl, 128 ), 128, 0, s>>>( tree.sx.get(), tree.sy.get(), tree.sz.get(),
+                                                     tree.scene.get(), n, nl,
                                                      left.get(), right.get(), parent_node.get(),
                                                      parent_leaf.get(), tree.nodes.get(), flags.get(),
                                                      tree.root_box.get(), status );

@@ -28,7 +28,10 @@
 // are tight (about 114 +- 13 for the quadratic basis), so divergence costs
 // little.  E (m x m), U (m x m) and column 0 of V live in shared memory,
 // interleaved by thread so that dynamic (p, q) accesses are conflict-free.
-// The argmax runs on the integer pipe over the IEEE bits of |E_ij|.
+// The argmax runs on the integer pipe over the IEEE bits of |E_ij|; the stop
+// test too, from exponent bounds, except within a factor of four of the
+// threshold where it sums the squares in FP64; the 2x2 rotation angles use
+// half-angle identities rather than atan2 and sincos.
 #include "dtk_common.cuh"
 
 #include <algorithm>
@@ -41,6 +44,32 @@ namespace
 constexpr int SETUP_BLOCK = 32;
 constexpr unsigned FULL = 0xffffffffu;
 
+// cos and sin of phi = atan2(y, x) / 2, phi in (-pi/2, pi/2], from the
+// half-angle identities (cos phi >= 0, sin phi has the sign of y) instead of
+// atan2 and sincos: ~45 FP64 operations instead of ~95, equally accurate.
+__device__ __forceinline__ void half_angle( double y, double x, double &c, double &s )
+{
+    double const r = sqrt( fma( x, x, y * y ) );
+    if ( r == 0.0 )
+    {
+        c = 1.0;
+        s = y; // atan2(+-0, +0) = +-0
+    }
+    else if ( x >= 0.0 )
+    {
+        c = sqrt( ( r + x ) / ( 2.0 * r ) );
+        s = y / ( 2.0 * r * c );
+    }
+    else
+    {
+        double const as = sqrt( ( r - x ) / ( 2.0 * r ) );
+        s = copysign( as, y );
+        c = fabs( y ) / ( 2.0 * r * as );
+    }
+}
+
+// 2x2 SVD rotations of DTK_DetailsSVDImpl.hpp:119-162 and the sr sign rule
+// of :260-263.
 __device__ __forceinline__ void svd_2x2( double a, double b, double c, double d, double &cl,
                                          double &sl, double &cr, double &sr )
 {
@@ -50,15 +79,15 @@ __device__ __forceinline__ void svd_2x2( double a, double b, double c, double d,
     double const q00 = a * a + c * c, q01 = a * b + c * d, q10 = b * a + d * c,
                  q11 = b * b + d * d;
     double sphi, cphi, sth, cth;
-    sincos( 0.5 * atan2( p01 + p10, p00 - p11 ), &sphi, &cphi );
-    sincos( 0.5 * atan2( q01 + q10, q00 - q11 ), &sth, &cth );
+    half_angle( p01 + p10, p00 - p11, cphi, sphi );
+    half_angle( q01 + q10, q00 - q11, cth, sth );
     // S = U^T A W diagonal signs (SVDImpl.hpp:149-159)
     double const aw00 = a * cth + b * sth, aw01 = a * -sth + b * cth;
     double const aw10 = c * cth + d * sth, aw11 = c * -sth + d * cth;
     double const s00 = cphi * aw00 + sphi * aw10;
     double const s11 = -sphi * aw01 + cphi * aw11;
     double const c0 = copysign( 1.0, s00 ), c1 = copysign( 1.0, s11 );
-    // V = W diag(c0, c1); sr sign rule of SVDImpl.hpp:260-263
+    // V = W diag(c0, c1)
     double const v00 = cth * c0, v01 = -sth * c1, v10 = sth * c0;
     cl = cphi;
     sl = -sphi;
@@ -93,8 +122,11 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
     unsigned it = 0;
     while ( true )
     {
-        // Fused scan: off-diagonal Frobenius norm and first largest |E_ij|.
-        double acc0 = 0.0, acc1 = 0.0;
+        // Fused scan: first largest |E_ij| (integer compare of |bits|) and
+        // FP32 bounds on the off-diagonal sum of squares from the exponents
+        // alone: 4^e <= x^2 < 4^(e+1) for x in [2^e, 2^(e+1)).
+        float lower = 0.f, upper = 0.f;
+        bool huge = false, special = false;
         long long best = -1;
         int p = 0, q = 1;
 #pragma unroll
@@ -104,21 +136,47 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
             {
                 if ( i == j )
                     continue;
-                double const x = s.e( i, j );
-                if ( ( i * M + j ) & 1 )
-                    acc1 = fma( x, x, acc1 );
-                else
-                    acc0 = fma( x, x, acc0 );
-                long long const ab = abs_bits( x );
+                long long const ab = abs_bits( s.e( i, j ) );
                 if ( ab > best )
                 {
                     best = ab;
                     p = i;
                     q = j;
                 }
+                int const e = (int)( ab >> 52 ) - 1023; // -1023 for zero/subnormal
+                if ( e == 1024 )
+                    special = true; // Inf/NaN: decide exactly as the reference
+                else if ( e > 62 )
+                    huge = true;
+                else if ( e >= -62 )
+                {
+                    lower += __int_as_float( ( 2 * e + 127 ) << 23 );
+                    upper += __int_as_float( ( 2 * e + 129 ) << 23 );
+                }
+                else
+                    upper += 4.70197740328915e-38f; // 2^-124 >= 4^(e+1)
             }
-        double const norm = sqrt( acc0 + acc1 );
-        if ( !( norm > tol ) )
+        // Stop test of the reference, sqrt(sum) > DBL_EPSILON, decided by the
+        // bounds unless they straddle DBL_EPSILON^2 = 2^-104; then the FP64
+        // row-major sum of squares as the reference forms it.
+        constexpr float tol2 = 4.930380657631324e-32f; // 2^-104 exactly
+        bool go;
+        if ( !special && ( huge || lower > tol2 * 1.0009765625f ) )
+            go = true;
+        else if ( !special && upper < tol2 * 0.9990234375f )
+            go = false;
+        else
+        {
+            double acc = 0.0;
+#pragma unroll
+            for ( int i = 0; i < M; ++i )
+#pragma unroll
+                for ( int j = 0; j < M; ++j )
+                    if ( i != j )
+                        acc = fma( s.e( i, j ), s.e( i, j ), acc );
+            go = sqrt( acc ) > tol;
+        }
+        if ( !go )
             break;
         if ( ++it > cap )
         {

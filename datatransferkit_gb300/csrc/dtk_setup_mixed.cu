@@ -39,6 +39,20 @@ namespace
 constexpr int MB = 32;      // threads per block (one warp)
 constexpr unsigned FULL = 0xffffffffu;
 
+// FP32 weight of a scaled neighbour.  The Buhmann functions are expanded
+// polynomials whose terms cancel (coefficients up to ~400 for values ~0.1),
+// so they are evaluated in FP64 and rounded once; the Wendland and Wu
+// functions are products (1 - x)^n p(x) and stay accurate in FP32.
+__device__ __forceinline__ float weight32( int rbf, float x, float y, float z )
+{
+    if ( rbf >= DTK_BUHMANN2 )
+    {
+        double const dx = x, dy = y, dz = z;
+        return (float)rbf_eval<double>( rbf, sqrt( dx * dx + dy * dy + dz * dz ) );
+    }
+    return rbf_eval<float>( rbf, sqrtf( x * x + y * y + z * z ) );
+}
+
 template <int M>
 __host__ __device__ constexpr int ut( int i, int j )
 {
@@ -166,7 +180,7 @@ __global__ void __launch_bounds__( MB )
                 scaled( j, x, y, z );
                 float P[M];
                 basis_eval<M, float>( x, y, z, P );
-                float const phi = rbf_eval<float>( rbf, sqrtf( x * x + y * y + z * z ) );
+                float const phi = weight32( rbf, x, y, z );
 #pragma unroll
                 for ( int a = 0; a < M; ++a )
                 {
@@ -302,7 +316,7 @@ __global__ void __launch_bounds__( MB )
                 scaled( j, x, y, z );
                 double P[M];
                 basis_eval<M, double>( (double)x, (double)y, (double)z, P );
-                double const phi = (double)rbf_eval<float>( rbf, sqrtf( x * x + y * y + z * z ) );
+                double const phi = (double)weight32( rbf, x, y, z );
                 double dot = 0.0;
 #pragma unroll
                 for ( int q = 0; q < M; ++q )
@@ -323,7 +337,7 @@ __global__ void __launch_bounds__( MB )
             scaled( j, x, y, z );
             double P[M];
             basis_eval<M, double>( (double)x, (double)y, (double)z, P );
-            float const phi = rbf_eval<float>( rbf, sqrtf( x * x + y * y + z * z ) );
+            float const phi = weight32( rbf, x, y, z );
             double dot = 0.0;
 #pragma unroll
             for ( int q = 0; q < M; ++q )
