@@ -45,26 +45,40 @@ constexpr int SETUP_BLOCK = 32;
 constexpr unsigned FULL = 0xffffffffu;
 
 // cos and sin of phi = atan2(y, x) / 2, phi in (-pi/2, pi/2], from the
-// half-angle identities (cos phi >= 0, sin phi has the sign of y) instead of
-// atan2 and sincos: ~45 FP64 operations instead of ~95, equally accurate.
+// half-angle identities (cos phi >= 0, sin phi has the sign of y):
+//   x >= 0: cos = (r + x) / sqrt(2r(r + x)),  sin = y / sqrt(2r(r + x))
+//   x <  0: |sin| = (r - x) / sqrt(2r(r - x)), cos = |y| / sqrt(2r(r - x))
+// with r = |(x, y)|: one sqrt and one reciprocal square root instead of
+// atan2 and sincos.  (x, y) is rescaled by a power of two when r^2 would
+// leave the normal range (atan2 is scale-invariant).
 __device__ __forceinline__ void half_angle( double y, double x, double &c, double &s )
 {
-    double const r = sqrt( fma( x, x, y * y ) );
-    if ( r == 0.0 )
+    double r2 = fma( x, x, y * y );
+    if ( !( r2 > 1e-280 && r2 < 1e280 ) && ( x != 0.0 || y != 0.0 ) )
+    {
+        int const e = ilogb( fmax( fabs( x ), fabs( y ) ) );
+        x = scalbn( x, -e );
+        y = scalbn( y, -e );
+        r2 = fma( x, x, y * y );
+    }
+    if ( r2 == 0.0 )
     {
         c = 1.0;
         s = y; // atan2(+-0, +0) = +-0
+        return;
     }
-    else if ( x >= 0.0 )
+    double const r = sqrt( r2 );
+    double const w = r + fabs( x );
+    double const t = rsqrt( 2.0 * r * w );
+    if ( x >= 0.0 )
     {
-        c = sqrt( ( r + x ) / ( 2.0 * r ) );
-        s = y / ( 2.0 * r * c );
+        c = w * t;
+        s = y * t;
     }
     else
     {
-        double const as = sqrt( ( r - x ) / ( 2.0 * r ) );
-        s = copysign( as, y );
-        c = fabs( y ) / ( 2.0 * r * as );
+        s = copysign( w * t, y );
+        c = fabs( y ) * t;
     }
 }
 
@@ -124,19 +138,19 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
     {
         // Fused scan: first largest |E_ij| (integer compare of |bits|) and
         // FP32 bounds on the off-diagonal sum of squares from the exponents
-        // alone: 4^e <= x^2 < 4^(e+1) for x in [2^e, 2^(e+1)).
+        // alone: 4^e <= x^2 < 4^(e+1) for x in [2^e, 2^(e+1)).  Rows loop
+        // (not unrolled) to keep the kernel's code small.
         float lower = 0.f, upper = 0.f;
         bool huge = false, special = false;
         long long best = -1;
         int p = 0, q = 1;
-#pragma unroll
+#pragma unroll 1
         for ( int i = 0; i < M; ++i )
+        {
 #pragma unroll
             for ( int j = 0; j < M; ++j )
             {
-                if ( i == j )
-                    continue;
-                long long const ab = abs_bits( s.e( i, j ) );
+                long long const ab = j == i ? -2 : abs_bits( s.e( i, j ) );
                 if ( ab > best )
                 {
                     best = ab;
@@ -144,18 +158,14 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
                     q = j;
                 }
                 int const e = (int)( ab >> 52 ) - 1023; // -1023 for zero/subnormal
-                if ( e == 1024 )
-                    special = true; // Inf/NaN: decide exactly as the reference
-                else if ( e > 62 )
-                    huge = true;
-                else if ( e >= -62 )
-                {
-                    lower += __int_as_float( ( 2 * e + 127 ) << 23 );
-                    upper += __int_as_float( ( 2 * e + 129 ) << 23 );
-                }
-                else
-                    upper += 4.70197740328915e-38f; // 2^-124 >= 4^(e+1)
+                special |= e == 1024;                   // Inf/NaN: decide exactly
+                huge |= e > 62 && e < 1024;
+                bool const mid = e >= -62 && e <= 62;
+                lower += mid ? __int_as_float( ( 2 * e + 127 ) << 23 ) : 0.f;
+                upper += mid ? __int_as_float( ( 2 * e + 129 ) << 23 )
+                             : ( e < -62 && j != i ? 4.70197740328915e-38f : 0.f ); // 2^-124
             }
+        }
         // Stop test of the reference, sqrt(sum) > DBL_EPSILON, decided by the
         // bounds unless they straddle DBL_EPSILON^2 = 2^-104; then the FP64
         // row-major sum of squares as the reference forms it.
