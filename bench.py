@@ -392,6 +392,10 @@ def run_ours(args, rank, world, local_rank):
                       "setup_ms": setup64_ms,
                       "setup_fp64_tflops": flops64 / (setup64_ms / 1e3) / 1e12},
         "mixed_over_fp64": ms_fp64 / ms_mixed,
+        "rotations_per_target": {
+            "mixed_fp64": float(np.mean([r[1] for r in rec_mixed])) / n_tgt,
+            "mixed_fp32": float(np.mean([r[2] for r in rec_mixed])) / n_tgt,
+            "fp64_form": rot_fp64_form / n_tgt},
         "accuracy_vs_fp64_oracle": acc,
         "stages_ms": {"search": search_ms, "setup": setup_ms,
                       "apply": ms_mixed - search_ms - setup_ms},
