@@ -148,13 +148,13 @@ __device__ int jacobi_sweep_rr( AAcc &a, VAcc &v, T skip )
             T const app = a( ut<M>( P[k], P[k] ) ), aqq = a( ut<M>( Q[k], Q[k] ) );
             T const apq = a( ut<M>( P[k], Q[k] ) );
             // a pair already negligible (a_pq^2 <= skip^2 |a_pp a_qq|) is
-            // not rotated; its parameter chain runs only if some lane of the
-            // warp needs it
+            // not rotated; the branch skips its parameter chain whenever no
+            // lane of the warp needs it
             on[k] = !( apq * apq <= skip * skip * fabs( app * aqq ) );
             C[k] = T( 1 );
             S[k] = T( 0 );
             Tn[k] = T( 0 );
-            if ( __any_sync( 0xffffffffu, on[k] ) && on[k] )
+            if ( on[k] )
                 rotation<T>( app, aqq, apq, C[k], S[k], Tn[k] );
             done += on[k];
         }
