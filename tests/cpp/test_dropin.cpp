@@ -1,0 +1,210 @@
+// The reference's MLS operator tests, written against the header-only
+// drop-in (include/dtk/DTK_MovingLeastSquaresOperator.hpp) as a DTK user would:
+//   tstMeshfreeOperators.cpp:130-376 (same_npoints_and_basis, grid, line)
+//   tstMeshfreeOperatorsSimpleProblem.cpp:113-147 (corner_cases)
+// plus a LayoutLeft input and the DTK_REQUIRE error convention.
+// Prints "PASS <n>" on success; exits non-zero on the first failure.
+#include <dtk/DTK_MovingLeastSquaresOperator.hpp>
+
+#include <cuda_runtime.h>
+
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <functional>
+#include <random>
+#include <vector>
+
+using namespace DataTransferKit;
+using Pt = std::array<double, 3>;
+static int g_checks = 0;
+
+#define CHECK( c )                                                                                  \
+    do                                                                                              \
+    {                                                                                               \
+        ++g_checks;                                                                                 \
+        if ( !( c ) )                                                                               \
+        {                                                                                           \
+            std::printf( "FAIL %s:%d: %s\n", __FILE__, __LINE__, #c );                              \
+            std::exit( 1 );                                                                         \
+        }                                                                                           \
+    } while ( 0 )
+
+struct Buf
+{
+    double *d = nullptr;
+    std::size_t n = 0;
+    explicit Buf( std::size_t n_ ) : n( n_ ) { cudaMalloc( &d, std::max<std::size_t>( 1, n ) * 8 ); }
+    ~Buf() { cudaFree( d ); }
+};
+
+// points: LayoutRight (i, d) at i*3 + d, or LayoutLeft at d*n + i
+DeviceView<double const> points( Buf &b, std::vector<Pt> const &p, bool left = false )
+{
+    std::vector<double> h( 3 * p.size() );
+    for ( std::size_t i = 0; i < p.size(); ++i )
+        for ( int d = 0; d < 3; ++d )
+            h[left ? d * p.size() + i : 3 * i + d] = p[i][d];
+    cudaMemcpy( b.d, h.data(), h.size() * 8, cudaMemcpyHostToDevice );
+    DeviceView<double const> v;
+    v.ptr = b.d;
+    v.n0 = p.size();
+    v.n1 = 3;
+    v.s0 = left ? 1 : 3;
+    v.s1 = left ? (std::ptrdiff_t)p.size() : 1;
+    return v;
+}
+
+DeviceView<double const> values( Buf &b, std::vector<double> const &x )
+{
+    cudaMemcpy( b.d, x.data(), x.size() * 8, cudaMemcpyHostToDevice );
+    DeviceView<double const> v;
+    v.ptr = b.d;
+    v.n0 = x.size();
+    return v;
+}
+
+DeviceView<double> out( Buf &b )
+{
+    DeviceView<double> v;
+    v.ptr = b.d;
+    v.n0 = b.n;
+    return v;
+}
+
+std::vector<double> host( Buf &b )
+{
+    std::vector<double> h( b.n );
+    cudaMemcpy( h.data(), b.d, b.n * 8, cudaMemcpyDeviceToHost );
+    return h;
+}
+
+std::function<double( Pt )> poly( int size )
+{
+    if ( size == 1 )
+        return []( Pt ) { return 3.0; };
+    if ( size == 4 )
+        return []( Pt p ) { return 4 + 2 * p[0] + 3 * p[1] - 2 * p[2]; };
+    return []( Pt p ) {
+        return 2 + 3 * p[0] - 5 * p[1] + 2 * p[2] + 3 * p[0] * p[0] + 4 * p[0] * p[1] -
+               2 * p[0] * p[2] + p[1] * p[1] - 3 * p[1] * p[2] + 4 * p[2] * p[2];
+    };
+}
+
+std::vector<Pt> grid( int nx, int ny, int nz, Pt o )
+{
+    std::vector<Pt> g;
+    for ( int i = 0; i < nx; ++i )
+        for ( int j = 0; j < ny; ++j )
+            for ( int k = 0; k < nz; ++k )
+                g.push_back( {o[0] + i, o[1] + j, o[2] + k} );
+    return g;
+}
+
+template <typename Basis>
+void run_basis()
+{
+    using Op = MovingLeastSquaresOperator<CudaDevice, Wendland<0>, Basis>;
+    int const m = Basis::size;
+    auto f = poly( m );
+    // same_npoints_and_basis: clusters, one target each, exactly m sources
+    {
+        std::mt19937_64 g( 7 );
+        std::uniform_real_distribution<double> rx( -0.5, 0.5 );
+        std::vector<Pt> src, tgt;
+        for ( int i = 0; i < 10; ++i )
+        {
+            double const c = i * std::ceil( 4 * 0.5 );
+            tgt.push_back( {c + 0.5 * rx( g ), c + 0.5 * rx( g ), c + 0.5 * rx( g )} );
+            for ( int k = 0; k < m; ++k )
+                src.push_back( {c + rx( g ), c + rx( g ), c + rx( g )} );
+        }
+        Buf bs( 3 * src.size() ), bt( 3 * tgt.size() ), bv( src.size() ), bo( tgt.size() );
+        std::vector<double> sv;
+        for ( auto &p : src )
+            sv.push_back( f( p ) );
+        Op op( 0, points( bs, src ), points( bt, tgt ) );
+        op.apply( values( bv, sv ), out( bo ) );
+        auto y = host( bo );
+        for ( std::size_t i = 0; i < tgt.size(); ++i )
+            CHECK( std::abs( y[i] - f( tgt[i] ) ) <= 1e-7 * std::abs( f( tgt[i] ) ) );
+    }
+    // grid 40x40x1, target (19,19,0); LayoutLeft inputs
+    {
+        auto src = grid( 40, 40, 1, {0, 0, 0} );
+        std::vector<Pt> tgt = {{19, 19, 0}};
+        Buf bs( 3 * src.size() ), bt( 3 ), bv( src.size() ), bo( 1 );
+        std::vector<double> sv;
+        for ( auto &p : src )
+            sv.push_back( f( p ) );
+        Op op( 0, points( bs, src, true ), points( bt, tgt, true ) );
+        op.apply( values( bv, sv ), out( bo ) );
+        CHECK( std::abs( host( bo )[0] - f( tgt[0] ) ) <= 1e-14 * std::abs( f( tgt[0] ) ) );
+    }
+    // line: 40 collinear sources, 39 midpoint targets
+    {
+        auto src = grid( 40, 1, 1, {0, 0, 0} );
+        auto tgt = grid( 39, 1, 1, {0.5, 0, 0} );
+        Buf bs( 3 * src.size() ), bt( 3 * tgt.size() ), bv( src.size() ), bo( tgt.size() );
+        std::vector<double> sv;
+        for ( auto &p : src )
+            sv.push_back( f( p ) );
+        Op op( 0, points( bs, src ), points( bt, tgt ) );
+        op.apply( values( bv, sv ), out( bo ) );
+        auto y = host( bo );
+        for ( std::size_t i = 0; i < tgt.size(); ++i )
+            CHECK( std::abs( y[i] - f( tgt[i] ) ) <= 1e-14 * std::abs( f( tgt[i] ) ) );
+    }
+}
+
+int main()
+{
+    run_basis<MultivariatePolynomialBasis<Constant, 3>>();
+    run_basis<MultivariatePolynomialBasis<Linear, 3>>();
+    run_basis<MultivariatePolynomialBasis<Quadratic, 3>>();
+    // corner_cases: two sources, k = 4 neighbours requested -> rows of 2
+    {
+        std::vector<Pt> src = {{1, 1, 1}, {2, 2, 2}}, tgt = {{1.5, 1.5, 1.5}};
+        Buf bs( 6 ), bt( 3 ), bv( 2 ), bo( 1 );
+        MovingLeastSquaresOperator<CudaDevice> op( 0, points( bs, src ), points( bt, tgt ) );
+        op.apply( values( bv, {255.0, 255.0} ), out( bo ) );
+        CHECK( std::abs( host( bo )[0] - 255.0 ) <= 1e-12 * 255.0 );
+    }
+    {
+        std::vector<Pt> src = {{1, 1, 1}}, tgt = {};
+        Buf bs( 3 ), bt( 3 ), bv( 1 ), bo( 0 );
+        MovingLeastSquaresOperator<CudaDevice> op( 0, points( bs, src ), points( bt, tgt ) );
+        op.apply( values( bv, {255.0} ), out( bo ) );
+    }
+    // error convention: DTK_REQUIRE -> DataTransferKitException
+    {
+        std::vector<Pt> src = {{1, 1, 1}, {2, 2, 2}}, tgt = {{1.5, 1.5, 1.5}};
+        Buf bs( 6 ), bt( 3 ), bv( 3 ), bo( 1 );
+        MovingLeastSquaresOperator<CudaDevice> op( 0, points( bs, src ), points( bt, tgt ) );
+        bool threw = false;
+        try
+        {
+            op.apply( values( bv, {1.0, 2.0, 3.0} ), out( bo ) ); // 3 values for 2 sources
+        }
+        catch ( DataTransferKitException const & )
+        {
+            threw = true;
+        }
+        CHECK( threw );
+        threw = false;
+        try
+        {
+            std::vector<Pt> none = {};
+            Buf b0( 3 );
+            MovingLeastSquaresOperator<CudaDevice> bad( 0, points( b0, none ), points( bt, tgt ) );
+        }
+        catch ( DataTransferKitException const & )
+        {
+            threw = true; // DTK_CHECK( !search_tree.empty() )
+        }
+        CHECK( threw );
+    }
+    std::printf( "PASS %d\n", g_checks );
+    return 0;
+}
