@@ -24,7 +24,7 @@ EXPORTED = [
     "dtk_mls_get_stage_times", "dtk_mls_get_rotation_count", "dtk_mls_destroy",
     "dtk_knn_search", "dtk_svd_pinv", "dtk_mls_batch_create", "dtk_mls_batch_apply",
     "dtk_mls_batch_get_csr", "dtk_mls_batch_destroy", "dtk_last_error", "dtk_status_string",
-    "dtk_kernel_launch_count",
+    "dtk_kernel_launch_count", "dtk_svd_pinv_noalloc",
 ]
 
 
@@ -73,6 +73,7 @@ def _declare(L):
     L.dtk_mls_destroy.argtypes = [_vp]
     L.dtk_knn_search.argtypes = [_vp, _i64, _i64, _i64, _vp, _i64, _i64, _i64, C.c_int32, _vp, _vp, _vp]
     L.dtk_svd_pinv.argtypes = [C.c_int32, _i64, _vp, _vp, C.POINTER(_i64), _vp]
+    L.dtk_svd_pinv_noalloc.argtypes = L.dtk_svd_pinv.argtypes
     L.dtk_mls_batch_create.argtypes = [C.c_int32, C.POINTER(Options), C.POINTER(_i64), _vp,
                                        C.POINTER(_i64), _vp, _vp, C.POINTER(_vp)]
     L.dtk_mls_batch_apply.argtypes = [_vp, _vp, _vp, C.c_int32, _vp]

@@ -323,6 +323,10 @@ void setup_mixed( SetupArgs const &a, cudaStream_t s );
 void svd_pinv_batched( int n, int64_t count, double const *a, double *pinv,
                        unsigned long long *underdetermined, unsigned *status,
                        cudaStream_t s );
+// The same kernel on a caller-provided work area of 3 n^2 count doubles.
+void svd_pinv_batched_work( int n, int64_t count, double const *a, double *pinv, double *work,
+                            unsigned long long *underdetermined, unsigned *status,
+                            cudaStream_t s );
 
 // Apply kernels.
 void apply_csr( int64_t n_tgt, int32_t const *offset, int32_t const *idx,

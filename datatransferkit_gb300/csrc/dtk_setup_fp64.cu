@@ -522,6 +522,16 @@ void setup_fp64( SetupArgs const &a, cudaStream_t s )
     }
 }
 
+void svd_pinv_batched_work( int n, int64_t count, double const *a, double *pinv, double *work,
+                            unsigned long long *underdetermined, unsigned *status, cudaStream_t s )
+{
+    if ( count == 0 )
+        return;
+    unsigned const blocks = (unsigned)( ( count + 63 ) / 64 );
+    k_svd_general<<<blocks, 64, 0, s>>>( n, count, a, pinv, work, underdetermined, status );
+    check_launch( "k_svd_general" );
+}
+
 void svd_pinv_batched( int n, int64_t count, double const *a, double *pinv,
                        unsigned long long *underdetermined, unsigned *status, cudaStream_t s )
 {

@@ -171,6 +171,26 @@ dtk_status dtk_svd_pinv(int32_t n, int64_t count, const double *a,
                         double *pinv, int64_t *underdetermined,
                         dtk_stream_t stream);
 
+/* The same batched pseudo-inverse without any device allocation; it has no
+ * counterpart in the reference.  It is for callers that cannot call
+ * cudaMalloc: code that runs under a fixed device-memory budget or inside a
+ * framework whose allocator owns the device memory, and code that cannot take
+ * the implicit device synchronisation an allocation may cause.  The work
+ * matrices (E, U, V: 3 n^2 doubles per matrix) and the counters live in one
+ * static device array of DTK_SVD_NOALLOC_MAX_DOUBLES doubles (8 MiB), which
+ * every GPU that loads this library holds until the process exits.  Requests
+ * with 3 * n * n * count > DTK_SVD_NOALLOC_MAX_DOUBLES are rejected with
+ * DTK_ERR_INVALID_ARG.  The first call on a device looks up the array's
+ * device address, so make it before any stream capture.  Every call shares
+ * the array (it keeps the last call's contents; each call clears its
+ * counters), so calls that overlap on the GPU -- other streams, other host
+ * threads -- race; serialise them.  Synchronises `stream` to return
+ * *underdetermined. */
+#define DTK_SVD_NOALLOC_MAX_DOUBLES (1 << 20)
+dtk_status dtk_svd_pinv_noalloc(int32_t n, int64_t count, const double *a,
+                                double *pinv, int64_t *underdetermined,
+                                dtk_stream_t stream);
+
 /* ---- batched uneven transfers (extension) ----
  * n_problems independent operators in one schedule.  Problem p uses
  * sources [src_offsets[p], src_offsets[p+1]) and targets
