@@ -31,7 +31,7 @@ EXPORTED = [
 class Options(C.Structure):
     _fields_ = [("rbf", C.c_int32), ("basis", C.c_int32), ("k", C.c_int32),
                 ("precision", C.c_int32), ("radius", C.c_double), ("comm_size", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("keep_points", C.c_int32)]
 
 
 class DTKError(RuntimeError):

@@ -7,6 +7,7 @@
 // count.  The reference's `_ranks` array is absent: on one rank every rank is
 // 0 and the fetch is a local gather fused into apply.
 #include "dtk_common.cuh"
+#include "dtk_handle.cuh"
 
 #include <cmath>
 #include <memory>
@@ -121,24 +122,6 @@ Geometry check_options( dtk_mls_options const *o )
 
 } // namespace dtk
 
-struct dtk_mls_s
-{
-    dtk_mls_options opts;
-    int64_t n_src = 0, n_tgt = 0, nnz = 0;
-    int m = 0;
-    int uniform_row = 0; // > 0 for kNN rows
-    int mean_row = 0;
-    dtk::DeviceBuffer<int32_t> offset, idx;
-    dtk::DeviceBuffer<double> coeff64;
-    dtk::DeviceBuffer<float> coeff32;
-    dtk::DeviceBuffer<uint32_t> order; // Morton order of targets
-    dtk::DeviceBuffer<double> src_copy, tgt_copy; // packed n x 3 (adjoint)
-    dtk::DeviceBuffer<int32_t> t_offset, t_entry, entry_row;
-    int64_t underdetermined = 0;
-    int64_t rotations = 0, rotations32 = 0;
-    float search_ms = 0.f, setup_ms = 0.f;
-};
-
 using namespace dtk;
 
 extern "C" {
@@ -153,7 +136,7 @@ void dtk_mls_default_options( dtk_mls_options *o )
     o->precision = DTK_FP64;
     o->radius = 0.0;
     o->comm_size = 1;
-    o->reserved = 0;
+    o->keep_points = 0;
 }
 
 const char *dtk_last_error( void ) { return g_error.c_str(); }
@@ -195,6 +178,19 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
         h->m = g.m;
         PointsView const sv{src, n_src, src_pt_stride, src_dim_stride};
         PointsView const tv{tgt, n_tgt, tgt_pt_stride, tgt_dim_stride};
+        if ( opts->keep_points )
+        {
+            // packed n x 3 copies for the coordinate adjoint
+            h->src_copy.allocate( 3 * n_src, s );
+            h->tgt_copy.allocate( std::max<int64_t>( 1, 3 * n_tgt ), s );
+            k_pack_points<<<(unsigned)( ( n_src + 255 ) / 256 ), 256, 0, s>>>( sv, h->src_copy.get() );
+            check_launch( "k_pack_points" );
+            if ( n_tgt )
+            {
+                k_pack_points<<<(unsigned)( ( n_tgt + 255 ) / 256 ), 256, 0, s>>>( tv, h->tgt_copy.get() );
+                check_launch( "k_pack_points" );
+            }
+        }
 
         cudaEvent_t ev[3];
         for ( auto &e : ev )

@@ -2,12 +2,6 @@
 #include "dtk_common.cuh"
 
 extern "C" {
-dtk_status dtk_mls_apply_adjoint( dtk_mls_handle, const double *, int64_t, const double *, double *,
-                                  double *, dtk_stream_t )
-{
-    dtk::set_error( "adjoint not built yet" );
-    return DTK_ERR_UNSUPPORTED;
-}
 dtk_status dtk_mls_batch_create( int32_t, const dtk_mls_options *, const int64_t *, const double *,
                                  const int64_t *, const double *, dtk_stream_t, dtk_mls_batch_handle * )
 {

@@ -143,12 +143,13 @@ class MovingLeastSquaresOperator(PointCloudOperator):
     GPU; ``apply(source_values, target_values)`` writes every target value.
     Extensions beyond the reference: ``k`` (neighbours, default the basis
     size as in the reference), ``radius`` (radius search instead of kNN) and
-    ``precision`` ("fp64" = the reference algorithm, "mixed").
+    ``precision`` ("fp64" = the reference algorithm, "mixed") and
+    ``keep_points`` (keep copies of the points for the coordinate adjoint).
     """
 
     def __init__(self, comm, source_points, target_points, rbf=None, basis=None, *,
                  k: int | None = None, radius: float | None = None, precision="fp64",
-                 stream=None):
+                 keep_points: bool = False, stream=None):
         self.polynomial_basis = basis or MultivariatePolynomialBasis(Linear, 3)
         self.radial_basis_function = rbf or Wendland(0)
         src = _check_points(source_points, "source_points")
@@ -167,6 +168,7 @@ class MovingLeastSquaresOperator(PointCloudOperator):
         o.radius = 0.0 if radius is None else float(radius)
         o.precision = _PRECISIONS[precision]
         o.comm_size = _comm_size(comm)
+        o.keep_points = 1 if keep_points else 0
         self.options = o
         self._h = C.c_void_p()
         self._stream = stream

@@ -82,11 +82,12 @@ typedef struct
     int32_t precision; /* dtk_precision */
     double radius;     /* > 0: radius search instead of kNN (extension) */
     int32_t comm_size; /* ranks of the communicator; must be 1 */
-    int32_t reserved;
+    int32_t keep_points; /* != 0: the handle keeps copies of the points
+                            (24 B per point) for the coordinate adjoint */
 } dtk_mls_options;
 
 /* Options of MovingLeastSquaresOperator<Device> with its template defaults:
- * Wendland<0>, Linear3, k = basis size, FP64, comm_size 1. */
+ * Wendland<0>, Linear3, k = basis size, FP64, comm_size 1, keep_points 0. */
 void dtk_mls_default_options(dtk_mls_options *opts);
 
 /* Setup.  Replaces the constructor, DTK_MovingLeastSquaresOperator_def.hpp:91-186.
@@ -111,12 +112,17 @@ dtk_status dtk_mls_apply(dtk_mls_handle h, const double *source_values,
                          int64_t n_target_values, dtk_stream_t stream);
 
 /* Adjoint of apply and of the setup (extension; the reference has none).
+ * cot = dL/d(target values), n_cot == n_tgt.
  * grad_values[s] = sum over entries j with idx_j == s of coeff_j * cot[row(j)]
- * (deterministic transpose gather, overwrites n_src values).  When
- * grad_coords is non-NULL it receives dL/d(source coordinates) as an n_src x 3
- * row-major array (overwritten), through the weights, the support radius and
- * the pseudo-inverse, recomputed per target with connectivity fixed; that
- * part needs `source_values` (the field the forward apply used). */
+ * (deterministic transpose gather in ascending entry order; overwrites n_src
+ * values).  When grad_coords is non-NULL it receives dL/d(source coordinates)
+ * as an n_src x 3 row-major array (overwritten), through the weights, the
+ * support radius (whose max sends its gradient to the farthest neighbour) and
+ * the pseudo-inverse, recomputed per target in FP64 with the connectivity
+ * fixed, and gathered deterministically like grad_values; this part needs
+ * `source_values` (the field of the forward apply) and a handle created with
+ * keep_points != 0.  Rows whose moments are rank-deficient use the truncated
+ * pseudo-inverse in place of the inverse.  Synchronous. */
 dtk_status dtk_mls_apply_adjoint(dtk_mls_handle h, const double *cot,
                                  int64_t n_cot, const double *source_values,
                                  double *grad_values, double *grad_coords,
