@@ -4,11 +4,12 @@ The compute path is ``libdtk_gb300.so`` (hand-written sm_103a CUDA behind the
 C ABI of ``include/dtk_gb300.h``); this package is its host-side mirror of
 DataTransferKit's operator API.  There is no CPU fallback.
 """
-from .operators import (FP64, MIXED, Buhmann, Constant, Linear, MovingLeastSquaresOperator,
+from .operators import (FP64, MIXED, Buhmann, Constant, Linear, MovingLeastSquaresBatch,
+                        MovingLeastSquaresOperator,
                         MultivariatePolynomialBasis, PointCloudOperator, Quadratic, Wendland, Wu,
                         kernel_launch_count, knn_search, svd_pinv)
 from ._capi import DTKError, InvalidArgument, Unsupported
 
-__all__ = ["MovingLeastSquaresOperator", "PointCloudOperator", "MultivariatePolynomialBasis",
+__all__ = ["MovingLeastSquaresOperator", "MovingLeastSquaresBatch", "PointCloudOperator", "MultivariatePolynomialBasis",
            "Constant", "Linear", "Quadratic", "Wendland", "Wu", "Buhmann", "FP64", "MIXED",
            "knn_search", "svd_pinv", "kernel_launch_count", "DTKError", "InvalidArgument", "Unsupported"]

@@ -13,6 +13,7 @@
 #include <memory>
 #include <new>
 #include <string>
+#include <vector>
 
 namespace dtk
 {
@@ -227,13 +228,13 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
                 h->offset.get(), n_tgt, row );
             check_launch( "k_fill_uniform_offsets" );
             h->idx.allocate( std::max<int64_t>( 1, h->nnz ), s );
-            knn_query( tree, tv, h->order.get(), g.k, h->idx.get(), status.get(), s );
+            knn_query( tree, tv, h->order.get(), g.k, GroupArgs{}, h->offset.get(), h->idx.get(), status.get(), s );
         }
         else
         {
             DeviceBuffer<int64_t> counts( std::max<int64_t>( 1, n_tgt ), s ),
                 offs( n_tgt + 1, s );
-            radius_count( tree, tv, h->order.get(), g.opts.radius, counts.get(), status.get(), s );
+            radius_count( tree, tv, h->order.get(), g.opts.radius, GroupArgs{}, counts.get(), status.get(), s );
             exclusive_scan_i64( counts.get(), offs.get(), n_tgt, s );
             int64_t total = 0;
             DTK_CUDA_OR_THROW( cudaMemcpyAsync( &total, offs.get() + n_tgt, sizeof( int64_t ),
@@ -246,7 +247,7 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
                                                                                   h->offset.get(), n_tgt );
             check_launch( "k_narrow_offsets" );
             h->idx.allocate( std::max<int64_t>( 1, total ), s );
-            radius_fill( tree, tv, h->order.get(), g.opts.radius, h->offset.get(), h->idx.get(),
+            radius_fill( tree, tv, h->order.get(), g.opts.radius, GroupArgs{}, h->offset.get(), h->idx.get(),
                          status.get(), s );
         }
         DTK_CUDA_OR_THROW( cudaEventRecord( ev[1], s ) );
@@ -270,14 +271,28 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
         {
             h->coeff64.allocate( std::max<int64_t>( 1, h->nnz ), s );
             a.coeff64 = h->coeff64.get();
-            setup_fp64( a, s );
         }
         else
         {
             h->coeff32.allocate( std::max<int64_t>( 1, h->nnz ), s );
             a.coeff32 = h->coeff32.get();
-            setup_mixed( a, s );
         }
+        if ( g.radius_mode )
+        {
+            // radius rows are uneven: the planner sends rows longer than
+            // LONG_ROW to the warp-cooperative kernels
+            std::vector<int32_t> off_h( n_tgt + 1 ), order_h( std::max<int64_t>( 1, n_tgt ) );
+            DTK_CUDA_OR_THROW( cudaMemcpyAsync( off_h.data(), h->offset.get(), ( n_tgt + 1 ) * sizeof( int32_t ),
+                                                cudaMemcpyDeviceToHost, s ) );
+            DTK_CUDA_OR_THROW( cudaMemcpyAsync( order_h.data(), h->order.get(), n_tgt * sizeof( int32_t ),
+                                                cudaMemcpyDeviceToHost, s ) );
+            DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+            run_setup_plan( a, g.opts.precision, order_h.data(), off_h.data(), nullptr, nullptr, s );
+        }
+        else if ( g.opts.precision == DTK_FP64 )
+            setup_fp64( a, s );
+        else
+            setup_mixed( a, s );
         DTK_CUDA_OR_THROW( cudaEventRecord( ev[2], s ) );
 
         unsigned st = 0;
@@ -417,7 +432,7 @@ dtk_status dtk_knn_search( const double *src, int64_t n_src, int64_t src_pt_stri
         build_lbvh( sv, tree, status.get(), s );
         DeviceBuffer<uint32_t> order;
         sort_queries( tree, tv, order, s );
-        knn_query( tree, tv, order.get(), k, indices, status.get(), s );
+        knn_query( tree, tv, order.get(), k, GroupArgs{}, offset, indices, status.get(), s );
         unsigned st = 0;
         DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, status.get(), sizeof( unsigned ),
                                             cudaMemcpyDeviceToHost, s ) );

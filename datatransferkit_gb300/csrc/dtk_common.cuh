@@ -276,28 +276,46 @@ struct Lbvh
     double lo[3], hi[3];  // scene bounds (host copy)
     DeviceBuffer<double> sx, sy, sz;  // Morton-sorted coordinates
     DeviceBuffer<float> fx, fy, fz;   // the same, centred on the scene box, FP32
-    DeviceBuffer<uint32_t> codes;     // sorted Morton codes
+    DeviceBuffer<uint32_t> codes;     // Morton codes in sorted order
+    DeviceBuffer<uint32_t> grp;       // group (problem) of each sorted point; empty if ungrouped
     DeviceBuffer<uint32_t> perm;      // sorted position -> original index
     DeviceBuffer<float4> nodes;       // 4 float4 per internal node
     DeviceBuffer<float4> root_box;    // box of the whole tree (2 float4)
     DeviceBuffer<double> scene;       // lo[3], Morton scale[3], hi[3], centre[3], bound S
 };
 
-void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s );
+// group (optional, per input point) makes the order problem-major: the
+// points of group g then occupy one contiguous range of sorted positions.
+void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
+                 uint32_t const *group = nullptr, int64_t n_groups = 0 );
 
-// Morton order of query points (sorted query ids) using the tree's scene box.
+// Morton order of query points (sorted query ids) using the tree's scene box;
+// with groups, problem-major and Morton within each problem.
 void sort_queries( Lbvh const &tree, PointsView tgt, DeviceBuffer<uint32_t> &order,
-                   cudaStream_t s );
+                   cudaStream_t s, uint32_t const *group = nullptr, int64_t n_groups = 0 );
 
-// kNN: writes idx rows (ascending (d2, index)); offset must be pre-filled.
+// Problems of a batch, all optional (null: one problem over all sources,
+// uniform k / radius): per group the sorted-position range of its sources,
+// the group of each target, per-group k and per-group radius.
+struct GroupArgs
+{
+    int64_t const *src_off = nullptr;
+    uint32_t const *tgt_grp = nullptr;
+    int32_t const *k = nullptr;
+    double const *r = nullptr;
+};
+
+// kNN: writes each row at offset[target] (ascending (d2, index)).
 void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
-                int32_t *idx, unsigned *status, cudaStream_t s );
+                GroupArgs const &groups, int32_t const *offset, int32_t *idx, unsigned *status,
+                cudaStream_t s );
 
 // Radius: count pass (counts[n_tgt]) and fill pass given offsets.
 void radius_count( Lbvh const &tree, PointsView tgt, uint32_t const *order, double r,
-                   int64_t *counts, unsigned *status, cudaStream_t s );
+                   GroupArgs const &groups, int64_t *counts, unsigned *status, cudaStream_t s );
 void radius_fill( Lbvh const &tree, PointsView tgt, uint32_t const *order, double r,
-                  int32_t const *offset, int32_t *idx, unsigned *status, cudaStream_t s );
+                  GroupArgs const &groups, int32_t const *offset, int32_t *idx, unsigned *status,
+                  cudaStream_t s );
 
 // Setup (coefficients) kernels.
 struct SetupArgs
@@ -318,6 +336,20 @@ struct SetupArgs
 };
 void setup_fp64( SetupArgs const &a, cudaStream_t s );
 void setup_mixed( SetupArgs const &a, cudaStream_t s );
+// Rows too long for one thread (radius neighbourhoods): warp-cooperative
+// FP64 moments and coefficients around the reference Jacobi, for the n
+// targets listed in `targets`; writes coeff64 or (rounded) coeff32.
+void setup_long_rows( SetupArgs const &a, int32_t const *targets, int64_t n, cudaStream_t s );
+constexpr int LONG_ROW = 96; // rows longer than this take the warp-cooperative path
+
+// Setup over targets of mixed classes: the targets (in `order_host`, the
+// processing order) are bucketed by (basis, rbf, row longer than LONG_ROW);
+// each bucket runs the fused kernel of the requested precision (short rows)
+// or the warp-cooperative FP64 path (long rows).  basis_of / rbf_of give a
+// class per target (null: the uniform a.basis / a.rbf).
+void run_setup_plan( SetupArgs const &a, int precision, int32_t const *order_host,
+                     int32_t const *offsets_host, uint8_t const *basis_of, uint8_t const *rbf_of,
+                     cudaStream_t s );
 
 // Batched SVD pseudo-inverse (general n <= 64), DTK SVDFunctor semantics.
 void svd_pinv_batched( int n, int64_t count, double const *a, double *pinv,

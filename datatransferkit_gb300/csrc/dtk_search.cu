@@ -159,6 +159,23 @@ __global__ void k_morton( PointsView p, double const *scene, uint32_t *codes,
     }
 }
 
+__global__ void k_group_of( uint32_t const *group, uint32_t const *perm, int64_t n, uint32_t *out )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i < n )
+        out[i] = group[perm[i]];
+}
+
+__global__ void k_morton_of( PointsView p, uint32_t const *perm, double const *scene, uint32_t *codes )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i < p.n )
+    {
+        int64_t const o = perm[i];
+        codes[i] = morton3( p( o, 0 ), p( o, 1 ), p( o, 2 ), scene );
+    }
+}
+
 __global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double const *scene,
                                  double *sx, double *sy, double *sz, float *fx, float *fy,
                                  float *fz )
@@ -180,41 +197,56 @@ __global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double cons
 // ---------------------------------------------------------------------------
 // Karras hierarchy over leaf keys.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int delta( uint32_t const *codes, int64_t nl, int64_t i,
-                                      int64_t j )
+// Leaf key: (group of the leaf's first point, its Morton code); groups are
+// the problems of a batch (absent for a single operator).
+__device__ __forceinline__ unsigned long long leaf_key( uint32_t const *codes, uint32_t const *grp,
+                                                        int64_t leaf )
+{
+    unsigned long long k = codes[leaf * LEAF];
+    if ( grp )
+        k |= (unsigned long long)grp[leaf * LEAF] << 32;
+    return k;
+}
+
+__device__ __forceinline__ int delta( uint32_t const *codes, uint32_t const *grp, int64_t nl,
+                                      int64_t i, int64_t j )
 {
     if ( j < 0 || j >= nl )
         return -1;
-    uint32_t const ki = codes[i * LEAF], kj = codes[j * LEAF];
+    unsigned long long const ki = leaf_key( codes, grp, i ), kj = leaf_key( codes, grp, j );
     if ( ki != kj )
-        return __clz( ki ^ kj );
-    // equal leaf keys: ranks by leaf index, always above any 32-bit key prefix
-    return 32 + __clzll( (unsigned long long)( i ^ j ) );
+        return __clzll( ki ^ kj );
+    // equal leaf keys: ranks by leaf index, always above any 64-bit key prefix
+    return 64 + __clzll( (unsigned long long)( i ^ j ) );
 }
 
-__global__ void k_karras( uint32_t const *codes, int64_t nl, int *left, int *right,
-                          int *parent_node, int *parent_leaf )
+// Internal node i covers leaves [lo[i], hi[i]]; its left child covers
+// [lo, gamma] and its right child [gamma + 1, hi], gamma being the index of
+// the left child (leaf or internal, Karras 2012).
+__global__ void k_karras( uint32_t const *codes, uint32_t const *grp, int64_t nl, int *left,
+                          int *right, int *parent_node, int *parent_leaf, int *range_lo,
+                          int *range_hi )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i >= nl - 1 )
         return;
-    int const d = ( delta( codes, nl, i, i + 1 ) - delta( codes, nl, i, i - 1 ) ) >= 0 ? 1 : -1;
-    int const dmin = delta( codes, nl, i, i - d );
+    int const d = ( delta( codes, grp, nl, i, i + 1 ) - delta( codes, grp, nl, i, i - 1 ) ) >= 0 ? 1 : -1;
+    int const dmin = delta( codes, grp, nl, i, i - d );
     int64_t lmax = 2;
-    while ( delta( codes, nl, i, i + lmax * d ) > dmin )
+    while ( delta( codes, grp, nl, i, i + lmax * d ) > dmin )
         lmax <<= 1;
     int64_t l = 0;
     for ( int64_t t = lmax >> 1; t >= 1; t >>= 1 )
-        if ( delta( codes, nl, i, i + ( l + t ) * d ) > dmin )
+        if ( delta( codes, grp, nl, i, i + ( l + t ) * d ) > dmin )
             l += t;
     int64_t const j = i + l * d;
-    int const dnode = delta( codes, nl, i, j );
+    int const dnode = delta( codes, grp, nl, i, j );
     int64_t s = 0;
     int64_t t = l;
     do
     {
         t = ( t + 1 ) >> 1;
-        if ( delta( codes, nl, i, i + ( s + t ) * d ) > dnode )
+        if ( delta( codes, grp, nl, i, i + ( s + t ) * d ) > dnode )
             s += t;
     } while ( t > 1 );
     int64_t const gamma = i + s * d + min( d, 0 );
@@ -242,6 +274,8 @@ __global__ void k_karras( uint32_t const *codes, int64_t nl, int *left, int *rig
     }
     left[i] = lc;
     right[i] = rc;
+    range_lo[i] = (int)lo;
+    range_hi[i] = (int)hi;
 }
 
 struct Box
@@ -350,17 +384,25 @@ __global__ void k_refit( double const *sx, double const *sy, double const *sz,
 }
 
 __global__ void k_pack_children( int64_t n_internal, int const *left, int const *right,
-                                 float4 *nodes )
+                                 int const *range_lo, int const *range_hi, float4 *nodes )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i < n_internal )
         nodes[4 * i + 3] = make_float4( __int_as_float( left[i] ), __int_as_float( right[i] ),
-                                        0.f, 0.f );
+                                        __int_as_float( range_lo[i] ), __int_as_float( range_hi[i] ) );
 }
 
 // ---------------------------------------------------------------------------
 // Queries
 // ---------------------------------------------------------------------------
+struct GroupView
+{
+    int64_t const *src_off;  // per group: its sources' sorted positions [src_off[g], src_off[g+1])
+    uint32_t const *tgt_grp; // group of each target
+    int32_t const *k;        // per-group k (kNN)
+    double const *r;         // per-group radius
+};
+
 struct TreeView
 {
     double const *sx, *sy, *sz;
@@ -424,7 +466,7 @@ __device__ __forceinline__ int64_t warp_lower_bound( uint32_t const *codes, int6
 
 __device__ __forceinline__ void load_node( float4 const *nodes, int node, float *l_lo,
                                            float *l_hi, float *r_lo, float *r_hi, int &lc,
-                                           int &rc )
+                                           int &rc, int &lo, int &hi )
 {
     float4 const a = __ldg( nodes + 4 * (int64_t)node );
     float4 const b = __ldg( nodes + 4 * (int64_t)node + 1 );
@@ -444,6 +486,41 @@ __device__ __forceinline__ void load_node( float4 const *nodes, int node, float 
     r_hi[2] = c.w;
     lc = __float_as_int( e.x );
     rc = __float_as_int( e.y );
+    lo = __float_as_int( e.z );
+    hi = __float_as_int( e.w );
+}
+
+// The problem (group) of a query: its sources' sorted-position range
+// [ps, pe) and leaf range [lps, lpe]; an ungrouped tree has one group.
+struct Range
+{
+    int64_t ps, pe;
+    int lps, lpe;
+    int g;
+};
+
+__device__ __forceinline__ Range query_range( TreeView const &tr, GroupView const &gv, int64_t qi )
+{
+    Range r;
+    r.g = gv.tgt_grp ? (int)gv.tgt_grp[qi] : 0;
+    r.ps = gv.src_off ? gv.src_off[r.g] : 0;
+    r.pe = gv.src_off ? gv.src_off[r.g + 1] : tr.n;
+    r.lps = (int)( r.ps / LEAF );
+    r.lpe = r.pe > r.ps ? (int)( ( r.pe - 1 ) / LEAF ) : -1;
+    return r;
+}
+
+// Leaf ranges of a node's children (left covers [lo, gamma], right
+// [gamma + 1, hi], gamma the left child's index) outside the query's leaf
+// range are pruned by giving them an infinite lower bound.
+__device__ __forceinline__ void clip_children( int lc, int lo, int hi, Range const &q, float &lbl,
+                                               float &lbr )
+{
+    int const gamma = lc >= 0 ? lc : ~lc;
+    if ( gamma < q.lps || lo > q.lpe )
+        lbl = __int_as_float( 0x7f800000 );
+    if ( hi < q.lps || gamma + 1 > q.lpe )
+        lbr = __int_as_float( 0x7f800000 );
 }
 
 // The query in the centred frame: an FP32 interval [qlo, qhi] certain to
@@ -495,8 +572,8 @@ __device__ __forceinline__ void d2_bounds( TreeView const &tr, Query const &q, i
 constexpr int QUEUE = 64;
 
 __global__ void __launch_bounds__( Q_WARPS * 32 )
-    k_knn( TreeView tr, PointsView tgt, uint32_t const *order, int k, int row,
-           int32_t *idx_out, unsigned *status )
+    k_knn( TreeView tr, PointsView tgt, uint32_t const *order, int k_all, GroupView gv,
+           int32_t const *offset, int32_t *idx_out, unsigned *status )
 {
     __shared__ int s_stack[Q_WARPS][STACK];
     __shared__ float s_lb[Q_WARPS][STACK];
@@ -506,19 +583,25 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     if ( w >= tgt.n )
         return;
     int64_t const qi = order ? (int64_t)order[w] : w;
+    Range const rg = query_range( tr, gv, qi );
+    int64_t const ng = rg.pe - rg.ps;
+    int const k = gv.k ? gv.k[rg.g] : k_all;
+    int const row = (int)( k < ng ? k : ng );
+    if ( row <= 0 )
+        return;
     Query const q = make_query( tr, tgt, qi );
     unsigned const lt_mask = ( 1u << lane ) - 1u;
 
-    // Initial candidates: the 32 Morton-sorted sources around the target,
-    // with exact keys.
+    // Initial candidates: the 32 Morton-sorted sources of the query's
+    // problem around the target's code, with exact keys.
     uint32_t const code = morton3( q.tx, q.ty, q.tz, tr.scene );
-    int64_t const pos = warp_lower_bound( tr.codes, tr.n, code, lane );
-    int64_t const W = tr.n < 32 ? tr.n : (int64_t)32;
+    int64_t const pos = rg.ps + warp_lower_bound( tr.codes + rg.ps, ng, code, lane );
+    int64_t const W = ng < 32 ? ng : (int64_t)32;
     int64_t s0 = pos - 16;
-    if ( s0 > tr.n - W )
-        s0 = tr.n - W;
-    if ( s0 < 0 )
-        s0 = 0;
+    if ( s0 > rg.pe - W )
+        s0 = rg.pe - W;
+    if ( s0 < rg.ps )
+        s0 = rg.ps;
     unsigned long long kd = KEY_INF;
     int ki = 0x7fffffff;
     if ( lane < W )
@@ -610,7 +693,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     auto process_leaf = [&]( int leaf ) {
         int64_t const p = (int64_t)leaf * LEAF + lane;
         bool surv = false;
-        if ( p < tr.n && !( p >= s0 && p < s0 + W ) )
+        if ( p >= rg.ps && p < rg.pe && !( p >= s0 && p < s0 + W ) )
         {
             float lo, hi;
             d2_bounds( tr, q, p, lo, hi );
@@ -645,10 +728,11 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
                 break;
             }
             float l_lo[3], l_hi[3], r_lo[3], r_hi[3];
-            int lc, rc;
-            load_node( tr.nodes, node, l_lo, l_hi, r_lo, r_hi, lc, rc );
-            float const lbl = box_lb( l_lo, l_hi, q.qlo, q.qhi );
-            float const lbr = box_lb( r_lo, r_hi, q.qlo, q.qhi );
+            int lc, rc, nlo, nhi;
+            load_node( tr.nodes, node, l_lo, l_hi, r_lo, r_hi, lc, rc, nlo, nhi );
+            float lbl = box_lb( l_lo, l_hi, q.qlo, q.qhi );
+            float lbr = box_lb( r_lo, r_hi, q.qlo, q.qhi );
+            clip_children( lc, nlo, nhi, rg, lbl, lbr );
             bool const near_left = lbl <= lbr;
             int const c_near = near_left ? lc : rc, c_far = near_left ? rc : lc;
             float const lb_near = near_left ? lbl : lbr, lb_far = near_left ? lbr : lbl;
@@ -696,7 +780,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     if ( qn > 0 )
         flush( qn );
     if ( lane < row )
-        idx_out[qi * (int64_t)row + lane] = ki;
+        idx_out[offset[qi] + lane] = ki;
 }
 
 // Radius traversal shared by the count and fill passes.  FILL=false counts
@@ -707,7 +791,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
 // only the rest pay for an FP64 distance.
 template <bool FILL>
 __global__ void __launch_bounds__( Q_WARPS * 32 )
-    k_radius( TreeView tr, PointsView tgt, uint32_t const *order, double r,
+    k_radius( TreeView tr, PointsView tgt, uint32_t const *order, double r_all, GroupView gv,
               int64_t *counts, int32_t const *offset, int32_t *idx_out, unsigned *status )
 {
     __shared__ int s_stack[Q_WARPS][STACK];
@@ -716,6 +800,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     if ( w >= tgt.n )
         return;
     int64_t const qi = order ? (int64_t)order[w] : w;
+    Range const rg = query_range( tr, gv, qi );
+    double const r = gv.r ? gv.r[rg.g] : r_all;
     Query const q = make_query( tr, tgt, qi );
     double const r2 = __dmul_ru( r, r );
     float const bound_f = prune_threshold( (unsigned long long)__double_as_longlong( r2 ) );
@@ -727,7 +813,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     auto process_leaf = [&]( int leaf ) {
         int64_t const p = (int64_t)leaf * LEAF + lane;
         bool hit = false, unsure = false;
-        if ( p < tr.n )
+        if ( p >= rg.ps && p < rg.pe )
         {
             float lo, hi;
             d2_bounds( tr, q, p, lo, hi );
@@ -771,10 +857,13 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
                 break;
             }
             float l_lo[3], l_hi[3], r_lo[3], r_hi[3];
-            int lc, rc;
-            load_node( tr.nodes, node, l_lo, l_hi, r_lo, r_hi, lc, rc );
-            bool const hl = box_lb( l_lo, l_hi, q.qlo, q.qhi ) <= bound_f;
-            bool const hr = box_lb( r_lo, r_hi, q.qlo, q.qhi ) <= bound_f;
+            int lc, rc, nlo, nhi;
+            load_node( tr.nodes, node, l_lo, l_hi, r_lo, r_hi, lc, rc, nlo, nhi );
+            float lbl = box_lb( l_lo, l_hi, q.qlo, q.qhi );
+            float lbr = box_lb( r_lo, r_hi, q.qlo, q.qhi );
+            clip_children( lc, nlo, nhi, rg, lbl, lbr );
+            bool const hl = lbl <= bound_f;
+            bool const hr = lbr <= bound_f;
             int next = -1;
             if ( hl )
             {
@@ -829,7 +918,8 @@ unsigned blocks_for( int64_t n, int threads )
 
 } // namespace
 
-void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s )
+void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
+                 uint32_t const *group, int64_t n_groups )
 {
     int64_t const n = src.n;
     tree.n = n;
@@ -849,6 +939,20 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s )
                                                      tree.perm.get() );
     check_launch( "k_morton" );
     radix_sort_pairs( tree.codes.get(), tree.perm.get(), n, 30, s );
+    if ( group )
+    {
+        // problem-major order: a stable sort of the Morton order by group
+        tree.grp.allocate( n, s );
+        k_group_of<<<blocks_for( n, 256 ), 256, 0, s>>>( group, tree.perm.get(), n, tree.grp.get() );
+        check_launch( "k_group_of" );
+        int bits = 1;
+        while ( ( int64_t( 1 ) << bits ) < n_groups )
+            ++bits;
+        radix_sort_pairs( tree.grp.get(), tree.perm.get(), n, ( bits + 7 ) / 8 * 8, s );
+        k_morton_of<<<blocks_for( n, 256 ), 256, 0, s>>>( src, tree.perm.get(), tree.scene.get(),
+                                                            tree.codes.get() );
+        check_launch( "k_morton_of" );
+    }
 
     tree.sx.allocate( n, s );
     tree.sy.allocate( n, s );
@@ -865,16 +969,18 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s )
     tree.nodes.allocate( 4 * std::max<int64_t>( 1, ni ), s );
     tree.root_box.allocate( 2, s );
     DeviceBuffer<int> left( std::max<int64_t>( 1, ni ), s ), right( std::max<int64_t>( 1, ni ), s ),
-        parent_node( std::max<int64_t>( 1, ni ), s ), parent_leaf( nl, s );
+        parent_node( std::max<int64_t>( 1, ni ), s ), parent_leaf( nl, s ),
+        range_lo( std::max<int64_t>( 1, ni ), s ), range_hi( std::max<int64_t>( 1, ni ), s );
     DeviceBuffer<unsigned> flags( std::max<int64_t>( 1, ni ), s );
     DTK_CUDA_OR_THROW( cudaMemsetAsync( flags.get(), 0, flags.n * sizeof( unsigned ), s ) );
     if ( ni > 0 )
     {
-        k_karras<<<blocks_for( ni, 256 ), 256, 0, s>>>( tree.codes.get(), nl, left.get(), right.get(),
-                                                          parent_node.get(), parent_leaf.get() );
+        k_karras<<<blocks_for( ni, 256 ), 256, 0, s>>>( tree.codes.get(), tree.grp.get(), nl, left.get(),
+                                                          right.get(), parent_node.get(), parent_leaf.get(),
+                                                          range_lo.get(), range_hi.get() );
         check_launch( "k_karras" );
-        k_pack_children<<<blocks_for( ni, 256 ), 256, 0, s>>>( ni, left.get(), right.get(),
-                                                                 tree.nodes.get() );
+        k_pack_children<<<blocks_for( ni, 256 ), 256, 0, s>>>( ni, left.get(), right.get(), range_lo.get(),
+                                                                 range_hi.get(), tree.nodes.get() );
         check_launch( "k_pack_children" );
     }
     k_refit<<<blocks_for( nl, 128 ), 128, 0, s>>>( tree.sx.get(), tree.sy.get(), tree.sz.get(),
@@ -886,7 +992,7 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s )
 }
 
 void sort_queries( Lbvh const &tree, PointsView tgt, DeviceBuffer<uint32_t> &order,
-                   cudaStream_t s )
+                   cudaStream_t s, uint32_t const *group, int64_t n_groups )
 {
     int64_t const n = tgt.n;
     order.allocate( std::max<int64_t>( 1, n ), s );
@@ -896,36 +1002,49 @@ void sort_queries( Lbvh const &tree, PointsView tgt, DeviceBuffer<uint32_t> &ord
     k_morton<<<blocks_for( n, 256 ), 256, 0, s>>>( tgt, tree.scene.get(), codes.get(), order.get() );
     check_launch( "k_morton(targets)" );
     radix_sort_pairs( codes.get(), order.get(), n, 30, s );
+    if ( group )
+    {
+        k_group_of<<<blocks_for( n, 256 ), 256, 0, s>>>( group, order.get(), n, codes.get() );
+        check_launch( "k_group_of(targets)" );
+        int bits = 1;
+        while ( ( int64_t( 1 ) << bits ) < n_groups )
+            ++bits;
+        radix_sort_pairs( codes.get(), order.get(), n, ( bits + 7 ) / 8 * 8, s );
+    }
 }
 
-void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k, int32_t *idx,
-                unsigned *status, cudaStream_t s )
+void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
+                GroupArgs const &groups, int32_t const *offset, int32_t *idx, unsigned *status,
+                cudaStream_t s )
 {
-    if ( tgt.n == 0 || tree.n == 0 || k == 0 )
+    if ( tgt.n == 0 || tree.n == 0 || ( k == 0 && !groups.k ) )
         return;
-    int const row = (int)std::min<int64_t>( k, tree.n );
-    k_knn<<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, k, row,
+    GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
+    k_knn<<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, k, gv, offset,
                                                                   idx, status );
     check_launch( "k_knn" );
 }
 
 void radius_count( Lbvh const &tree, PointsView tgt, uint32_t const *order, double r,
-                   int64_t *counts, unsigned *status, cudaStream_t s )
+                   GroupArgs const &groups, int64_t *counts, unsigned *status, cudaStream_t s )
 {
     if ( tgt.n == 0 )
         return;
+    GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
     k_radius<false><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
-        view_of( tree ), tgt, order, r, counts, nullptr, nullptr, status );
+        view_of( tree ), tgt, order, r, gv, counts, nullptr, nullptr, status );
     check_launch( "k_radius(count)" );
 }
 
 void radius_fill( Lbvh const &tree, PointsView tgt, uint32_t const *order, double r,
-                  int32_t const *offset, int32_t *idx, unsigned *status, cudaStream_t s )
+                  GroupArgs const &groups, int32_t const *offset, int32_t *idx, unsigned *status,
+                  cudaStream_t s )
 {
     if ( tgt.n == 0 )
         return;
+    GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
     k_radius<true><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
-        view_of( tree ), tgt, order, r, nullptr, offset, idx, status );
+        view_of( tree ), tgt, order, r, gv, nullptr, offset, idx, status );
     check_launch( "k_radius(fill)" );
 }
 

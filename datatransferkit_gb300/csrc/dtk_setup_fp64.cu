@@ -483,6 +483,208 @@ __global__ void k_svd_general( int n, int64_t count, double const *a, double *pi
         atomicAdd( under, 1ull );
 }
 
+// ---------------------------------------------------------------------------
+// Long rows (radius neighbourhoods of hundreds to tens of thousands of
+// sources): the same FP64 stages in three kernels so that no single thread
+// walks a long row.  A warp per target assembles the moments (lanes split the
+// neighbours; the 55 sums are combined by shuffles) and later the
+// coefficients; one thread per target runs the reference Jacobi in between.
+// Work area per long target: NU moments + radius + M row-0 values (doubles).
+// ---------------------------------------------------------------------------
+template <int M>
+__global__ void __launch_bounds__( 128 )
+    k_long_moments( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
+                    int32_t const *targets, int64_t n, int rbf, double *work, unsigned *status )
+{
+    constexpr int NU = M * ( M + 1 ) / 2;
+    constexpr int STRIDE = NU + 1 + M;
+    int const lane = threadIdx.x & 31;
+    int64_t const w = ( blockIdx.x * (int64_t)blockDim.x + threadIdx.x ) >> 5;
+    if ( w >= n )
+        return;
+    int64_t const i = targets[w];
+    int64_t const b = offset[i];
+    int const len = offset[i + 1] - (int)b;
+    double const tx = tgt( i, 0 ), ty = tgt( i, 1 ), tz = tgt( i, 2 );
+    double d2max = 0.0;
+    bool bad = false;
+    for ( int j = lane; j < len; j += 32 )
+    {
+        int64_t const sj = idx[b + j];
+        if ( (uint64_t)sj >= (uint64_t)src.n )
+        {
+            bad = true;
+            continue;
+        }
+        d2max = fmax( d2max, dist2_rn( src( sj, 0 ), src( sj, 1 ), src( sj, 2 ), tx, ty, tz ) );
+    }
+    if ( __any_sync( FULL, bad ) )
+    {
+        if ( lane == 0 )
+            atomicOr( status, DEV_BAD_INDEX );
+        return;
+    }
+    for ( int o = 16; o; o >>= 1 )
+        d2max = fmax( d2max, __shfl_xor_sync( FULL, d2max, o ) );
+    double distance = 10. * DBL_EPSILON;
+    double const dmax = __dsqrt_rn( d2max );
+    if ( dmax > distance )
+        distance = dmax;
+    double const radius = 1.1 * distance;
+    double A[NU];
+#pragma unroll
+    for ( int u = 0; u < NU; ++u )
+        A[u] = 0.0;
+    for ( int j = lane; j < len; j += 32 )
+    {
+        int64_t const sj = idx[b + j];
+        double const x = __dsub_rn( src( sj, 0 ), tx ), y = __dsub_rn( src( sj, 1 ), ty ),
+                     z = __dsub_rn( src( sj, 2 ), tz );
+        double P[M];
+        basis_eval<M>( x, y, z, P );
+        double const dist =
+            __dsqrt_rn( __dadd_rn( __dadd_rn( __dmul_rn( x, x ), __dmul_rn( y, y ) ), __dmul_rn( z, z ) ) );
+        double const phi = rbf_eval<double>( rbf, dist / radius );
+        int o = 0;
+#pragma unroll
+        for ( int a = 0; a < M; ++a )
+        {
+            double const pa = P[a] * phi;
+#pragma unroll
+            for ( int c = a; c < M; ++c, ++o )
+                A[o] = fma( pa, P[c], A[o] );
+        }
+    }
+#pragma unroll
+    for ( int u = 0; u < NU; ++u )
+        for ( int o = 16; o; o >>= 1 )
+            A[u] += __shfl_xor_sync( FULL, A[u], o );
+    if ( lane == 0 )
+    {
+        double *out = work + w * STRIDE;
+#pragma unroll
+        for ( int u = 0; u < NU; ++u )
+            out[u] = A[u];
+        out[NU] = radius;
+    }
+}
+
+template <int M>
+__global__ void __launch_bounds__( SETUP_BLOCK )
+    k_long_jacobi( int64_t n, double *work, unsigned long long *under_count,
+                   unsigned long long *rot_count, unsigned *status )
+{
+    constexpr int NU = M * ( M + 1 ) / 2;
+    constexpr int STRIDE = NU + 1 + M;
+    extern __shared__ double smem[];
+    Smem<M> s{smem, smem + M * M * SETUP_BLOCK, smem + 2 * M * M * SETUP_BLOCK, (int)threadIdx.x};
+    int64_t const g = blockIdx.x * (int64_t)SETUP_BLOCK + threadIdx.x;
+    unsigned iters = 0;
+    int dropped = 0;
+    if ( g < n )
+    {
+        double *rec = work + g * STRIDE;
+        int o = 0;
+        for ( int a = 0; a < M; ++a )
+            for ( int c = a; c < M; ++c, ++o )
+            {
+                s.e( a, c ) = rec[o];
+                s.e( c, a ) = rec[o];
+            }
+        for ( int a = 0; a < M; ++a )
+        {
+            for ( int c = 0; c < M; ++c )
+                s.u( a, c ) = ( a == c ) ? 1.0 : 0.0;
+            s.v( a ) = a == 0 ? 1.0 : 0.0;
+        }
+        double row0[M];
+        dropped = jacobi_row0<M>( s, row0, iters, 200u * M * M + 2000u, status );
+        for ( int a = 0; a < M; ++a )
+            rec[NU + 1 + a] = row0[a];
+    }
+    unsigned long long it64 = iters, dr64 = dropped;
+    for ( int o = 16; o; o >>= 1 )
+    {
+        it64 += __shfl_xor_sync( FULL, it64, o );
+        dr64 += __shfl_xor_sync( FULL, dr64, o );
+    }
+    if ( threadIdx.x == 0 )
+    {
+        if ( it64 )
+            atomicAdd( rot_count, it64 );
+        if ( dr64 )
+            atomicAdd( under_count, dr64 );
+    }
+}
+
+template <int M>
+__global__ void __launch_bounds__( 128 )
+    k_long_coeffs( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
+                   int32_t const *targets, int64_t n, int rbf, double const *work, double *coeff64,
+                   float *coeff32 )
+{
+    constexpr int NU = M * ( M + 1 ) / 2;
+    constexpr int STRIDE = NU + 1 + M;
+    int const lane = threadIdx.x & 31;
+    int64_t const w = ( blockIdx.x * (int64_t)blockDim.x + threadIdx.x ) >> 5;
+    if ( w >= n )
+        return;
+    int64_t const i = targets[w];
+    int64_t const b = offset[i];
+    int const len = offset[i + 1] - (int)b;
+    double const tx = tgt( i, 0 ), ty = tgt( i, 1 ), tz = tgt( i, 2 );
+    double const *rec = work + w * STRIDE;
+    double const radius = rec[NU];
+    double row0[M];
+#pragma unroll
+    for ( int a = 0; a < M; ++a )
+        row0[a] = rec[NU + 1 + a];
+    for ( int j = lane; j < len; j += 32 )
+    {
+        int64_t const sj = idx[b + j];
+        double const x = __dsub_rn( src( sj, 0 ), tx ), y = __dsub_rn( src( sj, 1 ), ty ),
+                     z = __dsub_rn( src( sj, 2 ), tz );
+        double P[M];
+        basis_eval<M>( x, y, z, P );
+        double const dist =
+            __dsqrt_rn( __dadd_rn( __dadd_rn( __dmul_rn( x, x ), __dmul_rn( y, y ) ), __dmul_rn( z, z ) ) );
+        double const phi = rbf_eval<double>( rbf, dist / radius );
+        double acc = 0.0;
+#pragma unroll
+        for ( int a = 0; a < M; ++a )
+            acc = fma( row0[a], P[a], acc );
+        if ( coeff32 )
+            coeff32[b + j] = (float)( acc * phi );
+        else
+            coeff64[b + j] = acc * phi;
+    }
+}
+
+template <int M>
+void launch_long( SetupArgs const &a, int32_t const *targets, int64_t n, cudaStream_t s )
+{
+    constexpr int NU = M * ( M + 1 ) / 2;
+    DeviceBuffer<double> work( n * ( NU + 1 + M ), s );
+    unsigned const wblocks = (unsigned)( ( n * 32 + 127 ) / 128 );
+    k_long_moments<M><<<wblocks, 128, 0, s>>>( a.src, a.tgt, a.offset, a.idx, targets, n, a.rbf,
+                                                work.get(), a.status );
+    check_launch( "k_long_moments" );
+    size_t const smem = ( 2 * M * M + M ) * SETUP_BLOCK * sizeof( double );
+    static bool configured = false;
+    if ( !configured )
+    {
+        DTK_CUDA_OR_THROW( cudaFuncSetAttribute( k_long_jacobi<M>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem ) );
+        configured = true;
+    }
+    k_long_jacobi<M><<<(unsigned)( ( n + SETUP_BLOCK - 1 ) / SETUP_BLOCK ), SETUP_BLOCK, smem, s>>>(
+        n, work.get(), a.underdetermined, a.rotations, a.status );
+    check_launch( "k_long_jacobi" );
+    k_long_coeffs<M><<<wblocks, 128, 0, s>>>( a.src, a.tgt, a.offset, a.idx, targets, n, a.rbf,
+                                               work.get(), a.coeff64, a.coeff32 );
+    check_launch( "k_long_coeffs" );
+}
+
 template <int M>
 void launch_fp64( SetupArgs const &a, cudaStream_t s )
 {
@@ -518,6 +720,24 @@ void setup_fp64( SetupArgs const &a, cudaStream_t s )
         break;
     default:
         launch_fp64<10>( a, s );
+        break;
+    }
+}
+
+void setup_long_rows( SetupArgs const &a, int32_t const *targets, int64_t n, cudaStream_t s )
+{
+    if ( n == 0 )
+        return;
+    switch ( a.basis )
+    {
+    case DTK_CONSTANT3:
+        launch_long<1>( a, targets, n, s );
+        break;
+    case DTK_LINEAR3:
+        launch_long<4>( a, targets, n, s );
+        break;
+    default:
+        launch_long<10>( a, targets, n, s );
         break;
     }
 }

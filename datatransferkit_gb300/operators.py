@@ -259,6 +259,96 @@ class MovingLeastSquaresOperator(PointCloudOperator):
             pass
 
 
+class MovingLeastSquaresBatch:
+    """Many independent MLS transfers set up and applied together (extension).
+
+    The reference builds one ``MovingLeastSquaresOperator`` per problem; this
+    batch gives each problem the same results while sharing one search tree,
+    one setup pass and one apply launch per row-length bin.  ``problems`` is a
+    sequence of dicts with keys ``source_points``, ``target_points`` (float64
+    CUDA (n, 3) tensors), and optionally ``rbf``, ``basis``, ``k`` or
+    ``radius`` (every problem kNN, or every problem radius).  Values are packed
+    problem after problem: ``apply(source_values, target_values)`` takes the
+    concatenation of every problem's source values and writes the
+    concatenation of the target values; ``source_offsets`` and
+    ``target_offsets`` give each problem's range.  ``graph=True`` replays the
+    apply schedule from a captured CUDA graph.
+    """
+
+    def __init__(self, problems, *, precision="fp64", stream=None):
+        problems = list(problems)
+        if not problems:
+            raise _capi.InvalidArgument(1, "a batch needs at least one problem")
+        n = len(problems)
+        opts = (Options * n)()
+        src_parts, tgt_parts = [], []
+        src_off, tgt_off = [0], [0]
+        for p, pr in enumerate(problems):
+            src = _check_points(pr["source_points"], "source_points")
+            tgt = _check_points(pr["target_points"], "target_points")
+            if src.shape[1] != 3 or tgt.shape[1] != 3:
+                raise _capi.InvalidArgument(1, "source_points.extent(1) == 3")
+            o = opts[p]
+            lib().dtk_mls_default_options(C.byref(o))
+            o.rbf = (pr.get("rbf") or Wendland(0)).id
+            o.basis = (pr.get("basis") or MultivariatePolynomialBasis(Linear, 3)).id
+            o.k = int(pr.get("k") or 0)
+            o.radius = float(pr.get("radius") or 0.0)
+            o.precision = _PRECISIONS[precision]
+            src_parts.append(src)
+            tgt_parts.append(tgt)
+            src_off.append(src_off[-1] + src.shape[0])
+            tgt_off.append(tgt_off[-1] + tgt.shape[0])
+        self.source_points = torch.cat(src_parts).contiguous()
+        self.target_points = torch.cat(tgt_parts).contiguous()
+        self.source_offsets = src_off
+        self.target_offsets = tgt_off
+        self.n_problems = n
+        self._stream = stream
+        so = (C.c_int64 * (n + 1))(*src_off)
+        to = (C.c_int64 * (n + 1))(*tgt_off)
+        self._h = C.c_void_p()
+        check(lib().dtk_mls_batch_create(n, opts, so, self.source_points.data_ptr(), to,
+                                         self.target_points.data_ptr(), _stream(stream),
+                                         C.byref(self._h)))
+
+    def apply(self, source_values: torch.Tensor, target_values: torch.Tensor, graph: bool = True,
+              stream=None) -> None:
+        for t, n, what in ((source_values, self.source_offsets[-1], "source_values"),
+                           (target_values, self.target_offsets[-1], "target_values")):
+            if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float64:
+                raise _capi.InvalidArgument(1, f"{what} must be a float64 CUDA tensor")
+            if t.dim() != 1 or t.shape[0] != n or (n > 1 and t.stride(0) != 1):
+                raise _capi.InvalidArgument(1, f"{what} must be contiguous of length {n}")
+        check(lib().dtk_mls_batch_apply(self._h, source_values.data_ptr(), target_values.data_ptr(),
+                                        1 if graph else 0,
+                                        _stream(stream if stream is not None else self._stream)))
+
+    def csr(self):
+        """(offset, indices, coefficients) over all problems; indices are packed source indices."""
+        off, idx, coeff = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        nnz, f32 = C.c_int64(), C.c_int32()
+        check(lib().dtk_mls_batch_get_csr(self._h, C.byref(off), C.byref(idx), C.byref(coeff),
+                                          C.byref(nnz), C.byref(f32)))
+        torch.cuda.synchronize()
+        n = nnz.value
+        o = _from_device(off.value, self.target_offsets[-1] + 1, torch.int32)
+        i = _from_device(idx.value, n, torch.int32)
+        c = _from_device(coeff.value, n, torch.float32 if f32.value else torch.float64)
+        return o, i, c
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().dtk_mls_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class _DeviceArray:
     """Exposes a raw device pointer through __cuda_array_interface__."""
 

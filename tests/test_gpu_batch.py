@@ -1,0 +1,143 @@
+"""Batched uneven transfers (MovingLeastSquaresBatch) against one operator per
+problem: the oracle per problem, and the single GPU operator per problem.
+
+kNN batches: neighbour indices bit-exact (packed source numbering), and the
+coefficients bitwise equal to the single operator's (the same per-target
+setup on the same neighbour rows).  Radius batches (the batched workload's
+shape: Gaussian-mixture sources, uniform targets, radius 0.05, linear and
+quadratic bases alternating, FP64): rows equal as sets, coefficients and
+target values within the FP64 parity bound max(1e-12, 100 x spread) of each
+problem's oracle, where spread is the oracle's own distance to its
+multiply-add-contracted build.
+"""
+import numpy as np
+import pytest
+import torch
+
+import datatransferkit_gb300 as dtk
+from datatransferkit_gb300 import synthetic as syn
+from oracle import cpu
+from tests.test_gpu_mls_fp64 import BASIS, RBF, dev, rel_l2, tolerances
+
+pytestmark = pytest.mark.gpu
+
+
+def batch_inputs(problems):
+    return [dict(source_points=dev(p["src"]), target_points=dev(p["tgt"]), rbf=RBF[p["rbf"]],
+                 basis=BASIS[p["basis"]], k=p.get("k"), radius=p.get("radius")) for p in problems]
+
+
+def run_batch(problems, precision="fp64", graph=True):
+    b = dtk.MovingLeastSquaresBatch(batch_inputs(problems), precision=precision)
+    vals = np.concatenate([syn.smooth_field(p["src"]) for p in problems])
+    out = torch.full((b.target_offsets[-1],), np.nan, dtype=torch.float64, device="cuda")
+    b.apply(dev(vals), out, graph=graph)
+    off, idx, coeff = b.csr()
+    return b, vals, out.cpu().numpy(), off.cpu().numpy(), idx.cpu().numpy(), coeff.double().cpu().numpy()
+
+
+def assert_apply_close(a, b, off, idx, coeff, vals):
+    """|a - b| <= 1e-14 * sum_j |c_j v_j| per row: two summation orders of one row."""
+    mag = cpu.apply(off, idx, np.abs(coeff), np.abs(vals))
+    assert np.all(np.abs(a - b) <= 1e-14 * mag + 1e-300)
+
+
+def knn_problems(seed=11):
+    rng = np.random.default_rng(seed)
+    out = []
+    for p in range(12):
+        n_s = int(rng.integers(5, 3000)) if p != 3 else 7  # problem 3: fewer sources than k
+        n_t = int(rng.integers(0, 800)) if p != 5 else 0   # problem 5: no targets
+        out.append(dict(src=syn.uniform_points(n_s, seed + 2 * p) * (1 + p),
+                        tgt=syn.uniform_points(n_t, seed + 2 * p + 1) * (1 + p),
+                        rbf=p % 9, basis=(0, 1, 2)[p % 3], k=int(rng.integers(1, 33))))
+    return out
+
+
+def test_knn_batch_matches_single_operators_bitwise():
+    problems = knn_problems()
+    b, vals, out, off, idx, coeff = run_batch(problems)
+    so, to = b.source_offsets, b.target_offsets
+    for p, pr in enumerate(problems):
+        op = dtk.MovingLeastSquaresOperator(None, dev(pr["src"]), dev(pr["tgt"]), RBF[pr["rbf"]],
+                                            BASIS[pr["basis"]], k=pr["k"])
+        o1, i1, c1 = (t.cpu().numpy() for t in op.csr())
+        rows = slice(off[to[p]], off[to[p + 1]])
+        assert np.array_equal(off[to[p]:to[p + 1] + 1] - off[to[p]], o1)
+        assert np.array_equal(idx[rows] - so[p], i1)
+        assert np.array_equal(coeff[rows], c1)
+        ref = cpu.knn(pr["src"], pr["tgt"], pr["k"])
+        assert np.array_equal(i1, ref[1])
+        y = torch.empty(len(pr["tgt"]), dtype=torch.float64, device="cuda")
+        f = vals[so[p]:so[p + 1]]
+        op.apply(dev(f), y)
+        assert_apply_close(out[to[p]:to[p + 1]], y.cpu().numpy(), o1, i1, c1, f)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_graph_and_direct_apply_agree(precision):
+    problems = knn_problems(seed=23)
+    b, vals, out, off, idx, coeff = run_batch(problems, precision=precision, graph=True)
+    v = dev(vals)
+    direct = torch.empty(b.target_offsets[-1], dtype=torch.float64, device="cuda")
+    b.apply(v, direct, graph=False)
+    again = torch.empty_like(direct)
+    for _ in range(3):  # replays of the captured graph
+        b.apply(v, again, graph=True)
+    d = direct.cpu().numpy()
+    assert_apply_close(d, cpu.apply(off, idx, coeff, vals), off, idx, coeff, vals)
+    assert np.array_equal(again.cpu().numpy(), d)  # same launches, same lanes: bitwise
+    assert np.array_equal(out, d)
+
+
+def radius_problems(n_problems=16, seed=5):
+    """The batched workload's generator at reduced sizes (200 to 6000 points)."""
+    out = []
+    for p, pr in enumerate(syn.batched_problems(n_problems, seed, lo=200, hi=6000)):
+        out.append(dict(src=pr["src"], tgt=pr["tgt"][: max(1, len(pr["tgt"]) // 4)], rbf=1,
+                        basis=pr["basis"], radius=0.05))
+    return out
+
+
+def test_radius_batch_against_oracle_per_problem():
+    problems = radius_problems()
+    b, vals, out, off, idx, coeff = run_batch(problems)
+    so, to = b.source_offsets, b.target_offsets
+    long_rows = 0
+    for p, pr in enumerate(problems):
+        f = vals[so[p]:so[p + 1]]
+        ref = cpu.mls_transfer(pr["src"], pr["tgt"], f, 1, pr["basis"], r=0.05)
+        o = off[to[p]:to[p + 1] + 1] - off[to[p]]
+        assert np.array_equal(o, ref["offset"])
+        long_rows += int((np.diff(o) > 96).sum())
+        base = off[to[p]]
+        tc, tt = tolerances(pr["src"], pr["tgt"], ref["offset"], ref["idx"], 1, pr["basis"], f,
+                            ref["coeff"])
+        for i in range(len(pr["tgt"])):
+            a = slice(base + o[i], base + o[i + 1])
+            r_ = slice(o[i], o[i + 1])
+            ia, ib = idx[a] - so[p], ref["idx"][r_]
+            oa, ob = np.argsort(ia), np.argsort(ib)
+            assert np.array_equal(ia[oa], ib[ob])
+            if o[i + 1] > o[i]:
+                ca, cb = coeff[a][oa], ref["coeff"][r_][ob]
+                assert np.abs(ca - cb).max() <= tc * max(np.abs(cb).max(), 1e-300), (p, i)
+        assert rel_l2(out[to[p]:to[p + 1]], ref["target"]) <= tt, p
+    assert long_rows > 0  # the warp-cooperative long-row setup ran
+
+
+def test_batch_preconditions():
+    src = dev(syn.uniform_points(50, 1))
+    tgt = dev(syn.uniform_points(10, 2))
+    with pytest.raises(dtk.InvalidArgument):  # kNN and radius problems mixed
+        dtk.MovingLeastSquaresBatch([dict(source_points=src, target_points=tgt, k=8),
+                                     dict(source_points=src, target_points=tgt, radius=0.1)])
+    with pytest.raises(dtk.InvalidArgument):  # a problem without sources
+        dtk.MovingLeastSquaresBatch([dict(source_points=src, target_points=tgt),
+                                     dict(source_points=src[:0], target_points=tgt)])
+    with pytest.raises(dtk.Unsupported):
+        dtk.MovingLeastSquaresBatch([dict(source_points=src, target_points=tgt, k=40)])
+    b = dtk.MovingLeastSquaresBatch([dict(source_points=src, target_points=tgt)])
+    with pytest.raises(dtk.InvalidArgument):
+        b.apply(torch.zeros(49, dtype=torch.float64, device="cuda"),
+                torch.zeros(10, dtype=torch.float64, device="cuda"))
