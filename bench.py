@@ -12,6 +12,11 @@ same metric through the public API with host buffers: the H2D copies of the
 points and the source field from pinned memory and the D2H copy of the
 target field are inside the timed region.
 
+At N=1 the line also carries ``rows``: short measurements (CUDA events,
+one warm-up, three steps) of the other workloads of the path -- the FP64
+form at 2M points with neighbour rows checked against the oracle, the
+256-problem batched radius transfer, and the 1M-point adjoint.
+
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Multi-GPU (torchrun, one process per GPU): targets shard across ranks
@@ -55,6 +60,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="mixed_8m", choices=sorted(WORKLOADS))
     ap.add_argument("--sample", type=int, default=20000, help="targets in the CPU/oracle sample")
+    ap.add_argument("--no-rows", action="store_true",
+                    help="skip the side measurements of the other workloads")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the timed steps of both forms (for profiler captures)")
     return ap.parse_args()
@@ -244,6 +251,151 @@ def run_reference(args, rank, world):
 
 
 # ---------------------------------------------------------------------------
+# side measurements: the other workloads of the path, one GPU
+# ---------------------------------------------------------------------------
+def _event_time(torch, stream, fn, steps, warmup):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def row_fp64_2m(torch, dtk, syn, dev, stream, sample):
+    """Plain FP64 form at scale: 2M U[0,1]^3 sources, 2M targets on a jittered
+    126^3 grid, Quadratic3, Wendland<2>, k = 32; neighbour rows of a target
+    sample compared bit-exact with the oracle, values by relative L2."""
+    from oracle import cpu as ocpu
+    src, tgt, rbf, basis_id, k = make_inputs("fp64_2m")
+    vals = syn.smooth_field(src)
+    s_d, t_d, v_d = (torch.from_numpy(a).to(dev) for a in (src, tgt, vals))
+    out = torch.empty(len(tgt), dtype=torch.float64, device=dev)
+    W2, Q = dtk.Wendland(2), dtk.MultivariatePolynomialBasis(dtk.Quadratic, 3)
+    ops = []
+
+    def step():
+        op = dtk.MovingLeastSquaresOperator(None, s_d, t_d, W2, Q, k=k, precision="fp64")
+        op.apply(v_d, out)
+        ops.append(op.stage_times_ms)
+
+    ms = _event_time(torch, stream, step, 3, 1)
+    op = dtk.MovingLeastSquaresOperator(None, s_d, t_d, W2, Q, k=k, precision="fp64")
+    op.apply(v_d, out)
+    off, idx, _ = op.csr()
+    sub = tgt[:sample]
+    o_off, o_idx, _ = ocpu.knn(src, sub, k)
+    coeff, _, _, _ = ocpu.mls_coefficients(src, sub, o_off, o_idx, rbf, basis_id)
+    y_ref = ocpu.apply(o_off, o_idx, coeff, vals)
+    y = out[:sample].cpu().numpy()
+    return {"workload": "2M U[0,1]^3 sources, 126^3 jittered-grid targets, Quadratic3, Wendland<2>, k=32, FP64",
+            "value": len(tgt) / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+            "stages_ms": {"search": float(np.mean([t[0] for t in ops[1:]])),
+                          "setup": float(np.mean([t[1] for t in ops[1:]]))},
+            "neighbours_bit_exact_sample": bool(np.array_equal(idx[: len(o_idx)].cpu().numpy(), o_idx)),
+            "rel_l2_vs_oracle_sample": float(np.linalg.norm(y - y_ref) / np.linalg.norm(y_ref)),
+            "sample_targets": int(sample)}
+
+
+def row_batch_256(torch, dtk, syn, dev, stream):
+    """Batched uneven transfers: 256 problems, sizes log-uniform 1e3..1e5,
+    Gaussian-mixture sources (8 clusters, sigma 0.02..0.2), U[0,1]^3 targets,
+    radius 0.05, linear/quadratic alternating, Wendland<2>, FP64.  One step =
+    batch setup (one search, one bucketed setup) + one graph-replayed apply."""
+    from oracle import cpu as ocpu
+    probs = syn.batched_problems(256, 5)
+    W2 = dtk.Wendland(2)
+    B = {1: dtk.MultivariatePolynomialBasis(dtk.Linear, 3), 2: dtk.MultivariatePolynomialBasis(dtk.Quadratic, 3)}
+    inputs = [dict(source_points=torch.from_numpy(p["src"]).to(dev),
+                   target_points=torch.from_numpy(p["tgt"]).to(dev), rbf=W2, basis=B[p["basis"]],
+                   radius=0.05) for p in probs]
+    vals = np.concatenate([syn.smooth_field(p["src"]) for p in probs])
+    v_d = torch.from_numpy(vals).to(dev)
+    n_tgt = sum(len(p["tgt"]) for p in probs)
+    out = torch.empty(n_tgt, dtype=torch.float64, device=dev)
+    holder = {}
+
+    def step():
+        b = dtk.MovingLeastSquaresBatch(inputs, precision="fp64")
+        b.apply(v_d, out, graph=True)
+        holder["b"] = b
+
+    ms = _event_time(torch, stream, step, 3, 1)
+    b = holder["b"]
+    ms_graph = _event_time(torch, stream, lambda: b.apply(v_d, out, graph=True), 20, 3)
+    ms_direct = _event_time(torch, stream, lambda: b.apply(v_d, out, graph=False), 20, 3)
+    off, idx, coeff = b.csr()
+    off = off.cpu().numpy()
+    rows = np.diff(off)
+    y = out.cpu().numpy()
+    # oracle on the smallest and the largest problem
+    sizes = [len(p["src"]) for p in probs]
+    errs = {}
+    for p in (int(np.argmin(sizes)), int(np.argmax(sizes))):
+        pr = probs[p]
+        f = vals[b.source_offsets[p]:b.source_offsets[p + 1]]
+        ref = ocpu.mls_transfer(pr["src"], pr["tgt"], f, 1, pr["basis"], r=0.05)
+        yp = y[b.target_offsets[p]:b.target_offsets[p + 1]]
+        errs[f"problem_{p}_n{sizes[p]}"] = float(np.linalg.norm(yp - ref["target"]) /
+                                                  max(np.linalg.norm(ref["target"]), 1e-300))
+    return {"workload": "256 problems, log-uniform 1e3..1e5 points, Gaussian-mixture sources, radius 0.05, "
+                        "Linear3/Quadratic3 alternating, Wendland<2>, FP64",
+            "value": n_tgt / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+            "n_sources": int(sum(sizes)), "n_targets": int(n_tgt), "nnz": int(off[-1]),
+            "row_length": {"mean": float(rows.mean()), "p50": float(np.percentile(rows, 50)),
+                           "p99": float(np.percentile(rows, 99)), "max": int(rows.max())},
+            "apply_ms": {"graph": ms_graph, "direct": ms_direct},
+            "rel_l2_vs_oracle": errs}
+
+
+def row_adjoint_1m(torch, dtk, syn, dev, stream):
+    """Adjoint: 1M/1M U[0,1]^3, Quadratic3, Wendland<2>, k = 32, FP64;
+    L = 1/2 ||T f - g||^2, g = f + 0.05 cos(4 pi z) at the targets.  One step =
+    setup + forward + adjoint (source values and source coordinates)."""
+    src = syn.uniform_points(1_000_000, 12)
+    tgt = syn.uniform_points(1_000_000, 13)
+    f = syn.smooth_field(src)
+    g = syn.smooth_field(tgt) + 0.05 * np.cos(4 * np.pi * tgt[:, 2])
+    s_d, t_d, f_d, g_d = (torch.from_numpy(a).to(dev) for a in (src, tgt, f, g))
+    y = torch.empty(len(tgt), dtype=torch.float64, device=dev)
+    W2, Q = dtk.Wendland(2), dtk.MultivariatePolynomialBasis(dtk.Quadratic, 3)
+    holder = {}
+
+    def step():
+        op = dtk.MovingLeastSquaresOperator(None, s_d, t_d, W2, Q, k=32, keep_points=True)
+        op.apply(f_d, y)
+        holder["g"] = op.apply_adjoint(y - g_d, f_d, coords=True)
+        holder["op"] = op
+
+    ms = _event_time(torch, stream, step, 3, 1)
+    op = holder["op"]
+    ms_adj = _event_time(torch, stream, lambda: op.apply_adjoint(y - g_d, f_d, coords=True), 3, 1)
+    ms_adj_v = _event_time(torch, stream, lambda: op.apply_adjoint(y - g_d), 5, 1)
+    return {"workload": "1M/1M U[0,1]^3, Quadratic3, Wendland<2>, k=32, FP64, L=1/2||Tf-g||^2",
+            "value": len(tgt) / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+            "adjoint_ms": {"values_and_coords": ms_adj, "values_only": ms_adj_v}}
+
+
+def run_rows(args, dev, stream):
+    import torch
+    import datatransferkit_gb300 as dtk
+    from datatransferkit_gb300 import synthetic as syn
+    rows = {}
+    for name, fn in (("fp64_2m", lambda: row_fp64_2m(torch, dtk, syn, dev, stream, args.sample)),
+                     ("batch_256", lambda: row_batch_256(torch, dtk, syn, dev, stream)),
+                     ("adjoint_1m", lambda: row_adjoint_1m(torch, dtk, syn, dev, stream))):
+        t0 = time.perf_counter()
+        rows[name] = fn()
+        rows[name]["wall_s"] = time.perf_counter() - t0
+        torch.cuda.empty_cache()
+    return rows
+
+
+# ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
 def run_ours(args, rank, world, local_rank):
@@ -365,6 +517,8 @@ def run_ours(args, rank, world, local_rank):
     barrier()
     ms_e2e = max_over_ranks(e0.elapsed_time(e1) / args.steps)
 
+    rows = run_rows(args, dev, stream) if (world == 1 and not args.no_rows) else None
+
     if rank != 0:
         return
     # -- roofline of the dominant kernel (the mixed setup kernel) ----------------
@@ -409,6 +563,8 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
+    if rows is not None:
+        line["rows"] = rows
     if cpu is not None:
         line["cpu_baseline"] = {
             "value": cpu["value"], "unit": UNIT, "cores": cpu["threads"], "kind": "port",
