@@ -23,7 +23,7 @@ EXPORTED = [
     "dtk_mls_get_csr", "dtk_mls_get_sizes", "dtk_mls_underdetermined_count",
     "dtk_mls_get_stage_times", "dtk_mls_get_rotation_count", "dtk_mls_destroy",
     "dtk_knn_search", "dtk_svd_pinv", "dtk_mls_batch_create", "dtk_mls_batch_apply",
-    "dtk_mls_batch_get_csr", "dtk_mls_batch_destroy", "dtk_last_error", "dtk_status_string",
+    "dtk_mls_batch_get_csr", "dtk_mls_batch_destroy", "dtk_mls_batch_get_stage_times", "dtk_last_error", "dtk_status_string",
     "dtk_kernel_launch_count", "dtk_svd_pinv_noalloc",
 ]
 
@@ -79,6 +79,8 @@ def _declare(L):
     L.dtk_mls_batch_apply.argtypes = [_vp, _vp, _vp, C.c_int32, _vp]
     L.dtk_mls_batch_get_csr.argtypes = L.dtk_mls_get_csr.argtypes
     L.dtk_mls_batch_destroy.argtypes = [_vp]
+    L.dtk_mls_batch_get_stage_times.argtypes = [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                                C.POINTER(C.c_float)]
     L.dtk_last_error.restype = C.c_char_p
     L.dtk_last_error.argtypes = []
     L.dtk_status_string.restype = C.c_char_p

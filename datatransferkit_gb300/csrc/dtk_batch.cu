@@ -5,19 +5,28 @@
 // problem-major Morton order: problem p's sources occupy one contiguous range
 // of sorted positions, every tree node records the leaf range it covers, and
 // a query only enters nodes and points of its own problem.  Targets are
-// processed in problem-major Morton order.  The setup buckets targets by
-// (basis, rbf, row length): rows up to LONG_ROW run the fused one-thread-per-
-// target kernel of the requested precision, longer radius rows the
-// warp-cooperative FP64 path.  Apply runs one launch per row-length bin
-// (rows of up to 2^b entries), each with the lanes-per-row an autotuner
-// picked on the first call by timing the candidates on the actual data; the
-// bin launches are captured once into a CUDA graph and replayed.
+// processed in problem-major Morton order.  The setup is planned on the
+// device: a stable key sort splits the processing order into buckets of
+// (basis, rbf, path).  kNN rows run the fused one-thread-per-target kernel of
+// the requested precision; radius rows (0 to thousands of entries) run the
+// split FP64 path, with 8 lanes per target for rows of up to 32 entries and
+// 32 lanes beyond, so that no thread walks a long row alone.
+//
+// Apply is one persistent launch over a schedule of warp tasks.  Rows are
+// binned by length (bin b holds rows of at most 2^b entries); a task is up to
+// 32/S rows of one bin that a warp reduces with S lanes per row.  S per bin
+// comes from an autotuner that times the candidates on the actual data on
+// the first apply; the schedule is then fixed (longest bins first, so that
+// the slow tasks start early) and its launch can be captured into a CUDA
+// graph and replayed.
 #include "dtk_common.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <tuple>
@@ -26,38 +35,87 @@
 namespace dtk
 {
 
-void run_setup_plan( SetupArgs const &a, int precision, int32_t const *order_host,
-                     int32_t const *offsets_host, uint8_t const *basis_of, uint8_t const *rbf_of,
+namespace
+{
+
+constexpr int N_BASIS = 3, N_RBF = 9, N_PATH = 3;
+constexpr int N_KEYS = N_BASIS * N_RBF * N_PATH;
+
+// Bucket key of every target in processing order, the targets themselves as
+// sort values, and a histogram of the keys.
+__global__ void k_plan_keys( int64_t n, uint32_t const *order, int32_t const *offset,
+                             uint32_t const *tgt_grp, uint8_t const *basis_g, uint8_t const *rbf_g,
+                             int basis, int rbf, bool split_all, uint32_t *keys, uint32_t *vals,
+                             unsigned *hist )
+{
+    __shared__ unsigned h[N_KEYS];
+    for ( int k = threadIdx.x; k < N_KEYS; k += blockDim.x )
+        h[k] = 0;
+    __syncthreads();
+    int64_t const g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( g < n )
+    {
+        uint32_t const i = order[g];
+        int const len = offset[i + 1] - offset[i];
+        uint32_t const grp = tgt_grp ? tgt_grp[i] : 0u;
+        int const b = basis_g ? basis_g[grp] : basis;
+        int const r = rbf_g ? rbf_g[grp] : rbf;
+        int const path = split_all ? ( len > 32 ? 2 : 1 ) : ( len > FUSED_MAX_ROW ? 2 : 0 );
+        uint32_t const key = (uint32_t)( ( b * N_RBF + r ) * N_PATH + path );
+        keys[g] = key;
+        vals[g] = i;
+        atomicAdd( &h[key], 1u );
+    }
+    __syncthreads();
+    for ( int k = threadIdx.x; k < N_KEYS; k += blockDim.x )
+        if ( h[k] )
+            atomicAdd( &hist[k], h[k] );
+}
+
+} // namespace
+
+void run_setup_plan( SetupArgs const &a, int precision, uint8_t const *basis_of_group,
+                     uint8_t const *rbf_of_group, uint32_t const *tgt_group, bool split_all,
                      cudaStream_t s )
 {
-    std::map<std::tuple<int, int, int>, std::vector<int32_t>> buckets;
-    for ( int64_t g = 0; g < a.n_tgt; ++g )
+    int64_t const n = a.n_tgt;
+    if ( n == 0 )
+        return;
+    DeviceBuffer<uint32_t> keys( n, s ), vals( n, s );
+    DeviceBuffer<unsigned> hist( N_KEYS, s );
+    DTK_CUDA_OR_THROW( cudaMemsetAsync( hist.get(), 0, N_KEYS * sizeof( unsigned ), s ) );
+    k_plan_keys<<<(unsigned)( ( n + 255 ) / 256 ), 256, 0, s>>>( n, a.order, a.offset, tgt_group, basis_of_group,
+                                                                  rbf_of_group, a.basis, a.rbf, split_all,
+                                                                  keys.get(), vals.get(), hist.get() );
+    check_launch( "k_plan_keys" );
+    // stable: each bucket keeps the processing order
+    radix_sort_pairs( keys.get(), vals.get(), n, 8, s );
+    unsigned h[N_KEYS];
+    DTK_CUDA_OR_THROW( cudaMemcpyAsync( h, hist.get(), sizeof( h ), cudaMemcpyDeviceToHost, s ) );
+    DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+    int64_t start = 0;
+    for ( int key = 0; key < N_KEYS; ++key )
     {
-        int32_t const i = order_host[g];
-        int const len = offsets_host[i + 1] - offsets_host[i];
-        int const b = basis_of ? basis_of[i] : a.basis;
-        int const r = rbf_of ? rbf_of[i] : a.rbf;
-        buckets[std::make_tuple( b, r, len > LONG_ROW ? 1 : 0 )].push_back( i );
-    }
-    for ( auto const &kv : buckets )
-    {
-        std::vector<int32_t> const &list = kv.second;
-        int64_t const n = (int64_t)list.size();
-        DeviceBuffer<int32_t> d( n, s );
-        DTK_CUDA_OR_THROW( cudaMemcpyAsync( d.get(), list.data(), n * sizeof( int32_t ),
-                                            cudaMemcpyHostToDevice, s ) );
+        int64_t const cnt = h[key];
+        if ( cnt == 0 )
+            continue;
+        uint32_t const *list = vals.get() + start;
+        start += cnt;
         SetupArgs b = a;
-        b.basis = std::get<0>( kv.first );
-        b.rbf = std::get<1>( kv.first );
-        b.n_tgt = n;
-        b.order = reinterpret_cast<uint32_t const *>( d.get() );
-        if ( std::get<2>( kv.first ) )
-            setup_long_rows( b, d.get(), n, s );
-        else if ( precision == DTK_FP64 )
-            setup_fp64( b, s );
+        int const path = key % N_PATH;
+        b.basis = key / N_PATH / N_RBF;
+        b.rbf = key / N_PATH % N_RBF;
+        b.n_tgt = cnt;
+        b.order = list;
+        if ( path == 0 )
+        {
+            if ( precision == DTK_FP64 )
+                setup_fp64( b, s );
+            else
+                setup_mixed( b, s );
+        }
         else
-            setup_mixed( b, s );
-        // the stream-ordered free of `d` follows the launches
+            setup_split( b, reinterpret_cast<int32_t const *>( list ), cnt, path == 1 ? 8 : 32, s );
     }
 }
 
@@ -88,54 +146,88 @@ __global__ void k_narrow32( int64_t const *in, int32_t *out, int64_t n )
         out[i] = (int32_t)in[i];
 }
 
-constexpr unsigned FULL = 0xffffffffu;
-
-// S lanes per row over a list of rows.
-template <int S, bool F32>
-__global__ void __launch_bounds__( 256 )
-    k_apply_rows( int64_t n_rows, int32_t const *__restrict__ rows, int32_t const *__restrict__ offset,
-                  int32_t const *__restrict__ idx, void const *__restrict__ coeff,
-                  double const *__restrict__ values, double *__restrict__ target )
+// kNN row length of every target: min(k of its problem, sources of its problem)
+__global__ void k_knn_rows( int64_t n, uint32_t const *tgt_grp, int64_t const *src_off, int32_t const *k,
+                            int64_t *counts )
 {
-    int64_t const gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    int64_t const r = gt / S;
-    int const sub = (int)( gt % S );
-    double acc = 0.0;
-    int64_t row = 0;
-    if ( r < n_rows )
-    {
-        row = rows[r];
-        int const b = offset[row], e = offset[row + 1];
-        for ( int j = b + sub; j < e; j += S )
-        {
-            double const c = F32 ? (double)static_cast<float const *>( coeff )[j]
-                                 : static_cast<double const *>( coeff )[j];
-            acc = fma( c, __ldg( values + idx[j] ), acc );
-        }
-    }
-#pragma unroll
-    for ( int o = S / 2; o > 0; o >>= 1 )
-        acc += __shfl_xor_sync( FULL, acc, o );
-    if ( r < n_rows && sub == 0 )
-        target[row] = acc;
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i >= n )
+        return;
+    uint32_t const g = tgt_grp[i];
+    int64_t const ns = src_off[g + 1] - src_off[g];
+    counts[i] = k[g] < ns ? k[g] : ns;
 }
 
-template <bool F32>
-void launch_rows( int lanes, int64_t n_rows, int32_t const *rows, int32_t const *offset,
-                  int32_t const *idx, void const *coeff, double const *values, double *target,
-                  cudaStream_t s )
+// Apply bin of every target in processing order (bin b: rows of at most 2^b
+// entries), the targets as sort values, and a histogram of the bins.
+__global__ void k_bin_keys( int64_t n, uint32_t const *order, int32_t const *offset, uint32_t *keys,
+                            uint32_t *vals, unsigned *hist )
 {
-    unsigned const blocks = (unsigned)std::max<int64_t>( 1, ( n_rows * lanes + 255 ) / 256 );
-    switch ( lanes )
+    __shared__ unsigned h[32];
+    if ( threadIdx.x < 32 )
+        h[threadIdx.x] = 0;
+    __syncthreads();
+    int64_t const g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( g < n )
     {
-    case 1: k_apply_rows<1, F32><<<blocks, 256, 0, s>>>( n_rows, rows, offset, idx, coeff, values, target ); break;
-    case 2: k_apply_rows<2, F32><<<blocks, 256, 0, s>>>( n_rows, rows, offset, idx, coeff, values, target ); break;
-    case 4: k_apply_rows<4, F32><<<blocks, 256, 0, s>>>( n_rows, rows, offset, idx, coeff, values, target ); break;
-    case 8: k_apply_rows<8, F32><<<blocks, 256, 0, s>>>( n_rows, rows, offset, idx, coeff, values, target ); break;
-    case 16: k_apply_rows<16, F32><<<blocks, 256, 0, s>>>( n_rows, rows, offset, idx, coeff, values, target ); break;
-    default: k_apply_rows<32, F32><<<blocks, 256, 0, s>>>( n_rows, rows, offset, idx, coeff, values, target ); break;
+        uint32_t const i = order[g];
+        int const len = offset[i + 1] - offset[i];
+        int const b = len <= 1 ? 0 : 32 - __clz( len - 1 );
+        keys[g] = (uint32_t)b;
+        vals[g] = i;
+        atomicAdd( &h[b], 1u );
     }
-    check_launch( "k_apply_rows" );
+    __syncthreads();
+    if ( threadIdx.x < 32 && h[threadIdx.x] )
+        atomicAdd( &hist[threadIdx.x], h[threadIdx.x] );
+}
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int APPLY_THREADS = 256;
+
+// Task: x = first entry of its rows in the schedule's row list, y = lanes per
+// row S (low 6 bits, a power of two) | number of rows (<= 32 / S) << 6.
+template <bool F32>
+__global__ void __launch_bounds__( APPLY_THREADS )
+    k_apply_sched( int64_t n_tasks, int2 const *__restrict__ tasks, int32_t const *__restrict__ rows,
+                   int32_t const *__restrict__ offset, int32_t const *__restrict__ idx,
+                   void const *__restrict__ coeff, double const *__restrict__ values,
+                   double *__restrict__ target )
+{
+    int const lane = threadIdx.x & 31;
+    int64_t const warps = (int64_t)gridDim.x * ( APPLY_THREADS / 32 );
+    for ( int64_t t = ( blockIdx.x * (int64_t)APPLY_THREADS + threadIdx.x ) >> 5; t < n_tasks; t += warps )
+    {
+        int2 const task = __ldg( tasks + t );
+        int const S = task.y & 63, cnt = task.y >> 6;
+        int const shift = __ffs( S ) - 1;
+        int const r = lane >> shift, sub = lane & ( S - 1 );
+        double acc = 0.0;
+        int64_t row = -1;
+        if ( r < cnt )
+        {
+            row = __ldg( rows + task.x + r );
+            int const b = __ldg( offset + row ), e = __ldg( offset + row + 1 );
+            for ( int j = b + sub; j < e; j += S )
+            {
+                double const c = F32 ? (double)__ldg( static_cast<float const *>( coeff ) + j )
+                                     : __ldg( static_cast<double const *>( coeff ) + j );
+                acc = fma( c, __ldg( values + __ldg( idx + j ) ), acc );
+            }
+        }
+        for ( int o = S >> 1; o > 0; o >>= 1 ) // S is warp-uniform
+            acc += __shfl_xor_sync( FULL, acc, o );
+        if ( r < cnt && sub == 0 )
+            target[row] = acc;
+    }
+}
+
+inline int bin_of64( int64_t n )
+{
+    int b = 0;
+    while ( ( int64_t( 1 ) << b ) < n )
+        ++b;
+    return b;
 }
 
 } // namespace
@@ -151,14 +243,13 @@ struct dtk_mls_batch_s
     DeviceBuffer<int32_t> offset, idx;
     DeviceBuffer<double> coeff64;
     DeviceBuffer<float> coeff32;
-    struct Bin
-    {
-        int max_len;
-        int lanes;
-        int64_t n;
-        DeviceBuffer<int32_t> rows;
-    };
-    std::vector<Bin> bins;
+    // row bins: rows of bin b (at most 2^b entries) at [bin_start[b], bin_start[b+1]) of `rows`
+    static constexpr int NBINS = 32;
+    std::vector<int64_t> bin_start;
+    int lanes[NBINS] = {};
+    DeviceBuffer<int32_t> rows;
+    DeviceBuffer<int2> tasks;
+    int64_t n_tasks = 0;
     bool tuned = false;
     cudaStream_t capture = nullptr;
     cudaGraph_t graph = nullptr;
@@ -166,6 +257,8 @@ struct dtk_mls_batch_s
     double const *g_src = nullptr;
     double *g_tgt = nullptr;
     int64_t underdetermined = 0, rotations = 0;
+    float search_ms = 0.f, setup_ms = 0.f, host_ms = 0.f;
+
     ~dtk_mls_batch_s()
     {
         if ( exec )
@@ -175,21 +268,116 @@ struct dtk_mls_batch_s
         if ( capture )
             cudaStreamDestroy( capture );
     }
-    void launch_bins( double const *src_values, double *tgt_values, cudaStream_t s )
+
+    // schedule over the bins in `which` (longest first) with the given lanes
+    std::vector<int2> schedule( std::vector<int> const &which, int const *lanes_of ) const
     {
-        bool const f32 = coeff32.get() != nullptr;
-        void const *coeff = f32 ? (void const *)coeff32.get() : (void const *)coeff64.get();
-        for ( auto const &b : bins )
+        std::vector<int2> t;
+        for ( int b : which )
         {
-            if ( !b.n )
-                continue;
-            if ( f32 )
-                launch_rows<true>( b.lanes, b.n, b.rows.get(), offset.get(), idx.get(), coeff,
-                                   src_values, tgt_values, s );
-            else
-                launch_rows<false>( b.lanes, b.n, b.rows.get(), offset.get(), idx.get(), coeff,
-                                    src_values, tgt_values, s );
+            int const S = lanes_of[b], per = 32 / S;
+            for ( int64_t r = bin_start[b]; r < bin_start[b + 1]; r += per )
+            {
+                int const cnt = (int)std::min<int64_t>( per, bin_start[b + 1] - r );
+                t.push_back( make_int2( (int)r, S | ( cnt << 6 ) ) );
+            }
         }
+        return t;
+    }
+
+    void launch( int2 const *t, int64_t n, double const *src_values, double *tgt_values, cudaStream_t s ) const
+    {
+        if ( n == 0 )
+            return;
+        int64_t const want = ( n * 32 + APPLY_THREADS - 1 ) / APPLY_THREADS;
+        unsigned const blocks = (unsigned)std::max<int64_t>( 1, std::min<int64_t>( want, 8 * num_sms() ) );
+        if ( coeff32.get() )
+            k_apply_sched<true><<<blocks, APPLY_THREADS, 0, s>>>( n, t, rows.get(), offset.get(), idx.get(),
+                                                                  coeff32.get(), src_values, tgt_values );
+        else
+            k_apply_sched<false><<<blocks, APPLY_THREADS, 0, s>>>( n, t, rows.get(), offset.get(), idx.get(),
+                                                                   coeff64.get(), src_values, tgt_values );
+        check_launch( "k_apply_sched" );
+    }
+
+    // Time each candidate lanes-per-row on each bin (median of 3 after one
+    // warm-up), then upload the schedule of the winners.  Winners are kept
+    // per process by (bin, coefficient type, order of magnitude of the bin's
+    // row count), so later batches of a similar shape skip the timing.
+    void tune( double const *src_values, double *tgt_values, cudaStream_t s )
+    {
+        static std::mutex cache_mutex;
+        static std::map<std::tuple<int, bool, int>, int> cache;
+        bool const f32 = coeff32.get() != nullptr;
+        cudaEvent_t e0, e1;
+        DTK_CUDA_OR_THROW( cudaEventCreate( &e0 ) );
+        DTK_CUDA_OR_THROW( cudaEventCreate( &e1 ) );
+        struct EvGuard
+        {
+            cudaEvent_t a, b;
+            ~EvGuard()
+            {
+                cudaEventDestroy( a );
+                cudaEventDestroy( b );
+            }
+        } guard{e0, e1};
+        for ( int b = 0; b < NBINS; ++b )
+        {
+            if ( bin_start[b + 1] == bin_start[b] )
+                continue;
+            auto const key = std::make_tuple( b, f32, bin_of64( bin_start[b + 1] - bin_start[b] ) );
+            {
+                std::lock_guard<std::mutex> lock( cache_mutex );
+                auto const it = cache.find( key );
+                if ( it != cache.end() )
+                {
+                    lanes[b] = it->second;
+                    continue;
+                }
+            }
+            float best = 3.4e38f;
+            int best_lanes = 1;
+            for ( int S = 1; S <= 32; S <<= 1 )
+            {
+                if ( S > 1 && ( S >> 1 ) >= ( 1 << b ) )
+                    break; // more lanes than entries
+                int cand[NBINS];
+                std::fill( cand, cand + NBINS, S );
+                std::vector<int2> const t = schedule( {b}, cand );
+                DeviceBuffer<int2> d( t.size(), s );
+                DTK_CUDA_OR_THROW( cudaMemcpyAsync( d.get(), t.data(), t.size() * sizeof( int2 ),
+                                                    cudaMemcpyHostToDevice, s ) );
+                float ms[4];
+                for ( int rep = 0; rep < 4; ++rep )
+                {
+                    DTK_CUDA_OR_THROW( cudaEventRecord( e0, s ) );
+                    launch( d.get(), (int64_t)t.size(), src_values, tgt_values, s );
+                    DTK_CUDA_OR_THROW( cudaEventRecord( e1, s ) );
+                    DTK_CUDA_OR_THROW( cudaEventSynchronize( e1 ) );
+                    DTK_CUDA_OR_THROW( cudaEventElapsedTime( &ms[rep], e0, e1 ) );
+                }
+                std::sort( ms + 1, ms + 4 );
+                if ( ms[2] < best )
+                {
+                    best = ms[2];
+                    best_lanes = S;
+                }
+            }
+            lanes[b] = best_lanes;
+            std::lock_guard<std::mutex> lock( cache_mutex );
+            cache[key] = best_lanes;
+        }
+        std::vector<int> order;
+        for ( int b = NBINS - 1; b >= 0; --b )
+            if ( bin_start[b + 1] > bin_start[b] )
+                order.push_back( b );
+        std::vector<int2> const t = schedule( order, lanes );
+        n_tasks = (int64_t)t.size();
+        tasks.allocate( std::max<int64_t>( 1, n_tasks ), s );
+        if ( n_tasks )
+            DTK_CUDA_OR_THROW( cudaMemcpyAsync( tasks.get(), t.data(), t.size() * sizeof( int2 ),
+                                                cudaMemcpyHostToDevice, s ) );
+        tuned = true;
     }
 };
 
@@ -221,12 +409,9 @@ dtk_status guarded_batch( F &&f )
     }
 }
 
-int pow2_ceil( int v )
+double ms_since( std::chrono::steady_clock::time_point t0 )
 {
-    int p = 1;
-    while ( p < v )
-        p <<= 1;
-    return p;
+    return std::chrono::duration<double, std::milli>( std::chrono::steady_clock::now() - t0 ).count();
 }
 
 } // namespace
@@ -246,32 +431,32 @@ dtk_status dtk_mls_batch_create( int32_t n_problems, const dtk_mls_options *opts
         DTK_REQUIRE_OR_THROW( src_offsets[0] == 0 && tgt_offsets[0] == 0, "offsets must start at 0" );
         bool const radius_mode = opts[0].radius > 0.0;
         int const precision = opts[0].precision;
+        DTK_REQUIRE_OR_THROW( precision == DTK_FP64 || precision == DTK_MIXED, "unknown precision" );
         std::vector<int32_t> kq( n_problems );
         std::vector<double> rq( n_problems );
         for ( int p = 0; p < n_problems; ++p )
         {
-            DTK_REQUIRE_OR_THROW( opts[p].comm_size == 1 || opts[p].comm_size == 0 ? true : false,
-                                  "problem " + std::to_string( p ) + ": only single-rank operators" );
-            dtk_mls_options o = opts[p];
-            o.comm_size = 1;
-            DTK_REQUIRE_OR_THROW( o.rbf >= DTK_WENDLAND0 && o.rbf <= DTK_BUHMANN4, "unknown rbf" );
-            DTK_REQUIRE_OR_THROW( o.basis >= DTK_CONSTANT3 && o.basis <= DTK_QUADRATIC3, "unknown basis" );
-            DTK_REQUIRE_OR_THROW( o.precision == precision, "all problems of a batch share one precision form" );
+            dtk_mls_options const &o = opts[p];
+            std::string const pre = "problem " + std::to_string( p ) + ": ";
+            if ( o.comm_size > 1 )
+                throw Error{DTK_ERR_UNSUPPORTED, pre + "only single-rank operators"};
+            DTK_REQUIRE_OR_THROW( o.rbf >= DTK_WENDLAND0 && o.rbf <= DTK_BUHMANN4, pre + "unknown rbf" );
+            DTK_REQUIRE_OR_THROW( o.basis >= DTK_CONSTANT3 && o.basis <= DTK_QUADRATIC3, pre + "unknown basis" );
+            DTK_REQUIRE_OR_THROW( o.precision == precision, pre + "all problems of a batch share one precision form" );
             DTK_REQUIRE_OR_THROW( ( o.radius > 0.0 ) == radius_mode,
-                                  "all problems of a batch use kNN, or all use a radius search" );
-            DTK_REQUIRE_OR_THROW( std::isfinite( o.radius ) && o.radius >= 0.0, "bad radius" );
-            DTK_REQUIRE_OR_THROW( o.k >= 0, "k is negative" );
+                                  pre + "all problems of a batch use kNN, or all use a radius search" );
+            DTK_REQUIRE_OR_THROW( std::isfinite( o.radius ) && o.radius >= 0.0, pre + "bad radius" );
+            DTK_REQUIRE_OR_THROW( o.k >= 0, pre + "k is negative" );
             kq[p] = o.k ? o.k : basis_size( o.basis );
             if ( !radius_mode && kq[p] > 32 )
-                throw Error{DTK_ERR_UNSUPPORTED, "kNN search supports k <= 32"};
+                throw Error{DTK_ERR_UNSUPPORTED, pre + "kNN search supports k <= 32"};
             rq[p] = o.radius;
             // DTK_CHECK( !search_tree.empty() ) for every problem
-            DTK_REQUIRE_OR_THROW( src_offsets[p + 1] > src_offsets[p],
-                                  "problem " + std::to_string( p ) + " has no source points" );
-            DTK_REQUIRE_OR_THROW( tgt_offsets[p + 1] >= tgt_offsets[p], "target offsets decrease" );
+            DTK_REQUIRE_OR_THROW( src_offsets[p + 1] > src_offsets[p], pre + "no source points" );
+            DTK_REQUIRE_OR_THROW( tgt_offsets[p + 1] >= tgt_offsets[p], pre + "target offsets decrease" );
         }
         int64_t const n_src = src_offsets[n_problems], n_tgt = tgt_offsets[n_problems];
-        DTK_REQUIRE_OR_THROW( n_src <= INT32_MAX && n_tgt <= INT32_MAX, "too many points" );
+        DTK_REQUIRE_OR_THROW( n_src <= INT32_MAX && n_tgt < INT32_MAX, "too many points" );
         DTK_REQUIRE_OR_THROW( src != nullptr && ( n_tgt == 0 || tgt != nullptr ), "null points" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
         auto h = std::make_unique<dtk_mls_batch_s>();
@@ -281,11 +466,25 @@ dtk_status dtk_mls_batch_create( int32_t n_problems, const dtk_mls_options *opts
         h->n_tgt = n_tgt;
         PointsView const sv{src, n_src, 3, 1};
         PointsView const tv{tgt, n_tgt, 3, 1};
+        double host_ms = 0.0;
 
+        cudaEvent_t ev[3];
+        for ( auto &e : ev )
+            DTK_CUDA_OR_THROW( cudaEventCreate( &e ) );
+        struct EvGuard
+        {
+            cudaEvent_t *e;
+            ~EvGuard()
+            {
+                for ( int i = 0; i < 3; ++i )
+                    cudaEventDestroy( e[i] );
+            }
+        } evg{ev};
         DeviceBuffer<unsigned> status( 1, s );
         DeviceBuffer<unsigned long long> counters( 3, s );
         DTK_CUDA_OR_THROW( cudaMemsetAsync( status.get(), 0, sizeof( unsigned ), s ) );
         DTK_CUDA_OR_THROW( cudaMemsetAsync( counters.get(), 0, 3 * sizeof( unsigned long long ), s ) );
+        DTK_CUDA_OR_THROW( cudaEventRecord( ev[0], s ) );
         DeviceBuffer<int64_t> d_src_off( n_problems + 1, s ), d_tgt_off( n_problems + 1, s );
         DTK_CUDA_OR_THROW( cudaMemcpyAsync( d_src_off.get(), src_offsets, ( n_problems + 1 ) * 8,
                                             cudaMemcpyHostToDevice, s ) );
@@ -317,31 +516,20 @@ dtk_status dtk_mls_batch_create( int32_t n_problems, const dtk_mls_options *opts
         ga.k = d_k.get();
         ga.r = d_r.get();
         h->offset.allocate( n_tgt + 1, s );
-        std::vector<int32_t> off_h( n_tgt + 1, 0 );
-        if ( !radius_mode )
         {
-            int64_t acc = 0;
-            for ( int p = 0; p < n_problems; ++p )
+            // row lengths: min(k_p, sources of p) for kNN, a count pass for radius
+            DeviceBuffer<int64_t> counts( std::max<int64_t>( 1, n_tgt ), s ), offs( n_tgt + 1, s );
+            if ( !radius_mode )
             {
-                int64_t const row = std::min<int64_t>( kq[p], src_offsets[p + 1] - src_offsets[p] );
-                for ( int64_t i = tgt_offsets[p]; i < tgt_offsets[p + 1]; ++i )
+                if ( n_tgt )
                 {
-                    off_h[i] = (int32_t)acc;
-                    acc += row;
-                    DTK_REQUIRE_OR_THROW( acc <= INT32_MAX, "neighbour count exceeds int32 offsets" );
+                    k_knn_rows<<<(unsigned)( ( n_tgt + 255 ) / 256 ), 256, 0, s>>>(
+                        n_tgt, tgt_grp.get(), d_src_off.get(), d_k.get(), counts.get() );
+                    check_launch( "k_knn_rows" );
                 }
             }
-            off_h[n_tgt] = (int32_t)acc;
-            h->nnz = acc;
-            DTK_CUDA_OR_THROW( cudaMemcpyAsync( h->offset.get(), off_h.data(), ( n_tgt + 1 ) * 4,
-                                                cudaMemcpyHostToDevice, s ) );
-            h->idx.allocate( std::max<int64_t>( 1, acc ), s );
-            knn_query( tree, tv, order.get(), 0, ga, h->offset.get(), h->idx.get(), status.get(), s );
-        }
-        else
-        {
-            DeviceBuffer<int64_t> counts( std::max<int64_t>( 1, n_tgt ), s ), offs( n_tgt + 1, s );
-            radius_count( tree, tv, order.get(), 0.0, ga, counts.get(), status.get(), s );
+            else
+                radius_count( tree, tv, order.get(), 0.0, ga, counts.get(), status.get(), s );
             exclusive_scan_i64( counts.get(), offs.get(), n_tgt, s );
             int64_t total = 0;
             DTK_CUDA_OR_THROW( cudaMemcpyAsync( &total, offs.get() + n_tgt, 8, cudaMemcpyDeviceToHost, s ) );
@@ -350,29 +538,31 @@ dtk_status dtk_mls_batch_create( int32_t n_problems, const dtk_mls_options *opts
             h->nnz = total;
             k_narrow32<<<(unsigned)( ( n_tgt + 256 ) / 256 ), 256, 0, s>>>( offs.get(), h->offset.get(), n_tgt );
             check_launch( "k_narrow32" );
-            h->idx.allocate( std::max<int64_t>( 1, total ), s );
-            radius_fill( tree, tv, order.get(), 0.0, ga, h->offset.get(), h->idx.get(), status.get(), s );
-            DTK_CUDA_OR_THROW( cudaMemcpyAsync( off_h.data(), h->offset.get(), ( n_tgt + 1 ) * 4,
-                                                cudaMemcpyDeviceToHost, s ) );
         }
-        std::vector<int32_t> order_h( std::max<int64_t>( 1, n_tgt ) );
-        DTK_CUDA_OR_THROW( cudaMemcpyAsync( order_h.data(), order.get(), n_tgt * 4, cudaMemcpyDeviceToHost, s ) );
+        h->idx.allocate( std::max<int64_t>( 1, h->nnz ), s );
+        if ( !radius_mode )
+            knn_query( tree, tv, order.get(), 0, ga, h->offset.get(), h->idx.get(), status.get(), s );
+        else
+            radius_fill( tree, tv, order.get(), 0.0, ga, h->offset.get(), h->idx.get(), status.get(), s );
         tree = Lbvh();
-        DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+        DTK_CUDA_OR_THROW( cudaEventRecord( ev[1], s ) );
 
-        // --- setup, bucketed by (basis, rbf, row length) ---
-        std::vector<uint8_t> basis_of( std::max<int64_t>( 1, n_tgt ) ), rbf_of( std::max<int64_t>( 1, n_tgt ) );
+        // --- setup, bucketed on the device by (basis, rbf, path) ---
+        std::vector<uint8_t> basis_h( n_problems ), rbf_h( n_problems );
         for ( int p = 0; p < n_problems; ++p )
-            for ( int64_t i = tgt_offsets[p]; i < tgt_offsets[p + 1]; ++i )
-            {
-                basis_of[i] = (uint8_t)opts[p].basis;
-                rbf_of[i] = (uint8_t)opts[p].rbf;
-            }
+        {
+            basis_h[p] = (uint8_t)opts[p].basis;
+            rbf_h[p] = (uint8_t)opts[p].rbf;
+        }
+        DeviceBuffer<uint8_t> basis_g( n_problems, s ), rbf_g( n_problems, s );
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( basis_g.get(), basis_h.data(), n_problems, cudaMemcpyHostToDevice, s ) );
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( rbf_g.get(), rbf_h.data(), n_problems, cudaMemcpyHostToDevice, s ) );
         SetupArgs a{};
         a.src = sv;
         a.tgt = tv;
         a.offset = h->offset.get();
         a.idx = h->idx.get();
+        a.order = order.get();
         a.n_tgt = n_tgt;
         a.rows_sorted = !radius_mode;
         a.underdetermined = counters.get();
@@ -389,23 +579,33 @@ dtk_status dtk_mls_batch_create( int32_t n_problems, const dtk_mls_options *opts
             h->coeff32.allocate( std::max<int64_t>( 1, h->nnz ), s );
             a.coeff32 = h->coeff32.get();
         }
-        run_setup_plan( a, precision, order_h.data(), off_h.data(), basis_of.data(), rbf_of.data(), s );
+        auto const t1 = std::chrono::steady_clock::now();
+        run_setup_plan( a, precision, basis_g.get(), rbf_g.get(), tgt_grp.get(), radius_mode, s );
+        host_ms += ms_since( t1 );
+        DTK_CUDA_OR_THROW( cudaEventRecord( ev[2], s ) );
 
-        // --- apply schedule: rows binned by length (power-of-two bounds) ---
-        std::map<int, std::vector<int32_t>> bins;
-        for ( int64_t i = 0; i < n_tgt; ++i )
-            bins[pow2_ceil( std::max( 1, off_h[i + 1] - off_h[i] ) )].push_back( (int32_t)i );
-        for ( auto const &kv : bins )
+        // --- apply bins: rows grouped by length, processing order within a bin ---
+        if ( n_tgt )
         {
-            dtk_mls_batch_s::Bin b;
-            b.max_len = kv.first;
-            b.lanes = std::min( 32, std::max( 1, pow2_ceil( kv.first / 4 ) ) );
-            b.n = (int64_t)kv.second.size();
-            b.rows.allocate( b.n, s );
-            DTK_CUDA_OR_THROW( cudaMemcpyAsync( b.rows.get(), kv.second.data(), b.n * 4,
-                                                cudaMemcpyHostToDevice, s ) );
-            h->bins.push_back( std::move( b ) );
+            DeviceBuffer<uint32_t> keys( n_tgt, s );
+            DeviceBuffer<unsigned> hist( dtk_mls_batch_s::NBINS, s );
+            h->rows.allocate( n_tgt, s );
+            DTK_CUDA_OR_THROW( cudaMemsetAsync( hist.get(), 0, dtk_mls_batch_s::NBINS * sizeof( unsigned ), s ) );
+            k_bin_keys<<<(unsigned)( ( n_tgt + 255 ) / 256 ), 256, 0, s>>>(
+                n_tgt, order.get(), h->offset.get(), keys.get(), reinterpret_cast<uint32_t *>( h->rows.get() ),
+                hist.get() );
+            check_launch( "k_bin_keys" );
+            radix_sort_pairs( keys.get(), reinterpret_cast<uint32_t *>( h->rows.get() ), n_tgt, 8, s );
+            unsigned hb[dtk_mls_batch_s::NBINS];
+            DTK_CUDA_OR_THROW( cudaMemcpyAsync( hb, hist.get(), sizeof( hb ), cudaMemcpyDeviceToHost, s ) );
+            DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+            h->bin_start.assign( dtk_mls_batch_s::NBINS + 1, 0 );
+            for ( int b = 0; b < dtk_mls_batch_s::NBINS; ++b )
+                h->bin_start[b + 1] = h->bin_start[b] + hb[b];
         }
+        else
+            h->bin_start.assign( dtk_mls_batch_s::NBINS + 1, 0 );
+
         unsigned st = 0;
         unsigned long long cnt[3] = {0, 0, 0};
         DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, status.get(), sizeof( st ), cudaMemcpyDeviceToHost, s ) );
@@ -417,6 +617,9 @@ dtk_status dtk_mls_batch_create( int32_t n_problems, const dtk_mls_options *opts
             throw Error{DTK_ERR_INTERNAL, "search or setup reported an internal error"};
         h->underdetermined = (int64_t)cnt[0];
         h->rotations = (int64_t)cnt[1];
+        DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->search_ms, ev[0], ev[1] ) );
+        DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->setup_ms, ev[1], ev[2] ) );
+        h->host_ms = (float)host_ms;
         *out = h.release();
     } );
 }
@@ -430,55 +633,10 @@ dtk_status dtk_mls_batch_apply( dtk_mls_batch_handle h, const double *src_values
                               "null values" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
         if ( !h->tuned )
-        {
-            // autotune the lanes per row of every bin on the actual data
-            cudaEvent_t e0, e1;
-            DTK_CUDA_OR_THROW( cudaEventCreate( &e0 ) );
-            DTK_CUDA_OR_THROW( cudaEventCreate( &e1 ) );
-            bool const f32 = h->coeff32.get() != nullptr;
-            void const *coeff = f32 ? (void const *)h->coeff32.get() : (void const *)h->coeff64.get();
-            for ( auto &b : h->bins )
-            {
-                if ( !b.n )
-                    continue;
-                float best = 1e30f;
-                int best_lanes = b.lanes;
-                for ( int lanes = 1; lanes <= 32; lanes <<= 1 )
-                {
-                    if ( lanes > 2 * b.max_len && lanes > 1 )
-                        break;
-                    float t = 0.f;
-                    for ( int rep = 0; rep < 3; ++rep )
-                    {
-                        DTK_CUDA_OR_THROW( cudaEventRecord( e0, s ) );
-                        if ( f32 )
-                            launch_rows<true>( lanes, b.n, b.rows.get(), h->offset.get(), h->idx.get(), coeff,
-                                               src_values, tgt_values, s );
-                        else
-                            launch_rows<false>( lanes, b.n, b.rows.get(), h->offset.get(), h->idx.get(), coeff,
-                                                src_values, tgt_values, s );
-                        DTK_CUDA_OR_THROW( cudaEventRecord( e1, s ) );
-                        DTK_CUDA_OR_THROW( cudaEventSynchronize( e1 ) );
-                        float ms = 0.f;
-                        DTK_CUDA_OR_THROW( cudaEventElapsedTime( &ms, e0, e1 ) );
-                        if ( rep > 0 )
-                            t += ms;
-                    }
-                    if ( t < best )
-                    {
-                        best = t;
-                        best_lanes = lanes;
-                    }
-                }
-                b.lanes = best_lanes;
-            }
-            cudaEventDestroy( e0 );
-            cudaEventDestroy( e1 );
-            h->tuned = true;
-        }
+            h->tune( src_values, tgt_values, s );
         if ( !use_graph )
         {
-            h->launch_bins( src_values, tgt_values, s );
+            h->launch( h->tasks.get(), h->n_tasks, src_values, tgt_values, s );
             return;
         }
         if ( !h->exec || h->g_src != src_values || h->g_tgt != tgt_values )
@@ -496,7 +654,7 @@ dtk_status dtk_mls_batch_apply( dtk_mls_batch_handle h, const double *src_values
             if ( !h->capture )
                 DTK_CUDA_OR_THROW( cudaStreamCreateWithFlags( &h->capture, cudaStreamNonBlocking ) );
             DTK_CUDA_OR_THROW( cudaStreamBeginCapture( h->capture, cudaStreamCaptureModeThreadLocal ) );
-            h->launch_bins( src_values, tgt_values, h->capture );
+            h->launch( h->tasks.get(), h->n_tasks, src_values, tgt_values, h->capture );
             DTK_CUDA_OR_THROW( cudaStreamEndCapture( h->capture, &h->graph ) );
             DTK_CUDA_OR_THROW( cudaGraphInstantiate( &h->exec, h->graph, 0 ) );
             h->g_src = src_values;
@@ -522,6 +680,20 @@ dtk_status dtk_mls_batch_get_csr( dtk_mls_batch_handle h, const int32_t **offset
             *nnz = h->nnz;
         if ( coeff_is_fp32 )
             *coeff_is_fp32 = f32 ? 1 : 0;
+    } );
+}
+
+dtk_status dtk_mls_batch_get_stage_times( dtk_mls_batch_handle h, float *search_ms, float *setup_ms,
+                                          float *host_ms )
+{
+    return guarded_batch( [&] {
+        DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
+        if ( search_ms )
+            *search_ms = h->search_ms;
+        if ( setup_ms )
+            *setup_ms = h->setup_ms;
+        if ( host_ms )
+            *host_ms = h->host_ms;
     } );
 }
 

@@ -278,17 +278,9 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
             a.coeff32 = h->coeff32.get();
         }
         if ( g.radius_mode )
-        {
-            // radius rows are uneven: the planner sends rows longer than
-            // LONG_ROW to the warp-cooperative kernels
-            std::vector<int32_t> off_h( n_tgt + 1 ), order_h( std::max<int64_t>( 1, n_tgt ) );
-            DTK_CUDA_OR_THROW( cudaMemcpyAsync( off_h.data(), h->offset.get(), ( n_tgt + 1 ) * sizeof( int32_t ),
-                                                cudaMemcpyDeviceToHost, s ) );
-            DTK_CUDA_OR_THROW( cudaMemcpyAsync( order_h.data(), h->order.get(), n_tgt * sizeof( int32_t ),
-                                                cudaMemcpyDeviceToHost, s ) );
-            DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
-            run_setup_plan( a, g.opts.precision, order_h.data(), off_h.data(), nullptr, nullptr, s );
-        }
+            // radius rows are uneven (0 to thousands of entries): the split
+            // setup with 8 or 32 lanes per target by row length
+            run_setup_plan( a, g.opts.precision, nullptr, nullptr, nullptr, true, s );
         else if ( g.opts.precision == DTK_FP64 )
             setup_fp64( a, s );
         else

@@ -336,19 +336,22 @@ struct SetupArgs
 };
 void setup_fp64( SetupArgs const &a, cudaStream_t s );
 void setup_mixed( SetupArgs const &a, cudaStream_t s );
-// Rows too long for one thread (radius neighbourhoods): warp-cooperative
-// FP64 moments and coefficients around the reference Jacobi, for the n
-// targets listed in `targets`; writes coeff64 or (rounded) coeff32.
-void setup_long_rows( SetupArgs const &a, int32_t const *targets, int64_t n, cudaStream_t s );
-constexpr int LONG_ROW = 96; // rows longer than this take the warp-cooperative path
+// Split setup for uneven rows: FP64 moments and coefficients with `lanes`
+// (8 or 32) lanes per target around one thread per target for the reference
+// Jacobi, for the n targets listed in `targets`; writes coeff64 or (rounded)
+// coeff32.
+void setup_split( SetupArgs const &a, int32_t const *targets, int64_t n, int lanes, cudaStream_t s );
+constexpr int FUSED_MAX_ROW = 32; // longest row the fused one-thread-per-target kernels take
 
-// Setup over targets of mixed classes: the targets (in `order_host`, the
-// processing order) are bucketed by (basis, rbf, row longer than LONG_ROW);
-// each bucket runs the fused kernel of the requested precision (short rows)
-// or the warp-cooperative FP64 path (long rows).  basis_of / rbf_of give a
-// class per target (null: the uniform a.basis / a.rbf).
-void run_setup_plan( SetupArgs const &a, int precision, int32_t const *order_host,
-                     int32_t const *offsets_host, uint8_t const *basis_of, uint8_t const *rbf_of,
+// Setup over targets of mixed classes, planned on the device: a stable key
+// sort of the processing order `a.order` partitions the targets into buckets
+// (basis, rbf, path), path 0 = the fused kernel of the requested precision
+// (rows up to FUSED_MAX_ROW, unless split_all), 1 = split with 8 lanes per
+// target (rows up to 32), 2 = split with 32 lanes.  The class of a target
+// comes from its group (basis_of_group / rbf_of_group indexed by
+// tgt_group[target]; null: the uniform a.basis / a.rbf).
+void run_setup_plan( SetupArgs const &a, int precision, uint8_t const *basis_of_group,
+                     uint8_t const *rbf_of_group, uint32_t const *tgt_group, bool split_all,
                      cudaStream_t s );
 
 // Batched SVD pseudo-inverse (general n <= 64), DTK SVDFunctor semantics.

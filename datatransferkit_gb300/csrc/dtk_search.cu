@@ -499,12 +499,13 @@ struct Range
     int g;
 };
 
+template <bool GROUPED>
 __device__ __forceinline__ Range query_range( TreeView const &tr, GroupView const &gv, int64_t qi )
 {
     Range r;
-    r.g = gv.tgt_grp ? (int)gv.tgt_grp[qi] : 0;
-    r.ps = gv.src_off ? gv.src_off[r.g] : 0;
-    r.pe = gv.src_off ? gv.src_off[r.g + 1] : tr.n;
+    r.g = GROUPED ? (int)gv.tgt_grp[qi] : 0;
+    r.ps = GROUPED ? gv.src_off[r.g] : 0;
+    r.pe = GROUPED ? gv.src_off[r.g + 1] : tr.n;
     r.lps = (int)( r.ps / LEAF );
     r.lpe = r.pe > r.ps ? (int)( ( r.pe - 1 ) / LEAF ) : -1;
     return r;
@@ -571,6 +572,7 @@ __device__ __forceinline__ void d2_bounds( TreeView const &tr, Query const &q, i
 
 constexpr int QUEUE = 64;
 
+template <bool GROUPED>
 __global__ void __launch_bounds__( Q_WARPS * 32 )
     k_knn( TreeView tr, PointsView tgt, uint32_t const *order, int k_all, GroupView gv,
            int32_t const *offset, int32_t *idx_out, unsigned *status )
@@ -583,9 +585,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     if ( w >= tgt.n )
         return;
     int64_t const qi = order ? (int64_t)order[w] : w;
-    Range const rg = query_range( tr, gv, qi );
+    Range const rg = query_range<GROUPED>( tr, gv, qi );
     int64_t const ng = rg.pe - rg.ps;
-    int const k = gv.k ? gv.k[rg.g] : k_all;
+    int const k = GROUPED ? gv.k[rg.g] : k_all;
     int const row = (int)( k < ng ? k : ng );
     if ( row <= 0 )
         return;
@@ -693,7 +695,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     auto process_leaf = [&]( int leaf ) {
         int64_t const p = (int64_t)leaf * LEAF + lane;
         bool surv = false;
-        if ( p >= rg.ps && p < rg.pe && !( p >= s0 && p < s0 + W ) )
+        if ( ( GROUPED ? p >= rg.ps : true ) && p < rg.pe && !( p >= s0 && p < s0 + W ) )
         {
             float lo, hi;
             d2_bounds( tr, q, p, lo, hi );
@@ -732,7 +734,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
             load_node( tr.nodes, node, l_lo, l_hi, r_lo, r_hi, lc, rc, nlo, nhi );
             float lbl = box_lb( l_lo, l_hi, q.qlo, q.qhi );
             float lbr = box_lb( r_lo, r_hi, q.qlo, q.qhi );
-            clip_children( lc, nlo, nhi, rg, lbl, lbr );
+            if ( GROUPED )
+                clip_children( lc, nlo, nhi, rg, lbl, lbr );
             bool const near_left = lbl <= lbr;
             int const c_near = near_left ? lc : rc, c_far = near_left ? rc : lc;
             float const lb_near = near_left ? lbl : lbr, lb_far = near_left ? lbr : lbl;
@@ -789,7 +792,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
 // is a hit iff sqrt(d2) <= r with the exact FP64 d2; the FP32 bounds decide
 // every source whose bound interval lies clear of r^2 (2^-20 margins), and
 // only the rest pay for an FP64 distance.
-template <bool FILL>
+template <bool FILL, bool GROUPED>
 __global__ void __launch_bounds__( Q_WARPS * 32 )
     k_radius( TreeView tr, PointsView tgt, uint32_t const *order, double r_all, GroupView gv,
               int64_t *counts, int32_t const *offset, int32_t *idx_out, unsigned *status )
@@ -800,8 +803,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     if ( w >= tgt.n )
         return;
     int64_t const qi = order ? (int64_t)order[w] : w;
-    Range const rg = query_range( tr, gv, qi );
-    double const r = gv.r ? gv.r[rg.g] : r_all;
+    Range const rg = query_range<GROUPED>( tr, gv, qi );
+    double const r = GROUPED ? gv.r[rg.g] : r_all;
     Query const q = make_query( tr, tgt, qi );
     double const r2 = __dmul_ru( r, r );
     float const bound_f = prune_threshold( (unsigned long long)__double_as_longlong( r2 ) );
@@ -813,7 +816,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     auto process_leaf = [&]( int leaf ) {
         int64_t const p = (int64_t)leaf * LEAF + lane;
         bool hit = false, unsure = false;
-        if ( p >= rg.ps && p < rg.pe )
+        if ( ( GROUPED ? p >= rg.ps : true ) && p < rg.pe )
         {
             float lo, hi;
             d2_bounds( tr, q, p, lo, hi );
@@ -861,7 +864,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
             load_node( tr.nodes, node, l_lo, l_hi, r_lo, r_hi, lc, rc, nlo, nhi );
             float lbl = box_lb( l_lo, l_hi, q.qlo, q.qhi );
             float lbr = box_lb( r_lo, r_hi, q.qlo, q.qhi );
-            clip_children( lc, nlo, nhi, rg, lbl, lbr );
+            if ( GROUPED )
+                clip_children( lc, nlo, nhi, rg, lbl, lbr );
             bool const hl = lbl <= bound_f;
             bool const hr = lbr <= bound_f;
             int next = -1;
@@ -1020,8 +1024,12 @@ void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
     if ( tgt.n == 0 || tree.n == 0 || ( k == 0 && !groups.k ) )
         return;
     GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
-    k_knn<<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, k, gv, offset,
-                                                                  idx, status );
+    if ( groups.tgt_grp )
+        k_knn<true><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, k, gv,
+                                                                            offset, idx, status );
+    else
+        k_knn<false><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, k, gv,
+                                                                             offset, idx, status );
     check_launch( "k_knn" );
 }
 
@@ -1031,8 +1039,12 @@ void radius_count( Lbvh const &tree, PointsView tgt, uint32_t const *order, doub
     if ( tgt.n == 0 )
         return;
     GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
-    k_radius<false><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
-        view_of( tree ), tgt, order, r, gv, counts, nullptr, nullptr, status );
+    if ( groups.tgt_grp )
+        k_radius<false, true><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
+            view_of( tree ), tgt, order, r, gv, counts, nullptr, nullptr, status );
+    else
+        k_radius<false, false><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
+            view_of( tree ), tgt, order, r, gv, counts, nullptr, nullptr, status );
     check_launch( "k_radius(count)" );
 }
 
@@ -1043,8 +1055,12 @@ void radius_fill( Lbvh const &tree, PointsView tgt, uint32_t const *order, doubl
     if ( tgt.n == 0 )
         return;
     GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
-    k_radius<true><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
-        view_of( tree ), tgt, order, r, gv, nullptr, offset, idx, status );
+    if ( groups.tgt_grp )
+        k_radius<true, true><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
+            view_of( tree ), tgt, order, r, gv, nullptr, offset, idx, status );
+    else
+        k_radius<true, false><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
+            view_of( tree ), tgt, order, r, gv, nullptr, offset, idx, status );
     check_launch( "k_radius(fill)" );
 }
 

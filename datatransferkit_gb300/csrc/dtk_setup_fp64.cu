@@ -484,31 +484,32 @@ __global__ void k_svd_general( int n, int64_t count, double const *a, double *pi
 }
 
 // ---------------------------------------------------------------------------
-// Long rows (radius neighbourhoods of hundreds to tens of thousands of
-// sources): the same FP64 stages in three kernels so that no single thread
-// walks a long row.  A warp per target assembles the moments (lanes split the
-// neighbours; the 55 sums are combined by shuffles) and later the
-// coefficients; one thread per target runs the reference Jacobi in between.
-// Work area per long target: NU moments + radius + M row-0 values (doubles).
+// Split setup for uneven rows (radius neighbourhoods of 0 to tens of
+// thousands of sources): the same FP64 stages in three kernels so that no
+// single thread walks a long row.  G lanes per target assemble the moments
+// (the lanes split the neighbours; the NU sums are combined by shuffles
+// within the group) and later the coefficients; one thread per target runs
+// the reference Jacobi in between.  Work area per target: NU moments +
+// radius + M row-0 values (doubles).
 // ---------------------------------------------------------------------------
-template <int M>
+template <int M, int G>
 __global__ void __launch_bounds__( 128 )
-    k_long_moments( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
-                    int32_t const *targets, int64_t n, int rbf, double *work, unsigned *status )
+    k_split_moments( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
+                     int32_t const *targets, int64_t n, int rbf, double *work, unsigned *status )
 {
     constexpr int NU = M * ( M + 1 ) / 2;
     constexpr int STRIDE = NU + 1 + M;
-    int const lane = threadIdx.x & 31;
-    int64_t const w = ( blockIdx.x * (int64_t)blockDim.x + threadIdx.x ) >> 5;
-    if ( w >= n )
-        return;
-    int64_t const i = targets[w];
-    int64_t const b = offset[i];
-    int const len = offset[i + 1] - (int)b;
-    double const tx = tgt( i, 0 ), ty = tgt( i, 1 ), tz = tgt( i, 2 );
+    int const sub = threadIdx.x & ( G - 1 );
+    int64_t const w = ( blockIdx.x * (int64_t)blockDim.x + threadIdx.x ) / G;
+    bool const active = w < n;
+    int64_t const i = active ? targets[w] : 0;
+    int64_t const b = active ? offset[i] : 0;
+    int len = active ? offset[i + 1] - (int)b : 0;
+    double const tx = active ? tgt( i, 0 ) : 0.0, ty = active ? tgt( i, 1 ) : 0.0,
+                 tz = active ? tgt( i, 2 ) : 0.0;
     double d2max = 0.0;
     bool bad = false;
-    for ( int j = lane; j < len; j += 32 )
+    for ( int j = sub; j < len; j += G )
     {
         int64_t const sj = idx[b + j];
         if ( (uint64_t)sj >= (uint64_t)src.n )
@@ -518,14 +519,18 @@ __global__ void __launch_bounds__( 128 )
         }
         d2max = fmax( d2max, dist2_rn( src( sj, 0 ), src( sj, 1 ), src( sj, 2 ), tx, ty, tz ) );
     }
-    if ( __any_sync( FULL, bad ) )
+#pragma unroll
+    for ( int o = G / 2; o; o >>= 1 )
     {
-        if ( lane == 0 )
-            atomicOr( status, DEV_BAD_INDEX );
-        return;
-    }
-    for ( int o = 16; o; o >>= 1 )
         d2max = fmax( d2max, __shfl_xor_sync( FULL, d2max, o ) );
+        bad |= __shfl_xor_sync( FULL, (int)bad, o ) != 0;
+    }
+    if ( bad )
+    {
+        if ( sub == 0 )
+            atomicOr( status, DEV_BAD_INDEX );
+        len = 0; // the row is not read again
+    }
     double distance = 10. * DBL_EPSILON;
     double const dmax = __dsqrt_rn( d2max );
     if ( dmax > distance )
@@ -535,7 +540,7 @@ __global__ void __launch_bounds__( 128 )
 #pragma unroll
     for ( int u = 0; u < NU; ++u )
         A[u] = 0.0;
-    for ( int j = lane; j < len; j += 32 )
+    for ( int j = sub; j < len; j += G )
     {
         int64_t const sj = idx[b + j];
         double const x = __dsub_rn( src( sj, 0 ), tx ), y = __dsub_rn( src( sj, 1 ), ty ),
@@ -557,9 +562,10 @@ __global__ void __launch_bounds__( 128 )
     }
 #pragma unroll
     for ( int u = 0; u < NU; ++u )
-        for ( int o = 16; o; o >>= 1 )
+#pragma unroll
+        for ( int o = G / 2; o; o >>= 1 )
             A[u] += __shfl_xor_sync( FULL, A[u], o );
-    if ( lane == 0 )
+    if ( active && sub == 0 )
     {
         double *out = work + w * STRIDE;
 #pragma unroll
@@ -571,8 +577,8 @@ __global__ void __launch_bounds__( 128 )
 
 template <int M>
 __global__ void __launch_bounds__( SETUP_BLOCK )
-    k_long_jacobi( int64_t n, double *work, unsigned long long *under_count,
-                   unsigned long long *rot_count, unsigned *status )
+    k_split_jacobi( int64_t n, double *work, unsigned long long *under_count,
+                    unsigned long long *rot_count, unsigned *status )
 {
     constexpr int NU = M * ( M + 1 ) / 2;
     constexpr int STRIDE = NU + 1 + M;
@@ -617,18 +623,18 @@ __global__ void __launch_bounds__( SETUP_BLOCK )
     }
 }
 
-template <int M>
+template <int M, int G>
 __global__ void __launch_bounds__( 128 )
-    k_long_coeffs( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
-                   int32_t const *targets, int64_t n, int rbf, double const *work, double *coeff64,
-                   float *coeff32 )
+    k_split_coeffs( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
+                    int32_t const *targets, int64_t n, int rbf, double const *work, double *coeff64,
+                    float *coeff32 )
 {
     constexpr int NU = M * ( M + 1 ) / 2;
     constexpr int STRIDE = NU + 1 + M;
-    int const lane = threadIdx.x & 31;
-    int64_t const w = ( blockIdx.x * (int64_t)blockDim.x + threadIdx.x ) >> 5;
+    int const sub = threadIdx.x & ( G - 1 );
+    int64_t const w = ( blockIdx.x * (int64_t)blockDim.x + threadIdx.x ) / G;
     if ( w >= n )
-        return;
+        return; // no shuffles below
     int64_t const i = targets[w];
     int64_t const b = offset[i];
     int const len = offset[i + 1] - (int)b;
@@ -639,9 +645,11 @@ __global__ void __launch_bounds__( 128 )
 #pragma unroll
     for ( int a = 0; a < M; ++a )
         row0[a] = rec[NU + 1 + a];
-    for ( int j = lane; j < len; j += 32 )
+    for ( int j = sub; j < len; j += G )
     {
         int64_t const sj = idx[b + j];
+        if ( (uint64_t)sj >= (uint64_t)src.n )
+            continue; // reported by the moments kernel
         double const x = __dsub_rn( src( sj, 0 ), tx ), y = __dsub_rn( src( sj, 1 ), ty ),
                      z = __dsub_rn( src( sj, 2 ), tz );
         double P[M];
@@ -660,29 +668,46 @@ __global__ void __launch_bounds__( 128 )
     }
 }
 
-template <int M>
-void launch_long( SetupArgs const &a, int32_t const *targets, int64_t n, cudaStream_t s )
+template <int M, int G>
+void launch_split( SetupArgs const &a, int32_t const *targets, int64_t n, cudaStream_t s )
 {
     constexpr int NU = M * ( M + 1 ) / 2;
     DeviceBuffer<double> work( n * ( NU + 1 + M ), s );
-    unsigned const wblocks = (unsigned)( ( n * 32 + 127 ) / 128 );
-    k_long_moments<M><<<wblocks, 128, 0, s>>>( a.src, a.tgt, a.offset, a.idx, targets, n, a.rbf,
-                                                work.get(), a.status );
-    check_launch( "k_long_moments" );
+    unsigned const gblocks = (unsigned)( ( n * G + 127 ) / 128 );
+    k_split_moments<M, G><<<gblocks, 128, 0, s>>>( a.src, a.tgt, a.offset, a.idx, targets, n, a.rbf,
+                                                    work.get(), a.status );
+    check_launch( "k_split_moments" );
     size_t const smem = ( 2 * M * M + M ) * SETUP_BLOCK * sizeof( double );
     static bool configured = false;
     if ( !configured )
     {
-        DTK_CUDA_OR_THROW( cudaFuncSetAttribute( k_long_jacobi<M>,
+        DTK_CUDA_OR_THROW( cudaFuncSetAttribute( k_split_jacobi<M>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem ) );
         configured = true;
     }
-    k_long_jacobi<M><<<(unsigned)( ( n + SETUP_BLOCK - 1 ) / SETUP_BLOCK ), SETUP_BLOCK, smem, s>>>(
+    k_split_jacobi<M><<<(unsigned)( ( n + SETUP_BLOCK - 1 ) / SETUP_BLOCK ), SETUP_BLOCK, smem, s>>>(
         n, work.get(), a.underdetermined, a.rotations, a.status );
-    check_launch( "k_long_jacobi" );
-    k_long_coeffs<M><<<wblocks, 128, 0, s>>>( a.src, a.tgt, a.offset, a.idx, targets, n, a.rbf,
-                                               work.get(), a.coeff64, a.coeff32 );
-    check_launch( "k_long_coeffs" );
+    check_launch( "k_split_jacobi" );
+    k_split_coeffs<M, G><<<gblocks, 128, 0, s>>>( a.src, a.tgt, a.offset, a.idx, targets, n, a.rbf,
+                                                   work.get(), a.coeff64, a.coeff32 );
+    check_launch( "k_split_coeffs" );
+}
+
+template <int G>
+void launch_split_basis( SetupArgs const &a, int32_t const *targets, int64_t n, cudaStream_t s )
+{
+    switch ( a.basis )
+    {
+    case DTK_CONSTANT3:
+        launch_split<1, G>( a, targets, n, s );
+        break;
+    case DTK_LINEAR3:
+        launch_split<4, G>( a, targets, n, s );
+        break;
+    default:
+        launch_split<10, G>( a, targets, n, s );
+        break;
+    }
 }
 
 template <int M>
@@ -724,22 +749,14 @@ void setup_fp64( SetupArgs const &a, cudaStream_t s )
     }
 }
 
-void setup_long_rows( SetupArgs const &a, int32_t const *targets, int64_t n, cudaStream_t s )
+void setup_split( SetupArgs const &a, int32_t const *targets, int64_t n, int lanes, cudaStream_t s )
 {
     if ( n == 0 )
         return;
-    switch ( a.basis )
-    {
-    case DTK_CONSTANT3:
-        launch_long<1>( a, targets, n, s );
-        break;
-    case DTK_LINEAR3:
-        launch_long<4>( a, targets, n, s );
-        break;
-    default:
-        launch_long<10>( a, targets, n, s );
-        break;
-    }
+    if ( lanes >= 32 )
+        launch_split_basis<32>( a, targets, n, s );
+    else
+        launch_split_basis<8>( a, targets, n, s );
 }
 
 void svd_pinv_batched_work( int n, int64_t count, double const *a, double *pinv, double *work,

@@ -337,6 +337,13 @@ class MovingLeastSquaresBatch:
         c = _from_device(coeff.value, n, torch.float32 if f32.value else torch.float64)
         return o, i, c
 
+    @property
+    def stage_times_ms(self):
+        """(search, setup) device milliseconds and the host planning milliseconds."""
+        a, b, c = C.c_float(), C.c_float(), C.c_float()
+        check(lib().dtk_mls_batch_get_stage_times(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             lib().dtk_mls_batch_destroy(self._h)

@@ -209,9 +209,9 @@ dtk_status dtk_mls_batch_create(int32_t n_problems, const dtk_mls_options *opts,
                                 const int64_t *src_offsets, const double *src,
                                 const int64_t *tgt_offsets, const double *tgt,
                                 dtk_stream_t stream, dtk_mls_batch_handle *out);
-/* All problems' apply in one launch: values/targets are packed like the
- * points.  When use_graph != 0 the launch sequence is captured once into a
- * CUDA graph and replayed. */
+/* All problems' apply: values/targets are packed like the points.  When
+ * use_graph != 0 the apply schedule is captured once into a CUDA graph and
+ * replayed. */
 dtk_status dtk_mls_batch_apply(dtk_mls_batch_handle h, const double *src_values,
                                double *tgt_values, int32_t use_graph,
                                dtk_stream_t stream);
@@ -219,6 +219,10 @@ dtk_status dtk_mls_batch_get_csr(dtk_mls_batch_handle h, const int32_t **offset,
                                  const int32_t **indices, const void **coeff,
                                  int64_t *nnz, int32_t *coeff_is_fp32);
 dtk_status dtk_mls_batch_destroy(dtk_mls_batch_handle h);
+/* Device time of the batch's search and setup stages (CUDA events), and the
+ * host time the create call spent planning (bucketing targets, binning rows). */
+dtk_status dtk_mls_batch_get_stage_times(dtk_mls_batch_handle h, float *search_ms,
+                                         float *setup_ms, float *host_ms);
 
 /* Last error message of the calling host thread (never NULL). */
 const char *dtk_last_error(void);

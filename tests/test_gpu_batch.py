@@ -103,13 +103,13 @@ def test_radius_batch_against_oracle_per_problem():
     problems = radius_problems()
     b, vals, out, off, idx, coeff = run_batch(problems)
     so, to = b.source_offsets, b.target_offsets
-    long_rows = 0
+    lens = []
     for p, pr in enumerate(problems):
         f = vals[so[p]:so[p + 1]]
         ref = cpu.mls_transfer(pr["src"], pr["tgt"], f, 1, pr["basis"], r=0.05)
         o = off[to[p]:to[p + 1] + 1] - off[to[p]]
         assert np.array_equal(o, ref["offset"])
-        long_rows += int((np.diff(o) > 96).sum())
+        lens.append(np.diff(o))
         base = off[to[p]]
         tc, tt = tolerances(pr["src"], pr["tgt"], ref["offset"], ref["idx"], 1, pr["basis"], f,
                             ref["coeff"])
@@ -123,7 +123,8 @@ def test_radius_batch_against_oracle_per_problem():
                 ca, cb = coeff[a][oa], ref["coeff"][r_][ob]
                 assert np.abs(ca - cb).max() <= tc * max(np.abs(cb).max(), 1e-300), (p, i)
         assert rel_l2(out[to[p]:to[p + 1]], ref["target"]) <= tt, p
-    assert long_rows > 0  # the warp-cooperative long-row setup ran
+    lens = np.concatenate(lens)
+    assert (lens > 32).any() and ((lens > 0) & (lens <= 32)).any()  # both split widths ran
 
 
 def test_batch_preconditions():
