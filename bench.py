@@ -146,15 +146,16 @@ def fp64_form_flops(n_tgt, k, m, rotations):
     return rotations * per_rot + n_tgt * k * per_nb + n_tgt * (2 * m * m + m)
 
 
-def mixed_form_flops(n_tgt, k, m, rotations64):
-    """Mixed form, FP64 part only.  Per target: the centring/scaling in three
-    passes 3 x k x 6; B = V32^T A V32, 2 m^3 + m^2 (m+1); row 0, 2 m^2; the
-    refinement residual k (4m + 7) and its solve 4 m^2 + m; the coefficient
-    dot products k (2m + 7); the radius ~10.  Per FP64 rotation 12 m + 16."""
-    per_rot = 12 * m + 16
-    per_tgt = (3 * k * 6 + 2 * m ** 3 + m * m * (m + 1) + 2 * m * m + k * (4 * m + 7)
-               + 4 * m * m + m + k * (2 * m + 7) + 10)
-    return rotations64 * per_rot + n_tgt * per_tgt
+def mixed_form_flops(n_tgt, k, m):
+    """Mixed form, FP64-pipe work only, in FLOP with an FMA as 2 and every
+    other FP64-pipe operation (add, multiply, FP32<->FP64 conversion) as 1.
+    Per neighbour: the centring in three passes 3 x 3 subtractions and
+    3 x 1 + 2 x 4 conversions (coordinates and weight); the FP64 residual
+    (quadratic basis products m - 4, dot 2m, weight product 1, update 2m);
+    the coefficient dot (m - 4 + 2m + 1) and its FP32 store 1.  Per target:
+    radius ~10, refinement conversions 3m."""
+    per_nb = 9 + 11 + (m - 4 + 4 * m + 1) + (m - 4 + 2 * m + 2)
+    return n_tgt * (k * per_nb + 10 + 3 * m)
 
 
 def measure_fp64_peak(torch, dev):
@@ -556,8 +557,7 @@ def run_ours(args, rank, world, local_rank):
     # -- roofline of the dominant kernel (the mixed setup kernel) ----------------
     setup_ms = float(np.mean([r[0][1] for r in rec_mixed]))
     search_ms = float(np.mean([r[0][0] for r in rec_mixed]))
-    rot64 = float(np.mean([r[1] for r in rec_mixed]))
-    flops = mixed_form_flops(n_tgt, k, m, rot64)
+    flops = mixed_form_flops(n_tgt, k, m)
     achieved = flops / (setup_ms / 1e3) / 1e12
     peak = measure_fp64_peak(torch, dev)
     traffic_pt = read_profile_traffic()
@@ -579,7 +579,6 @@ def run_ours(args, rank, world, local_rank):
                       "setup_fp64_tflops": flops64 / (setup64_ms / 1e3) / 1e12},
         "mixed_over_fp64": ms_fp64 / ms_mixed,
         "rotations_per_target": {
-            "mixed_fp64": float(np.mean([r[1] for r in rec_mixed])) / n_tgt,
             "mixed_fp32": float(np.mean([r[2] for r in rec_mixed])) / n_tgt,
             "fp64_form": rot_fp64_form / n_tgt},
         "accuracy_vs_fp64_oracle": acc,

@@ -2,37 +2,40 @@
 //
 // Same stages as the FP64 form (DTK_DetailsMovingLeastSquaresOperatorImpl.hpp
 // :72-336 after the search), one thread per target, but:
-//   * centring and scaling by the support radius: x^ = (s - t) / r, formed
-//     in FP64 and rounded once to FP32, so the basis and the weights see
-//     O(1) arguments (P(x) / r^deg = P(x^), and rbf(|x| / r) = rbf(|x^|));
-//   * FP32 weights, basis and moment assembly, the 55 upper-triangle sums
-//     Kahan-compensated (plain FP32 sums lose ~2e-6 at k = 32);
-//   * the eigen-decomposition of the scaled moments A^ = V L V^T as a
-//     symmetric Jacobi method in round-robin (parallel) order -- each round's
-//     M/2 disjoint rotations have independent parameter chains, which hides
-//     the FP64 latency -- run to FP32 convergence, then
-//     finished in FP64: B = V32^T A^ V32 (A^ with its compensation terms,
-//     exactly in FP64) is nearly diagonal and one FP64 sweep (pairs below
-//     1e-15 relative are skipped) converges it quadratically, accumulating
-//     W = V32 V64;
-//   * FP64 truncation relative to the scaled spectrum: lambda_k <= 2^-20
-//     lambda_max is dropped (the scaled moments are well conditioned, cond
-//     ~1e3-1e4 at the benchmark densities, so only geometric rank deficiency
-//     falls below it);
-//   * one FP64 iterative-refinement step of row 0 of the pseudo-inverse
-//     against the exact residual e0 - sum_j phi_j P_j (P_j . a) (the basis
-//     of FP32 coordinates is exact in FP64), which removes the FP32
-//     assembly error (the step contracts it by ~cond(A^) * 2^-24);
-//   * coefficients c_j = phi_j (P(x^_j) . a), stored in FP32.
-// Row 0 of the pseudo-inverse is applied without forming it:
-//   A^+ v = W L^+ W^T v.
-// GB300 issues one FP64 warp instruction per 64 cycles per SM sub-partition,
-// so all Jacobi state lives in shared memory (thread-interleaved, 1640 B per
-// thread at M = 10: four warps per SM, one per sub-partition) and the FP64
-// work is what sets the time: ~11k FP64 operations per target against ~57k
-// for the FP64 form's reference Jacobi.
+//   * centring and scaling by the support radius: x^ = fl32(s - t) * (1/r)
+//     (FP64 difference, FP32 scale), so the basis and the weights see O(1)
+//     arguments (P(x) / r^deg = P(x^), and rbf(|x| / r) = rbf(|x^|));
+//   * FP32 weights, basis and moment assembly (registers);
+//   * an FP32 inverse of the scaled moments A^ as the preconditioner of one
+//     FP64 iterative-refinement step for row 0 of the pseudo-inverse,
+//     a = M e0, a += M (e0 - A a), the residual in FP64 from the neighbours
+//     themselves (the basis of FP32 coordinates is exact in FP64, phi_j is
+//     the FP32 weight).  The step contracts the FP32 error by
+//     ~cond(A^) 2^-24, which leaves the FP32 rounding of the coordinates as
+//     the only error (~2.5e-8 rel L2 on the 8M-point workload; an FP64
+//     eigen-solve, or Kahan-compensated moments, give the same error);
+//   * coefficients c_j = phi_j (P(x^_j) . a) as FP64 dots, stored in FP32.
+// The preconditioner M:
+//   * fast path (k_setup_mixed): Cholesky A^ = R^T R in FP32 registers,
+//     S = R^-1, M = S S^T.  It is taken when the factorization succeeds and
+//     trace(A^) ||S||_F^2 <= 2^20: since lambda_max <= trace and
+//     1/lambda_min = ||S||_2^2 <= ||S||_F^2, that bounds cond(A^) by 2^20, so
+//     the truncation below would drop nothing and M ~ A^-1 = A^+.  Above
+//     2^16 a second refinement step is taken.
+//   * otherwise (k_setup_mixed_eig, the targets the fast path lists): the
+//     symmetric Jacobi method in round-robin order, in FP32 to FP32
+//     convergence, truncation lambda_k <= 2^-20 lambda_max (geometric rank
+//     deficiency), M = V L^+ V^T.
+// GB300 issues one FP64 warp instruction per 64 cycles per SM sub-partition;
+// the FP64 work here is the centring, the residual and the coefficient dots
+// (~2.3k FP64 operations per target against ~57k for the FP64 form's
+// reference Jacobi).  The fast path keeps all state in registers; the
+// Jacobi path keeps A^ and V (FP32) thread-interleaved in shared memory,
+// 620 B per thread at M = 10.
 #include "dtk_common.cuh"
 #include "dtk_jacobi.cuh"
+
+#include <algorithm>
 
 namespace dtk
 {
@@ -56,36 +59,244 @@ __device__ __forceinline__ float weight32( int rbf, float x, float y, float z )
     return rbf_eval<float>( rbf, sqrtf( x * x + y * y + z * z ) );
 }
 
+// Refinement and coefficients shared by both paths: a += M (e0 - A a) with
+// the FP64 residual over the neighbours, `steps` times, then
+// c_j = phi_j (P_j . a) stored in FP32.  `pinv32(v, y)` applies M in FP32.
+template <int M, class Scaled, class Pinv>
+__device__ __forceinline__ void refine_and_store( int len, int rbf, int steps, Scaled const &scaled,
+                                                  Pinv const &pinv32, double *a, float *coeff_row )
+{
+    for ( int step = 0; step < steps; ++step )
+    {
+        double r[M];
+#pragma unroll
+        for ( int q = 0; q < M; ++q )
+            r[q] = q == 0 ? 1.0 : 0.0;
+        for ( int j = 0; j < len; ++j )
+        {
+            float x, y, z;
+            scaled( j, x, y, z );
+            double P[M];
+            basis_eval<M, double>( (double)x, (double)y, (double)z, P );
+            double const phi = (double)weight32( rbf, x, y, z );
+            double dot = 0.0;
+#pragma unroll
+            for ( int q = 0; q < M; ++q )
+                dot = fma( P[q], a[q], dot );
+            double const w = phi * dot;
+#pragma unroll
+            for ( int q = 0; q < M; ++q )
+                r[q] = fma( -w, P[q], r[q] );
+        }
+        float rf[M], d[M];
+#pragma unroll
+        for ( int q = 0; q < M; ++q )
+            rf[q] = (float)r[q];
+        pinv32( rf, d );
+#pragma unroll
+        for ( int q = 0; q < M; ++q )
+            a[q] += (double)d[q];
+    }
+    for ( int j = 0; j < len; ++j )
+    {
+        float x, y, z;
+        scaled( j, x, y, z );
+        double P[M];
+        basis_eval<M, double>( (double)x, (double)y, (double)z, P );
+        float const phi = weight32( rbf, x, y, z );
+        double dot = 0.0;
+#pragma unroll
+        for ( int q = 0; q < M; ++q )
+            dot = fma( P[q], a[q], dot );
+        coeff_row[j] = (float)( dot * (double)phi );
+    }
+}
+
+// Fast path: FP32 Cholesky preconditioner in registers; targets it cannot
+// take (factorization fails, or the condition bound exceeds 2^20) are
+// appended to `list` for k_setup_mixed_eig.
 template <int M>
-__global__ void __launch_bounds__( MB )
+__global__ void __launch_bounds__( 128 )
     k_setup_mixed( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
-                   uint32_t const *order, int64_t n_tgt, int rbf, bool rows_sorted,
-                   float *coeff, unsigned long long *under_count,
-                   unsigned long long *rot_count, unsigned long long *rot32_count,
-                   unsigned *status )
+                   uint32_t const *order, int64_t n_tgt, int rbf, bool rows_sorted, float *coeff,
+                   int32_t *list, unsigned *count, unsigned *status )
 {
     constexpr int NU = M * ( M + 1 ) / 2;
-    extern __shared__ unsigned char smem_raw[];
+    int64_t const g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( g >= n_tgt )
+        return; // no warp-wide operations below
+    int64_t const i = order ? (int64_t)order[g] : g;
+    int64_t const b = offset[i];
+    int len = offset[i + 1] - (int)b;
+    for ( int j = 0; j < len; ++j )
+        if ( (uint32_t)idx[b + j] >= (uint64_t)src.n )
+        {
+            atomicOr( status, DEV_BAD_INDEX );
+            len = 0;
+        }
+    double const tx = tgt( i, 0 ), ty = tgt( i, 1 ), tz = tgt( i, 2 );
+    double d2max = 0.0;
+    for ( int j = rows_sorted ? max( 0, len - 1 ) : 0; j < len; ++j )
+    {
+        int64_t const sj = idx[b + j];
+        d2max = fmax( d2max, dist2_rn( src( sj, 0 ), src( sj, 1 ), src( sj, 2 ), tx, ty, tz ) );
+    }
+    double distance = 10. * DBL_EPSILON;
+    double const dmax = __dsqrt_rn( d2max );
+    if ( dmax > distance )
+        distance = dmax;
+    float const inv_r = (float)( 1.0 / ( 1.1 * distance ) );
+    auto scaled = [&]( int j, float &x, float &y, float &z ) {
+        int64_t const sj = idx[b + j];
+        x = __fmul_rn( (float)( src( sj, 0 ) - tx ), inv_r );
+        y = __fmul_rn( (float)( src( sj, 1 ) - ty ), inv_r );
+        z = __fmul_rn( (float)( src( sj, 2 ) - tz ), inv_r );
+    };
+
+    // FP32 moments, upper triangle R(a, c) = A[ut(a, c)], a <= c
+    float A[NU];
+#pragma unroll
+    for ( int u = 0; u < NU; ++u )
+        A[u] = 0.f;
+    for ( int j = 0; j < len; ++j )
+    {
+        float x, y, z;
+        scaled( j, x, y, z );
+        float P[M];
+        basis_eval<M, float>( x, y, z, P );
+        float const phi = weight32( rbf, x, y, z );
+#pragma unroll
+        for ( int a = 0; a < M; ++a )
+        {
+            float const pa = P[a] * phi;
+#pragma unroll
+            for ( int c = a; c < M; ++c )
+                A[ut<M>( a, c )] = fmaf( pa, P[c], A[ut<M>( a, c )] );
+        }
+    }
+    float trace = 0.f;
+#pragma unroll
+    for ( int k = 0; k < M; ++k )
+        trace += A[ut<M>( k, k )];
+
+    // Cholesky A = R^T R in place (R upper triangular, row-major packed)
+    bool ok = trace > 0.f;
+    float rinv[M];
+#pragma unroll
+    for ( int j = 0; j < M; ++j )
+    {
+        float d = A[ut<M>( j, j )];
+#pragma unroll
+        for ( int k = 0; k < j; ++k )
+            d = fmaf( -A[ut<M>( k, j )], A[ut<M>( k, j )], d );
+        ok = ok && d > 0.f;
+        float const inv = d > 0.f ? rsqrtf( d ) : 0.f;
+        rinv[j] = inv;
+        A[ut<M>( j, j )] = d * inv; // sqrt(d)
+#pragma unroll
+        for ( int c = j + 1; c < M; ++c )
+        {
+            float v = A[ut<M>( j, c )];
+#pragma unroll
+            for ( int k = 0; k < j; ++k )
+                v = fmaf( -A[ut<M>( k, j )], A[ut<M>( k, c )], v );
+            A[ut<M>( j, c )] = v * inv;
+        }
+    }
+    // S = R^-1 in place, column by column: S(j,j) = 1/R(j,j),
+    // S(r,j) = -(sum_{k=r}^{j-1} S(r,k) R(k,j)) / R(j,j), r ascending
+    float fro = 0.f;
+#pragma unroll
+    for ( int j = 0; j < M; ++j )
+    {
+#pragma unroll
+        for ( int r = 0; r < j; ++r )
+        {
+            float v = 0.f;
+#pragma unroll
+            for ( int k = r; k < j; ++k )
+                v = fmaf( k == r ? A[ut<M>( r, r )] : A[ut<M>( r, k )], A[ut<M>( k, j )], v );
+            // S(r, r) is already stored at (r, r); S(r, k) for k < j too
+            A[ut<M>( r, j )] = -v * rinv[j];
+        }
+        A[ut<M>( j, j )] = rinv[j];
+    }
+#pragma unroll
+    for ( int u = 0; u < NU; ++u )
+        fro = fmaf( A[u], A[u], fro );
+    float const crit = trace * fro;
+    if ( !ok || !( crit <= 1048576.f ) ) // 2^20; false for NaN
+    {
+        unsigned const slot = atomicAdd( count, 1u );
+        list[slot] = (int32_t)i;
+        return;
+    }
+    // M v = S (S^T v)
+    auto pinv32 = [&]( float const *v, float *y ) {
+        float w[M];
+#pragma unroll
+        for ( int k = 0; k < M; ++k )
+        {
+            float acc = 0.f;
+#pragma unroll
+            for ( int r = 0; r <= k; ++r )
+                acc = fmaf( A[ut<M>( r, k )], v[r], acc );
+            w[k] = acc;
+        }
+#pragma unroll
+        for ( int r = 0; r < M; ++r )
+        {
+            float acc = 0.f;
+#pragma unroll
+            for ( int k = r; k < M; ++k )
+                acc = fmaf( A[ut<M>( r, k )], w[k], acc );
+            y[r] = acc;
+        }
+    };
+    double a[M];
+    {
+        float e0[M], y[M];
+#pragma unroll
+        for ( int r = 0; r < M; ++r )
+            e0[r] = r == 0 ? 1.f : 0.f;
+        pinv32( e0, y );
+#pragma unroll
+        for ( int r = 0; r < M; ++r )
+            a[r] = (double)y[r];
+    }
+    refine_and_store<M>( len, rbf, crit <= 65536.f ? 1 : 2, scaled, pinv32, a, coeff + b );
+}
+
+// Jacobi path over the targets the fast path listed: list[0 .. *count),
+// persistent blocks striding over the list.
+template <int M>
+__global__ void __launch_bounds__( MB, 8 )
+    k_setup_mixed_eig( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
+                       int32_t const *list, unsigned const *count, int rbf, bool rows_sorted,
+                       float *coeff, unsigned long long *under_count,
+                       unsigned long long *rot32_count, unsigned *status )
+{
+    constexpr int NU = M * ( M + 1 ) / 2;
+    extern __shared__ float smem_f[];
     // Per-thread regions, thread-interleaved (conflict-free):
-    //   R1: M*M doubles  -- A64 (compensated moments), later W = V32 V64
-    //   R3: NU doubles   -- A32 (FP32 copy, first half), later B
-    //   R2: M*M floats   -- V32
-    double *r1 = reinterpret_cast<double *>( smem_raw );
-    double *r3 = r1 + M * M * MB;
-    float *r2 = reinterpret_cast<float *>( r3 + NU * MB );
+    //   R1: NU floats  -- A^ (upper triangle); after the Jacobi its diagonal
+    //                     holds 1 / lambda_k (0 where truncated)
+    //   R2: M*M floats -- V
+    float *r1 = smem_f;
+    float *r2 = r1 + NU * MB;
     int const t = threadIdx.x;
-    auto A64 = [&]( int u ) -> double & { return r1[u * MB + t]; };
-    auto W = [&]( int r, int c ) -> double & { return r1[( r * M + c ) * MB + t]; };
-    auto A32 = [&]( int u ) -> float & { return reinterpret_cast<float *>( r3 )[u * MB + t]; };
-    auto B = [&]( int u ) -> double & { return r3[u * MB + t]; };
+    auto A32 = [&]( int u ) -> float & { return r1[u * MB + t]; };
     auto V32 = [&]( int r, int c ) -> float & { return r2[( r * M + c ) * MB + t]; };
 
-    int64_t const g = blockIdx.x * (int64_t)MB + threadIdx.x;
-    unsigned rotations = 0, rotations32 = 0;
+    int64_t const n_list = *count;
+    unsigned rotations32 = 0;
     int dropped = 0;
-    if ( g < n_tgt )
+    for ( int64_t g = blockIdx.x * (int64_t)MB + threadIdx.x; g - threadIdx.x < n_list;
+          g += (int64_t)gridDim.x * MB )
     {
-        int64_t const i = order ? (int64_t)order[g] : g;
+        if ( g >= n_list )
+            continue;
+        int64_t const i = list[g];
         int64_t const b = offset[i];
         int len = offset[i + 1] - (int)b;
         for ( int j = 0; j < len; ++j )
@@ -107,24 +318,21 @@ __global__ void __launch_bounds__( MB )
         double const dmax = __dsqrt_rn( d2max );
         if ( dmax > distance )
             distance = dmax;
-        double const inv_r = 1.0 / ( 1.1 * distance );
-        // centred, scaled neighbour coordinates: FP64 difference, one rounding
+        float const inv_r = (float)( 1.0 / ( 1.1 * distance ) );
+        // centred, scaled neighbour coordinates: FP64 difference, FP32 scale
         auto scaled = [&]( int j, float &x, float &y, float &z ) {
             int64_t const sj = idx[b + j];
-            x = (float)( ( src( sj, 0 ) - tx ) * inv_r );
-            y = (float)( ( src( sj, 1 ) - ty ) * inv_r );
-            z = (float)( ( src( sj, 2 ) - tz ) * inv_r );
+            x = __fmul_rn( (float)( src( sj, 0 ) - tx ), inv_r );
+            y = __fmul_rn( (float)( src( sj, 1 ) - ty ), inv_r );
+            z = __fmul_rn( (float)( src( sj, 2 ) - tz ), inv_r );
         };
 
-        // FP32 moments with Kahan compensation (registers)
+        // FP32 moments (registers)
         {
-            float A[NU], C[NU];
+            float A[NU];
 #pragma unroll
             for ( int u = 0; u < NU; ++u )
-            {
                 A[u] = 0.f;
-                C[u] = 0.f;
-            }
             for ( int j = 0; j < len; ++j )
             {
                 float x, y, z;
@@ -138,26 +346,15 @@ __global__ void __launch_bounds__( MB )
                     float const pa = P[a] * phi;
 #pragma unroll
                     for ( int c = a; c < M; ++c )
-                    {
-                        int const u = ut<M>( a, c );
-                        float const term = __fmul_rn( pa, P[c] );
-                        float const yv = __fsub_rn( term, C[u] );
-                        float const tt = __fadd_rn( A[u], yv );
-                        C[u] = __fsub_rn( __fsub_rn( tt, A[u] ), yv );
-                        A[u] = tt;
-                    }
+                        A[ut<M>( a, c )] = fmaf( pa, P[c], A[ut<M>( a, c )] );
                 }
             }
 #pragma unroll
             for ( int u = 0; u < NU; ++u )
-            {
-                double const v = (double)A[u] - (double)C[u]; // exact in FP64
-                A64( u ) = v;
-                A32( u ) = (float)v;
-            }
+                A32( u ) = A[u];
         }
 
-        // FP32 cyclic Jacobi to FP32 convergence
+        // FP32 round-robin Jacobi to FP32 convergence
 #pragma unroll
         for ( int r = 0; r < M; ++r )
 #pragma unroll
@@ -171,88 +368,56 @@ __global__ void __launch_bounds__( MB )
                 break;
         }
 
-        // B = V32^T A64 V32 (upper triangle, FP64), written over A32
+        // truncation relative to the scaled spectrum: 1/lambda_k or 0 on the diagonal
+        float lmax = 0.f;
+        for ( int k = 0; k < M; ++k )
+            lmax = fmaxf( lmax, fabsf( A32( ut<M>( k, k ) ) ) );
+        float const cut = lmax * 9.5367431640625e-07f; // 2^-20
+        int dropped_here = 0;
         for ( int k = 0; k < M; ++k )
         {
-            double ck[M];
-#pragma unroll
-            for ( int r = 0; r < M; ++r )
-            {
-                double acc = 0.0;
-#pragma unroll
-                for ( int c = 0; c < M; ++c )
-                    acc = fma( A64( ut<M>( r, c ) ), (double)V32( c, k ), acc );
-                ck[r] = acc;
-            }
-            for ( int jj = 0; jj <= k; ++jj )
-            {
-                double acc = 0.0;
-#pragma unroll
-                for ( int r = 0; r < M; ++r )
-                    acc = fma( (double)V32( r, jj ), ck[r], acc );
-                B( ut<M>( jj, k ) ) = acc;
-            }
-        }
-        // W = V32 in FP64 (over A64), then FP64 sweeps on the nearly
-        // diagonal B until no pair is above 1e-15 relative
-#pragma unroll
-        for ( int r = 0; r < M; ++r )
-#pragma unroll
-            for ( int c = 0; c < M; ++c )
-                W( r, c ) = (double)V32( r, c );
-        // one FP64 sweep: B is FP32-converged (off-diagonal ~1e-7
-        // relative), so one quadratically convergent sweep takes it to
-        // ~1e-14; the refinement step below absorbs what is left
-        rotations += jacobi_sweep<M, double>( B, W, 1e-15 );
-
-        // truncation relative to the scaled spectrum: keep 1/lambda_k (or 0)
-        // on the diagonal of B for the pseudo-inverse A^+ = W L^+ W^T
-        double lmax = 0.0;
-        for ( int k = 0; k < M; ++k )
-            lmax = fmax( lmax, fabs( B( ut<M>( k, k ) ) ) );
-        double const cut = lmax * 9.5367431640625e-07; // 2^-20
-        for ( int k = 0; k < M; ++k )
-        {
-            double const lk = B( ut<M>( k, k ) );
-            if ( fabs( lk ) > cut && lk != 0.0 )
-                B( ut<M>( k, k ) ) = 1.0 / lk;
+            float const lk = A32( ut<M>( k, k ) );
+            if ( fabsf( lk ) > cut && lk != 0.f )
+                A32( ut<M>( k, k ) ) = 1.f / lk;
             else
             {
-                B( ut<M>( k, k ) ) = 0.0;
-                dropped = 1;
+                A32( ut<M>( k, k ) ) = 0.f;
+                dropped_here = 1;
             }
         }
-        // y += A^+ v (FP64), one eigen-direction at a time
-        auto pinv_add = [&]( double const *v, double *y ) {
+        dropped += dropped_here;
+        // y = M v = V L^+ V^T v (FP32), one eigen-direction at a time
+        auto pinv32 = [&]( float const *v, float *y ) {
+#pragma unroll
+            for ( int r = 0; r < M; ++r )
+                y[r] = 0.f;
             for ( int k = 0; k < M; ++k )
             {
-                double acc = 0.0;
+                float acc = 0.f;
 #pragma unroll
                 for ( int r = 0; r < M; ++r )
-                    acc = fma( W( r, k ), v[r], acc );
-                acc *= B( ut<M>( k, k ) );
+                    acc = fmaf( V32( r, k ), v[r], acc );
+                acc *= A32( ut<M>( k, k ) );
 #pragma unroll
                 for ( int r = 0; r < M; ++r )
-                    y[r] = fma( W( r, k ), acc, y[r] );
+                    y[r] = fmaf( V32( r, k ), acc, y[r] );
             }
         };
         double a[M];
-#pragma unroll
-        for ( int r = 0; r < M; ++r )
-            a[r] = 0.0;
-        for ( int k = 0; k < M; ++k )
         {
-            double const g = W( 0, k ) * B( ut<M>( k, k ) );
+            float e0[M], y[M];
 #pragma unroll
             for ( int r = 0; r < M; ++r )
-                a[r] = fma( W( r, k ), g, a[r] );
+                e0[r] = r == 0 ? 1.f : 0.f;
+            pinv32( e0, y );
+#pragma unroll
+            for ( int r = 0; r < M; ++r )
+                a[r] = (double)y[r];
         }
 
-        // One FP64 refinement step of row 0: the FP32 moments carry
-        // ~cond * 6e-8 relative error; the residual r = e0 - sum_j phi_j
-        // P_j (P_j . a) is exact up to FP64 rounding (P of the FP32
-        // coordinates is exact in FP64, phi_j is the FP32 weight), and
-        // a += A32^+ r contracts the error by ~cond(A^) * 2^-24.
+        // One refinement step of row 0: r = e0 - sum_j phi_j P_j (P_j . a) in
+        // FP64 (P of the FP32 coordinates is exact in FP64, phi_j is the FP32
+        // weight), a += M r.
         {
             double r[M];
 #pragma unroll
@@ -274,7 +439,14 @@ __global__ void __launch_bounds__( MB )
                 for ( int q = 0; q < M; ++q )
                     r[q] = fma( -w, P[q], r[q] );
             }
-            pinv_add( r, a );
+            float rf[M], d[M];
+#pragma unroll
+            for ( int q = 0; q < M; ++q )
+                rf[q] = (float)r[q];
+            pinv32( rf, d );
+#pragma unroll
+            for ( int q = 0; q < M; ++q )
+                a[q] += (double)d[q];
         }
 
         // coefficients c_j = phi_j (P_j . a): FP64 dot of exact FP64 basis
@@ -293,17 +465,14 @@ __global__ void __launch_bounds__( MB )
             coeff[b + j] = (float)( dot * (double)phi );
         }
     }
-    unsigned long long it64 = rotations, it32 = rotations32, dr64 = dropped;
+    unsigned long long it32 = rotations32, dr64 = dropped;
     for ( int o = 16; o; o >>= 1 )
     {
-        it64 += __shfl_xor_sync( FULL, it64, o );
         it32 += __shfl_xor_sync( FULL, it32, o );
         dr64 += __shfl_xor_sync( FULL, dr64, o );
     }
     if ( threadIdx.x == 0 )
     {
-        if ( it64 )
-            atomicAdd( rot_count, it64 );
         if ( it32 )
             atomicAdd( rot32_count, it32 );
         if ( dr64 )
@@ -314,21 +483,29 @@ __global__ void __launch_bounds__( MB )
 template <int M>
 void launch_mixed( SetupArgs const &a, cudaStream_t s )
 {
-    size_t const smem = ( (size_t)M * M * sizeof( double ) + (size_t)M * ( M + 1 ) / 2 * sizeof( double ) +
-                          (size_t)M * M * sizeof( float ) ) * MB;
+    DeviceBuffer<int32_t> list( a.n_tgt, s );
+    DeviceBuffer<unsigned> count( 1, s );
+    DTK_CUDA_OR_THROW( cudaMemsetAsync( count.get(), 0, sizeof( unsigned ), s ) );
+    k_setup_mixed<M><<<(unsigned)( ( a.n_tgt + 127 ) / 128 ), 128, 0, s>>>(
+        a.src, a.tgt, a.offset, a.idx, a.order, a.n_tgt, a.rbf, a.rows_sorted, a.coeff32, list.get(),
+        count.get(), a.status );
+    check_launch( "k_setup_mixed" );
+    // the listed targets (count known only on the device): persistent blocks
+    size_t const smem = ( (size_t)M * ( M + 1 ) / 2 + (size_t)M * M ) * sizeof( float ) * MB;
     static bool configured = false;
     if ( !configured )
     {
-        DTK_CUDA_OR_THROW( cudaFuncSetAttribute( k_setup_mixed<M>,
+        DTK_CUDA_OR_THROW( cudaFuncSetAttribute( k_setup_mixed_eig<M>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)smem ) );
         configured = true;
     }
-    unsigned const blocks = (unsigned)( ( a.n_tgt + MB - 1 ) / MB );
-    k_setup_mixed<M><<<blocks, MB, smem, s>>>( a.src, a.tgt, a.offset, a.idx, a.order, a.n_tgt,
-                                                a.rbf, a.rows_sorted, a.coeff32, a.underdetermined,
-                                                a.rotations, a.rotations32, a.status );
-    check_launch( "k_setup_mixed" );
+    int64_t const want = ( a.n_tgt + MB - 1 ) / MB;
+    unsigned const blocks = (unsigned)std::max<int64_t>( 1, std::min<int64_t>( want, 8 * num_sms() ) );
+    k_setup_mixed_eig<M><<<blocks, MB, smem, s>>>( a.src, a.tgt, a.offset, a.idx, list.get(), count.get(),
+                                                    a.rbf, a.rows_sorted, a.coeff32, a.underdetermined,
+                                                    a.rotations32, a.status );
+    check_launch( "k_setup_mixed_eig" );
 }
 
 } // namespace

@@ -129,4 +129,5 @@ def test_mixed_coefficients_are_fp32():
     _, op = transfer(src, tgt, syn.smooth_field(src), RBF[2], Q, k=32)
     _, _, coeff = op.csr()
     assert coeff.dtype == torch.float32
-    assert op.rotations > 0 and op.rotations_fp32 > 0
+    # no FP64 rotations; FP32 Jacobi rotations only for targets the Cholesky path hands over
+    assert op.rotations == 0 and op.rotations_fp32 >= 0
