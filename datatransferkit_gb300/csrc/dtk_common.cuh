@@ -279,7 +279,9 @@ struct Lbvh
     DeviceBuffer<uint32_t> codes;     // Morton codes in sorted order
     DeviceBuffer<uint32_t> grp;       // group (problem) of each sorted point; empty if ungrouped
     DeviceBuffer<uint32_t> perm;      // sorted position -> original index
-    DeviceBuffer<float4> nodes;       // 4 float4 per internal node
+    DeviceBuffer<float4> nodes;       // 4 float4 per binary internal node (released after the collapse)
+    DeviceBuffer<float4> wide;        // 24 float4 per 8-wide node (the queries' tree)
+    int64_t n_wide = 0;
     DeviceBuffer<float4> root_box;    // box of the whole tree (2 float4)
     DeviceBuffer<double> scene;       // lo[3], Morton scale[3], hi[3], centre[3], bound S
 };

@@ -22,6 +22,8 @@
 // so its IEEE bits are monotone), lexicographic with the source index.
 #include "dtk_common.cuh"
 
+#include <climits>
+
 #include <algorithm>
 #include <vector>
 
@@ -31,7 +33,7 @@ namespace
 {
 
 constexpr int LEAF = 32;
-constexpr int STACK = 64;
+constexpr int STACK = 192; // wide-node stack entries per warp (7 per level along the path)
 constexpr int Q_WARPS = 4; // warps per block in the query kernels
 constexpr unsigned FULL = 0xffffffffu;
 constexpr unsigned long long KEY_INF = 0xffffffffffffffffull;
@@ -393,6 +395,168 @@ __global__ void k_pack_children( int64_t n_internal, int const *left, int const 
 }
 
 // ---------------------------------------------------------------------------
+// 8-wide BVH: the binary radix tree collapsed three levels at a time.  Every
+// binary node at a depth divisible by 3 becomes a wide node whose children
+// are its descendants three levels down (or the leaves met on the way), in
+// binary left-to-right order, so child leaf ranges ascend.  Child slot c of
+// wide node w is 3 float4 at wide[24 w + 3 c]: (lo.x, lo.y, lo.z, hi.x),
+// (hi.y, hi.z, ref, -), (range_lo, range_hi, -, -), with ref >= 0 a wide
+// node, ref < 0 the leaf ~ref, and WIDE_EMPTY an unused slot (box lo = +inf,
+// hi = -inf, so its lower bound is +inf).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void load_node( float4 const *nodes, int node, float *l_lo,
+                                           float *l_hi, float *r_lo, float *r_hi, int &lc,
+                                           int &rc, int &lo, int &hi )
+{
+    float4 const a = __ldg( nodes + 4 * (int64_t)node );
+    float4 const b = __ldg( nodes + 4 * (int64_t)node + 1 );
+    float4 const c = __ldg( nodes + 4 * (int64_t)node + 2 );
+    float4 const e = __ldg( nodes + 4 * (int64_t)node + 3 );
+    l_lo[0] = a.x;
+    l_lo[1] = a.y;
+    l_lo[2] = a.z;
+    l_hi[0] = a.w;
+    l_hi[1] = b.x;
+    l_hi[2] = b.y;
+    r_lo[0] = b.z;
+    r_lo[1] = b.w;
+    r_lo[2] = c.x;
+    r_hi[0] = c.y;
+    r_hi[1] = c.z;
+    r_hi[2] = c.w;
+    lc = __float_as_int( e.x );
+    rc = __float_as_int( e.y );
+    lo = __float_as_int( e.z );
+    hi = __float_as_int( e.w );
+}
+
+constexpr int WIDE = 8;
+constexpr int WIDE_EMPTY = INT_MIN;
+
+// Child slot c of wide node `node`: its box, ref and (RANGE) leaf range.
+template <bool RANGE>
+__device__ __forceinline__ void load_wide( float4 const *wide, int node, int c, float *lo, float *hi,
+                                           int &ref, int &rlo, int &rhi )
+{
+    float4 const *p = wide + 24 * (int64_t)node + 3 * c;
+    float4 const a = __ldg( p ), b = __ldg( p + 1 );
+    lo[0] = a.x;
+    lo[1] = a.y;
+    lo[2] = a.z;
+    hi[0] = a.w;
+    hi[1] = b.x;
+    hi[2] = b.y;
+    ref = __float_as_int( b.z );
+    if ( RANGE )
+    {
+        float4 const e = __ldg( p + 2 );
+        rlo = __float_as_int( e.x );
+        rhi = __float_as_int( e.y );
+    }
+}
+
+__global__ void k_depth_flags( int64_t ni, int const *parent_node, int64_t *flag, unsigned *status )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i >= ni )
+        return;
+    int64_t d = 0;
+    int j = (int)i;
+    while ( j != 0 )
+    {
+        j = parent_node[j];
+        ++d;
+        if ( d > ni || j < 0 || j >= ni )
+        {
+            atomicOr( status, DEV_BAD_INDEX ); // malformed tree
+            break;
+        }
+    }
+    flag[i] = d % 3 == 0 ? 1 : 0;
+}
+
+__global__ void k_collapse( int64_t ni, float4 const *nodes, int64_t const *flag, int64_t const *widx,
+                            float4 *wide )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i >= ni || !flag[i] )
+        return;
+    int ref[WIDE];
+    Box box[WIDE];
+    int rlo[WIDE], rhi[WIDE];
+    int cnt = 0;
+    // the children of binary node j from its record
+    auto append_children = [&]( int j, int *r, Box *bx, int *lo, int *hi, int &c ) {
+        float l_lo[3], l_hi[3], r_lo[3], r_hi[3];
+        int lc, rc, nlo, nhi;
+        load_node( nodes, j, l_lo, l_hi, r_lo, r_hi, lc, rc, nlo, nhi );
+        int const gamma = lc >= 0 ? lc : ~lc;
+        r[c] = lc;
+        lo[c] = nlo;
+        hi[c] = gamma;
+        for ( int d = 0; d < 3; ++d )
+        {
+            bx[c].lo[d] = l_lo[d];
+            bx[c].hi[d] = l_hi[d];
+        }
+        ++c;
+        r[c] = rc;
+        lo[c] = gamma + 1;
+        hi[c] = nhi;
+        for ( int d = 0; d < 3; ++d )
+        {
+            bx[c].lo[d] = r_lo[d];
+            bx[c].hi[d] = r_hi[d];
+        }
+        ++c;
+    };
+    append_children( (int)i, ref, box, rlo, rhi, cnt );
+    for ( int round = 0; round < 2; ++round )
+    {
+        int nref[WIDE], nlo[WIDE], nhi[WIDE], n2 = 0;
+        Box nbox[WIDE];
+        for ( int c = 0; c < cnt; ++c )
+        {
+            if ( ref[c] >= 0 )
+                append_children( ref[c], nref, nbox, nlo, nhi, n2 );
+            else
+            {
+                nref[n2] = ref[c];
+                nbox[n2] = box[c];
+                nlo[n2] = rlo[c];
+                nhi[n2] = rhi[c];
+                ++n2;
+            }
+        }
+        for ( int c = 0; c < n2; ++c )
+        {
+            ref[c] = nref[c];
+            box[c] = nbox[c];
+            rlo[c] = nlo[c];
+            rhi[c] = nhi[c];
+        }
+        cnt = n2;
+    }
+    float4 *out = wide + 24 * widx[i];
+    for ( int c = 0; c < WIDE; ++c )
+    {
+        if ( c < cnt )
+        {
+            int const r = ref[c] >= 0 ? (int)widx[ref[c]] : ref[c];
+            out[3 * c] = make_float4( box[c].lo[0], box[c].lo[1], box[c].lo[2], box[c].hi[0] );
+            out[3 * c + 1] = make_float4( box[c].hi[1], box[c].hi[2], __int_as_float( r ), 0.f );
+            out[3 * c + 2] = make_float4( __int_as_float( rlo[c] ), __int_as_float( rhi[c] ), 0.f, 0.f );
+        }
+        else
+        {
+            out[3 * c] = make_float4( INFINITY, INFINITY, INFINITY, -INFINITY );
+            out[3 * c + 1] = make_float4( -INFINITY, -INFINITY, __int_as_float( WIDE_EMPTY ), 0.f );
+            out[3 * c + 2] = make_float4( __int_as_float( 1 ), __int_as_float( 0 ), 0.f, 0.f );
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Queries
 // ---------------------------------------------------------------------------
 struct GroupView
@@ -408,9 +572,9 @@ struct TreeView
     double const *sx, *sy, *sz;
     float const *fx, *fy, *fz;
     uint32_t const *codes, *perm;
-    float4 const *nodes;
+    float4 const *wide; // 8-wide nodes (24 float4 each)
     double const *scene;
-    int64_t n, nl;
+    int64_t n, nl, nw;
 };
 
 // FP32 lower bound of the squared distance between any point of [lo, hi]
@@ -464,31 +628,6 @@ __device__ __forceinline__ int64_t warp_lower_bound( uint32_t const *codes, int6
     return lo + __popc( __ballot_sync( FULL, pred ) );
 }
 
-__device__ __forceinline__ void load_node( float4 const *nodes, int node, float *l_lo,
-                                           float *l_hi, float *r_lo, float *r_hi, int &lc,
-                                           int &rc, int &lo, int &hi )
-{
-    float4 const a = __ldg( nodes + 4 * (int64_t)node );
-    float4 const b = __ldg( nodes + 4 * (int64_t)node + 1 );
-    float4 const c = __ldg( nodes + 4 * (int64_t)node + 2 );
-    float4 const e = __ldg( nodes + 4 * (int64_t)node + 3 );
-    l_lo[0] = a.x;
-    l_lo[1] = a.y;
-    l_lo[2] = a.z;
-    l_hi[0] = a.w;
-    l_hi[1] = b.x;
-    l_hi[2] = b.y;
-    r_lo[0] = b.z;
-    r_lo[1] = b.w;
-    r_lo[2] = c.x;
-    r_hi[0] = c.y;
-    r_hi[1] = c.z;
-    r_hi[2] = c.w;
-    lc = __float_as_int( e.x );
-    rc = __float_as_int( e.y );
-    lo = __float_as_int( e.z );
-    hi = __float_as_int( e.w );
-}
 
 // The problem (group) of a query: its sources' sorted-position range
 // [ps, pe) and leaf range [lps, lpe]; an ungrouped tree has one group.
@@ -509,19 +648,6 @@ __device__ __forceinline__ Range query_range( TreeView const &tr, GroupView cons
     r.lps = (int)( r.ps / LEAF );
     r.lpe = r.pe > r.ps ? (int)( ( r.pe - 1 ) / LEAF ) : -1;
     return r;
-}
-
-// Leaf ranges of a node's children (left covers [lo, gamma], right
-// [gamma + 1, hi], gamma the left child's index) outside the query's leaf
-// range are pruned by giving them an infinite lower bound.
-__device__ __forceinline__ void clip_children( int lc, int lo, int hi, Range const &q, float &lbl,
-                                               float &lbr )
-{
-    int const gamma = lc >= 0 ? lc : ~lc;
-    if ( gamma < q.lps || lo > q.lpe )
-        lbl = __int_as_float( 0x7f800000 );
-    if ( hi < q.lps || gamma + 1 > q.lpe )
-        lbr = __int_as_float( 0x7f800000 );
 }
 
 // The query in the centred frame: an FP32 interval [qlo, qhi] certain to
@@ -716,65 +842,80 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     }
     else
     {
-        // Near-first depth-first traversal; the farther child goes on the
-        // stack with its lower bound and is re-tested when popped.
+        // Wide-node traversal: lanes 0..7 test the 8 children of a node at
+        // once; leaf children are screened nearest first, internal children
+        // go on the stack with the nearest on top, and every popped entry is
+        // re-tested against the current bound.
         int sp = 0;
         int node = 0;
-        // every internal node is entered at most once
+        // every wide node is entered at most once
         for ( int64_t guard = 0;; ++guard )
         {
-            if ( guard >= tr.nl )
+            if ( guard >= tr.nw )
             {
                 if ( lane == 0 )
                     atomicOr( status, DEV_TIMEOUT );
                 break;
             }
-            float l_lo[3], l_hi[3], r_lo[3], r_hi[3];
-            int lc, rc, nlo, nhi;
-            load_node( tr.nodes, node, l_lo, l_hi, r_lo, r_hi, lc, rc, nlo, nhi );
-            float lbl = box_lb( l_lo, l_hi, q.qlo, q.qhi );
-            float lbr = box_lb( r_lo, r_hi, q.qlo, q.qhi );
-            if ( GROUPED )
-                clip_children( lc, nlo, nhi, rg, lbl, lbr );
-            bool const near_left = lbl <= lbr;
-            int const c_near = near_left ? lc : rc, c_far = near_left ? rc : lc;
-            float const lb_near = near_left ? lbl : lbr, lb_far = near_left ? lbr : lbl;
-            int next = -1;
-            if ( lb_far <= bound_f )
+            float lb = __int_as_float( 0x7f800000 );
+            int ref = WIDE_EMPTY;
+            bool ok = false;
+            if ( lane < WIDE )
             {
-                if ( sp < STACK )
+                float lo[3], hi[3];
+                int rlo = 0, rhi = 0;
+                load_wide<GROUPED>( tr.wide, node, lane, lo, hi, ref, rlo, rhi );
+                lb = box_lb( lo, hi, q.qlo, q.qhi );
+                ok = ref != WIDE_EMPTY && ( GROUPED ? !( rhi < rg.lps || rlo > rg.lpe ) : true );
+            }
+            bool const cand = ok && lb <= bound_f;
+            // order of the candidates by (lb, slot)
+            unsigned less = 0;
+#pragma unroll
+            for ( int o = 0; o < WIDE; ++o )
+            {
+                float const lo_ = __shfl_sync( FULL, lb, o );
+                less |= ( lo_ < lb || ( lo_ == lb && o < lane ) ? 1u : 0u ) << o;
+            }
+            unsigned const ml = __ballot_sync( FULL, cand && ref < 0 );
+            unsigned const mi = __ballot_sync( FULL, cand && ref >= 0 );
+            int const n_int = __popc( mi );
+            if ( sp + n_int <= STACK )
+            {
+                if ( cand && ref >= 0 )
                 {
-                    if ( lane == 0 )
-                    {
-                        s_stack[wib][sp] = c_far;
-                        s_lb[wib][sp] = lb_far;
-                    }
-                    ++sp;
+                    int const pos = sp + n_int - 1 - __popc( mi & less );
+                    s_stack[wib][pos] = ref;
+                    s_lb[wib][pos] = lb;
                 }
-                else if ( lane == 0 )
-                    atomicOr( status, DEV_STACK_OVERFLOW );
+                sp += n_int;
             }
-            if ( lb_near <= bound_f )
-            {
-                if ( c_near < 0 )
-                    process_leaf( ~c_near );
-                else
-                    next = c_near;
-            }
+            else if ( lane == 0 )
+                atomicOr( status, DEV_STACK_OVERFLOW );
             __syncwarp();
-            while ( next < 0 && sp > 0 )
+            int const n_leaf = __popc( ml );
+            for ( int r = 0; r < n_leaf; ++r )
+            {
+                unsigned const sel = __ballot_sync( FULL, ( ( ml >> lane ) & 1u ) && __popc( ml & less ) == r );
+                int const from = __ffs( sel ) - 1;
+                float const lbr = __shfl_sync( FULL, lb, from );
+                int const lref = __shfl_sync( FULL, ref, from );
+                if ( lbr <= bound_f )
+                    process_leaf( ~lref );
+            }
+            int next = -1;
+            while ( sp > 0 )
             {
                 --sp;
-                int const cand = s_stack[wib][sp];
-                float const lb = s_lb[wib][sp];
-                __syncwarp();
-                if ( lb > bound_f )
-                    continue;
-                if ( cand < 0 )
-                    process_leaf( ~cand );
-                else
-                    next = cand;
+                int const c = s_stack[wib][sp];
+                float const l = s_lb[wib][sp];
+                if ( l <= bound_f )
+                {
+                    next = c;
+                    break;
+                }
             }
+            __syncwarp();
             if ( next < 0 )
                 break;
             node = next;
@@ -850,57 +991,48 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     {
         int sp = 0;
         int node = 0;
-        // every internal node is entered at most once
+        unsigned const lt_mask = ( 1u << lane ) - 1u;
+        // every wide node is entered at most once
         for ( int64_t guard = 0;; ++guard )
         {
-            if ( guard >= tr.nl )
+            if ( guard >= tr.nw )
             {
                 if ( lane == 0 )
                     atomicOr( status, DEV_TIMEOUT );
                 break;
             }
-            float l_lo[3], l_hi[3], r_lo[3], r_hi[3];
-            int lc, rc, nlo, nhi;
-            load_node( tr.nodes, node, l_lo, l_hi, r_lo, r_hi, lc, rc, nlo, nhi );
-            float lbl = box_lb( l_lo, l_hi, q.qlo, q.qhi );
-            float lbr = box_lb( r_lo, r_hi, q.qlo, q.qhi );
-            if ( GROUPED )
-                clip_children( lc, nlo, nhi, rg, lbl, lbr );
-            bool const hl = lbl <= bound_f;
-            bool const hr = lbr <= bound_f;
-            int next = -1;
-            if ( hl )
+            bool cand = false;
+            int ref = WIDE_EMPTY;
+            if ( lane < WIDE )
             {
-                if ( lc < 0 )
-                    process_leaf( ~lc );
-                else
-                    next = lc;
+                float lo[3], hi[3];
+                int rlo = 0, rhi = 0;
+                load_wide<GROUPED>( tr.wide, node, lane, lo, hi, ref, rlo, rhi );
+                cand = ref != WIDE_EMPTY && box_lb( lo, hi, q.qlo, q.qhi ) <= bound_f &&
+                       ( GROUPED ? !( rhi < rg.lps || rlo > rg.lpe ) : true );
             }
-            if ( hr )
+            unsigned const ml = __ballot_sync( FULL, cand && ref < 0 );
+            unsigned const mi = __ballot_sync( FULL, cand && ref >= 0 );
+            int const n_int = __popc( mi );
+            if ( sp + n_int <= STACK )
             {
-                if ( rc < 0 )
-                    process_leaf( ~rc );
-                else if ( next < 0 )
-                    next = rc;
-                else if ( sp < STACK )
-                {
-                    if ( lane == 0 )
-                        s_stack[wib][sp] = rc;
-                    ++sp;
-                }
-                else if ( lane == 0 )
-                    atomicOr( status, DEV_STACK_OVERFLOW );
+                if ( cand && ref >= 0 )
+                    s_stack[wib][sp + __popc( mi & lt_mask )] = ref;
+                sp += n_int;
             }
+            else if ( lane == 0 )
+                atomicOr( status, DEV_STACK_OVERFLOW );
             __syncwarp();
-            if ( next < 0 )
+            for ( unsigned m = ml; m; m &= m - 1 )
             {
-                if ( sp == 0 )
-                    break;
-                --sp;
-                next = s_stack[wib][sp];
-                __syncwarp();
+                int const lref = __shfl_sync( FULL, ref, __ffs( m ) - 1 );
+                process_leaf( ~lref );
             }
-            node = next;
+            if ( sp == 0 )
+                break;
+            --sp;
+            node = s_stack[wib][sp];
+            __syncwarp();
         }
     }
     if ( !FILL && lane == 0 )
@@ -912,7 +1044,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
 TreeView view_of( Lbvh const &t )
 {
     return TreeView{t.sx.get(), t.sy.get(), t.sz.get(), t.fx.get(), t.fy.get(), t.fz.get(),
-                    t.codes.get(), t.perm.get(), t.nodes.get(), t.scene.get(), t.n, t.n_leaves};
+                    t.codes.get(), t.perm.get(), t.wide.get(), t.scene.get(), t.n, t.n_leaves, t.n_wide};
 }
 
 unsigned blocks_for( int64_t n, int threads )
@@ -993,6 +1125,23 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
                                                      parent_leaf.get(), tree.nodes.get(), flags.get(),
                                                      tree.root_box.get(), status );
     check_launch( "k_refit" );
+    tree.n_wide = 0;
+    if ( ni > 0 )
+    {
+        DeviceBuffer<int64_t> flag( ni, s ), widx( ni + 1, s );
+        k_depth_flags<<<blocks_for( ni, 256 ), 256, 0, s>>>( ni, parent_node.get(), flag.get(), status );
+        check_launch( "k_depth_flags" );
+        exclusive_scan_i64( flag.get(), widx.get(), ni, s );
+        int64_t nw = 0;
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( &nw, widx.get() + ni, sizeof( int64_t ), cudaMemcpyDeviceToHost, s ) );
+        DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+        tree.n_wide = nw;
+        tree.wide.allocate( 24 * std::max<int64_t>( 1, nw ), s );
+        k_collapse<<<blocks_for( ni, 128 ), 128, 0, s>>>( ni, tree.nodes.get(), flag.get(), widx.get(),
+                                                           tree.wide.get() );
+        check_launch( "k_collapse" );
+    }
+    tree.nodes = DeviceBuffer<float4>(); // the queries use the wide nodes
 }
 
 void sort_queries( Lbvh const &tree, PointsView tgt, DeviceBuffer<uint32_t> &order,
