@@ -21,7 +21,7 @@ STATUS_NAMES = {0: "DTK_OK", 1: "DTK_ERR_INVALID_ARG", 2: "DTK_ERR_UNSUPPORTED",
 EXPORTED = [
     "dtk_mls_default_options", "dtk_mls_create", "dtk_mls_apply", "dtk_mls_apply_adjoint",
     "dtk_mls_get_csr", "dtk_mls_get_sizes", "dtk_mls_underdetermined_count",
-    "dtk_mls_get_stage_times", "dtk_mls_get_rotation_count", "dtk_mls_destroy",
+    "dtk_mls_get_stage_times", "dtk_mls_get_search_times", "dtk_mls_get_rotation_count", "dtk_mls_destroy",
     "dtk_knn_search", "dtk_svd_pinv", "dtk_mls_batch_create", "dtk_mls_batch_apply",
     "dtk_mls_batch_get_csr", "dtk_mls_batch_destroy", "dtk_mls_batch_get_stage_times", "dtk_last_error", "dtk_status_string",
     "dtk_kernel_launch_count", "dtk_svd_pinv_noalloc",
@@ -68,6 +68,7 @@ def _declare(L):
     L.dtk_mls_get_sizes.argtypes = [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)]
     L.dtk_mls_underdetermined_count.argtypes = [_vp, C.POINTER(_i64)]
     L.dtk_mls_get_stage_times.argtypes = [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.dtk_mls_get_search_times.argtypes = [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.dtk_mls_get_rotation_count.argtypes = [_vp, C.POINTER(_i64), C.POINTER(_i64)]
     L.dtk_kernel_launch_count.argtypes = []
     L.dtk_mls_destroy.argtypes = [_vp]

@@ -193,7 +193,7 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
             }
         }
 
-        cudaEvent_t ev[3];
+        cudaEvent_t ev[4];
         for ( auto &e : ev )
             DTK_CUDA_OR_THROW( cudaEventCreate( &e ) );
         struct EvGuard
@@ -201,7 +201,7 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
             cudaEvent_t *e;
             ~EvGuard()
             {
-                for ( int i = 0; i < 3; ++i )
+                for ( int i = 0; i < 4; ++i )
                     cudaEventDestroy( e[i] );
             }
         } evg{ev};
@@ -215,6 +215,7 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
         Lbvh tree;
         build_lbvh( sv, tree, status.get(), s );
         sort_queries( tree, tv, h->order, s );
+        DTK_CUDA_OR_THROW( cudaEventRecord( ev[3], s ) );
         h->offset.allocate( n_tgt + 1, s );
         if ( !g.radius_mode )
         {
@@ -305,6 +306,8 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
         h->rotations32 = (int64_t)cnt[2];
         DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->search_ms, ev[0], ev[1] ) );
         DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->setup_ms, ev[1], ev[2] ) );
+        DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->build_ms, ev[0], ev[3] ) );
+        DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->query_ms, ev[3], ev[1] ) );
         *out = guard.release();
     } );
 }
@@ -375,6 +378,17 @@ dtk_status dtk_mls_get_stage_times( dtk_mls_handle h, float *search_ms, float *s
             *search_ms = h->search_ms;
         if ( setup_ms )
             *setup_ms = h->setup_ms;
+    } );
+}
+
+dtk_status dtk_mls_get_search_times( dtk_mls_handle h, float *build_ms, float *query_ms )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
+        if ( build_ms )
+            *build_ms = h->build_ms;
+        if ( query_ms )
+            *query_ms = h->query_ms;
     } );
 }
 

@@ -27,4 +27,5 @@ struct dtk_mls_s
     int64_t underdetermined = 0;
     int64_t rotations = 0, rotations32 = 0;
     float search_ms = 0.f, setup_ms = 0.f;
+    float build_ms = 0.f, query_ms = 0.f; // the search split: tree build + query sort, kNN/radius queries
 };

@@ -247,6 +247,13 @@ class MovingLeastSquaresOperator(PointCloudOperator):
         check(lib().dtk_mls_get_stage_times(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    @property
+    def search_times_ms(self):
+        """(tree build + target sort, query kernels) device milliseconds of the create."""
+        a, b = C.c_float(), C.c_float()
+        check(lib().dtk_mls_get_search_times(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             lib().dtk_mls_destroy(self._h)

@@ -145,6 +145,10 @@ dtk_status dtk_mls_underdetermined_count(dtk_mls_handle h, int64_t *count);
 /* Device-side timings of the last create (milliseconds): search, setup. */
 dtk_status dtk_mls_get_stage_times(dtk_mls_handle h, float *search_ms,
                                    float *setup_ms);
+/* The search stage split (milliseconds): tree build with the Morton sort of
+ * the targets, and the kNN / radius query kernels. */
+dtk_status dtk_mls_get_search_times(dtk_mls_handle h, float *build_ms,
+                                    float *query_ms);
 
 /* Jacobi rotations the create performed, in FP64 and (mixed form) in FP32;
  * the basis of the FLOP counts in the benchmark.  Either pointer may be NULL. */
