@@ -5,11 +5,11 @@ C ABI of ``include/dtk_gb300.h``); this package is its host-side mirror of
 DataTransferKit's operator API.  There is no CPU fallback.
 """
 from .operators import (FP64, MIXED, Buhmann, Constant, Linear, MovingLeastSquaresBatch,
-                        MovingLeastSquaresOperator,
+                        MovingLeastSquaresOperator, NearestNeighborOperator,
                         MultivariatePolynomialBasis, PointCloudOperator, Quadratic, Wendland, Wu,
                         kernel_launch_count, knn_search, svd_pinv)
 from ._capi import DTKError, InvalidArgument, Unsupported
 
-__all__ = ["MovingLeastSquaresOperator", "MovingLeastSquaresBatch", "PointCloudOperator", "MultivariatePolynomialBasis",
+__all__ = ["MovingLeastSquaresOperator", "MovingLeastSquaresBatch", "NearestNeighborOperator", "PointCloudOperator", "MultivariatePolynomialBasis",
            "Constant", "Linear", "Quadratic", "Wendland", "Wu", "Buhmann", "FP64", "MIXED",
            "knn_search", "svd_pinv", "kernel_launch_count", "DTKError", "InvalidArgument", "Unsupported"]

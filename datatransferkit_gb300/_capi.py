@@ -24,7 +24,8 @@ EXPORTED = [
     "dtk_mls_get_stage_times", "dtk_mls_get_search_times", "dtk_mls_get_rotation_count", "dtk_mls_destroy",
     "dtk_knn_search", "dtk_svd_pinv", "dtk_mls_batch_create", "dtk_mls_batch_apply",
     "dtk_mls_batch_get_csr", "dtk_mls_batch_destroy", "dtk_mls_batch_get_stage_times", "dtk_last_error", "dtk_status_string",
-    "dtk_kernel_launch_count", "dtk_svd_pinv_noalloc",
+    "dtk_kernel_launch_count", "dtk_svd_pinv_noalloc", "dtk_mls_apply_multi", "dtk_nn_create",
+    "dtk_nn_apply", "dtk_nn_apply_multi", "dtk_nn_get_indices", "dtk_nn_destroy",
 ]
 
 
@@ -80,6 +81,12 @@ def _declare(L):
     L.dtk_mls_batch_apply.argtypes = [_vp, _vp, _vp, C.c_int32, _vp]
     L.dtk_mls_batch_get_csr.argtypes = L.dtk_mls_get_csr.argtypes
     L.dtk_mls_batch_destroy.argtypes = [_vp]
+    L.dtk_mls_apply_multi.argtypes = [_vp, _vp, _i64, _i64, _i64, _i64, _vp, _i64, _i64, _i64, _vp]
+    L.dtk_nn_create.argtypes = [_vp, _i64, _i64, _i64, _vp, _i64, _i64, _i64, C.c_int32, _vp, C.POINTER(_vp)]
+    L.dtk_nn_apply.argtypes = [_vp, _vp, _i64, _vp, _i64, _vp]
+    L.dtk_nn_apply_multi.argtypes = L.dtk_mls_apply_multi.argtypes
+    L.dtk_nn_get_indices.argtypes = [_vp, C.POINTER(_vp), C.POINTER(_i64)]
+    L.dtk_nn_destroy.argtypes = [_vp]
     L.dtk_mls_batch_get_stage_times.argtypes = [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                                 C.POINTER(C.c_float)]
     L.dtk_last_error.restype = C.c_char_p

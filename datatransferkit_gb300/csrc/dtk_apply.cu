@@ -138,6 +138,61 @@ bool is_pow2( int v ) { return v > 0 && ( v & ( v - 1 ) ) == 0; }
 
 // uniform_row > 0: every row has that length (offset[i] = i * uniform_row);
 // otherwise mean_row picks the lanes per row.
+namespace
+{
+
+// Rank-2 fields: 8 lanes per row, 4 components per pass; the row's indices
+// and coefficients are read once per pass for 4 components.
+template <bool F32>
+__global__ void __launch_bounds__( 256 )
+    k_apply_multi( int64_t n_tgt, int32_t const *__restrict__ offset, int32_t const *__restrict__ idx,
+                   void const *__restrict__ coeff, FieldView in, FieldView out )
+{
+    constexpr int S = 8, CB = 4;
+    int64_t const gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t const row = gt / S;
+    int const sub = (int)( gt % S );
+    bool const live = row < n_tgt;
+    int const b = live ? offset[row] : 0, e = live ? offset[row + 1] : 0;
+    for ( int c0 = 0; c0 < in.n_comp; c0 += CB ) // uniform across the warp
+    {
+        double acc[CB] = {0.0, 0.0, 0.0, 0.0};
+        for ( int j = b + sub; j < e; j += S )
+        {
+            double const cj = F32 ? (double)__ldg( static_cast<float const *>( coeff ) + j )
+                                  : __ldg( static_cast<double const *>( coeff ) + j );
+            int64_t const sj = __ldg( idx + j );
+#pragma unroll
+            for ( int q = 0; q < CB; ++q )
+                if ( c0 + q < in.n_comp )
+                    acc[q] = fma( cj, __ldg( in.base + sj * in.ps + ( c0 + q ) * in.cs ), acc[q] );
+        }
+#pragma unroll
+        for ( int q = 0; q < CB; ++q )
+            acc[q] = group_sum<S>( acc[q] );
+        if ( live && sub == 0 )
+#pragma unroll
+            for ( int q = 0; q < CB; ++q )
+                if ( c0 + q < in.n_comp )
+                    out.wbase[row * out.ps + ( c0 + q ) * out.cs] = acc[q];
+    }
+}
+
+} // namespace
+
+void apply_csr_multi( int64_t n_tgt, int32_t const *offset, int32_t const *idx, double const *coeff64,
+                      float const *coeff32, FieldView in, FieldView out, cudaStream_t s )
+{
+    if ( n_tgt == 0 )
+        return;
+    unsigned const blocks = (unsigned)( ( n_tgt * 8 + 255 ) / 256 );
+    if ( coeff32 )
+        k_apply_multi<true><<<blocks, 256, 0, s>>>( n_tgt, offset, idx, coeff32, in, out );
+    else
+        k_apply_multi<false><<<blocks, 256, 0, s>>>( n_tgt, offset, idx, coeff64, in, out );
+    check_launch( "k_apply_multi" );
+}
+
 void apply_csr( int64_t n_tgt, int32_t const *offset, int32_t const *idx, double const *coeff64,
                 float const *coeff32, int uniform_row, int mean_row, double const *values,
                 double *target, cudaStream_t s )

@@ -384,31 +384,6 @@ struct dtk_mls_batch_s
 namespace
 {
 
-template <class F>
-dtk_status guarded_batch( F &&f )
-{
-    try
-    {
-        f();
-        return DTK_OK;
-    }
-    catch ( Error const &e )
-    {
-        set_error( e.msg );
-        return e.status;
-    }
-    catch ( std::bad_alloc const & )
-    {
-        set_error( "host allocation failed" );
-        return DTK_ERR_OOM;
-    }
-    catch ( std::exception const &e )
-    {
-        set_error( e.what() );
-        return DTK_ERR_INTERNAL;
-    }
-}
-
 double ms_since( std::chrono::steady_clock::time_point t0 )
 {
     return std::chrono::duration<double, std::milli>( std::chrono::steady_clock::now() - t0 ).count();
@@ -423,7 +398,7 @@ dtk_status dtk_mls_batch_create( int32_t n_problems, const dtk_mls_options *opts
                                  const int64_t *tgt_offsets, const double *tgt,
                                  dtk_stream_t stream_, dtk_mls_batch_handle *out )
 {
-    return guarded_batch( [&] {
+    return guarded( [&] {
         DTK_REQUIRE_OR_THROW( out != nullptr, "output handle pointer is null" );
         *out = nullptr;
         DTK_REQUIRE_OR_THROW( n_problems >= 1, "n_problems must be >= 1" );
@@ -627,7 +602,7 @@ dtk_status dtk_mls_batch_create( int32_t n_problems, const dtk_mls_options *opts
 dtk_status dtk_mls_batch_apply( dtk_mls_batch_handle h, const double *src_values, double *tgt_values,
                                 int32_t use_graph, dtk_stream_t stream_ )
 {
-    return guarded_batch( [&] {
+    return guarded( [&] {
         DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
         DTK_REQUIRE_OR_THROW( src_values != nullptr && ( h->n_tgt == 0 || tgt_values != nullptr ),
                               "null values" );
@@ -667,7 +642,7 @@ dtk_status dtk_mls_batch_apply( dtk_mls_batch_handle h, const double *src_values
 dtk_status dtk_mls_batch_get_csr( dtk_mls_batch_handle h, const int32_t **offset, const int32_t **indices,
                                   const void **coeff, int64_t *nnz, int32_t *coeff_is_fp32 )
 {
-    return guarded_batch( [&] {
+    return guarded( [&] {
         DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
         bool const f32 = h->coeff32.get() != nullptr;
         if ( offset )
@@ -686,7 +661,7 @@ dtk_status dtk_mls_batch_get_csr( dtk_mls_batch_handle h, const int32_t **offset
 dtk_status dtk_mls_batch_get_stage_times( dtk_mls_batch_handle h, float *search_ms, float *setup_ms,
                                           float *host_ms )
 {
-    return guarded_batch( [&] {
+    return guarded( [&] {
         DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
         if ( search_ms )
             *search_ms = h->search_ms;
@@ -699,7 +674,7 @@ dtk_status dtk_mls_batch_get_stage_times( dtk_mls_batch_handle h, float *search_
 
 dtk_status dtk_mls_batch_destroy( dtk_mls_batch_handle h )
 {
-    return guarded_batch( [&] { delete h; } );
+    return guarded( [&] { delete h; } );
 }
 
 } // extern "C"

@@ -31,31 +31,6 @@ long long &launch_counter()
     return n;
 }
 
-template <class F>
-dtk_status guarded( F &&f )
-{
-    try
-    {
-        f();
-        return DTK_OK;
-    }
-    catch ( Error const &e )
-    {
-        set_error( e.msg );
-        return e.status;
-    }
-    catch ( std::bad_alloc const & )
-    {
-        set_error( "host allocation failed" );
-        return DTK_ERR_OOM;
-    }
-    catch ( std::exception const &e )
-    {
-        set_error( e.what() );
-        return DTK_ERR_INTERNAL;
-    }
-}
-
 __global__ void k_fill_uniform_offsets( int32_t *offset, int64_t n_tgt, int row )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -79,15 +54,6 @@ __global__ void k_pack_points( PointsView p, double *out )
         out[3 * i + 1] = p( i, 1 );
         out[3 * i + 2] = p( i, 2 );
     }
-}
-
-void validate_points( double const *p, int64_t n, int64_t ps, int64_t ds, char const *what )
-{
-    DTK_REQUIRE_OR_THROW( n >= 0, std::string( what ) + " count is negative" );
-    DTK_REQUIRE_OR_THROW( n == 0 || p != nullptr, std::string( what ) + " pointer is null" );
-    DTK_REQUIRE_OR_THROW( n <= INT32_MAX, std::string( what ) + " count exceeds int32 indices" );
-    DTK_REQUIRE_OR_THROW( n == 0 || ( ps != 0 || n == 1 ) && ds != 0,
-                          std::string( what ) + " strides are zero" );
 }
 
 struct Geometry

@@ -4,7 +4,10 @@
 #include <cuda_runtime.h>
 
 #include <cfloat>
+#include <climits>
 #include <cstdint>
+#include <exception>
+#include <new>
 #include <string>
 
 #include "../../include/dtk_gb300.h"
@@ -44,6 +47,43 @@ struct Error
                                std::string( "DTK_REQUIRE( " #cond " ): " ) +   \
                                    ( msg )};                                   \
     } while ( 0 )
+
+// Runs f and maps what it throws to a dtk_status (and the thread's last
+// error message): every extern "C" entry point is one guarded call.
+template <class F>
+inline dtk_status guarded( F &&f )
+{
+    try
+    {
+        f();
+        return DTK_OK;
+    }
+    catch ( Error const &e )
+    {
+        set_error( e.msg );
+        return e.status;
+    }
+    catch ( std::bad_alloc const & )
+    {
+        set_error( "host allocation failed" );
+        return DTK_ERR_OOM;
+    }
+    catch ( std::exception const &e )
+    {
+        set_error( e.what() );
+        return DTK_ERR_INTERNAL;
+    }
+}
+
+// Point-cloud arguments of an entry point: count, pointer and strides.
+inline void validate_points( double const *p, int64_t n, int64_t ps, int64_t ds, char const *what )
+{
+    DTK_REQUIRE_OR_THROW( n >= 0, std::string( what ) + " count is negative" );
+    DTK_REQUIRE_OR_THROW( n == 0 || p != nullptr, std::string( what ) + " pointer is null" );
+    DTK_REQUIRE_OR_THROW( n <= INT32_MAX, std::string( what ) + " count exceeds int32 indices" );
+    DTK_REQUIRE_OR_THROW( n == 0 || ( ps != 0 || n == 1 ) && ds != 0,
+                          std::string( what ) + " strides are zero" );
+}
 
 // Stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync).
 template <class T>
@@ -244,6 +284,15 @@ __device__ __forceinline__ void basis_eval( T x, T y, T z, T *p )
     }
 }
 
+// Rank-2 field (n points x n_comp components): element (i, c) at
+// base[i*ps + c*cs] (LayoutRight: cs = 1; LayoutLeft: ps = 1, cs = n).
+struct FieldView
+{
+    double const *base;
+    double *wbase;
+    int64_t n, n_comp, ps, cs;
+};
+
 // Strided point access: element (i, d) at base[i*ps + d*ds].
 struct PointsView
 {
@@ -366,6 +415,9 @@ void svd_pinv_batched_work( int n, int64_t count, double const *a, double *pinv,
                             cudaStream_t s );
 
 // Apply kernels.
+// Rank-2 fields: out(i, c) = sum_j coeff_j in(idx_j, c).
+void apply_csr_multi( int64_t n_tgt, int32_t const *offset, int32_t const *idx, double const *coeff64,
+                      float const *coeff32, FieldView in, FieldView out, cudaStream_t s );
 void apply_csr( int64_t n_tgt, int32_t const *offset, int32_t const *idx,
                 double const *coeff64, float const *coeff32, int uniform_row, int mean_row,
                 double const *values, double *target, cudaStream_t s );

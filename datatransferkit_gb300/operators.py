@@ -180,14 +180,19 @@ class MovingLeastSquaresOperator(PointCloudOperator):
 
     # -- reference API ------------------------------------------------------
     def apply(self, source_values: torch.Tensor, target_values: torch.Tensor, stream=None) -> None:
+        """target_values = T source_values; rank-1 fields, or rank-2 (n, n_comp) fields
+        with any strides (each component transferred alike)."""
+        st = _stream(stream if stream is not None else self._stream)
+        if source_values.dim() == 2 or target_values.dim() == 2:
+            check(lib().dtk_mls_apply_multi(self._h, *_fields(source_values, target_values), st))
+            return
         for t, what in ((source_values, "source_values"), (target_values, "target_values")):
             if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float64:
                 raise _capi.InvalidArgument(1, f"{what} must be a float64 CUDA tensor")
             if t.dim() != 1 or (t.numel() > 1 and t.stride(0) != 1):
                 raise _capi.InvalidArgument(1, f"{what} must be rank 1 and contiguous")
         check(lib().dtk_mls_apply(self._h, source_values.data_ptr(), source_values.shape[0],
-                                  target_values.data_ptr(), target_values.shape[0],
-                                  _stream(stream if stream is not None else self._stream)))
+                                  target_values.data_ptr(), target_values.shape[0], st))
 
     # -- extensions ------------------------------------------------------------
     def apply_adjoint(self, cot: torch.Tensor, source_values: torch.Tensor | None = None,
@@ -354,6 +359,73 @@ class MovingLeastSquaresBatch:
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             lib().dtk_mls_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _fields(source_values, target_values):
+    """(ptr, n, n_comp, point stride, component stride) of both rank-2 fields, flattened
+    into the argument order of the *_apply_multi entry points (stream excluded)."""
+    out = []
+    n_comp = None
+    for t, what in ((source_values, "source_values"), (target_values, "target_values")):
+        if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float64:
+            raise _capi.InvalidArgument(1, f"{what} must be a float64 CUDA tensor")
+        if t.dim() == 1:
+            t = t.unsqueeze(1)
+        if t.dim() != 2:
+            raise _capi.InvalidArgument(1, f"{what} must be rank 1 or 2")
+        if n_comp is not None and t.shape[1] != n_comp:
+            raise _capi.InvalidArgument(1, "source_values.extent(1) == target_values.extent(1)")
+        n_comp = t.shape[1]
+        out.append((t.data_ptr(), t.shape[0], t.stride(0), t.stride(1)))
+    (sp, sn, sps, scs), (tp, tn, tps, tcs) = out
+    return sp, sn, n_comp, sps, scs, tp, tn, tps, tcs
+
+
+class NearestNeighborOperator(PointCloudOperator):
+    """Nearest-neighbour transfer between point clouds (one rank).
+
+    ``NearestNeighborOperator(comm, source_points, target_points)`` finds the
+    nearest source of every target (ties to the smaller source index);
+    ``apply(source_values, target_values)`` copies each target's nearest
+    source value (rank-1 or rank-2 fields).
+    Mirrors DTK_NearestNeighborOperator_decl.hpp:27-49.
+    """
+
+    def __init__(self, comm, source_points, target_points, *, stream=None):
+        src = _check_points(source_points, "source_points")
+        tgt = _check_points(target_points, "target_points")
+        if src.shape[1] != tgt.shape[1] or src.shape[1] != 3:
+            raise _capi.InvalidArgument(1, "source_points.extent(1) == target_points.extent(1) == 3")
+        self._h = C.c_void_p()
+        self._stream = stream
+        check(lib().dtk_nn_create(src.data_ptr(), src.shape[0], src.stride(0), src.stride(1),
+                                  tgt.data_ptr(), tgt.shape[0], tgt.stride(0), tgt.stride(1),
+                                  _comm_size(comm), _stream(stream), C.byref(self._h)))
+        self.n_source_points = int(src.shape[0])
+        self.n_target_points = int(tgt.shape[0])
+
+    def apply(self, source_values: torch.Tensor, target_values: torch.Tensor, stream=None) -> None:
+        check(lib().dtk_nn_apply_multi(self._h, *_fields(source_values, target_values),
+                                       _stream(stream if stream is not None else self._stream)))
+
+    @property
+    def indices(self) -> torch.Tensor:
+        """Nearest source index of every target (a copy)."""
+        p, n = C.c_void_p(), C.c_int64()
+        check(lib().dtk_nn_get_indices(self._h, C.byref(p), C.byref(n)))
+        torch.cuda.synchronize()
+        return _from_device(p.value, n.value, torch.int32)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().dtk_nn_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

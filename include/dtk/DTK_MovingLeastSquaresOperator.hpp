@@ -387,6 +387,21 @@ class MovingLeastSquaresOperator : public PointCloudOperator<DeviceType>
     }
 
     // Extensions
+    // Rank-2 fields (n x n_comp views, any layout): every component alike.
+    template <typename SourceValues, typename TargetValues>
+    void apply_fields( SourceValues const &source_values, TargetValues const &target_values ) const
+    {
+        if ( source_values.extent( 1 ) != target_values.extent( 1 ) )
+            throw DataTransferKitException(
+                "DTK_REQUIRE( source_values.extent( 1 ) == target_values.extent( 1 ) )" );
+        Details::check( dtk_mls_apply_multi(
+            _handle.get(), reinterpret_cast<double const *>( source_values.data() ),
+            (int64_t)source_values.extent( 0 ), (int64_t)source_values.extent( 1 ),
+            (int64_t)source_values.stride( 0 ), (int64_t)source_values.stride( 1 ),
+            const_cast<double *>( reinterpret_cast<double const *>( target_values.data() ) ),
+            (int64_t)target_values.extent( 0 ), (int64_t)target_values.stride( 0 ),
+            (int64_t)target_values.stride( 1 ), _stream ) );
+    }
     int64_t underdetermined() const
     {
         int64_t n = 0;

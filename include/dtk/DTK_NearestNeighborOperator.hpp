@@ -1,0 +1,87 @@
+/*
+ * Header-only drop-in for DataTransferKit's NearestNeighborOperator on one
+ * rank, over the C ABI of dtk_gb300.h (link with libdtk_gb300.so).
+ *
+ * Mirrors (paths inside the DataTransferKit project):
+ *   DataTransferKit::NearestNeighborOperator<DeviceType>
+ *       packages/Meshfree/src/DTK_NearestNeighborOperator_decl.hpp:27-49
+ *       packages/Meshfree/src/DTK_NearestNeighborOperator_def.hpp:23-81
+ *
+ * Views, communicator and exceptions as in DTK_MovingLeastSquaresOperator.hpp.
+ * The nearest source of a target is the smallest (d^2, source index): ties
+ * go to the smaller source index.
+ */
+#ifndef DTK_GB300_NEAREST_NEIGHBOR_OPERATOR_HPP
+#define DTK_GB300_NEAREST_NEIGHBOR_OPERATOR_HPP
+
+#include "DTK_MovingLeastSquaresOperator.hpp"
+
+namespace DataTransferKit
+{
+
+template <typename DeviceType>
+class NearestNeighborOperator : public PointCloudOperator<DeviceType>
+{
+  public:
+    using device_type = DeviceType;
+    using ExecutionSpace = typename DeviceType::execution_space;
+
+    template <typename Comm, typename SourceView, typename TargetView>
+    NearestNeighborOperator( Comm comm, SourceView const &source_points, TargetView const &target_points,
+                             dtk_stream_t stream = nullptr )
+        : _size( source_points.extent( 0 ) )
+        , _n_target_points( target_points.extent( 0 ) )
+        , _stream( stream )
+    {
+        dtk_nn_handle h = nullptr;
+        Details::check( dtk_nn_create(
+            reinterpret_cast<double const *>( source_points.data() ), (int64_t)source_points.extent( 0 ),
+            (int64_t)source_points.stride( 0 ), (int64_t)source_points.stride( 1 ),
+            reinterpret_cast<double const *>( target_points.data() ), (int64_t)target_points.extent( 0 ),
+            (int64_t)target_points.stride( 0 ), (int64_t)target_points.stride( 1 ),
+            Details::comm_size( comm ), _stream, &h ) );
+        _handle.reset( h, []( dtk_nn_handle p ) { dtk_nn_destroy( p ); } );
+    }
+
+    template <typename SourceValues, typename TargetValues>
+    void apply_values( SourceValues const &source_values, TargetValues const &target_values ) const
+    {
+        // DTK_REQUIRE at DTK_NearestNeighborOperator_def.hpp:73-74
+        if ( (std::size_t)target_values.extent( 0 ) != _n_target_points )
+            throw DataTransferKitException( "DTK_REQUIRE( _indices.extent( 0 ) == target_values.extent( 0 ) )" );
+        if ( (std::size_t)source_values.extent( 0 ) != _size )
+            throw DataTransferKitException( "DTK_REQUIRE( _size == source_values.extent_int( 0 ) )" );
+        Details::check( dtk_nn_apply_multi(
+            _handle.get(), reinterpret_cast<double const *>( source_values.data() ),
+            (int64_t)source_values.extent( 0 ), (int64_t)source_values.extent( 1 ),
+            (int64_t)source_values.stride( 0 ), (int64_t)source_values.stride( 1 ),
+            const_cast<double *>( reinterpret_cast<double const *>( target_values.data() ) ),
+            (int64_t)target_values.extent( 0 ), (int64_t)target_values.stride( 0 ),
+            (int64_t)target_values.stride( 1 ), _stream ) );
+    }
+
+    void apply( DeviceView<double const> source_values, DeviceView<double> target_values ) const override
+    {
+        apply_values( source_values, target_values );
+    }
+
+    // apply(source_values, target_values) for any view type (Kokkos::View),
+    // rank 1 or rank 2 (the reference's fetch handles both).
+    template <typename SourceValues, typename TargetValues,
+              typename = std::enable_if_t<!std::is_same<SourceValues, DeviceView<double const>>::value>>
+    void apply( SourceValues const &source_values, TargetValues const &target_values ) const
+    {
+        apply_values( source_values, target_values );
+    }
+
+    dtk_nn_handle handle() const { return _handle.get(); }
+
+  private:
+    std::size_t _size, _n_target_points;
+    dtk_stream_t _stream;
+    std::shared_ptr<struct dtk_nn_s> _handle;
+};
+
+} // namespace DataTransferKit
+
+#endif

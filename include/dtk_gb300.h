@@ -173,6 +173,45 @@ dtk_status dtk_knn_search(const double *src, int64_t n_src,
                           int32_t k, int32_t *offset, int32_t *indices,
                           dtk_stream_t stream);
 
+/* ---- rank-2 (multi-component) fields ----
+ * apply for n x n_comp fields with (point, component) strides in elements:
+ * LayoutRight (component fastest): (n_comp, 1); LayoutLeft: (1, n).  Each
+ * component is the rank-1 apply of that column.  Extension: the reference's
+ * MLS apply takes rank-1 views (DTK_MovingLeastSquaresOperator_decl.hpp:52-54);
+ * its fetch handles rank 2 (DTK_DetailsNearestNeighborOperatorImpl.hpp:53-56,89-93). */
+dtk_status dtk_mls_apply_multi(dtk_mls_handle h, const double *source_values,
+                               int64_t n_source_values, int64_t n_comp,
+                               int64_t src_pt_stride, int64_t src_comp_stride,
+                               double *target_values, int64_t n_target_values,
+                               int64_t tgt_pt_stride, int64_t tgt_comp_stride,
+                               dtk_stream_t stream);
+
+/* ---- NearestNeighborOperator (DTK_NearestNeighborOperator_decl.hpp:27-49) ----
+ * create (DTK_NearestNeighborOperator_def.hpp:23-66): the nearest source of
+ * every target, (d^2, index) order (ties to the smaller source index);
+ * comm_size > 1 -> DTK_ERR_UNSUPPORTED; an empty source cloud ->
+ * DTK_ERR_INVALID_ARG (the reference's DTK_CHECK(!search_tree.empty())).
+ * apply (:68-81): target_values[i] = source_values[nearest(i)]; the
+ * DTK_REQUIREs on the extents -> DTK_ERR_INVALID_ARG.  Device pointers. */
+typedef struct dtk_nn_s *dtk_nn_handle;
+dtk_status dtk_nn_create(const double *src, int64_t n_src, int64_t src_pt_stride,
+                         int64_t src_dim_stride, const double *tgt, int64_t n_tgt,
+                         int64_t tgt_pt_stride, int64_t tgt_dim_stride,
+                         int32_t comm_size, dtk_stream_t stream, dtk_nn_handle *out);
+dtk_status dtk_nn_apply(dtk_nn_handle h, const double *source_values,
+                        int64_t n_source_values, double *target_values,
+                        int64_t n_target_values, dtk_stream_t stream);
+dtk_status dtk_nn_apply_multi(dtk_nn_handle h, const double *source_values,
+                              int64_t n_source_values, int64_t n_comp,
+                              int64_t src_pt_stride, int64_t src_comp_stride,
+                              double *target_values, int64_t n_target_values,
+                              int64_t tgt_pt_stride, int64_t tgt_comp_stride,
+                              dtk_stream_t stream);
+/* The nearest source index of every target (device array of n_targets). */
+dtk_status dtk_nn_get_indices(dtk_nn_handle h, const int32_t **indices,
+                              int64_t *n_targets);
+dtk_status dtk_nn_destroy(dtk_nn_handle h);
+
 /* ---- batched pseudo-inverse (the SVDFunctor kernel, DTK_DetailsSVDImpl.hpp:39-309) ----
  * count row-major n x n matrices -> their pseudo-inverses with DTK's
  * absolute DBL_EPSILON tolerances; *underdetermined (host) receives the

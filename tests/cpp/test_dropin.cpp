@@ -1,10 +1,14 @@
-// The reference's MLS operator tests, written against the header-only
-// drop-in (include/dtk/DTK_MovingLeastSquaresOperator.hpp) as a DTK user would:
+// The reference's MLS and nearest-neighbour operator tests, written against
+// the header-only drop-ins (include/dtk/DTK_MovingLeastSquaresOperator.hpp,
+// include/dtk/DTK_NearestNeighborOperator.hpp) as a DTK user would:
 //   tstMeshfreeOperators.cpp:130-376 (same_npoints_and_basis, grid, line)
 //   tstMeshfreeOperatorsSimpleProblem.cpp:113-147 (corner_cases)
-// plus a LayoutLeft input and the DTK_REQUIRE error convention.
+//   tstNearestNeighborOperator.cpp:85-273 (unique_source_point,
+//     structured_clouds, mixed_clouds) on one rank
+// plus a LayoutLeft input, a rank-2 field and the DTK_REQUIRE error convention.
 // Prints "PASS <n>" on success; exits non-zero on the first failure.
 #include <dtk/DTK_MovingLeastSquaresOperator.hpp>
+#include <dtk/DTK_NearestNeighborOperator.hpp>
 
 #include <cuda_runtime.h>
 
@@ -158,8 +162,107 @@ void run_basis()
     }
 }
 
+// makeStructuredCloud of the reference tests: (i Lx / nx, j Ly / ny, k Lz / nz) + offset
+std::vector<Pt> structured( double Lx, double Ly, double Lz, int nx, int ny, int nz )
+{
+    std::vector<Pt> c;
+    for ( int k = 0; k < nz; ++k )
+        for ( int j = 0; j < ny; ++j )
+            for ( int i = 0; i < nx; ++i )
+                c.push_back( {i * Lx / nx, j * Ly / ny, k * Lz / nz} );
+    return c;
+}
+
+void run_nearest()
+{
+    using NN = NearestNeighborOperator<CudaDevice>;
+    // unique_source_point: source at (comm_size, ...) = (1, 1, 1), target at the origin
+    {
+        std::vector<Pt> src = {{1, 1, 1}}, tgt = {{0, 0, 0}};
+        Buf bs( 3 ), bt( 3 ), bv( 1 ), bo( 1 );
+        NN op( 0, points( bs, src ), points( bt, tgt ) );
+        op.apply( values( bv, {255.0} ), out( bo ) );
+        CHECK( host( bo )[0] == 255.0 );
+    }
+    // structured_clouds: the target cloud is the source cloud
+    {
+        auto src = structured( 2., 3., 5., 7, 11, 13 );
+        Buf bs( 3 * src.size() ), bt( 3 * src.size() ), bv( src.size() ), bo( src.size() );
+        std::vector<double> sv;
+        for ( auto &p : src )
+            sv.push_back( p[0] );
+        NN op( 0, points( bs, src ), points( bt, src, true ) );
+        op.apply( values( bv, sv ), out( bo ) );
+        auto y = host( bo );
+        for ( std::size_t i = 0; i < src.size(); ++i )
+            CHECK( std::abs( y[i] - src[i][0] ) <= 1e-14 * std::abs( src[i][0] ) );
+    }
+    // mixed_clouds: random targets in the structured source box
+    {
+        double const Lx = 17., Ly = 19., Lz = 23.;
+        int const nx = 29;
+        auto src = structured( Lx, Ly, Lz, nx, 31, 37 );
+        std::mt19937_64 g( 0 );
+        std::uniform_real_distribution<double> u( 0., 1. );
+        std::vector<Pt> tgt;
+        for ( int i = 0; i < 41; ++i )
+            tgt.push_back( {Lx * u( g ), Ly * u( g ), Lz * u( g )} );
+        Buf bs( 3 * src.size() ), bt( 3 * tgt.size() ), bv( src.size() ), bo( tgt.size() );
+        std::vector<double> sv;
+        for ( auto &p : src )
+            sv.push_back( p[0] );
+        NN op( 0, points( bs, src ), points( bt, tgt ) );
+        op.apply( values( bv, sv ), out( bo ) );
+        auto y = host( bo );
+        for ( std::size_t i = 0; i < tgt.size(); ++i )
+        {
+            double ref = std::round( tgt[i][0] / Lx * nx ) * Lx / nx;
+            if ( ref == Lx )
+                ref -= Lx / nx;
+            CHECK( std::abs( y[i] - ref ) <= 1e-14 * std::abs( ref ) );
+        }
+    }
+    // rank-2 field (LayoutRight, 2 components) and the error convention
+    {
+        auto src = structured( 1., 1., 1., 4, 4, 4 );
+        Buf bs( 3 * src.size() ), bt( 3 * src.size() ), bv( 2 * src.size() ), bo( 2 * src.size() );
+        std::vector<double> sv;
+        for ( auto &p : src )
+        {
+            sv.push_back( p[0] );
+            sv.push_back( p[2] );
+        }
+        NN op( 0, points( bs, src ), points( bt, src ) );
+        cudaMemcpy( bv.d, sv.data(), sv.size() * 8, cudaMemcpyHostToDevice );
+        DeviceView<double const> in;
+        in.ptr = bv.d;
+        in.n0 = src.size();
+        in.n1 = 2;
+        in.s0 = 2;
+        DeviceView<double> o;
+        o.ptr = bo.d;
+        o.n0 = src.size();
+        o.n1 = 2;
+        o.s0 = 2;
+        op.apply( in, o );
+        CHECK( host( bo ) == sv );
+        bool threw = false;
+        try
+        {
+            in.n0 = src.size() - 1;
+            op.apply( in, o );
+        }
+        catch ( DataTransferKitException const & )
+        {
+            threw = true; // DTK_REQUIRE( _size == source_values.extent_int( 0 ) )
+        }
+        CHECK( threw );
+    }
+}
+
 int main()
 {
+    run_nearest();
     run_basis<MultivariatePolynomialBasis<Constant, 3>>();
     run_basis<MultivariatePolynomialBasis<Linear, 3>>();
     run_basis<MultivariatePolynomialBasis<Quadratic, 3>>();
