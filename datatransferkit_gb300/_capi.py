@@ -26,6 +26,7 @@ EXPORTED = [
     "dtk_mls_batch_get_csr", "dtk_mls_batch_destroy", "dtk_mls_batch_get_stage_times", "dtk_last_error", "dtk_status_string",
     "dtk_kernel_launch_count", "dtk_svd_pinv_noalloc", "dtk_mls_apply_multi", "dtk_nn_create",
     "dtk_nn_apply", "dtk_nn_apply_multi", "dtk_nn_get_indices", "dtk_nn_destroy",
+    "dtk_mls_export_size", "dtk_mls_export", "dtk_mls_import",
 ]
 
 
@@ -87,6 +88,9 @@ def _declare(L):
     L.dtk_nn_apply_multi.argtypes = L.dtk_mls_apply_multi.argtypes
     L.dtk_nn_get_indices.argtypes = [_vp, C.POINTER(_vp), C.POINTER(_i64)]
     L.dtk_nn_destroy.argtypes = [_vp]
+    L.dtk_mls_export_size.argtypes = [_vp, C.POINTER(_i64)]
+    L.dtk_mls_export.argtypes = [_vp, _vp, _i64, _vp]
+    L.dtk_mls_import.argtypes = [_vp, _i64, _vp, C.POINTER(_vp)]
     L.dtk_mls_batch_get_stage_times.argtypes = [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                                 C.POINTER(C.c_float)]
     L.dtk_last_error.restype = C.c_char_p

@@ -207,6 +207,36 @@ class MovingLeastSquaresOperator(PointCloudOperator):
             _stream(stream if stream is not None else self._stream)))
         return gv, gc
 
+    def to_bytes(self) -> bytes:
+        """The operator product (offset, indices, coefficients) as a byte string."""
+        n = C.c_int64()
+        check(lib().dtk_mls_export_size(self._h, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        check(lib().dtk_mls_export(self._h, buf, n.value, _stream(self._stream)))
+        return buf.raw
+
+    @classmethod
+    def from_bytes(cls, data: bytes, stream=None) -> "MovingLeastSquaresOperator":
+        """An operator whose apply uses a product written by ``to_bytes`` (no setup)."""
+        op = cls.__new__(cls)
+        op._h = C.c_void_p()
+        op._stream = stream
+        check(lib().dtk_mls_import(data, len(data), _stream(stream), C.byref(op._h)))
+        n_src, n_tgt = C.c_int64(), C.c_int64()
+        check(lib().dtk_mls_get_sizes(op._h, C.byref(n_src), C.byref(n_tgt), None))
+        op.n_source_points, op.n_target_points = n_src.value, n_tgt.value
+        op.polynomial_basis = op.radial_basis_function = op.options = None
+        return op
+
+    def save(self, path) -> None:
+        with open(path, "wb") as f:
+            f.write(self.to_bytes())
+
+    @classmethod
+    def load(cls, path, stream=None) -> "MovingLeastSquaresOperator":
+        with open(path, "rb") as f:
+            return cls.from_bytes(f.read(), stream)
+
     def csr(self):
         """(offset, indices, coefficients) device tensors (copies)."""
         off, idx, coeff = C.c_void_p(), C.c_void_p(), C.c_void_p()

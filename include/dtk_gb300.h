@@ -173,6 +173,22 @@ dtk_status dtk_knn_search(const double *src, int64_t n_src,
                           int32_t k, int32_t *offset, int32_t *indices,
                           dtk_stream_t stream);
 
+/* ---- the operator product on disk and on the wire (extension) ----
+ * The CSR that create produces (offset, source indices, coefficients, the
+ * members of DTK_MovingLeastSquaresOperator_decl.hpp:56-62) as a flat
+ * little-endian byte string with a header and a checksum (layout in
+ * csrc/dtk_io.cu), so that apply can be reused across restarts and shared
+ * with other processes.  export copies into a HOST buffer of
+ * dtk_mls_export_size bytes (synchronous); import validates a buffer
+ * (magic, version, sizes, offsets, index range, checksum: otherwise
+ * DTK_ERR_INVALID_ARG) and returns a handle whose apply and values-adjoint
+ * work as the original's (no coordinate adjoint: the points are not stored). */
+dtk_status dtk_mls_export_size(dtk_mls_handle h, int64_t *bytes);
+dtk_status dtk_mls_export(dtk_mls_handle h, void *host_buffer, int64_t bytes,
+                          dtk_stream_t stream);
+dtk_status dtk_mls_import(const void *host_buffer, int64_t bytes,
+                          dtk_stream_t stream, dtk_mls_handle *out);
+
 /* ---- rank-2 (multi-component) fields ----
  * apply for n x n_comp fields with (point, component) strides in elements:
  * LayoutRight (component fastest): (n_comp, 1); LayoutLeft: (1, n).  Each
