@@ -146,16 +146,39 @@ def fp64_form_flops(n_tgt, k, m, rotations):
     return rotations * per_rot + n_tgt * k * per_nb + n_tgt * (2 * m * m + m)
 
 
-def mixed_form_flops(n_tgt, k, m):
-    """Mixed form, FP64-pipe work only, in FLOP with an FMA as 2 and every
-    other FP64-pipe operation (add, multiply, FP32<->FP64 conversion) as 1.
-    Per neighbour: the centring in three passes 3 x 3 subtractions and
-    3 x 1 + 2 x 4 conversions (coordinates and weight); the FP64 residual
-    (quadratic basis products m - 4, dot 2m, weight product 1, update 2m);
-    the coefficient dot (m - 4 + 2m + 1) and its FP32 store 1.  Per target:
-    radius ~10, refinement conversions 3m."""
-    per_nb = 9 + 11 + (m - 4 + 4 * m + 1) + (m - 4 + 2 * m + 2)
-    return n_tgt * (k * per_nb + 10 + 3 * m)
+def mixed_form_fp32_ops(n_tgt, k, m):
+    """Mixed form (Cholesky path), FP32-pipe operations (an FMA counts as one
+    operation).  Per neighbour: the centring, three times 3 x 4; the moment
+    pass (basis m - 4, weight ~13, m products, m(m+1)/2 FMAs); the double-float
+    residual (basis TwoProds 2(m - 4), weight 13, compensated dot 12m, weight
+    product 3, update 12m); the double-float coefficient dot (2(m - 4) + 13 +
+    12m + 4).  Per target: Cholesky and triangular inverse ~m^3/3, the bound
+    m(m+1)/2, two preconditioner applications 2 m(m+1)."""
+    nu = m * (m + 1) // 2
+    per_nb = (36 + (m - 4 + 13 + m + nu) + (2 * (m - 4) + 13 + 24 * m + 3)
+              + (2 * (m - 4) + 13 + 12 * m + 4))
+    return n_tgt * (k * per_nb + m ** 3 // 3 + nu + 2 * m * (m + 1))
+
+
+def measure_fp32_peak(torch, dev):
+    """cuBLAS FP32 GEMM rate (no TF32): the FP32-pipe analogue of the measured bf16 peak."""
+    n = 8192
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    a = torch.rand(n, n, dtype=torch.float32, device=dev)
+    b = torch.rand(n, n, dtype=torch.float32, device=dev)
+    best = 0.0
+    for _ in range(4):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b
+    return best
 
 
 def measure_fp64_peak(torch, dev):
@@ -569,9 +592,10 @@ def run_ours(args, rank, world, local_rank):
     search_ms = float(np.mean([r[0][0] for r in rec_mixed]))
     query_ms = float(np.mean([r[4][1] for r in rec_mixed]))
     build_ms = float(np.mean([r[4][0] for r in rec_mixed]))
-    flops = mixed_form_flops(n_tgt, k, m)
-    achieved = flops / (setup_ms / 1e3) / 1e12
-    peak = measure_fp64_peak(torch, dev)
+    ops32 = mixed_form_fp32_ops(n_tgt, k, m)
+    achieved = ops32 / (setup_ms / 1e3) / 1e12          # Top/s, FMA = 1 operation
+    peak = measure_fp32_peak(torch, dev) / 2.0           # FMA operations/s of the SGEMM
+    peak64 = measure_fp64_peak(torch, dev)
     hbm, hbm_src = hbm_peak()
     traffic_pt = read_profile_traffic("setup_mixed_traffic.txt", "bytes_per_target")
     traffic_q = read_profile_traffic("knn_traffic.txt", "bytes_per_query")
@@ -603,7 +627,8 @@ def run_ours(args, rank, world, local_rank):
                    "l2_flush": "inputs larger than L2 (192 MB coordinates per cloud)"},
         "fp64_form": {"value": total_targets / (ms_fp64 / 1e3), "ms_per_step": ms_fp64,
                       "setup_ms": setup64_ms,
-                      "setup_fp64_tflops": flops64 / (setup64_ms / 1e3) / 1e12},
+                      "setup_fp64_tflops": flops64 / (setup64_ms / 1e3) / 1e12,
+                      "setup_fp64_frac_of_dgemm": flops64 / (setup64_ms / 1e3) / 1e12 / peak64},
         "mixed_over_fp64": ms_fp64 / ms_mixed,
         "rotations_per_target": {
             "mixed_fp32": float(np.mean([r[2] for r in rec_mixed])) / n_tgt,
@@ -623,9 +648,9 @@ def run_ours(args, rank, world, local_rank):
             "search_build_ms": build_ms,
             "query": {"bound": "hbm", "achieved": q_gbs, "peak": hbm, "unit": "GB/s",
                       "frac": q_gbs / hbm, "ms": query_ms},
-            "setup": {"bound": "fp64", "kernel": "k_setup_mixed<10>", "achieved": achieved,
-                      "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "ms": setup_ms,
-                      "peak_source": "measured cuBLAS DGEMM 4096^3 in this run",
+            "setup": {"bound": "fp32", "kernel": "k_setup_mixed<10>", "achieved": achieved,
+                      "peak": peak, "unit": "T FP32 ops/s (FMA = 1)", "frac": achieved / peak, "ms": setup_ms,
+                      "peak_source": "measured cuBLAS SGEMM 8192^3 (no TF32) in this run, FMA/s",
                       "traffic": (traffic_pt * n_tgt) if traffic_pt else None},
             "apply": {"bound": "hbm", "kernel": "k_apply_vec<8,1>", "achieved": a_gbs, "peak": hbm,
                       "unit": "GB/s", "frac": a_gbs / hbm, "ms": apply_ms},

@@ -112,14 +112,169 @@ __device__ __forceinline__ void refine_and_store( int len, int rbf, int steps, S
     }
 }
 
+// ---------------------------------------------------------------------------
+// Double-float arithmetic on the FP32 pipe (GB300's FP64 rate is 1/58 of its
+// FP32 rate): a value is an unevaluated sum hi + lo of two floats.  TwoSum
+// (Knuth) and TwoProd (with an FMA) are error-free; the dot products follow
+// the compensated "Dot2" scheme of Ogita, Rump and Oishi (2005): the rounding
+// errors of every product and partial sum are collected in a second float,
+// which gives the result as if computed in twice the working precision.
+// The explicit _rn intrinsics keep the compiler from contracting the
+// error-free steps into FMAs.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum( float a, float b, float &s, float &e )
+{
+    s = __fadd_rn( a, b );
+    float const bb = __fsub_rn( s, a );
+    e = __fadd_rn( __fsub_rn( a, __fsub_rn( s, bb ) ), __fsub_rn( b, bb ) );
+}
+
+__device__ __forceinline__ void two_prod( float a, float b, float &p, float &e )
+{
+    p = __fmul_rn( a, b );
+    e = __fmaf_rn( a, b, -p );
+}
+
+// Basis values of FP32 coordinates as double-floats (exact: the quadratic
+// products are TwoProds).
+template <int M>
+__device__ __forceinline__ void basis_df( float x, float y, float z, float *ph, float *pl )
+{
+    ph[0] = 1.f;
+    pl[0] = 0.f;
+    if constexpr ( M >= 4 )
+    {
+        ph[1] = x;
+        ph[2] = y;
+        ph[3] = z;
+        pl[1] = pl[2] = pl[3] = 0.f;
+    }
+    if constexpr ( M == 10 )
+    {
+        two_prod( x, x, ph[4], pl[4] );
+        two_prod( x, y, ph[5], pl[5] );
+        two_prod( x, z, ph[6], pl[6] );
+        two_prod( y, y, ph[7], pl[7] );
+        two_prod( y, z, ph[8], pl[8] );
+        two_prod( z, z, ph[9], pl[9] );
+    }
+}
+
+// P . a as (s, c) with s + c the compensated dot, a = ah + al
+template <int M>
+__device__ __forceinline__ void dot_df( float const *ph, float const *pl, float const *ah, float const *al,
+                                        float &s, float &c )
+{
+    s = 0.f;
+    c = 0.f;
+#pragma unroll
+    for ( int q = 0; q < M; ++q )
+    {
+        float p, e, t, f;
+        two_prod( ph[q], ah[q], p, e );
+        two_sum( s, p, t, f );
+        s = t;
+        c = __fadd_rn( c, __fadd_rn( e, f ) );
+        c = __fmaf_rn( ph[q], al[q], c );
+        c = __fmaf_rn( pl[q], ah[q], c );
+    }
+}
+
+// Refinement and coefficients of the fast path in double-float: a = ah + al
+// on entry (the FP32 solve, al = 0); r = e0 - sum_j phi_j P_j (P_j . a)
+// accumulated per component as rh + rl; a += M r; c_j = phi_j (P_j . a)
+// rounded once to FP32.
+template <int M, class Scaled, class Pinv>
+__device__ __forceinline__ void refine_and_store_df( int len, int rbf, int steps, Scaled const &scaled,
+                                                     Pinv const &pinv32, float *ah, float *al,
+                                                     float *coeff_row )
+{
+    for ( int step = 0; step < steps; ++step )
+    {
+        float rh[M], rl[M];
+#pragma unroll
+        for ( int q = 0; q < M; ++q )
+        {
+            rh[q] = q == 0 ? 1.f : 0.f;
+            rl[q] = 0.f;
+        }
+        for ( int j = 0; j < len; ++j )
+        {
+            float x, y, z;
+            scaled( j, x, y, z );
+            float ph[M], pl[M];
+            basis_df<M>( x, y, z, ph, pl );
+            float const phi = weight32( rbf, x, y, z );
+            float s, c;
+            dot_df<M>( ph, pl, ah, al, s, c );
+            float wh, wl;
+            two_prod( phi, s, wh, wl );
+            wl = __fmaf_rn( phi, c, wl );
+#pragma unroll
+            for ( int q = 0; q < M; ++q )
+            {
+                float p, e, t, f;
+                two_prod( wh, ph[q], p, e );
+                e = __fmaf_rn( wh, pl[q], e );
+                e = __fmaf_rn( wl, ph[q], e );
+                two_sum( rh[q], -p, t, f );
+                rh[q] = t;
+                rl[q] = __fadd_rn( rl[q], __fsub_rn( f, e ) );
+            }
+        }
+        float rf[M], d[M];
+#pragma unroll
+        for ( int q = 0; q < M; ++q )
+            rf[q] = __fadd_rn( rh[q], rl[q] );
+        pinv32( rf, d );
+#pragma unroll
+        for ( int q = 0; q < M; ++q )
+        {
+            float t, f;
+            two_sum( ah[q], d[q], t, f );
+            ah[q] = t;
+            al[q] = __fadd_rn( al[q], f );
+        }
+    }
+    for ( int j = 0; j < len; ++j )
+    {
+        float x, y, z;
+        scaled( j, x, y, z );
+        float ph[M], pl[M];
+        basis_df<M>( x, y, z, ph, pl );
+        float const phi = weight32( rbf, x, y, z );
+        float s, c;
+        dot_df<M>( ph, pl, ah, al, s, c );
+        float wh, wl;
+        two_prod( phi, s, wh, wl );
+        coeff_row[j] = __fadd_rn( wh, __fmaf_rn( phi, c, wl ) );
+    }
+}
+
+// Sources as double-floats: hi = fl32(v), lo = fl32(v - hi), (hi, lo) per
+// coordinate, 3 float2 per point in the caller's point order.
+__global__ void k_split_points( PointsView p, float2 *out )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i >= p.n )
+        return;
+#pragma unroll
+    for ( int d = 0; d < 3; ++d )
+    {
+        double const v = p( i, d );
+        float const hi = __double2float_rn( v );
+        out[3 * i + d] = make_float2( hi, __double2float_rn( v - (double)hi ) );
+    }
+}
+
 // Fast path: FP32 Cholesky preconditioner in registers; targets it cannot
 // take (factorization fails, or the condition bound exceeds 2^20) are
 // appended to `list` for k_setup_mixed_eig.
 template <int M>
 __global__ void __launch_bounds__( 128 )
-    k_setup_mixed( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
-                   uint32_t const *order, int64_t n_tgt, int rbf, bool rows_sorted, float *coeff,
-                   int32_t *list, unsigned *count, unsigned *status )
+    k_setup_mixed( PointsView src, float2 const *__restrict__ split, PointsView tgt, int32_t const *offset,
+                   int32_t const *idx, uint32_t const *order, int64_t n_tgt, int rbf, bool rows_sorted,
+                   float *coeff, int32_t *list, unsigned *count, unsigned *status )
 {
     constexpr int NU = M * ( M + 1 ) / 2;
     int64_t const g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -146,11 +301,24 @@ __global__ void __launch_bounds__( 128 )
     if ( dmax > distance )
         distance = dmax;
     float const inv_r = (float)( 1.0 / ( 1.1 * distance ) );
+    // the target as double-floats; x^ = ((sh - th) + (sl - tl)) / r in FP32
+    // (sh - th is exact for nearby points, Sterbenz)
+    float th[3], tl[3];
+    {
+        double const t3[3] = {tx, ty, tz};
+#pragma unroll
+        for ( int d = 0; d < 3; ++d )
+        {
+            th[d] = __double2float_rn( t3[d] );
+            tl[d] = __double2float_rn( t3[d] - (double)th[d] );
+        }
+    }
     auto scaled = [&]( int j, float &x, float &y, float &z ) {
         int64_t const sj = idx[b + j];
-        x = __fmul_rn( (float)( src( sj, 0 ) - tx ), inv_r );
-        y = __fmul_rn( (float)( src( sj, 1 ) - ty ), inv_r );
-        z = __fmul_rn( (float)( src( sj, 2 ) - tz ), inv_r );
+        float2 const a0 = __ldg( split + 3 * sj ), a1 = __ldg( split + 3 * sj + 1 ), a2 = __ldg( split + 3 * sj + 2 );
+        x = __fmul_rn( __fadd_rn( __fsub_rn( a0.x, th[0] ), __fsub_rn( a0.y, tl[0] ) ), inv_r );
+        y = __fmul_rn( __fadd_rn( __fsub_rn( a1.x, th[1] ), __fsub_rn( a1.y, tl[1] ) ), inv_r );
+        z = __fmul_rn( __fadd_rn( __fsub_rn( a2.x, th[2] ), __fsub_rn( a2.y, tl[2] ) ), inv_r );
     };
 
     // FP32 moments, upper triangle R(a, c) = A[ut(a, c)], a <= c
@@ -253,18 +421,18 @@ __global__ void __launch_bounds__( 128 )
             y[r] = acc;
         }
     };
-    double a[M];
+    float ah[M], al[M];
     {
-        float e0[M], y[M];
+        float e0[M];
 #pragma unroll
         for ( int r = 0; r < M; ++r )
+        {
             e0[r] = r == 0 ? 1.f : 0.f;
-        pinv32( e0, y );
-#pragma unroll
-        for ( int r = 0; r < M; ++r )
-            a[r] = (double)y[r];
+            al[r] = 0.f;
+        }
+        pinv32( e0, ah );
     }
-    refine_and_store<M>( len, rbf, crit <= 65536.f ? 1 : 2, scaled, pinv32, a, coeff + b );
+    refine_and_store_df<M>( len, rbf, crit <= 65536.f ? 1 : 2, scaled, pinv32, ah, al, coeff + b );
 }
 
 // Jacobi path over the targets the fast path listed: list[0 .. *count),
@@ -486,9 +654,12 @@ void launch_mixed( SetupArgs const &a, cudaStream_t s )
     DeviceBuffer<int32_t> list( a.n_tgt, s );
     DeviceBuffer<unsigned> count( 1, s );
     DTK_CUDA_OR_THROW( cudaMemsetAsync( count.get(), 0, sizeof( unsigned ), s ) );
+    DeviceBuffer<float2> split( 3 * a.src.n, s );
+    k_split_points<<<(unsigned)( ( a.src.n + 255 ) / 256 ), 256, 0, s>>>( a.src, split.get() );
+    check_launch( "k_split_points" );
     k_setup_mixed<M><<<(unsigned)( ( a.n_tgt + 127 ) / 128 ), 128, 0, s>>>(
-        a.src, a.tgt, a.offset, a.idx, a.order, a.n_tgt, a.rbf, a.rows_sorted, a.coeff32, list.get(),
-        count.get(), a.status );
+        a.src, split.get(), a.tgt, a.offset, a.idx, a.order, a.n_tgt, a.rbf, a.rows_sorted, a.coeff32,
+        list.get(), count.get(), a.status );
     check_launch( "k_setup_mixed" );
     // the listed targets (count known only on the device): persistent blocks
     size_t const smem = ( (size_t)M * ( M + 1 ) / 2 + (size_t)M * M ) * sizeof( float ) * MB;
