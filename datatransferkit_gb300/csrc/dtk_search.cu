@@ -35,6 +35,7 @@ namespace
 constexpr int LEAF = 32;
 constexpr int STACK = 192; // wide-node stack entries per warp (7 per level along the path)
 constexpr int Q_WARPS = 4; // warps per block in the query kernels
+constexpr int Q_SEQ = 8;   // consecutive kNN queries per warp (each seeds the next)
 constexpr unsigned FULL = 0xffffffffu;
 constexpr unsigned long long KEY_INF = 0xffffffffffffffffull;
 
@@ -699,7 +700,7 @@ __device__ __forceinline__ void d2_bounds( TreeView const &tr, Query const &q, i
 constexpr int QUEUE = 64;
 
 template <bool GROUPED>
-__global__ void __launch_bounds__( Q_WARPS * 32 )
+__global__ void __launch_bounds__( Q_WARPS * 32, 8 )
     k_knn( TreeView tr, PointsView tgt, uint32_t const *order, int k_all, GroupView gv,
            int32_t const *offset, int32_t *idx_out, unsigned *status )
 {
@@ -707,37 +708,67 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     __shared__ float s_lb[Q_WARPS][STACK];
     __shared__ int s_queue[Q_WARPS][QUEUE];
     int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    int64_t const w = blockIdx.x * (int64_t)Q_WARPS + wib;
-    if ( w >= tgt.n )
+    int64_t const w0 = ( blockIdx.x * (int64_t)Q_WARPS + wib ) * Q_SEQ;
+    if ( w0 >= tgt.n )
         return;
+    unsigned const lt_mask = ( 1u << lane ) - 1u;
+    // the list of the previous query (its sorted positions kp and indices ki)
+    // seeds the next one: Morton-consecutive queries share most neighbours
+    int prev_g = -1, prev_row = 0;
+    unsigned long long kd = KEY_INF;
+    int ki = 0x7fffffff, kp = -1;
+    for ( int64_t w = w0; w < w0 + Q_SEQ && w < tgt.n; ++w )
+    {
     int64_t const qi = order ? (int64_t)order[w] : w;
     Range const rg = query_range<GROUPED>( tr, gv, qi );
     int64_t const ng = rg.pe - rg.ps;
     int const k = GROUPED ? gv.k[rg.g] : k_all;
     int const row = (int)( k < ng ? k : ng );
     if ( row <= 0 )
-        return;
-    Query const q = make_query( tr, tgt, qi );
-    unsigned const lt_mask = ( 1u << lane ) - 1u;
-
-    // Initial candidates: the 32 Morton-sorted sources of the query's
-    // problem around the target's code, with exact keys.
-    uint32_t const code = morton3( q.tx, q.ty, q.tz, tr.scene );
-    int64_t const pos = rg.ps + warp_lower_bound( tr.codes + rg.ps, ng, code, lane );
-    int64_t const W = ng < 32 ? ng : (int64_t)32;
-    int64_t s0 = pos - 16;
-    if ( s0 > rg.pe - W )
-        s0 = rg.pe - W;
-    if ( s0 < rg.ps )
-        s0 = rg.ps;
-    unsigned long long kd = KEY_INF;
-    int ki = 0x7fffffff;
-    if ( lane < W )
     {
-        int64_t const p = s0 + lane;
-        kd = (unsigned long long)__double_as_longlong(
-            dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), q.tx, q.ty, q.tz ) );
-        ki = (int)__ldg( tr.perm + p );
+        prev_row = 0;
+        continue;
+    }
+    Query const q = make_query( tr, tgt, qi );
+    bool const seeded = prev_row == row && ( !GROUPED || prev_g == rg.g );
+
+    if ( seeded )
+    {
+        // the previous list with exact keys for this query (lanes past the
+        // row hold entries that insertions shifted out: cleared)
+        if ( lane < row )
+            kd = (unsigned long long)__double_as_longlong(
+                dist2_rn( __ldg( tr.sx + kp ), __ldg( tr.sy + kp ), __ldg( tr.sz + kp ), q.tx, q.ty, q.tz ) );
+        else
+        {
+            kd = KEY_INF;
+            ki = 0x7fffffff;
+            kp = -1;
+        }
+    }
+    else
+    {
+        // the 32 Morton-sorted sources of the query's problem around the
+        // target's code, with exact keys
+        uint32_t const code = morton3( q.tx, q.ty, q.tz, tr.scene );
+        int64_t const pos = rg.ps + warp_lower_bound( tr.codes + rg.ps, ng, code, lane );
+        int64_t const W = ng < 32 ? ng : (int64_t)32;
+        int64_t s0 = pos - 16;
+        if ( s0 > rg.pe - W )
+            s0 = rg.pe - W;
+        if ( s0 < rg.ps )
+            s0 = rg.ps;
+        kd = KEY_INF;
+        ki = 0x7fffffff;
+        kp = -1;
+        if ( lane < W )
+        {
+            int64_t const p = s0 + lane;
+            kd = (unsigned long long)__double_as_longlong(
+                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), q.tx, q.ty, q.tz ) );
+            ki = (int)__ldg( tr.perm + p );
+            kp = (int)p;
+        }
     }
     // Bitonic sort of the 32 keys across lanes (ascending).
 #pragma unroll
@@ -747,6 +778,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
         {
             unsigned long long const od = __shfl_xor_sync( FULL, kd, stride );
             int const oi = __shfl_xor_sync( FULL, ki, stride );
+            int const op = __shfl_xor_sync( FULL, kp, stride );
             bool const up = ( lane & size ) == 0 || size == 32;
             bool const lower = ( lane & stride ) == 0;
             bool const mine_less = key_less( kd, ki, od, oi );
@@ -755,12 +787,14 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
             {
                 kd = od;
                 ki = oi;
+                kp = op;
             }
         }
     if ( lane >= k )
     {
         kd = KEY_INF;
         ki = 0x7fffffff;
+        kp = -1;
     }
     unsigned long long bd = __shfl_sync( FULL, kd, k - 1 );
     int bi = __shfl_sync( FULL, ki, k - 1 );
@@ -775,6 +809,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
         int ci = 0x7fffffff;
         if ( p >= 0 )
         {
+            // (a point already in the list is rejected at insertion)
             cd = (unsigned long long)__double_as_longlong(
                 dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), q.tx, q.ty, q.tz ) );
             ci = (int)__ldg( tr.perm + p );
@@ -788,19 +823,25 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
             int const ni = __shfl_sync( FULL, ci, src_lane );
             if ( !key_less( nd, ni, bd, bi ) )
                 continue;
+            if ( __ballot_sync( FULL, ki == ni ) ) // already in the list
+                continue;
+            int const np = __shfl_sync( FULL, p, src_lane );
             unsigned const gt = __ballot_sync( FULL, key_less( nd, ni, kd, ki ) );
             int const at = __ffs( gt ) - 1;
             unsigned long long const ud = __shfl_up_sync( FULL, kd, 1 );
             int const ui = __shfl_up_sync( FULL, ki, 1 );
+            int const up = __shfl_up_sync( FULL, kp, 1 );
             if ( lane > at )
             {
                 kd = ud;
                 ki = ui;
+                kp = up;
             }
             else if ( lane == at )
             {
                 kd = nd;
                 ki = ni;
+                kp = np;
             }
             bd = __shfl_sync( FULL, kd, k - 1 );
             bi = __shfl_sync( FULL, ki, k - 1 );
@@ -821,7 +862,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     auto process_leaf = [&]( int leaf ) {
         int64_t const p = (int64_t)leaf * LEAF + lane;
         bool surv = false;
-        if ( ( GROUPED ? p >= rg.ps : true ) && p < rg.pe && !( p >= s0 && p < s0 + W ) )
+        if ( ( GROUPED ? p >= rg.ps : true ) && p < rg.pe )
         {
             float lo, hi;
             d2_bounds( tr, q, p, lo, hi );
@@ -925,6 +966,10 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
         flush( qn );
     if ( lane < row )
         idx_out[offset[qi] + lane] = ki;
+    prev_g = rg.g;
+    prev_row = row;
+    __syncwarp();
+    }
 }
 
 // Radius traversal shared by the count and fill passes.  FILL=false counts
@@ -1174,11 +1219,11 @@ void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
         return;
     GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
     if ( groups.tgt_grp )
-        k_knn<true><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, k, gv,
-                                                                            offset, idx, status );
+        k_knn<true><<<blocks_for( ( tgt.n + Q_SEQ - 1 ) / Q_SEQ, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
+            view_of( tree ), tgt, order, k, gv, offset, idx, status );
     else
-        k_knn<false><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, k, gv,
-                                                                             offset, idx, status );
+        k_knn<false><<<blocks_for( ( tgt.n + Q_SEQ - 1 ) / Q_SEQ, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
+            view_of( tree ), tgt, order, k, gv, offset, idx, status );
     check_launch( "k_knn" );
 }
 
