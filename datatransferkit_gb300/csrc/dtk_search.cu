@@ -707,6 +707,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
     __shared__ int s_stack[Q_WARPS][STACK];
     __shared__ float s_lb[Q_WARPS][STACK];
     __shared__ int s_queue[Q_WARPS][QUEUE];
+    __shared__ int s_hash[Q_WARPS][64];
     int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     int64_t const w0 = ( blockIdx.x * (int64_t)Q_WARPS + wib ) * Q_SEQ;
     if ( w0 >= tgt.n )
@@ -801,47 +802,113 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
     float bound_f = prune_threshold( bd );
     int qn = 0; // queued survivors (warp-uniform)
 
-    // Exact FP64 keys for up to 32 queued sources, inserted into the list.
+    // Exact FP64 keys for up to 32 queued sources, merged into the list as a
+    // batch: the candidates below the bound that are not in the list already
+    // (a 64-slot hash of the list's indices) are sorted (bitonic) and merged
+    // with the list (elementwise minimum against the reversed candidates, then
+    // a bitonic clean), keeping the k smallest (d2, index).
     auto flush = [&]( int count ) {
         int const p = lane < count ? s_queue[wib][lane] : -1;
         __syncwarp();
         unsigned long long cd = KEY_INF;
-        int ci = 0x7fffffff;
+        int ci = 0x7fffffff, cp = -1;
         if ( p >= 0 )
         {
-            // (a point already in the list is rejected at insertion)
             cd = (unsigned long long)__double_as_longlong(
                 dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), q.tx, q.ty, q.tz ) );
             ci = (int)__ldg( tr.perm + p );
+            cp = p;
         }
-        unsigned cand = __ballot_sync( FULL, key_less( cd, ci, bd, bi ) );
-        while ( cand )
+        bool live = key_less( cd, ci, bd, bi );
+        if ( __ballot_sync( FULL, live ) )
         {
-            int const src_lane = __ffs( cand ) - 1;
-            cand &= cand - 1;
-            unsigned long long const nd = __shfl_sync( FULL, cd, src_lane );
-            int const ni = __shfl_sync( FULL, ci, src_lane );
-            if ( !key_less( nd, ni, bd, bi ) )
-                continue;
-            if ( __ballot_sync( FULL, ki == ni ) ) // already in the list
-                continue;
-            int const np = __shfl_sync( FULL, p, src_lane );
-            unsigned const gt = __ballot_sync( FULL, key_less( nd, ni, kd, ki ) );
-            int const at = __ffs( gt ) - 1;
-            unsigned long long const ud = __shfl_up_sync( FULL, kd, 1 );
-            int const ui = __shfl_up_sync( FULL, ki, 1 );
-            int const up = __shfl_up_sync( FULL, kp, 1 );
-            if ( lane > at )
+            int *hash = s_hash[wib];
+            hash[lane] = -1;
+            hash[lane + 32] = -1;
+            __syncwarp();
+            auto slot = []( int v ) { return (int)( ( (unsigned)v * 2654435761u ) >> 26 ); };
+            if ( ki != 0x7fffffff )
             {
-                kd = ud;
-                ki = ui;
-                kp = up;
+                int h = slot( ki );
+                for ( int t = 0; t < 64; ++t, h = ( h + 1 ) & 63 )
+                {
+                    int const old = atomicCAS( hash + h, -1, ki );
+                    if ( old == -1 || old == ki )
+                        break;
+                }
             }
-            else if ( lane == at )
+            __syncwarp();
+            if ( live )
             {
-                kd = nd;
-                ki = ni;
-                kp = np;
+                int h = slot( ci );
+                for ( int t = 0; t < 64; ++t, h = ( h + 1 ) & 63 )
+                {
+                    int const v = hash[h];
+                    if ( v == ci )
+                        live = false; // already in the list
+                    if ( v == ci || v == -1 )
+                        break;
+                }
+            }
+            __syncwarp();
+            if ( !live )
+            {
+                cd = KEY_INF;
+                ci = 0x7fffffff;
+                cp = -1;
+            }
+            // candidates ascending
+#pragma unroll
+            for ( int size = 2; size <= 32; size <<= 1 )
+#pragma unroll
+                for ( int stride = size >> 1; stride > 0; stride >>= 1 )
+                {
+                    unsigned long long const od = __shfl_xor_sync( FULL, cd, stride );
+                    int const oi = __shfl_xor_sync( FULL, ci, stride );
+                    int const op = __shfl_xor_sync( FULL, cp, stride );
+                    bool const up = ( lane & size ) == 0 || size == 32;
+                    bool const lower = ( lane & stride ) == 0;
+                    bool const mine_less = key_less( cd, ci, od, oi );
+                    if ( ( lower == up ) ? !mine_less : mine_less )
+                    {
+                        cd = od;
+                        ci = oi;
+                        cp = op;
+                    }
+                }
+            // the list (ascending) against the reversed candidates: the 32
+            // smallest as a bitonic sequence, then sorted
+            {
+                unsigned long long const rd = __shfl_sync( FULL, cd, 31 - lane );
+                int const ri = __shfl_sync( FULL, ci, 31 - lane );
+                int const rp = __shfl_sync( FULL, cp, 31 - lane );
+                if ( key_less( rd, ri, kd, ki ) )
+                {
+                    kd = rd;
+                    ki = ri;
+                    kp = rp;
+                }
+            }
+#pragma unroll
+            for ( int stride = 16; stride > 0; stride >>= 1 )
+            {
+                unsigned long long const od = __shfl_xor_sync( FULL, kd, stride );
+                int const oi = __shfl_xor_sync( FULL, ki, stride );
+                int const op = __shfl_xor_sync( FULL, kp, stride );
+                bool const lower = ( lane & stride ) == 0;
+                bool const mine_less = key_less( kd, ki, od, oi );
+                if ( lower ? !mine_less : mine_less )
+                {
+                    kd = od;
+                    ki = oi;
+                    kp = op;
+                }
+            }
+            if ( lane >= k )
+            {
+                kd = KEY_INF;
+                ki = 0x7fffffff;
+                kp = -1;
             }
             bd = __shfl_sync( FULL, kd, k - 1 );
             bi = __shfl_sync( FULL, ki, k - 1 );
@@ -910,14 +977,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
                 ok = ref != WIDE_EMPTY && ( GROUPED ? !( rhi < rg.lps || rlo > rg.lpe ) : true );
             }
             bool const cand = ok && lb <= bound_f;
-            // order of the candidates by (lb, slot)
-            unsigned less = 0;
-#pragma unroll
-            for ( int o = 0; o < WIDE; ++o )
-            {
-                float const lo_ = __shfl_sync( FULL, lb, o );
-                less |= ( lo_ < lb || ( lo_ == lb && o < lane ) ? 1u : 0u ) << o;
-            }
+            // slot order: with a seeded bound close to the final one the
+            // visit order changes little of what is pruned
             unsigned const ml = __ballot_sync( FULL, cand && ref < 0 );
             unsigned const mi = __ballot_sync( FULL, cand && ref >= 0 );
             int const n_int = __popc( mi );
@@ -925,7 +986,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
             {
                 if ( cand && ref >= 0 )
                 {
-                    int const pos = sp + n_int - 1 - __popc( mi & less );
+                    int const pos = sp + __popc( mi & lt_mask );
                     s_stack[wib][pos] = ref;
                     s_lb[wib][pos] = lb;
                 }
@@ -934,11 +995,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
             else if ( lane == 0 )
                 atomicOr( status, DEV_STACK_OVERFLOW );
             __syncwarp();
-            int const n_leaf = __popc( ml );
-            for ( int r = 0; r < n_leaf; ++r )
+            for ( unsigned m = ml; m; m &= m - 1 )
             {
-                unsigned const sel = __ballot_sync( FULL, ( ( ml >> lane ) & 1u ) && __popc( ml & less ) == r );
-                int const from = __ffs( sel ) - 1;
+                int const from = __ffs( m ) - 1;
                 float const lbr = __shfl_sync( FULL, lb, from );
                 int const lref = __shfl_sync( FULL, ref, from );
                 if ( lbr <= bound_f )
