@@ -707,7 +707,6 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
     __shared__ int s_stack[Q_WARPS][STACK];
     __shared__ float s_lb[Q_WARPS][STACK];
     __shared__ int s_queue[Q_WARPS][QUEUE];
-    __shared__ int s_hash[Q_WARPS][64];
     int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     int64_t const w0 = ( blockIdx.x * (int64_t)Q_WARPS + wib ) * Q_SEQ;
     if ( w0 >= tgt.n )
@@ -797,16 +796,19 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
         ki = 0x7fffffff;
         kp = -1;
     }
+    // the list's starting members by leaf and lane: a leaf screens them out
+    int const seed_leaf = kp >= 0 ? kp / LEAF : -1;
+    unsigned const seed_bit = kp >= 0 ? 1u << ( kp % LEAF ) : 0u;
     unsigned long long bd = __shfl_sync( FULL, kd, k - 1 );
     int bi = __shfl_sync( FULL, ki, k - 1 );
     float bound_f = prune_threshold( bd );
     int qn = 0; // queued survivors (warp-uniform)
 
     // Exact FP64 keys for up to 32 queued sources, merged into the list as a
-    // batch: the candidates below the bound that are not in the list already
-    // (a 64-slot hash of the list's indices) are sorted (bitonic) and merged
+    // batch: the candidates below the bound are sorted (bitonic) and merged
     // with the list (elementwise minimum against the reversed candidates, then
-    // a bitonic clean), keeping the k smallest (d2, index).
+    // a bitonic clean), keeping the k smallest (d2, index).  No candidate is
+    // in the list already: the list's starting members are screened out.
     auto flush = [&]( int count ) {
         int const p = lane < count ? s_queue[wib][lane] : -1;
         __syncwarp();
@@ -822,35 +824,6 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
         bool live = key_less( cd, ci, bd, bi );
         if ( __ballot_sync( FULL, live ) )
         {
-            int *hash = s_hash[wib];
-            hash[lane] = -1;
-            hash[lane + 32] = -1;
-            __syncwarp();
-            auto slot = []( int v ) { return (int)( ( (unsigned)v * 2654435761u ) >> 26 ); };
-            if ( ki != 0x7fffffff )
-            {
-                int h = slot( ki );
-                for ( int t = 0; t < 64; ++t, h = ( h + 1 ) & 63 )
-                {
-                    int const old = atomicCAS( hash + h, -1, ki );
-                    if ( old == -1 || old == ki )
-                        break;
-                }
-            }
-            __syncwarp();
-            if ( live )
-            {
-                int h = slot( ci );
-                for ( int t = 0; t < 64; ++t, h = ( h + 1 ) & 63 )
-                {
-                    int const v = hash[h];
-                    if ( v == ci )
-                        live = false; // already in the list
-                    if ( v == ci || v == -1 )
-                        break;
-                }
-            }
-            __syncwarp();
             if ( !live )
             {
                 cd = KEY_INF;
@@ -929,7 +902,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
     auto process_leaf = [&]( int leaf ) {
         int64_t const p = (int64_t)leaf * LEAF + lane;
         bool surv = false;
-        if ( ( GROUPED ? p >= rg.ps : true ) && p < rg.pe )
+        unsigned const seen = __reduce_or_sync( FULL, seed_leaf == leaf ? seed_bit : 0u );
+        if ( ( GROUPED ? p >= rg.ps : true ) && p < rg.pe && !( ( seen >> lane ) & 1u ) )
         {
             float lo, hi;
             d2_bounds( tr, q, p, lo, hi );
