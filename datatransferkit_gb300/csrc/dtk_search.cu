@@ -4,20 +4,27 @@
 // (packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:114-129).
 //
 // Build: scene box -> 30-bit Morton codes -> stable radix sort (codes, ids)
-// -> Morton-sorted FP64 coordinates (SoA) -> leaf buckets of 32 consecutive
-// points -> Karras (2012) binary radix tree over the leaf keys (first code of
-// each leaf, ties broken by leaf index) -> bottom-up refit with atomic flags.
-// Boxes are FP32, rounded outward, stored as both children's boxes inside
-// the parent (64 B per internal node), so one node fetch tests two children.
+// -> Morton-sorted FP64 coordinates (SoA, plus FP32 copies centred on the
+// scene) -> leaf buckets of 32 consecutive points -> Karras (2012) binary
+// radix tree over the leaf keys (first code of each leaf, ties broken by leaf
+// index) -> bottom-up refit of FP32 boxes rounded outward -> collapse into an
+// 8-wide BVH (three binary levels per wide node), so that 8 lanes test the 8
+// children of a node at once.
 //
-// Query: one warp per target, targets in Morton order.  kNN keeps the k best
-// (d2, index) keys distributed one per lane (sorted across lanes).  The
-// initial bound comes from the 32 Morton-sorted sources around the target's
-// code (a valid upper bound on the k-th distance); traversal is near-first
-// with a per-warp shared-memory stack; a box is pruned only when its FP32
-// round-down lower bound exceeds the round-up bound with a 2^-20 relative
-// margin, so no point whose FP64 distance could tie or beat the bound is
-// skipped.  Distances of points are exact FP64 with separately rounded
+// kNN query: a warp runs 16 Morton-consecutive targets one after the other;
+// the k best (d2, index) keys sit one per lane, sorted across lanes.  The
+// first target of a warp starts from the 32 Morton-sorted sources around its
+// code, every later one from the previous target's final list re-keyed for
+// it (neighbouring targets share most neighbours, so the starting bound is
+// close to the final one).  The starting members are screened out of their
+// leaves (a warp OR-reduction of a per-leaf lane mask), so no source enters
+// the list twice.  A box is pruned only when its FP32 round-down lower bound
+// exceeds the round-up bound with a 2^-20 relative margin, and a leaf point
+// only when its FP32 lower bound (with a rigorous rounding bound) does, so no
+// point whose FP64 distance could tie or beat the bound is skipped.  The
+// survivors get exact FP64 keys 32 at a time and are merged into the list as
+// a batch (bitonic sort, merge against the reversed candidates, bitonic
+// clean).  Distances of points are exact FP64 with separately rounded
 // operations: (dx*dx + dy*dy) + dz*dz.  Keys compare as integers (d2 >= 0,
 // so its IEEE bits are monotone), lexicographic with the source index.
 #include "dtk_common.cuh"
@@ -35,7 +42,7 @@ namespace
 constexpr int LEAF = 32;
 constexpr int STACK = 192; // wide-node stack entries per warp (7 per level along the path)
 constexpr int Q_WARPS = 4; // warps per block in the query kernels
-constexpr int Q_SEQ = 8;   // consecutive kNN queries per warp (each seeds the next)
+constexpr int Q_SEQ = 16;  // consecutive kNN queries per warp (each seeds the next)
 constexpr unsigned FULL = 0xffffffffu;
 constexpr unsigned long long KEY_INF = 0xffffffffffffffffull;
 
