@@ -131,3 +131,25 @@ def test_mixed_coefficients_are_fp32():
     assert coeff.dtype == torch.float32
     # no FP64 rotations; FP32 Jacobi rotations only for targets the Cholesky path hands over
     assert op.rotations == 0 and op.rotations_fp32 >= 0
+
+
+def test_cholesky_and_jacobi_paths_in_one_operator():
+    """Targets over a full 3-D cloud take the Cholesky path; targets whose 32
+    neighbours all lie in the plane z = 0.5 have rank-deficient quadratic
+    moments and are handed to the Jacobi path (truncation).  The first match
+    the oracle to the mixed tolerance; the second still reproduce a quadratic
+    in the plane (the truncated pseudo-inverse keeps the in-plane monomials)."""
+    rng = np.random.default_rng(17)
+    cloud = 0.1 * rng.random((20000, 3))                                    # [0, 0.1]^3
+    plane = np.column_stack([0.5 + 0.1 * rng.random((20000, 2)), np.full(20000, 0.5)])
+    src = np.vstack([cloud, plane])
+    t_cloud = 0.02 + 0.06 * rng.random((500, 3))
+    t_plane = np.column_stack([0.52 + 0.06 * rng.random((500, 2)), np.full(500, 0.5)])
+    tgt = np.vstack([t_cloud, t_plane])
+    f = lambda p: 2 + 3 * p[:, 0] - 5 * p[:, 1] + 4 * p[:, 0] * p[:, 1] + p[:, 1] ** 2
+    y, op = transfer(src, tgt, f(src), RBF[2], Q, k=32)
+    assert op.rotations_fp32 > 0                  # the Jacobi path ran
+    assert op.underdetermined == len(t_plane)     # exactly the planar targets were truncated
+    ref = cpu.mls_transfer(src, t_cloud, f(src), 2, 2, k=32)
+    assert rel_l2(y[:len(t_cloud)], ref["target"]) <= MIXED_TOL
+    np.testing.assert_allclose(y[len(t_cloud):], f(t_plane), rtol=1e-5)
