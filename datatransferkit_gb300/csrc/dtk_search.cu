@@ -40,7 +40,9 @@ namespace
 {
 
 constexpr int LEAF = 32;
-constexpr int STACK = 192; // wide-node stack entries per warp (7 per level along the path)
+constexpr int STACK = 256; // wide-node stack entries per warp
+constexpr int NODE_GROUPS = 4; // wide nodes a kNN warp tests per step (8 lanes each)
+static_assert( NODE_GROUPS * 8 == 32, "one lane per child slot" );
 constexpr int Q_WARPS = 4; // warps per block in the query kernels
 constexpr int Q_SEQ = 16;  // consecutive kNN queries per warp (each seeds the next)
 constexpr unsigned FULL = 0xffffffffu;
@@ -931,13 +933,17 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
     }
     else
     {
-        // Wide-node traversal: lanes 0..7 test the 8 children of a node at
-        // once; leaf children are screened nearest first, internal children
-        // go on the stack with the nearest on top, and every popped entry is
-        // re-tested against the current bound.
+        // Wide-node traversal, up to NODE_GROUPS nodes a step: lane group g
+        // (lanes 8g .. 8g+7) tests the 8 children of its node; leaf children
+        // are screened in lane order, internal children go on the stack in
+        // lane order, and the next step takes the top entries that still
+        // pass the current bound.  A step takes at most (STACK - sp) / 7
+        // entries (at least one), so its children fit on the stack.
         int sp = 0;
-        int node = 0;
-        // every wide node is entered at most once
+        int const grp = lane >> 3, slot = lane & 7;
+        int node = grp == 0 ? 0 : -1;
+        // every step enters at least one wide node, and every wide node is
+        // entered at most once
         for ( int64_t guard = 0;; ++guard )
         {
             if ( guard >= tr.nw )
@@ -949,17 +955,15 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
             float lb = __int_as_float( 0x7f800000 );
             int ref = WIDE_EMPTY;
             bool ok = false;
-            if ( lane < WIDE )
+            if ( node >= 0 )
             {
                 float lo[3], hi[3];
                 int rlo = 0, rhi = 0;
-                load_wide<GROUPED>( tr.wide, node, lane, lo, hi, ref, rlo, rhi );
+                load_wide<GROUPED>( tr.wide, node, slot, lo, hi, ref, rlo, rhi );
                 lb = box_lb( lo, hi, q.qlo, q.qhi );
                 ok = ref != WIDE_EMPTY && ( GROUPED ? !( rhi < rg.lps || rlo > rg.lpe ) : true );
             }
             bool const cand = ok && lb <= bound_f;
-            // slot order: with a seeded bound close to the final one the
-            // visit order changes little of what is pruned
             unsigned const ml = __ballot_sync( FULL, cand && ref < 0 );
             unsigned const mi = __ballot_sync( FULL, cand && ref >= 0 );
             int const n_int = __popc( mi );
@@ -984,22 +988,49 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
                 if ( lbr <= bound_f )
                     process_leaf( ~lref );
             }
-            int next = -1;
+            // the next nodes: entry j from the top (lane j) is taken when it
+            // still passes the bound, up to P of them; the others above the
+            // last one taken are dropped
+            int const room = ( STACK - sp ) / ( WIDE - 1 );
+            int const P = room >= NODE_GROUPS ? NODE_GROUPS : ( room > 0 ? room : 1 );
+            int taken = 0;
+            node = -1;
             while ( sp > 0 )
             {
-                --sp;
-                int const c = s_stack[wib][sp];
-                float const l = s_lb[wib][sp];
-                if ( l <= bound_f )
+                int const avail = sp < 32 ? sp : 32;
+                int e_node = 0;
+                bool pass = false;
+                if ( lane < avail )
                 {
-                    next = c;
-                    break;
+                    e_node = s_stack[wib][sp - 1 - lane];
+                    pass = s_lb[wib][sp - 1 - lane] <= bound_f;
                 }
+                unsigned const v0 = __ballot_sync( FULL, pass );
+                unsigned const v1 = v0 & ( v0 - 1 ), v2 = v1 & ( v1 - 1 ), v3 = v2 & ( v2 - 1 );
+                int const nv = __popc( v0 );
+                int consumed;
+                if ( nv >= P )
+                {
+                    unsigned const vp = P == 1 ? v0 : P == 2 ? v1 : P == 3 ? v2 : v3;
+                    consumed = __ffs( vp ); // one past the P-th entry taken
+                    taken = P;
+                }
+                else
+                {
+                    consumed = avail;
+                    taken = nv;
+                }
+                unsigned const vg = grp == 0 ? v0 : grp == 1 ? v1 : grp == 2 ? v2 : v3;
+                int const src = grp < taken ? __ffs( vg ) - 1 : 0;
+                int const got = __shfl_sync( FULL, e_node, src );
+                node = grp < taken ? got : -1;
+                sp -= consumed;
+                if ( taken > 0 )
+                    break;
             }
             __syncwarp();
-            if ( next < 0 )
+            if ( taken == 0 )
                 break;
-            node = next;
         }
     }
     if ( qn > 0 )
