@@ -1105,10 +1105,15 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     }
     else
     {
+        // up to NODE_GROUPS wide nodes a step, lane group g testing the
+        // children of its node, as in the kNN traversal; the bound is fixed,
+        // so the next step takes the top entries of the stack as they are
         int sp = 0;
-        int node = 0;
+        int const grp = lane >> 3, slot = lane & 7;
+        int node = grp == 0 ? 0 : -1;
         unsigned const lt_mask = ( 1u << lane ) - 1u;
-        // every wide node is entered at most once
+        // every step enters at least one wide node, and every wide node is
+        // entered at most once
         for ( int64_t guard = 0;; ++guard )
         {
             if ( guard >= tr.nw )
@@ -1119,11 +1124,11 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
             }
             bool cand = false;
             int ref = WIDE_EMPTY;
-            if ( lane < WIDE )
+            if ( node >= 0 )
             {
                 float lo[3], hi[3];
                 int rlo = 0, rhi = 0;
-                load_wide<GROUPED>( tr.wide, node, lane, lo, hi, ref, rlo, rhi );
+                load_wide<GROUPED>( tr.wide, node, slot, lo, hi, ref, rlo, rhi );
                 cand = ref != WIDE_EMPTY && box_lb( lo, hi, q.qlo, q.qhi ) <= bound_f &&
                        ( GROUPED ? !( rhi < rg.lps || rlo > rg.lpe ) : true );
             }
@@ -1146,8 +1151,11 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
             }
             if ( sp == 0 )
                 break;
-            --sp;
-            node = s_stack[wib][sp];
+            int const room = ( STACK - sp ) / ( WIDE - 1 );
+            int const P = room >= NODE_GROUPS ? NODE_GROUPS : ( room > 0 ? room : 1 );
+            int const take = P < sp ? P : sp;
+            node = grp < take ? s_stack[wib][sp - 1 - grp] : -1;
+            sp -= take;
             __syncwarp();
         }
     }
