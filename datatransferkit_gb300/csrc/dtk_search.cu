@@ -11,7 +11,7 @@
 // 8-wide BVH (three binary levels per wide node), so that 8 lanes test the 8
 // children of a node at once.
 //
-// kNN query: a warp runs 16 Morton-consecutive targets one after the other;
+// kNN query: a warp runs 32 Morton-consecutive targets one after the other;
 // the k best (d2, index) keys sit one per lane, sorted across lanes.  The
 // first target of a warp starts from the 32 Morton-sorted sources around its
 // code, every later one from the previous target's final list re-keyed for
@@ -44,7 +44,7 @@ constexpr int STACK = 256; // wide-node stack entries per warp
 constexpr int NODE_GROUPS = 4; // wide nodes a kNN warp tests per step (8 lanes each)
 static_assert( NODE_GROUPS * 8 == 32, "one lane per child slot" );
 constexpr int Q_WARPS = 4; // warps per block in the query kernels
-constexpr int Q_SEQ = 16;  // consecutive kNN queries per warp (each seeds the next)
+constexpr int Q_SEQ = 32;  // consecutive kNN queries per warp (each seeds the next)
 constexpr unsigned FULL = 0xffffffffu;
 constexpr unsigned long long KEY_INF = 0xffffffffffffffffull;
 

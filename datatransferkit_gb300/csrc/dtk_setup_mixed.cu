@@ -2,19 +2,24 @@
 //
 // Same stages as the FP64 form (DTK_DetailsMovingLeastSquaresOperatorImpl.hpp
 // :72-336 after the search), one thread per target, but:
-//   * centring and scaling by the support radius: x^ = fl32(s - t) * (1/r)
-//     (FP64 difference, FP32 scale), so the basis and the weights see O(1)
-//     arguments (P(x) / r^deg = P(x^), and rbf(|x| / r) = rbf(|x^|));
+//   * centring and scaling by the support radius, x^ = (s - t) (1/r) with
+//     the difference rounded to FP32 (from double-float splits of s and t
+//     in the fast path, in FP64 in the Jacobi path) and an FP32 scale, so the
+//     basis and the weights see O(1) arguments (P(x) / r^deg = P(x^), and
+//     rbf(|x| / r) = rbf(|x^|));
 //   * FP32 weights, basis and moment assembly (registers);
-//   * an FP32 inverse of the scaled moments A^ as the preconditioner of one
-//     FP64 iterative-refinement step for row 0 of the pseudo-inverse,
-//     a = M e0, a += M (e0 - A a), the residual in FP64 from the neighbours
-//     themselves (the basis of FP32 coordinates is exact in FP64, phi_j is
-//     the FP32 weight).  The step contracts the FP32 error by
-//     ~cond(A^) 2^-24, which leaves the FP32 rounding of the coordinates as
-//     the only error (~2.5e-8 rel L2 on the 8M-point workload; an FP64
-//     eigen-solve, or Kahan-compensated moments, give the same error);
-//   * coefficients c_j = phi_j (P(x^_j) . a) as FP64 dots, stored in FP32.
+//   * an FP32 inverse M of the scaled moments A^ as the preconditioner of
+//     iterative refinement for row 0 of the pseudo-inverse, a = M e0,
+//     a += M (e0 - A a), the residual summed over the neighbours themselves
+//     (not from the FP32 moments): in double-float arithmetic on the FP32
+//     pipe in the fast path, in FP64 in the Jacobi path.  The basis of FP32
+//     coordinates is exact there and phi_j is the FP32 weight.  A step
+//     contracts the FP32 error by ~cond(A^) 2^-24, which leaves the FP32
+//     rounding of the coordinates as the only error (~2.5e-8 rel L2 on the
+//     8M-point workload; an FP64 eigen-solve, or Kahan-compensated moments,
+//     give the same error);
+//   * coefficients c_j = phi_j (P(x^_j) . a) as compensated dots, stored in
+//     FP32.
 // The preconditioner M:
 //   * fast path (k_setup_mixed): Cholesky A^ = R^T R in FP32 registers,
 //     S = R^-1, M = S S^T.  It is taken when the factorization succeeds and
@@ -27,10 +32,10 @@
 //     convergence, truncation lambda_k <= 2^-20 lambda_max (geometric rank
 //     deficiency), M = V L^+ V^T.
 // GB300 issues one FP64 warp instruction per 64 cycles per SM sub-partition;
-// the FP64 work here is the centring, the residual and the coefficient dots
-// (~2.3k FP64 operations per target against ~57k for the FP64 form's
-// reference Jacobi).  The fast path keeps all state in registers; the
-// Jacobi path keeps A^ and V (FP32) thread-interleaved in shared memory,
+// the FP64 work left in the fast path is the support radius (one FP64
+// distance per target for sorted rows).  The fast path stages each warp's
+// rows in shared memory (12.4 KB per warp) and keeps the rest in registers;
+// the Jacobi path keeps A^ and V (FP32) thread-interleaved in shared memory,
 // 620 B per thread at M = 10.
 #include "dtk_common.cuh"
 #include "dtk_jacobi.cuh"
@@ -183,11 +188,11 @@ __device__ __forceinline__ void dot_df( float const *ph, float const *pl, float 
 // Refinement and coefficients of the fast path in double-float: a = ah + al
 // on entry (the FP32 solve, al = 0); r = e0 - sum_j phi_j P_j (P_j . a)
 // accumulated per component as rh + rl; a += M r; c_j = phi_j (P_j . a)
-// rounded once to FP32.
-template <int M, class Scaled, class Pinv>
+// rounded once to FP32 and handed to store(j, c_j).
+template <int M, class Scaled, class Pinv, class Store>
 __device__ __forceinline__ void refine_and_store_df( int len, int rbf, int steps, Scaled const &scaled,
                                                      Pinv const &pinv32, float *ah, float *al,
-                                                     float *coeff_row )
+                                                     Store const &store )
 {
     for ( int step = 0; step < steps; ++step )
     {
@@ -247,7 +252,7 @@ __device__ __forceinline__ void refine_and_store_df( int len, int rbf, int steps
         dot_df<M>( ph, pl, ah, al, s, c );
         float wh, wl;
         two_prod( phi, s, wh, wl );
-        coeff_row[j] = __fadd_rn( wh, __fmaf_rn( phi, c, wl ) );
+        store( j, __fadd_rn( wh, __fmaf_rn( phi, c, wl ) ) );
     }
 }
 
@@ -269,42 +274,47 @@ __global__ void k_split_points( PointsView p, float2 *out )
 
 // Fast path: FP32 Cholesky preconditioner in registers; targets it cannot
 // take (factorization fails, or the condition bound exceeds 2^20) are
-// appended to `list` for k_setup_mixed_eig.
+// appended to `list` for k_setup_mixed_eig.  A warp first stages the
+// neighbours of its 32 targets in shared memory, one row at a time with one
+// lane per neighbour (coalesced index loads, 32 independent gathers in
+// flight), as centred FP32 coordinates (sh - th) + (sl - tl); the three
+// per-target passes (moments, residual, coefficients) then read them from
+// there, and the coefficients go back out row by row.
+constexpr int SMX = 64;       // threads per block of the fast kernel (two warps)
+constexpr int ROW_PITCH = 33; // staged rows: [axis][neighbour][target lane], 33 floats a neighbour
+
 template <int M>
-__global__ void __launch_bounds__( 128 )
+__global__ void __launch_bounds__( SMX, 8 )
     k_setup_mixed( PointsView src, float2 const *__restrict__ split, PointsView tgt, int32_t const *offset,
                    int32_t const *idx, uint32_t const *order, int64_t n_tgt, int rbf, bool rows_sorted,
                    float *coeff, int32_t *list, unsigned *count, unsigned *status )
 {
     constexpr int NU = M * ( M + 1 ) / 2;
-    int64_t const g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if ( g >= n_tgt )
-        return; // no warp-wide operations below
-    int64_t const i = order ? (int64_t)order[g] : g;
-    int64_t const b = offset[i];
-    int len = offset[i + 1] - (int)b;
-    for ( int j = 0; j < len; ++j )
-        if ( (uint32_t)idx[b + j] >= (uint64_t)src.n )
-        {
-            atomicOr( status, DEV_BAD_INDEX );
-            len = 0;
-        }
-    double const tx = tgt( i, 0 ), ty = tgt( i, 1 ), tz = tgt( i, 2 );
-    double d2max = 0.0;
-    for ( int j = rows_sorted ? max( 0, len - 1 ) : 0; j < len; ++j )
+    static_assert( FUSED_MAX_ROW <= 32, "one lane per neighbour when staging a row" );
+    // pitch 33: the row-wise fill (lanes = neighbours) and the per-target
+    // reads (lanes = targets) both touch 32 distinct banks; after the last
+    // pass the x plane holds the coefficients
+    __shared__ float s_nb[SMX / 32][3][32 * ROW_PITCH];
+    int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    int64_t const g = blockIdx.x * (int64_t)SMX + threadIdx.x;
+    if ( g - lane >= n_tgt )
+        return; // the whole warp is past the end; below, all 32 lanes take part
+    bool const active = g < n_tgt;
+    int64_t const i = active ? ( order ? (int64_t)order[g] : g ) : 0;
+    int64_t const b = active ? offset[i] : 0;
+    int len = active ? offset[i + 1] - (int)b : 0;
+    if ( len > FUSED_MAX_ROW || len < 0 )
     {
-        int64_t const sj = idx[b + j];
-        d2max = fmax( d2max, dist2_rn( src( sj, 0 ), src( sj, 1 ), src( sj, 2 ), tx, ty, tz ) );
+        atomicOr( status, DEV_BAD_INDEX );
+        len = 0;
     }
-    double distance = 10. * DBL_EPSILON;
-    double const dmax = __dsqrt_rn( d2max );
-    if ( dmax > distance )
-        distance = dmax;
-    float const inv_r = (float)( 1.0 / ( 1.1 * distance ) );
-    // the target as double-floats; x^ = ((sh - th) + (sl - tl)) / r in FP32
-    // (sh - th is exact for nearby points, Sterbenz)
-    float th[3], tl[3];
+    double const tx = active ? tgt( i, 0 ) : 0.0, ty = active ? tgt( i, 1 ) : 0.0,
+                 tz = active ? tgt( i, 2 ) : 0.0;
+    float *const sx = s_nb[wib][0], *const sy = s_nb[wib][1], *const sz = s_nb[wib][2];
     {
+        // the target as double-floats; (sh - th) is exact for nearby points
+        // (Sterbenz)
+        float th[3], tl[3];
         double const t3[3] = {tx, ty, tz};
 #pragma unroll
         for ( int d = 0; d < 3; ++d )
@@ -312,127 +322,191 @@ __global__ void __launch_bounds__( 128 )
             th[d] = __double2float_rn( t3[d] );
             tl[d] = __double2float_rn( t3[d] - (double)th[d] );
         }
+        unsigned bad_rows = 0;
+        for ( int t = 0; t < 32; ++t )
+        {
+            int const lt = __shfl_sync( FULL, len, t );
+            if ( lt == 0 )
+                continue; // warp-uniform
+            int64_t const bt = __shfl_sync( FULL, b, t );
+            float const hx = __shfl_sync( FULL, th[0], t ), hy = __shfl_sync( FULL, th[1], t ),
+                        hz = __shfl_sync( FULL, th[2], t );
+            float const lx = __shfl_sync( FULL, tl[0], t ), ly = __shfl_sync( FULL, tl[1], t ),
+                        lz = __shfl_sync( FULL, tl[2], t );
+            bool bad = false;
+            if ( lane < lt )
+            {
+                uint32_t const sj = (uint32_t)idx[bt + lane];
+                if ( sj >= (uint64_t)src.n )
+                    bad = true;
+                else
+                {
+                    float2 const a0 = __ldg( split + 3 * (int64_t)sj ), a1 = __ldg( split + 3 * (int64_t)sj + 1 ),
+                                 a2 = __ldg( split + 3 * (int64_t)sj + 2 );
+                    sx[lane * ROW_PITCH + t] = __fadd_rn( __fsub_rn( a0.x, hx ), __fsub_rn( a0.y, lx ) );
+                    sy[lane * ROW_PITCH + t] = __fadd_rn( __fsub_rn( a1.x, hy ), __fsub_rn( a1.y, ly ) );
+                    sz[lane * ROW_PITCH + t] = __fadd_rn( __fsub_rn( a2.x, hz ), __fsub_rn( a2.y, lz ) );
+                }
+            }
+            if ( __any_sync( FULL, bad ) )
+                bad_rows |= 1u << t;
+        }
+        __syncwarp();
+        if ( ( bad_rows >> lane ) & 1u )
+        {
+            atomicOr( status, DEV_BAD_INDEX );
+            len = 0;
+        }
     }
-    auto scaled = [&]( int j, float &x, float &y, float &z ) {
-        int64_t const sj = idx[b + j];
-        float2 const a0 = __ldg( split + 3 * sj ), a1 = __ldg( split + 3 * sj + 1 ), a2 = __ldg( split + 3 * sj + 2 );
-        x = __fmul_rn( __fadd_rn( __fsub_rn( a0.x, th[0] ), __fsub_rn( a0.y, tl[0] ) ), inv_r );
-        y = __fmul_rn( __fadd_rn( __fsub_rn( a1.x, th[1] ), __fsub_rn( a1.y, tl[1] ) ), inv_r );
-        z = __fmul_rn( __fadd_rn( __fsub_rn( a2.x, th[2] ), __fsub_rn( a2.y, tl[2] ) ), inv_r );
-    };
+    bool fast = false;
+    if ( active )
+    {
+        double d2max = 0.0;
+        for ( int j = rows_sorted ? max( 0, len - 1 ) : 0; j < len; ++j )
+        {
+            int64_t const sj = idx[b + j];
+            d2max = fmax( d2max, dist2_rn( src( sj, 0 ), src( sj, 1 ), src( sj, 2 ), tx, ty, tz ) );
+        }
+        double distance = 10. * DBL_EPSILON;
+        double const dmax = __dsqrt_rn( d2max );
+        if ( dmax > distance )
+            distance = dmax;
+        float const inv_r = (float)( 1.0 / ( 1.1 * distance ) );
+        auto scaled = [&]( int j, float &x, float &y, float &z ) {
+            x = __fmul_rn( sx[j * ROW_PITCH + lane], inv_r );
+            y = __fmul_rn( sy[j * ROW_PITCH + lane], inv_r );
+            z = __fmul_rn( sz[j * ROW_PITCH + lane], inv_r );
+        };
 
-    // FP32 moments, upper triangle R(a, c) = A[ut(a, c)], a <= c
-    float A[NU];
+        // FP32 moments, upper triangle R(a, c) = A[ut(a, c)], a <= c
+        float A[NU];
 #pragma unroll
-    for ( int u = 0; u < NU; ++u )
-        A[u] = 0.f;
-    for ( int j = 0; j < len; ++j )
-    {
-        float x, y, z;
-        scaled( j, x, y, z );
-        float P[M];
-        basis_eval<M, float>( x, y, z, P );
-        float const phi = weight32( rbf, x, y, z );
-#pragma unroll
-        for ( int a = 0; a < M; ++a )
+        for ( int u = 0; u < NU; ++u )
+            A[u] = 0.f;
+        for ( int j = 0; j < len; ++j )
         {
-            float const pa = P[a] * phi;
+            float x, y, z;
+            scaled( j, x, y, z );
+            float P[M];
+            basis_eval<M, float>( x, y, z, P );
+            float const phi = weight32( rbf, x, y, z );
 #pragma unroll
-            for ( int c = a; c < M; ++c )
-                A[ut<M>( a, c )] = fmaf( pa, P[c], A[ut<M>( a, c )] );
+            for ( int a = 0; a < M; ++a )
+            {
+                float const pa = P[a] * phi;
+#pragma unroll
+                for ( int c = a; c < M; ++c )
+                    A[ut<M>( a, c )] = fmaf( pa, P[c], A[ut<M>( a, c )] );
+            }
         }
-    }
-    float trace = 0.f;
-#pragma unroll
-    for ( int k = 0; k < M; ++k )
-        trace += A[ut<M>( k, k )];
-
-    // Cholesky A = R^T R in place (R upper triangular, row-major packed)
-    bool ok = trace > 0.f;
-    float rinv[M];
-#pragma unroll
-    for ( int j = 0; j < M; ++j )
-    {
-        float d = A[ut<M>( j, j )];
-#pragma unroll
-        for ( int k = 0; k < j; ++k )
-            d = fmaf( -A[ut<M>( k, j )], A[ut<M>( k, j )], d );
-        ok = ok && d > 0.f;
-        float const inv = d > 0.f ? rsqrtf( d ) : 0.f;
-        rinv[j] = inv;
-        A[ut<M>( j, j )] = d * inv; // sqrt(d)
-#pragma unroll
-        for ( int c = j + 1; c < M; ++c )
-        {
-            float v = A[ut<M>( j, c )];
-#pragma unroll
-            for ( int k = 0; k < j; ++k )
-                v = fmaf( -A[ut<M>( k, j )], A[ut<M>( k, c )], v );
-            A[ut<M>( j, c )] = v * inv;
-        }
-    }
-    // S = R^-1 in place, column by column: S(j,j) = 1/R(j,j),
-    // S(r,j) = -(sum_{k=r}^{j-1} S(r,k) R(k,j)) / R(j,j), r ascending
-    float fro = 0.f;
-#pragma unroll
-    for ( int j = 0; j < M; ++j )
-    {
-#pragma unroll
-        for ( int r = 0; r < j; ++r )
-        {
-            float v = 0.f;
-#pragma unroll
-            for ( int k = r; k < j; ++k )
-                v = fmaf( k == r ? A[ut<M>( r, r )] : A[ut<M>( r, k )], A[ut<M>( k, j )], v );
-            // S(r, r) is already stored at (r, r); S(r, k) for k < j too
-            A[ut<M>( r, j )] = -v * rinv[j];
-        }
-        A[ut<M>( j, j )] = rinv[j];
-    }
-#pragma unroll
-    for ( int u = 0; u < NU; ++u )
-        fro = fmaf( A[u], A[u], fro );
-    float const crit = trace * fro;
-    if ( !ok || !( crit <= 1048576.f ) ) // 2^20; false for NaN
-    {
-        unsigned const slot = atomicAdd( count, 1u );
-        list[slot] = (int32_t)i;
-        return;
-    }
-    // M v = S (S^T v)
-    auto pinv32 = [&]( float const *v, float *y ) {
-        float w[M];
+        float trace = 0.f;
 #pragma unroll
         for ( int k = 0; k < M; ++k )
-        {
-            float acc = 0.f;
+            trace += A[ut<M>( k, k )];
+
+        // Cholesky A = R^T R in place (R upper triangular, row-major packed)
+        bool ok = trace > 0.f;
+        float rinv[M];
 #pragma unroll
-            for ( int r = 0; r <= k; ++r )
-                acc = fmaf( A[ut<M>( r, k )], v[r], acc );
-            w[k] = acc;
+        for ( int j = 0; j < M; ++j )
+        {
+            float d = A[ut<M>( j, j )];
+#pragma unroll
+            for ( int k = 0; k < j; ++k )
+                d = fmaf( -A[ut<M>( k, j )], A[ut<M>( k, j )], d );
+            ok = ok && d > 0.f;
+            float const inv = d > 0.f ? rsqrtf( d ) : 0.f;
+            rinv[j] = inv;
+            A[ut<M>( j, j )] = d * inv; // sqrt(d)
+#pragma unroll
+            for ( int c = j + 1; c < M; ++c )
+            {
+                float v = A[ut<M>( j, c )];
+#pragma unroll
+                for ( int k = 0; k < j; ++k )
+                    v = fmaf( -A[ut<M>( k, j )], A[ut<M>( k, c )], v );
+                A[ut<M>( j, c )] = v * inv;
+            }
+        }
+        // S = R^-1 in place, column by column: S(j,j) = 1/R(j,j),
+        // S(r,j) = -(sum_{k=r}^{j-1} S(r,k) R(k,j)) / R(j,j), r ascending
+        float fro = 0.f;
+#pragma unroll
+        for ( int j = 0; j < M; ++j )
+        {
+#pragma unroll
+            for ( int r = 0; r < j; ++r )
+            {
+                float v = 0.f;
+#pragma unroll
+                for ( int k = r; k < j; ++k )
+                    v = fmaf( k == r ? A[ut<M>( r, r )] : A[ut<M>( r, k )], A[ut<M>( k, j )], v );
+                // S(r, r) is already stored at (r, r); S(r, k) for k < j too
+                A[ut<M>( r, j )] = -v * rinv[j];
+            }
+            A[ut<M>( j, j )] = rinv[j];
         }
 #pragma unroll
-        for ( int r = 0; r < M; ++r )
+        for ( int u = 0; u < NU; ++u )
+            fro = fmaf( A[u], A[u], fro );
+        float const crit = trace * fro;
+        if ( !ok || !( crit <= 1048576.f ) ) // 2^20; false for NaN
         {
-            float acc = 0.f;
-#pragma unroll
-            for ( int k = r; k < M; ++k )
-                acc = fmaf( A[ut<M>( r, k )], w[k], acc );
-            y[r] = acc;
+            unsigned const slot = atomicAdd( count, 1u );
+            list[slot] = (int32_t)i;
         }
-    };
-    float ah[M], al[M];
-    {
-        float e0[M];
-#pragma unroll
-        for ( int r = 0; r < M; ++r )
+        else
         {
-            e0[r] = r == 0 ? 1.f : 0.f;
-            al[r] = 0.f;
+            fast = true;
+            // M v = S (S^T v)
+            auto pinv32 = [&]( float const *v, float *y ) {
+                float w[M];
+#pragma unroll
+                for ( int k = 0; k < M; ++k )
+                {
+                    float acc = 0.f;
+#pragma unroll
+                    for ( int r = 0; r <= k; ++r )
+                        acc = fmaf( A[ut<M>( r, k )], v[r], acc );
+                    w[k] = acc;
+                }
+#pragma unroll
+                for ( int r = 0; r < M; ++r )
+                {
+                    float acc = 0.f;
+#pragma unroll
+                    for ( int k = r; k < M; ++k )
+                        acc = fmaf( A[ut<M>( r, k )], w[k], acc );
+                    y[r] = acc;
+                }
+            };
+            float ah[M], al[M];
+            {
+                float e0[M];
+#pragma unroll
+                for ( int r = 0; r < M; ++r )
+                {
+                    e0[r] = r == 0 ? 1.f : 0.f;
+                    al[r] = 0.f;
+                }
+                pinv32( e0, ah );
+            }
+            refine_and_store_df<M>( len, rbf, crit <= 65536.f ? 1 : 2, scaled, pinv32, ah, al,
+                                    [&]( int j, float c ) { sx[j * ROW_PITCH + lane] = c; } );
         }
-        pinv32( e0, ah );
     }
-    refine_and_store_df<M>( len, rbf, crit <= 65536.f ? 1 : 2, scaled, pinv32, ah, al, coeff + b );
+    // the coefficients of the fast rows, row by row (one lane per entry)
+    int const out_len = fast ? len : 0;
+    __syncwarp();
+    for ( int t = 0; t < 32; ++t )
+    {
+        int const lt = __shfl_sync( FULL, out_len, t );
+        if ( lt == 0 )
+            continue; // warp-uniform
+        int64_t const bt = __shfl_sync( FULL, b, t );
+        if ( lane < lt )
+            coeff[bt + lane] = sx[lane * ROW_PITCH + t];
+    }
 }
 
 // Jacobi path over the targets the fast path listed: list[0 .. *count),
@@ -657,7 +731,7 @@ void launch_mixed( SetupArgs const &a, cudaStream_t s )
     DeviceBuffer<float2> split( 3 * a.src.n, s );
     k_split_points<<<(unsigned)( ( a.src.n + 255 ) / 256 ), 256, 0, s>>>( a.src, split.get() );
     check_launch( "k_split_points" );
-    k_setup_mixed<M><<<(unsigned)( ( a.n_tgt + 127 ) / 128 ), 128, 0, s>>>(
+    k_setup_mixed<M><<<(unsigned)( ( a.n_tgt + SMX - 1 ) / SMX ), SMX, 0, s>>>(
         a.src, split.get(), a.tgt, a.offset, a.idx, a.order, a.n_tgt, a.rbf, a.rows_sorted, a.coeff32,
         list.get(), count.get(), a.status );
     check_launch( "k_setup_mixed" );
