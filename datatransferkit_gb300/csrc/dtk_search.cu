@@ -707,6 +707,7 @@ __device__ __forceinline__ void d2_bounds( TreeView const &tr, Query const &q, i
 }
 
 constexpr int QUEUE = 64;
+constexpr float SPEC_GROWTH = 1.25f; // speculative k-th squared distance over the previous query's
 
 template <bool GROUPED>
 __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
@@ -724,6 +725,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
     // the list of the previous query (its sorted positions kp and indices ki)
     // seeds the next one: Morton-consecutive queries share most neighbours
     int prev_g = -1, prev_row = 0;
+    // the previous query's k-th distance (squared) times SPEC_GROWTH: a guess
+    // of this query's, proven or retried after the search
+    float next_spec = __int_as_float( 0x7f800000 );
     unsigned long long kd = KEY_INF;
     int ki = 0x7fffffff, kp = -1;
     for ( int64_t w = w0; w < w0 + Q_SEQ && w < tgt.n; ++w )
@@ -806,11 +810,14 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
         kp = -1;
     }
     // the list's starting members by leaf and lane: a leaf screens them out
-    int const seed_leaf = kp >= 0 ? kp / LEAF : -1;
-    unsigned const seed_bit = kp >= 0 ? 1u << ( kp % LEAF ) : 0u;
+    int seed_leaf = kp >= 0 ? kp / LEAF : -1;
+    unsigned seed_bit = kp >= 0 ? 1u << ( kp % LEAF ) : 0u;
     unsigned long long bd = __shfl_sync( FULL, kd, k - 1 );
     int bi = __shfl_sync( FULL, ki, k - 1 );
-    float bound_f = prune_threshold( bd );
+    // speculative bound (seeded queries with full rows): boxes and points
+    // beyond it are skipped as if the list were already that tight
+    float spec = seeded && row == k ? next_spec : __int_as_float( 0x7f800000 );
+    float bound_f = fminf( prune_threshold( bd ), spec );
     int qn = 0; // queued survivors (warp-uniform)
 
     // Exact FP64 keys for up to 32 queued sources, merged into the list as a
@@ -895,7 +902,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
             bd = __shfl_sync( FULL, kd, k - 1 );
             bi = __shfl_sync( FULL, ki, k - 1 );
         }
-        bound_f = prune_threshold( bd );
+        bound_f = fminf( prune_threshold( bd ), spec );
         // move the remaining queue entries to the front
         int const rest = qn - count;
         int const v = lane < rest ? s_queue[wib][count + lane] : 0;
@@ -927,118 +934,138 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
             flush( 32 );
     };
 
-    if ( tr.nl == 1 )
+    // A pass searches the tree; a second one follows only when the
+    // speculative bound is not proven: the k-th key exceeds it (or the list
+    // is not full), so points it skipped may belong to the list.  The second
+    // pass screens out the whole list and prunes with the list's own bound.
+    for ( ;; )
     {
-        process_leaf( 0 );
-    }
-    else
-    {
-        // Wide-node traversal, up to NODE_GROUPS nodes a step: lane group g
-        // (lanes 8g .. 8g+7) tests the 8 children of its node; leaf children
-        // are screened in lane order, internal children go on the stack in
-        // lane order, and the next step takes the top entries that still
-        // pass the current bound.  A step takes at most (STACK - sp) / 7
-        // entries (at least one), so its children fit on the stack.
-        int sp = 0;
-        int const grp = lane >> 3, slot = lane & 7;
-        int node = grp == 0 ? 0 : -1;
-        // every step enters at least one wide node, and every wide node is
-        // entered at most once
-        for ( int64_t guard = 0;; ++guard )
+        if ( tr.nl == 1 )
         {
-            if ( guard >= tr.nw )
+            process_leaf( 0 );
+        }
+        else
+        {
+            // Wide-node traversal, up to NODE_GROUPS nodes a step: lane group g
+            // (lanes 8g .. 8g+7) tests the 8 children of its node; leaf children
+            // are screened in lane order, internal children go on the stack in
+            // lane order, and the next step takes the top entries that still
+            // pass the current bound.  A step takes at most (STACK - sp) / 7
+            // entries (at least one), so its children fit on the stack.
+            int sp = 0;
+            int const grp = lane >> 3, slot = lane & 7;
+            int node = grp == 0 ? 0 : -1;
+            // every step enters at least one wide node, and every wide node is
+            // entered at most once
+            for ( int64_t guard = 0;; ++guard )
             {
-                if ( lane == 0 )
-                    atomicOr( status, DEV_TIMEOUT );
-                break;
-            }
-            float lb = __int_as_float( 0x7f800000 );
-            int ref = WIDE_EMPTY;
-            bool ok = false;
-            if ( node >= 0 )
-            {
-                float lo[3], hi[3];
-                int rlo = 0, rhi = 0;
-                load_wide<GROUPED>( tr.wide, node, slot, lo, hi, ref, rlo, rhi );
-                lb = box_lb( lo, hi, q.qlo, q.qhi );
-                ok = ref != WIDE_EMPTY && ( GROUPED ? !( rhi < rg.lps || rlo > rg.lpe ) : true );
-            }
-            bool const cand = ok && lb <= bound_f;
-            unsigned const ml = __ballot_sync( FULL, cand && ref < 0 );
-            unsigned const mi = __ballot_sync( FULL, cand && ref >= 0 );
-            int const n_int = __popc( mi );
-            if ( sp + n_int <= STACK )
-            {
-                if ( cand && ref >= 0 )
+                if ( guard >= tr.nw )
                 {
-                    int const pos = sp + __popc( mi & lt_mask );
-                    s_stack[wib][pos] = ref;
-                    s_lb[wib][pos] = lb;
+                    if ( lane == 0 )
+                        atomicOr( status, DEV_TIMEOUT );
+                    break;
                 }
-                sp += n_int;
-            }
-            else if ( lane == 0 )
-                atomicOr( status, DEV_STACK_OVERFLOW );
-            __syncwarp();
-            for ( unsigned m = ml; m; m &= m - 1 )
-            {
-                int const from = __ffs( m ) - 1;
-                float const lbr = __shfl_sync( FULL, lb, from );
-                int const lref = __shfl_sync( FULL, ref, from );
-                if ( lbr <= bound_f )
-                    process_leaf( ~lref );
-            }
-            // the next nodes: entry j from the top (lane j) is taken when it
-            // still passes the bound, up to P of them; the others above the
-            // last one taken are dropped
-            int const room = ( STACK - sp ) / ( WIDE - 1 );
-            int const P = room >= NODE_GROUPS ? NODE_GROUPS : ( room > 0 ? room : 1 );
-            int taken = 0;
-            node = -1;
-            while ( sp > 0 )
-            {
-                int const avail = sp < 32 ? sp : 32;
-                int e_node = 0;
-                bool pass = false;
-                if ( lane < avail )
+                float lb = __int_as_float( 0x7f800000 );
+                int ref = WIDE_EMPTY;
+                bool ok = false;
+                if ( node >= 0 )
                 {
-                    e_node = s_stack[wib][sp - 1 - lane];
-                    pass = s_lb[wib][sp - 1 - lane] <= bound_f;
+                    float lo[3], hi[3];
+                    int rlo = 0, rhi = 0;
+                    load_wide<GROUPED>( tr.wide, node, slot, lo, hi, ref, rlo, rhi );
+                    lb = box_lb( lo, hi, q.qlo, q.qhi );
+                    ok = ref != WIDE_EMPTY && ( GROUPED ? !( rhi < rg.lps || rlo > rg.lpe ) : true );
                 }
-                unsigned const v0 = __ballot_sync( FULL, pass );
-                unsigned const v1 = v0 & ( v0 - 1 ), v2 = v1 & ( v1 - 1 ), v3 = v2 & ( v2 - 1 );
-                int const nv = __popc( v0 );
-                int consumed;
-                if ( nv >= P )
+                bool const cand = ok && lb <= bound_f;
+                unsigned const ml = __ballot_sync( FULL, cand && ref < 0 );
+                unsigned const mi = __ballot_sync( FULL, cand && ref >= 0 );
+                int const n_int = __popc( mi );
+                if ( sp + n_int <= STACK )
                 {
-                    unsigned const vp = P == 1 ? v0 : P == 2 ? v1 : P == 3 ? v2 : v3;
-                    consumed = __ffs( vp ); // one past the P-th entry taken
-                    taken = P;
+                    if ( cand && ref >= 0 )
+                    {
+                        int const pos = sp + __popc( mi & lt_mask );
+                        s_stack[wib][pos] = ref;
+                        s_lb[wib][pos] = lb;
+                    }
+                    sp += n_int;
                 }
-                else
+                else if ( lane == 0 )
+                    atomicOr( status, DEV_STACK_OVERFLOW );
+                __syncwarp();
+                for ( unsigned m = ml; m; m &= m - 1 )
                 {
-                    consumed = avail;
-                    taken = nv;
+                    int const from = __ffs( m ) - 1;
+                    float const lbr = __shfl_sync( FULL, lb, from );
+                    int const lref = __shfl_sync( FULL, ref, from );
+                    if ( lbr <= bound_f )
+                        process_leaf( ~lref );
                 }
-                unsigned const vg = grp == 0 ? v0 : grp == 1 ? v1 : grp == 2 ? v2 : v3;
-                int const src = grp < taken ? __ffs( vg ) - 1 : 0;
-                int const got = __shfl_sync( FULL, e_node, src );
-                node = grp < taken ? got : -1;
-                sp -= consumed;
-                if ( taken > 0 )
+                // the next nodes: entry j from the top (lane j) is taken when it
+                // still passes the bound, up to P of them; the others above the
+                // last one taken are dropped
+                int const room = ( STACK - sp ) / ( WIDE - 1 );
+                int const P = room >= NODE_GROUPS ? NODE_GROUPS : ( room > 0 ? room : 1 );
+                int taken = 0;
+                node = -1;
+                while ( sp > 0 )
+                {
+                    int const avail = sp < 32 ? sp : 32;
+                    int e_node = 0;
+                    bool pass = false;
+                    if ( lane < avail )
+                    {
+                        e_node = s_stack[wib][sp - 1 - lane];
+                        pass = s_lb[wib][sp - 1 - lane] <= bound_f;
+                    }
+                    unsigned const v0 = __ballot_sync( FULL, pass );
+                    unsigned const v1 = v0 & ( v0 - 1 ), v2 = v1 & ( v1 - 1 ), v3 = v2 & ( v2 - 1 );
+                    int const nv = __popc( v0 );
+                    int consumed;
+                    if ( nv >= P )
+                    {
+                        unsigned const vp = P == 1 ? v0 : P == 2 ? v1 : P == 3 ? v2 : v3;
+                        consumed = __ffs( vp ); // one past the P-th entry taken
+                        taken = P;
+                    }
+                    else
+                    {
+                        consumed = avail;
+                        taken = nv;
+                    }
+                    unsigned const vg = grp == 0 ? v0 : grp == 1 ? v1 : grp == 2 ? v2 : v3;
+                    int const src = grp < taken ? __ffs( vg ) - 1 : 0;
+                    int const got = __shfl_sync( FULL, e_node, src );
+                    node = grp < taken ? got : -1;
+                    sp -= consumed;
+                    if ( taken > 0 )
+                        break;
+                }
+                __syncwarp();
+                if ( taken == 0 )
                     break;
             }
-            __syncwarp();
-            if ( taken == 0 )
-                break;
         }
+        if ( qn > 0 )
+            flush( qn );
+        // Proof: a skipped box or point had an FP32 lower bound above spec,
+        // so its exact squared distance exceeds spec and its FP64 key (a few
+        // ulps off the exact value) exceeds spec (1 - 2^-40); a k-th key at
+        // or below that loses nothing.  d2 >= 0, so the bits of doubles
+        // compare as integers.
+        if ( !( spec < __int_as_float( 0x7f800000 ) ) ||
+             bd <= (unsigned long long)__double_as_longlong( __dmul_rd( (double)spec, 1.0 - 0x1p-40 ) ) )
+            break;
+        seed_leaf = kp >= 0 ? kp / LEAF : -1;
+        seed_bit = kp >= 0 ? 1u << ( kp % LEAF ) : 0u;
+        spec = __int_as_float( 0x7f800000 );
+        bound_f = prune_threshold( bd );
     }
-    if ( qn > 0 )
-        flush( qn );
     if ( lane < row )
         idx_out[offset[qi] + lane] = ki;
     prev_g = rg.g;
     prev_row = row;
+    next_spec = __fmul_ru( prune_threshold( bd ), SPEC_GROWTH );
     __syncwarp();
     }
 }
