@@ -11,14 +11,17 @@
 // 8-wide BVH (three binary levels per wide node), so that 8 lanes test the 8
 // children of a node at once.
 //
-// kNN query: a warp runs 32 Morton-consecutive targets one after the other;
-// the k best (d2, index) keys sit one per lane, sorted across lanes.  The
-// first target of a warp starts from the 32 Morton-sorted sources around its
-// code, every later one from the previous target's final list re-keyed for
-// it (neighbouring targets share most neighbours, so the starting bound is
-// close to the final one).  The starting members are screened out of their
-// leaves (a warp OR-reduction of a per-leaf lane mask), so no source enters
-// the list twice.  A box is pruned only when its FP32 round-down lower bound
+// kNN query: a warp runs up to 64 Morton-consecutive targets one after the
+// other; the k best (d2, index) keys sit one per lane, sorted across lanes.
+// The first target of a warp starts from the 32 Morton-sorted sources around
+// its code, every later one from the previous target's final list re-keyed
+// for it (neighbouring targets share most neighbours).  The starting members
+// are screened out of their leaves (a warp OR-reduction of a per-leaf lane
+// mask), so no source enters the list twice.  A seeded target also prunes
+// with a speculative bound, 1.25 times the previous target's k-th squared
+// distance; when the search ends with a k-th key above it, a second pass
+// (with the whole list screened out and the list's own bound) finds what it
+// skipped.  A box is pruned only when its FP32 round-down lower bound
 // exceeds the round-up bound with a 2^-20 relative margin, and a leaf point
 // only when its FP32 lower bound (with a rigorous rounding bound) does, so no
 // point whose FP64 distance could tie or beat the bound is skipped.  The
@@ -44,7 +47,7 @@ constexpr int STACK = 256; // wide-node stack entries per warp
 constexpr int NODE_GROUPS = 4; // wide nodes a kNN warp tests per step (8 lanes each)
 static_assert( NODE_GROUPS * 8 == 32, "one lane per child slot" );
 constexpr int Q_WARPS = 4; // warps per block in the query kernels
-constexpr int Q_SEQ = 32;  // consecutive kNN queries per warp (each seeds the next)
+constexpr int Q_SEQ = 64;  // most consecutive kNN queries per warp (each seeds the next)
 constexpr unsigned FULL = 0xffffffffu;
 constexpr unsigned long long KEY_INF = 0xffffffffffffffffull;
 
@@ -711,14 +714,14 @@ constexpr float SPEC_GROWTH = 1.25f; // speculative k-th squared distance over t
 
 template <bool GROUPED>
 __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
-    k_knn( TreeView tr, PointsView tgt, uint32_t const *order, int k_all, GroupView gv,
+    k_knn( TreeView tr, PointsView tgt, uint32_t const *order, int k_all, int seq, GroupView gv,
            int32_t const *offset, int32_t *idx_out, unsigned *status )
 {
     __shared__ int s_stack[Q_WARPS][STACK];
     __shared__ float s_lb[Q_WARPS][STACK];
     __shared__ int s_queue[Q_WARPS][QUEUE];
     int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    int64_t const w0 = ( blockIdx.x * (int64_t)Q_WARPS + wib ) * Q_SEQ;
+    int64_t const w0 = ( blockIdx.x * (int64_t)Q_WARPS + wib ) * seq;
     if ( w0 >= tgt.n )
         return;
     unsigned const lt_mask = ( 1u << lane ) - 1u;
@@ -730,7 +733,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
     float next_spec = __int_as_float( 0x7f800000 );
     unsigned long long kd = KEY_INF;
     int ki = 0x7fffffff, kp = -1;
-    for ( int64_t w = w0; w < w0 + Q_SEQ && w < tgt.n; ++w )
+    for ( int64_t w = w0; w < w0 + seq && w < tgt.n; ++w )
     {
     int64_t const qi = order ? (int64_t)order[w] : w;
     Range const rg = query_range<GROUPED>( tr, gv, qi );
@@ -1324,12 +1327,19 @@ void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
     if ( tgt.n == 0 || tree.n == 0 || ( k == 0 && !groups.k ) )
         return;
     GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
+    // queries per warp: up to Q_SEQ, fewer when that leaves under four waves
+    // of resident warps (8 blocks of Q_WARPS per SM)
+    int seq = Q_SEQ;
+    int64_t const resident = (int64_t)num_sms() * 8 * Q_WARPS;
+    while ( seq > 1 && ( tgt.n + seq - 1 ) / seq < 4 * resident )
+        seq /= 2;
+    unsigned const blocks = blocks_for( ( tgt.n + seq - 1 ) / seq, Q_WARPS );
     if ( groups.tgt_grp )
-        k_knn<true><<<blocks_for( ( tgt.n + Q_SEQ - 1 ) / Q_SEQ, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
-            view_of( tree ), tgt, order, k, gv, offset, idx, status );
+        k_knn<true><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, k, seq, gv, offset, idx,
+                                                     status );
     else
-        k_knn<false><<<blocks_for( ( tgt.n + Q_SEQ - 1 ) / Q_SEQ, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
-            view_of( tree ), tgt, order, k, gv, offset, idx, status );
+        k_knn<false><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, k, seq, gv, offset, idx,
+                                                      status );
     check_launch( "k_knn" );
 }
 
