@@ -642,7 +642,7 @@ def run_ours(args, rank, world, local_rank):
                      "algorithmic_bytes": q_bytes, "launch_ms": query_ms,
                      "note": ("the dominant kernel of a mixed step; algorithmic bytes = N_t (24 + 4k + 4) "
                               "+ N_s (24 + 12 + 4); measured traffic matches them (no re-reads) and the "
-                              "kernel is instruction-issue bound (78% of issue slots, profiles/k_knn_1m.md), "
+                              "kernel is instruction-issue bound (69% of issue slots, profiles/k_knn_1m.md), "
                               "not HBM bound")},
         "roofline_stages": {
             "search_build_ms": build_ms,
