@@ -48,6 +48,10 @@ constexpr int NODE_GROUPS = 4; // wide nodes a kNN warp tests per step (8 lanes 
 static_assert( NODE_GROUPS * 8 == 32, "one lane per child slot" );
 constexpr int Q_WARPS = 4; // warps per block in the query kernels
 constexpr int Q_SEQ = 64;  // most consecutive kNN queries per warp (each seeds the next)
+// kNN blocks per SM: 11 blocks of 4 warps cap the kernel at 40 registers; the
+// few values spilled cost less than the warps gained (39.0 ms at 8 blocks,
+// 36.5 ms at 11, on the 8M-point query)
+constexpr int KNN_BLOCKS_PER_SM = 11;
 constexpr unsigned FULL = 0xffffffffu;
 constexpr unsigned long long KEY_INF = 0xffffffffffffffffull;
 
@@ -713,13 +717,14 @@ constexpr int QUEUE = 64;
 constexpr float SPEC_GROWTH = 1.25f; // speculative k-th squared distance over the previous query's
 
 template <bool GROUPED>
-__global__ void __launch_bounds__( Q_WARPS * 32, 8 )
+__global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     k_knn( TreeView tr, PointsView tgt, uint32_t const *order, int k_all, int seq, GroupView gv,
            int32_t const *offset, int32_t *idx_out, unsigned *status )
 {
     __shared__ int s_stack[Q_WARPS][STACK];
     __shared__ float s_lb[Q_WARPS][STACK];
     __shared__ int s_queue[Q_WARPS][QUEUE];
+    __shared__ double s_t[Q_WARPS][3];
     int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     int64_t const w0 = ( blockIdx.x * (int64_t)Q_WARPS + wib ) * seq;
     if ( w0 >= tgt.n )
@@ -746,6 +751,15 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
         continue;
     }
     Query const q = make_query( tr, tgt, qi );
+    // the target's FP64 coordinates, needed only for exact keys, wait in
+    // shared memory (registers limit how many warps an SM holds)
+    if ( lane == 0 )
+    {
+        s_t[wib][0] = q.tx;
+        s_t[wib][1] = q.ty;
+        s_t[wib][2] = q.tz;
+    }
+    __syncwarp();
     bool const seeded = prev_row == row && ( !GROUPED || prev_g == rg.g );
 
     if ( seeded )
@@ -754,7 +768,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
         // row hold entries that insertions shifted out: cleared)
         if ( lane < row )
             kd = (unsigned long long)__double_as_longlong(
-                dist2_rn( __ldg( tr.sx + kp ), __ldg( tr.sy + kp ), __ldg( tr.sz + kp ), q.tx, q.ty, q.tz ) );
+                dist2_rn( __ldg( tr.sx + kp ), __ldg( tr.sy + kp ), __ldg( tr.sz + kp ), s_t[wib][0], s_t[wib][1], s_t[wib][2] ) );
         else
         {
             kd = KEY_INF;
@@ -766,7 +780,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
     {
         // the 32 Morton-sorted sources of the query's problem around the
         // target's code, with exact keys
-        uint32_t const code = morton3( q.tx, q.ty, q.tz, tr.scene );
+        uint32_t const code = morton3( s_t[wib][0], s_t[wib][1], s_t[wib][2], tr.scene );
         int64_t const pos = rg.ps + warp_lower_bound( tr.codes + rg.ps, ng, code, lane );
         int64_t const W = ng < 32 ? ng : (int64_t)32;
         int64_t s0 = pos - 16;
@@ -781,7 +795,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
         {
             int64_t const p = s0 + lane;
             kd = (unsigned long long)__double_as_longlong(
-                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), q.tx, q.ty, q.tz ) );
+                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), s_t[wib][0], s_t[wib][1], s_t[wib][2] ) );
             ki = (int)__ldg( tr.perm + p );
             kp = (int)p;
         }
@@ -815,12 +829,10 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
     // the list's starting members by leaf and lane: a leaf screens them out
     int seed_leaf = kp >= 0 ? kp / LEAF : -1;
     unsigned seed_bit = kp >= 0 ? 1u << ( kp % LEAF ) : 0u;
-    unsigned long long bd = __shfl_sync( FULL, kd, k - 1 );
-    int bi = __shfl_sync( FULL, ki, k - 1 );
     // speculative bound (seeded queries with full rows): boxes and points
     // beyond it are skipped as if the list were already that tight
     float spec = seeded && row == k ? next_spec : __int_as_float( 0x7f800000 );
-    float bound_f = fminf( prune_threshold( bd ), spec );
+    float bound_f = fminf( prune_threshold( __shfl_sync( FULL, kd, k - 1 ) ), spec );
     int qn = 0; // queued survivors (warp-uniform)
 
     // Exact FP64 keys for up to 32 queued sources, merged into the list as a
@@ -836,10 +848,13 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
         if ( p >= 0 )
         {
             cd = (unsigned long long)__double_as_longlong(
-                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), q.tx, q.ty, q.tz ) );
+                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), s_t[wib][0], s_t[wib][1], s_t[wib][2] ) );
             ci = (int)__ldg( tr.perm + p );
             cp = p;
         }
+        // the list's k-th key, the bound a candidate must beat
+        unsigned long long const bd = __shfl_sync( FULL, kd, k - 1 );
+        int const bi = __shfl_sync( FULL, ki, k - 1 );
         bool live = key_less( cd, ci, bd, bi );
         if ( __ballot_sync( FULL, live ) )
         {
@@ -902,10 +917,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
                 ki = 0x7fffffff;
                 kp = -1;
             }
-            bd = __shfl_sync( FULL, kd, k - 1 );
-            bi = __shfl_sync( FULL, ki, k - 1 );
         }
-        bound_f = fminf( prune_threshold( bd ), spec );
+        bound_f = fminf( prune_threshold( __shfl_sync( FULL, kd, k - 1 ) ), spec );
         // move the remaining queue entries to the front
         int const rest = qn - count;
         int const v = lane < rest ? s_queue[wib][count + lane] : 0;
@@ -1056,6 +1069,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
         // ulps off the exact value) exceeds spec (1 - 2^-40); a k-th key at
         // or below that loses nothing.  d2 >= 0, so the bits of doubles
         // compare as integers.
+        unsigned long long const bd = __shfl_sync( FULL, kd, k - 1 );
         if ( !( spec < __int_as_float( 0x7f800000 ) ) ||
              bd <= (unsigned long long)__double_as_longlong( __dmul_rd( (double)spec, 1.0 - 0x1p-40 ) ) )
             break;
@@ -1068,7 +1082,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, 8 )
         idx_out[offset[qi] + lane] = ki;
     prev_g = rg.g;
     prev_row = row;
-    next_spec = __fmul_ru( prune_threshold( bd ), SPEC_GROWTH );
+    next_spec = __fmul_ru( prune_threshold( __shfl_sync( FULL, kd, k - 1 ) ), SPEC_GROWTH );
     __syncwarp();
     }
 }
@@ -1328,9 +1342,9 @@ void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
         return;
     GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
     // queries per warp: up to Q_SEQ, fewer when that leaves under four waves
-    // of resident warps (8 blocks of Q_WARPS per SM)
+    // of resident warps
     int seq = Q_SEQ;
-    int64_t const resident = (int64_t)num_sms() * 8 * Q_WARPS;
+    int64_t const resident = (int64_t)num_sms() * KNN_BLOCKS_PER_SM * Q_WARPS;
     while ( seq > 1 && ( tgt.n + seq - 1 ) / seq < 4 * resident )
         seq /= 2;
     unsigned const blocks = blocks_for( ( tgt.n + seq - 1 ) / seq, Q_WARPS );
