@@ -48,10 +48,11 @@ constexpr int NODE_GROUPS = 4; // wide nodes a kNN warp tests per step (8 lanes 
 static_assert( NODE_GROUPS * 8 == 32, "one lane per child slot" );
 constexpr int Q_WARPS = 4; // warps per block in the query kernels
 constexpr int Q_SEQ = 64;  // most consecutive kNN queries per warp (each seeds the next)
-// kNN blocks per SM: 11 blocks of 4 warps cap the kernel at 40 registers; the
-// few values spilled cost less than the warps gained (39.0 ms at 8 blocks,
-// 36.5 ms at 11, on the 8M-point query)
-constexpr int KNN_BLOCKS_PER_SM = 11;
+// kNN blocks per SM: 16 blocks of 4 warps (all 64 warp slots) cap the kernel
+// at 32 registers, with the query in shared memory; the values spilled cost
+// less than the warps gained (8M-point query: 39.0 ms at 8 blocks, 34.5 ms
+// at 16)
+constexpr int KNN_BLOCKS_PER_SM = 16;
 constexpr unsigned FULL = 0xffffffffu;
 constexpr unsigned long long KEY_INF = 0xffffffffffffffffull;
 
@@ -724,7 +725,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     __shared__ int s_stack[Q_WARPS][STACK];
     __shared__ float s_lb[Q_WARPS][STACK];
     __shared__ int s_queue[Q_WARPS][QUEUE];
-    __shared__ double s_t[Q_WARPS][3];
+    __shared__ Query s_query[Q_WARPS];
     int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     int64_t const w0 = ( blockIdx.x * (int64_t)Q_WARPS + wib ) * seq;
     if ( w0 >= tgt.n )
@@ -750,16 +751,15 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         prev_row = 0;
         continue;
     }
-    Query const q = make_query( tr, tgt, qi );
-    // the target's FP64 coordinates, needed only for exact keys, wait in
-    // shared memory (registers limit how many warps an SM holds)
-    if ( lane == 0 )
+    // the query waits in shared memory: registers limit how many warps an
+    // SM holds, and values there can be re-read instead of spilled
     {
-        s_t[wib][0] = q.tx;
-        s_t[wib][1] = q.ty;
-        s_t[wib][2] = q.tz;
+        Query const qv = make_query( tr, tgt, qi );
+        if ( lane == 0 )
+            s_query[wib] = qv;
     }
     __syncwarp();
+    Query const &q = s_query[wib];
     bool const seeded = prev_row == row && ( !GROUPED || prev_g == rg.g );
 
     if ( seeded )
@@ -768,7 +768,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         // row hold entries that insertions shifted out: cleared)
         if ( lane < row )
             kd = (unsigned long long)__double_as_longlong(
-                dist2_rn( __ldg( tr.sx + kp ), __ldg( tr.sy + kp ), __ldg( tr.sz + kp ), s_t[wib][0], s_t[wib][1], s_t[wib][2] ) );
+                dist2_rn( __ldg( tr.sx + kp ), __ldg( tr.sy + kp ), __ldg( tr.sz + kp ), q.tx, q.ty, q.tz ) );
         else
         {
             kd = KEY_INF;
@@ -780,7 +780,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     {
         // the 32 Morton-sorted sources of the query's problem around the
         // target's code, with exact keys
-        uint32_t const code = morton3( s_t[wib][0], s_t[wib][1], s_t[wib][2], tr.scene );
+        uint32_t const code = morton3( q.tx, q.ty, q.tz, tr.scene );
         int64_t const pos = rg.ps + warp_lower_bound( tr.codes + rg.ps, ng, code, lane );
         int64_t const W = ng < 32 ? ng : (int64_t)32;
         int64_t s0 = pos - 16;
@@ -795,7 +795,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         {
             int64_t const p = s0 + lane;
             kd = (unsigned long long)__double_as_longlong(
-                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), s_t[wib][0], s_t[wib][1], s_t[wib][2] ) );
+                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), q.tx, q.ty, q.tz ) );
             ki = (int)__ldg( tr.perm + p );
             kp = (int)p;
         }
@@ -848,7 +848,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         if ( p >= 0 )
         {
             cd = (unsigned long long)__double_as_longlong(
-                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), s_t[wib][0], s_t[wib][1], s_t[wib][2] ) );
+                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), q.tx, q.ty, q.tz ) );
             ci = (int)__ldg( tr.perm + p );
             cp = p;
         }
