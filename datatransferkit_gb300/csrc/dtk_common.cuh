@@ -332,7 +332,7 @@ struct Lbvh
     DeviceBuffer<float4> wide;        // 24 float4 per 8-wide node (the queries' tree)
     int64_t n_wide = 0;
     DeviceBuffer<float4> root_box;    // box of the whole tree (2 float4)
-    DeviceBuffer<double> scene;       // lo[3], Morton scale[3], hi[3], centre[3], bound S
+    DeviceBuffer<double> scene;       // lo[3], Morton scale[3], hi[3], centre[3], bound S, FP32 lo/scale
 };
 
 // group (optional, per input point) makes the order problem-major: the

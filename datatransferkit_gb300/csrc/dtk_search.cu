@@ -66,12 +66,16 @@ __device__ __forceinline__ uint32_t expand10( uint32_t v )
     return v;
 }
 
-__device__ __forceinline__ uint32_t quantize( double c, double lo, double scale )
+// Morton codes only order the points (the tree's shape and the order of the
+// queries), they never decide a result, so they are computed in FP32 (the
+// FP64 pipe is 1/64 of the FP32 rate): one rounding of each coordinate, then
+// the FP32 copies of lo and 1024 / extent written at scene[13..15].
+__device__ __forceinline__ uint32_t quantize( float c, float lo, float scale )
 {
-    double const u = ( c - lo ) * scale;
-    if ( !( u > 0.0 ) )
+    float const u = ( c - lo ) * scale;
+    if ( !( u > 0.f ) )
         return 0u;
-    if ( u >= 1023.0 )
+    if ( u >= 1023.f )
         return 1023u;
     return (uint32_t)u;
 }
@@ -79,10 +83,10 @@ __device__ __forceinline__ uint32_t quantize( double c, double lo, double scale 
 __device__ __forceinline__ uint32_t morton3( double x, double y, double z,
                                              double const *scene )
 {
-    // scene: lo[3], scale[3] (1024 / extent, or 0 for a flat axis)
-    return ( expand10( quantize( x, scene[0], scene[3] ) ) << 2 ) |
-           ( expand10( quantize( y, scene[1], scene[4] ) ) << 1 ) |
-           expand10( quantize( z, scene[2], scene[5] ) );
+    float const *sf = reinterpret_cast<float const *>( scene + 13 ); // lo[3], scale[3]
+    return ( expand10( quantize( __double2float_rn( x ), sf[0], sf[3] ) ) << 2 ) |
+           ( expand10( quantize( __double2float_rn( y ), sf[1], sf[4] ) ) << 1 ) |
+           expand10( quantize( __double2float_rn( z ), sf[2], sf[5] ) );
 }
 
 // ---------------------------------------------------------------------------
@@ -140,24 +144,39 @@ __global__ void __launch_bounds__( BND_THREADS )
 }
 
 // scene[0..2] = lo, scene[3..5] = 1024/extent (0 when flat), scene[6..8] = hi,
-// scene[9..11] = centre c, scene[12] = S >= max_i,d |p_id - c_d| (with slack)
+// scene[9..11] = centre c, scene[12] = S >= max_i,d |p_id - c_d| (with slack),
+// scene[13..15] = lo and 1024/extent as six floats (the Morton codes)
 __global__ void k_bounds_final( unsigned long long const *partial, int nblocks,
                                 double *scene )
 {
     __shared__ double half[3];
+    // one warp: lane l folds the partials of blocks l, l + 32, ..., then a
+    // shuffle reduction per axis
+    int const lane = threadIdx.x & 31;
+    unsigned long long pmn[3] = {KEY_INF, KEY_INF, KEY_INF}, pmx[3] = {0, 0, 0};
+    for ( int b = lane; b < nblocks; b += 32 )
+        for ( int d = 0; d < 3; ++d )
+        {
+            pmn[d] = min( pmn[d], partial[b * 6 + d] );
+            pmx[d] = max( pmx[d], partial[b * 6 + 3 + d] );
+        }
+    for ( int d = 0; d < 3; ++d )
+        for ( int o = 16; o; o >>= 1 )
+        {
+            pmn[d] = min( pmn[d], __shfl_xor_sync( FULL, pmn[d], o ) );
+            pmx[d] = max( pmx[d], __shfl_xor_sync( FULL, pmx[d], o ) );
+        }
     if ( threadIdx.x < 3 )
     {
         int const d = threadIdx.x;
-        unsigned long long mn = KEY_INF, mx = 0;
-        for ( int b = 0; b < nblocks; ++b )
-        {
-            mn = min( mn, partial[b * 6 + d] );
-            mx = max( mx, partial[b * 6 + 3 + d] );
-        }
+        unsigned long long const mn = d == 0 ? pmn[0] : d == 1 ? pmn[1] : pmn[2];
+        unsigned long long const mx = d == 0 ? pmx[0] : d == 1 ? pmx[1] : pmx[2];
         double const lo = double_of( mn ), hi = double_of( mx );
         double const e = hi - lo;
         scene[d] = lo;
         scene[3 + d] = e > 0.0 ? 1024.0 / e : 0.0;
+        reinterpret_cast<float *>( scene + 13 )[d] = __double2float_rn( lo );
+        reinterpret_cast<float *>( scene + 13 )[3 + d] = __double2float_rn( scene[3 + d] );
         scene[6 + d] = hi;
         double const c = 0.5 * lo + 0.5 * hi;
         scene[9 + d] = c;
@@ -1229,7 +1248,7 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
     tree.n = n;
     tree.n_leaves = ( n + LEAF - 1 ) / LEAF;
     int64_t const nl = tree.n_leaves;
-    tree.scene.allocate( 13, s );
+    tree.scene.allocate( 16, s );
     int const nb = std::max( 1, std::min<int>( 4 * num_sms(), (int)( ( n + BND_THREADS - 1 ) / BND_THREADS ) ) );
     DeviceBuffer<unsigned long long> partial( 6 * nb, s );
     k_bounds_partial<<<nb, BND_THREADS, 0, s>>>( src, partial.get() );
