@@ -145,7 +145,8 @@ __global__ void __launch_bounds__( BND_THREADS )
 
 // scene[0..2] = lo, scene[3..5] = 1024/extent (0 when flat), scene[6..8] = hi,
 // scene[9..11] = centre c, scene[12] = S >= max_i,d |p_id - c_d| (with slack),
-// scene[13..15] = lo and 1024/extent as six floats (the Morton codes)
+// scene[13..16] = lo and 1024/extent as six floats (the Morton codes), then
+// S rounded up to a float
 __global__ void k_bounds_final( unsigned long long const *partial, int nblocks,
                                 double *scene )
 {
@@ -184,7 +185,10 @@ __global__ void k_bounds_final( unsigned long long const *partial, int nblocks,
     }
     __syncthreads();
     if ( threadIdx.x == 0 )
+    {
         scene[12] = fmax( half[0], fmax( half[1], half[2] ) ) * ( 1.0 + 1e-6 ) + 1e-300;
+        reinterpret_cast<float *>( scene + 13 )[6] = __double2float_ru( scene[12] );
+    }
 }
 
 __global__ void k_morton( PointsView p, double const *scene, uint32_t *codes,
@@ -710,12 +714,14 @@ __device__ __forceinline__ Query make_query( TreeView const &tr, PointsView cons
 #pragma unroll
     for ( int d = 0; d < 3; ++d )
     {
-        q.qlo[d] = nextafterf( __double2float_rd( tc[d] ), -INFINITY );
-        q.qhi[d] = nextafterf( __double2float_ru( tc[d] ), INFINITY );
-        q.tf[d] = (float)tc[d];
+        // one rounding to nearest (within half an ulp of t - c), widened by
+        // an ulp each way: the conversions run on the FP64 pipe
+        q.tf[d] = __double2float_rn( tc[d] );
+        q.qlo[d] = nextafterf( q.tf[d], -INFINITY );
+        q.qhi[d] = nextafterf( q.tf[d], INFINITY );
         tmax = fmaxf( tmax, fmaxf( fabsf( q.qlo[d] ), fabsf( q.qhi[d] ) ) );
     }
-    q.err = ( (float)tr.scene[12] + tmax ) * 2.384185791015625e-07f; // 2^-22
+    q.err = ( reinterpret_cast<float const *>( tr.scene + 13 )[6] + tmax ) * 2.384185791015625e-07f; // 2^-22
     return q;
 }
 
@@ -1248,7 +1254,7 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
     tree.n = n;
     tree.n_leaves = ( n + LEAF - 1 ) / LEAF;
     int64_t const nl = tree.n_leaves;
-    tree.scene.allocate( 16, s );
+    tree.scene.allocate( 17, s );
     int const nb = std::max( 1, std::min<int>( 4 * num_sms(), (int)( ( n + BND_THREADS - 1 ) / BND_THREADS ) ) );
     DeviceBuffer<unsigned long long> partial( 6 * nb, s );
     k_bounds_partial<<<nb, BND_THREADS, 0, s>>>( src, partial.get() );
