@@ -739,6 +739,24 @@ __device__ __forceinline__ void d2_bounds( TreeView const &tr, Query const &q, i
     hi = d2 + spread;
 }
 
+// Screen threshold for the computed FP32 squared distance d2_f of a point
+// (d2_bounds without the spread): every point whose rigorous lower bound
+// d2_f - spread(p) is at most b, spread(p) = E (4 (|dx| + |dy| + |dz|) + 3E)
+// + d2_f 2^-20, has d2_f <= T.  With |dx| + |dy| + |dz| <= sqrt(3.0001 d2_f)
+// (Cauchy-Schwarz and the FP32 rounding of d2_f), x = sqrt(d2_f) satisfies
+// (1 - 2^-20) x^2 - 7E x - c <= 0 for c = b + 3E^2, so
+// d2_f <= (c + 14E sqrt(c) + 49E^2) / (1 - 2^-20)^2; every step rounds up
+// and the factor 1 + 2^-16 covers the division.
+__device__ __forceinline__ float screen_threshold( float b, float err )
+{
+    if ( !( b < __int_as_float( 0x7f800000 ) ) )
+        return __int_as_float( 0x7f800000 );
+    float const c = __fmaf_ru( __fmul_ru( 3.f, err ), err, b );
+    float const e7 = __fmul_ru( 7.f, err );
+    float const t = __fmaf_ru( e7, e7, __fmaf_ru( __fmul_ru( 2.f, e7 ), __fsqrt_ru( c ), c ) );
+    return __fmul_ru( t, 1.0000152587890625f ); // 1 + 2^-16
+}
+
 constexpr int QUEUE = 64;
 constexpr float SPEC_GROWTH = 1.25f; // speculative k-th squared distance over the previous query's
 
@@ -858,6 +876,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     // beyond it are skipped as if the list were already that tight
     float spec = seeded && row == k ? next_spec : __int_as_float( 0x7f800000 );
     float bound_f = fminf( prune_threshold( __shfl_sync( FULL, kd, k - 1 ) ), spec );
+    float screen_f = screen_threshold( bound_f, q.err ); // the leaf screen's bound
     int qn = 0; // queued survivors (warp-uniform)
 
     // Exact FP64 keys for up to 32 queued sources, merged into the list as a
@@ -944,6 +963,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
             }
         }
         bound_f = fminf( prune_threshold( __shfl_sync( FULL, kd, k - 1 ) ), spec );
+        screen_f = screen_threshold( bound_f, q.err );
         // move the remaining queue entries to the front
         int const rest = qn - count;
         int const v = lane < rest ? s_queue[wib][count + lane] : 0;
@@ -955,16 +975,18 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     };
 
     // FP32 screen of a leaf: a source whose FP32 lower bound exceeds the
-    // bound cannot beat or tie it; the others queue for exact keys.
+    // bound cannot beat or tie it (screen_threshold keeps all the others);
+    // the survivors queue for exact keys.
     auto process_leaf = [&]( int leaf ) {
         int64_t const p = (int64_t)leaf * LEAF + lane;
         bool surv = false;
         unsigned const seen = __reduce_or_sync( FULL, seed_leaf == leaf ? seed_bit : 0u );
         if ( ( GROUPED ? p >= rg.ps : true ) && p < rg.pe && !( ( seen >> lane ) & 1u ) )
         {
-            float lo, hi;
-            d2_bounds( tr, q, p, lo, hi );
-            surv = lo <= bound_f;
+            float const dx = __ldg( tr.fx + p ) - q.tf[0];
+            float const dy = __ldg( tr.fy + p ) - q.tf[1];
+            float const dz = __ldg( tr.fz + p ) - q.tf[2];
+            surv = fmaf( dz, dz, fmaf( dy, dy, dx * dx ) ) <= screen_f;
         }
         unsigned const m = __ballot_sync( FULL, surv );
         if ( surv )
@@ -1045,8 +1067,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                 // the next nodes: entry j from the top (lane j) is taken when it
                 // still passes the bound, up to P of them; the others above the
                 // last one taken are dropped
-                int const room = ( STACK - sp ) / ( WIDE - 1 );
-                int const P = room >= NODE_GROUPS ? NODE_GROUPS : ( room > 0 ? room : 1 );
+                int const P = sp <= STACK - NODE_GROUPS * ( WIDE - 1 )
+                                  ? NODE_GROUPS
+                                  : max( 1, ( STACK - sp ) / ( WIDE - 1 ) );
                 int taken = 0;
                 node = -1;
                 while ( sp > 0 )
@@ -1102,6 +1125,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         seed_bit = kp >= 0 ? 1u << ( kp % LEAF ) : 0u;
         spec = __int_as_float( 0x7f800000 );
         bound_f = prune_threshold( bd );
+        screen_f = screen_threshold( bound_f, q.err );
     }
     if ( lane < row )
         idx_out[offset[qi] + lane] = ki;
