@@ -648,6 +648,77 @@ __device__ __forceinline__ bool key_less( unsigned long long ad, int ai,
     return ad < bd || ( ad == bd && ai < bi );
 }
 
+// Bitonic network over the warp's 32 (d, i, p) entries, ascending by
+// (d, i): every stage (FULL_SORT), or only the final merge of size 32 (for a
+// bitonic input).
+template <bool FULL_SORT>
+__device__ __forceinline__ void exact_network( unsigned long long &d, int &i, int &p, int lane )
+{
+#pragma unroll
+    for ( int size = FULL_SORT ? 2 : 32; size <= 32; size <<= 1 )
+#pragma unroll
+        for ( int stride = size >> 1; stride > 0; stride >>= 1 )
+        {
+            unsigned long long const od = __shfl_xor_sync( FULL, d, stride );
+            int const oi = __shfl_xor_sync( FULL, i, stride );
+            int const op = __shfl_xor_sync( FULL, p, stride );
+            bool const up = ( lane & size ) == 0 || size == 32;
+            bool const lower = ( lane & stride ) == 0;
+            bool const mine_less = key_less( d, i, od, oi );
+            if ( ( lower == up ) ? !mine_less : mine_less )
+            {
+                d = od;
+                i = oi;
+                p = op;
+            }
+        }
+}
+
+// The same order at a third of the cost: the network runs on 32-bit keys
+// (bits 62..31 of d, order-preserving for d >= 0) with the source lane as the
+// only payload, and each lane then fetches its entry from its source lane.
+// On equal keys a compare-exchange copies one entry over the other, but the
+// keys themselves are sorted all the same, so two real entries with equal
+// keys (distances within 2^-21, or tied) end up side by side: the warp then
+// runs the exact network on its untouched entries.  Sentinels (d = KEY_INF,
+// key 0xffffffff, all alike) may be copied freely.
+template <bool FULL_SORT>
+__device__ __forceinline__ void sort_entries( unsigned long long &d, int &i, int &p, int lane )
+{
+    uint32_t key = (uint32_t)( d >> 31 );
+    int src = lane;
+#pragma unroll
+    for ( int size = FULL_SORT ? 2 : 32; size <= 32; size <<= 1 )
+#pragma unroll
+        for ( int stride = size >> 1; stride > 0; stride >>= 1 )
+        {
+            uint32_t const ok = __shfl_xor_sync( FULL, key, stride );
+            int const os = __shfl_xor_sync( FULL, src, stride );
+            bool const up = ( lane & size ) == 0 || size == 32;
+            bool const lower = ( lane & stride ) == 0;
+            bool const mine_less = key < ok;
+            if ( ( lower == up ) ? !mine_less : mine_less )
+            {
+                key = ok;
+                src = os;
+            }
+        }
+    uint32_t const next = __shfl_down_sync( FULL, key, 1 );
+    bool const tie = lane < 31 && key == next && key != 0xffffffffu;
+    if ( __ballot_sync( FULL, tie ) )
+        exact_network<FULL_SORT>( d, i, p, lane );
+    else
+    {
+        unsigned long long const nd = __shfl_sync( FULL, d, src );
+        int const ni = __shfl_sync( FULL, i, src );
+        int const np = __shfl_sync( FULL, p, src );
+        d = nd;
+        i = ni;
+        p = np;
+    }
+}
+
+
 // 32-ary lower_bound of `code` in the sorted codes (warp-uniform result).
 __device__ __forceinline__ int64_t warp_lower_bound( uint32_t const *codes, int64_t n,
                                                      uint32_t code, int lane )
@@ -843,26 +914,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
             kp = (int)p;
         }
     }
-    // Bitonic sort of the 32 keys across lanes (ascending).
-#pragma unroll
-    for ( int size = 2; size <= 32; size <<= 1 )
-#pragma unroll
-        for ( int stride = size >> 1; stride > 0; stride >>= 1 )
-        {
-            unsigned long long const od = __shfl_xor_sync( FULL, kd, stride );
-            int const oi = __shfl_xor_sync( FULL, ki, stride );
-            int const op = __shfl_xor_sync( FULL, kp, stride );
-            bool const up = ( lane & size ) == 0 || size == 32;
-            bool const lower = ( lane & stride ) == 0;
-            bool const mine_less = key_less( kd, ki, od, oi );
-            bool const take = ( lower == up ) ? !mine_less : mine_less;
-            if ( take )
-            {
-                kd = od;
-                ki = oi;
-                kp = op;
-            }
-        }
+    // the 32 keys ascending across lanes
+    sort_entries<true>( kd, ki, kp, lane );
     if ( lane >= k )
     {
         kd = KEY_INF;
@@ -909,24 +962,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                 cp = -1;
             }
             // candidates ascending
-#pragma unroll
-            for ( int size = 2; size <= 32; size <<= 1 )
-#pragma unroll
-                for ( int stride = size >> 1; stride > 0; stride >>= 1 )
-                {
-                    unsigned long long const od = __shfl_xor_sync( FULL, cd, stride );
-                    int const oi = __shfl_xor_sync( FULL, ci, stride );
-                    int const op = __shfl_xor_sync( FULL, cp, stride );
-                    bool const up = ( lane & size ) == 0 || size == 32;
-                    bool const lower = ( lane & stride ) == 0;
-                    bool const mine_less = key_less( cd, ci, od, oi );
-                    if ( ( lower == up ) ? !mine_less : mine_less )
-                    {
-                        cd = od;
-                        ci = oi;
-                        cp = op;
-                    }
-                }
+            sort_entries<true>( cd, ci, cp, lane );
             // the list (ascending) against the reversed candidates: the 32
             // smallest as a bitonic sequence, then sorted
             {
@@ -940,21 +976,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                     kp = rp;
                 }
             }
-#pragma unroll
-            for ( int stride = 16; stride > 0; stride >>= 1 )
-            {
-                unsigned long long const od = __shfl_xor_sync( FULL, kd, stride );
-                int const oi = __shfl_xor_sync( FULL, ki, stride );
-                int const op = __shfl_xor_sync( FULL, kp, stride );
-                bool const lower = ( lane & stride ) == 0;
-                bool const mine_less = key_less( kd, ki, od, oi );
-                if ( lower ? !mine_less : mine_less )
-                {
-                    kd = od;
-                    ki = oi;
-                    kp = op;
-                }
-            }
+            sort_entries<false>( kd, ki, kp, lane );
             if ( lane >= k )
             {
                 kd = KEY_INF;

@@ -91,6 +91,25 @@ def test_knn_large_coordinates_offset():
     assert np.array_equal(gpu_knn(src, tgt, 20)[1], cpu.knn(src, tgt, 20)[1])
 
 
+def test_knn_near_ties_resolved_exactly():
+    # shells of sources whose distances to their centre agree to ~1e-9
+    # (relative): the 32-bit keys of the sorting networks collide and the
+    # exact network decides; the centres and their twins 1e-12 away run as
+    # consecutive, seeded queries
+    rng = np.random.default_rng(12)
+    centres = 0.2 + 0.6 * rng.random((40, 3))
+    parts = []
+    for c in centres:
+        u = rng.standard_normal((120, 3))
+        u /= np.linalg.norm(u, axis=1)[:, None]
+        r = 0.01 * (1 + 1e-9 * rng.integers(0, 50, 120))
+        parts.append(c + u * r[:, None])
+    src = np.concatenate(parts + [syn.uniform_points(20000, 13)])
+    tgt = np.concatenate([centres, centres + 1e-12 * rng.standard_normal(centres.shape)])
+    for k in (16, 32):
+        assert np.array_equal(gpu_knn(src, tgt, k)[1], cpu.knn(src, tgt, k)[1]), k
+
+
 def test_radius_sets_bit_exact():
     src = syn.gaussian_mixture(20000, 11)
     tgt = syn.uniform_points(3000, 12)
