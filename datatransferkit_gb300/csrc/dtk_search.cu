@@ -628,7 +628,7 @@ __device__ __forceinline__ float box_lb( float const *lo, float const *hi,
     for ( int d = 0; d < 3; ++d )
     {
         float g = fmaxf( 0.f, fmaxf( __fsub_rd( lo[d], qhi[d] ), __fsub_rd( qlo[d], hi[d] ) ) );
-        acc = __fadd_rd( acc, __fmul_rd( g, g ) );
+        acc = __fmaf_rd( g, g, acc );
     }
     return acc;
 }
@@ -840,6 +840,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     __shared__ float s_lb[Q_WARPS][STACK];
     __shared__ int s_queue[Q_WARPS][QUEUE];
     __shared__ Query s_query[Q_WARPS];
+    __shared__ int s_pop[Q_WARPS][NODE_GROUPS];
     int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     int64_t const w0 = ( blockIdx.x * (int64_t)Q_WARPS + wib ) * seq;
     if ( w0 >= tgt.n )
@@ -1093,7 +1094,6 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                                   ? NODE_GROUPS
                                   : max( 1, ( STACK - sp ) / ( WIDE - 1 ) );
                 int taken = 0;
-                node = -1;
                 while ( sp > 0 )
                 {
                     int const avail = sp < 32 ? sp : 32;
@@ -1105,31 +1105,22 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                         pass = s_lb[wib][sp - 1 - lane] <= bound_f;
                     }
                     unsigned const v0 = __ballot_sync( FULL, pass );
-                    unsigned const v1 = v0 & ( v0 - 1 ), v2 = v1 & ( v1 - 1 ), v3 = v2 & ( v2 - 1 );
+                    // the passing entry of rank r (from the top) goes to group r
+                    int const rank = __popc( v0 & lt_mask );
+                    if ( pass && rank < P )
+                        s_pop[wib][rank] = e_node;
                     int const nv = __popc( v0 );
-                    int consumed;
-                    if ( nv >= P )
-                    {
-                        unsigned const vp = P == 1 ? v0 : P == 2 ? v1 : P == 3 ? v2 : v3;
-                        consumed = __ffs( vp ); // one past the P-th entry taken
-                        taken = P;
-                    }
-                    else
-                    {
-                        consumed = avail;
-                        taken = nv;
-                    }
-                    unsigned const vg = grp == 0 ? v0 : grp == 1 ? v1 : grp == 2 ? v2 : v3;
-                    int const src = grp < taken ? __ffs( vg ) - 1 : 0;
-                    int const got = __shfl_sync( FULL, e_node, src );
-                    node = grp < taken ? got : -1;
-                    sp -= consumed;
+                    taken = nv < P ? nv : P;
+                    // one past the P-th entry taken, or all that were examined
+                    unsigned const last = __ballot_sync( FULL, pass && rank == P - 1 );
+                    sp -= last ? __ffs( last ) : avail;
                     if ( taken > 0 )
                         break;
                 }
                 __syncwarp();
                 if ( taken == 0 )
                     break;
+                node = grp < taken ? s_pop[wib][grp] : -1;
             }
         }
         if ( qn > 0 )
