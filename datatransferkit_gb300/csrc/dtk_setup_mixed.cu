@@ -311,6 +311,19 @@ __global__ void __launch_bounds__( SMX, 8 )
     double const tx = active ? tgt( i, 0 ) : 0.0, ty = active ? tgt( i, 1 ) : 0.0,
                  tz = active ? tgt( i, 2 ) : 0.0;
     float *const sx = s_nb[wib][0], *const sy = s_nb[wib][1], *const sz = s_nb[wib][2];
+    // sorted rows: the farthest neighbour (the last) sets the support radius;
+    // its FP64 coordinates are fetched now, to arrive during the staging
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    if ( rows_sorted && len > 0 )
+    {
+        uint32_t const sj = (uint32_t)idx[b + len - 1];
+        if ( sj < (uint64_t)src.n )
+        {
+            fx = src( sj, 0 );
+            fy = src( sj, 1 );
+            fz = src( sj, 2 );
+        }
+    }
     {
         // the target as double-floats; (sh - th) is exact for nearby points
         // (Sterbenz)
@@ -323,6 +336,7 @@ __global__ void __launch_bounds__( SMX, 8 )
             tl[d] = __double2float_rn( t3[d] - (double)th[d] );
         }
         unsigned bad_rows = 0;
+#pragma unroll 4
         for ( int t = 0; t < 32; ++t )
         {
             int const lt = __shfl_sync( FULL, len, t );
@@ -361,8 +375,8 @@ __global__ void __launch_bounds__( SMX, 8 )
     bool fast = false;
     if ( active )
     {
-        double d2max = 0.0;
-        for ( int j = rows_sorted ? max( 0, len - 1 ) : 0; j < len; ++j )
+        double d2max = rows_sorted && len > 0 ? dist2_rn( fx, fy, fz, tx, ty, tz ) : 0.0;
+        for ( int j = 0; !rows_sorted && j < len; ++j )
         {
             int64_t const sj = idx[b + j];
             d2max = fmax( d2max, dist2_rn( src( sj, 0 ), src( sj, 1 ), src( sj, 2 ), tx, ty, tz ) );
