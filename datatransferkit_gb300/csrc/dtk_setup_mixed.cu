@@ -336,7 +336,7 @@ __global__ void __launch_bounds__( SMX, 8 )
             tl[d] = __double2float_rn( t3[d] - (double)th[d] );
         }
         unsigned bad_rows = 0;
-#pragma unroll 4
+#pragma unroll 2
         for ( int t = 0; t < 32; ++t )
         {
             int const lt = __shfl_sync( FULL, len, t );
