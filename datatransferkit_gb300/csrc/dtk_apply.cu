@@ -8,9 +8,10 @@
 // into one kernel that reads idx/coeff once and writes each target once.
 //
 // Rows of equal length R with R % 4 == 0 and R/4 a power of two (kNN rows,
-// e.g. R = 32) use R/4 lanes per row with 128-bit loads: int4 of indices and
-// two double2 (FP64 form) or one float4 (mixed form) of coefficients, then a
-// shuffle reduction.  Other rows use S lanes per row (S a power of two chosen
+// e.g. R = 32) use R/8 lanes per row (8 entries each; R/4 lanes of 4 for
+// FP64 coefficients) with 128-bit loads:
+// int4 of indices and two double2 (FP64 form) or one float4 (mixed form) of
+// coefficients per 4 entries, then a shuffle reduction.  Other rows use S lanes per row (S a power of two chosen
 // from the mean row length) with coalesced scalar loads.  Source values are
 // gathered through the read-only path; at 8M sources they are 64 MB and stay
 // resident in the 129 MB L2 while the CSR streams from HBM.
@@ -34,35 +35,40 @@ __device__ __forceinline__ double group_sum( double v )
     return v;
 }
 
-// L lanes per row, each lane 4 consecutive entries.
-template <int L, bool F32>
+// L lanes per row, each lane EPL consecutive entries (EPL a multiple of 4).
+template <int L, int EPL, bool F32>
 __global__ void __launch_bounds__( 256 )
     k_apply_vec( int64_t n_tgt, int32_t const *__restrict__ idx,
                  void const *__restrict__ coeff, double const *__restrict__ values,
                  double *__restrict__ target )
 {
-    constexpr int R = 4 * L;
+    constexpr int R = EPL * L;
     int64_t const gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int64_t const row = gt / L;
     int const sub = (int)( gt % L );
     double acc = 0.0;
     if ( row < n_tgt )
     {
-        int64_t const e = row * R + 4 * sub;
-        int4 const ix = __ldcs( reinterpret_cast<int4 const *>( idx + e ) );
-        if constexpr ( F32 )
+#pragma unroll
+        for ( int q = 0; q < EPL; q += 4 )
         {
-            float4 const c = __ldcs( reinterpret_cast<float4 const *>( static_cast<float const *>( coeff ) + e ) );
-            acc = (double)c.x * __ldg( values + ix.x ) + (double)c.y * __ldg( values + ix.y ) +
-                  (double)c.z * __ldg( values + ix.z ) + (double)c.w * __ldg( values + ix.w );
-        }
-        else
-        {
-            double const *cp = static_cast<double const *>( coeff ) + e;
-            double2 const c0 = __ldcs( reinterpret_cast<double2 const *>( cp ) );
-            double2 const c1 = __ldcs( reinterpret_cast<double2 const *>( cp + 2 ) );
-            acc = c0.x * __ldg( values + ix.x ) + c0.y * __ldg( values + ix.y ) +
-                  c1.x * __ldg( values + ix.z ) + c1.y * __ldg( values + ix.w );
+            int64_t const e = row * R + EPL * sub + q;
+            int4 const ix = __ldcs( reinterpret_cast<int4 const *>( idx + e ) );
+            if constexpr ( F32 )
+            {
+                float4 const c =
+                    __ldcs( reinterpret_cast<float4 const *>( static_cast<float const *>( coeff ) + e ) );
+                acc += (double)c.x * __ldg( values + ix.x ) + (double)c.y * __ldg( values + ix.y ) +
+                       (double)c.z * __ldg( values + ix.z ) + (double)c.w * __ldg( values + ix.w );
+            }
+            else
+            {
+                double const *cp = static_cast<double const *>( coeff ) + e;
+                double2 const c0 = __ldcs( reinterpret_cast<double2 const *>( cp ) );
+                double2 const c1 = __ldcs( reinterpret_cast<double2 const *>( cp + 2 ) );
+                acc += c0.x * __ldg( values + ix.x ) + c0.y * __ldg( values + ix.y ) +
+                       c1.x * __ldg( values + ix.z ) + c1.y * __ldg( values + ix.w );
+            }
         }
     }
     acc = group_sum<L>( acc );
@@ -96,21 +102,43 @@ __global__ void __launch_bounds__( 256 )
         target[row] = acc;
 }
 
+// Row length R = 4 * 2^j (at most 128): R / EPL lanes per row, each EPL
+// entries (4 entries a lane for rows shorter than EPL).  FP32 coefficients
+// take EPL = 8 (one reduction level fewer: -9% at 8M x 32), FP64 ones 4
+// (twice the coefficient bytes a lane: +5% at 8).
 template <bool F32>
-void launch_vec( int L, int64_t n_tgt, int32_t const *idx, void const *coeff,
-                 double const *values, double *target, cudaStream_t s )
+constexpr int apply_epl()
 {
-    int64_t const threads = n_tgt * L;
-    unsigned const blocks = (unsigned)( ( threads + 255 ) / 256 );
+    return F32 ? 8 : 4;
+}
+
+template <int EPL, bool F32>
+void launch_vec_epl( int L, unsigned blocks, int64_t n_tgt, int32_t const *idx, void const *coeff,
+                     double const *values, double *target, cudaStream_t s )
+{
     switch ( L )
     {
-    case 1: k_apply_vec<1, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
-    case 2: k_apply_vec<2, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
-    case 4: k_apply_vec<4, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
-    case 8: k_apply_vec<8, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
-    case 16: k_apply_vec<16, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
-    default: k_apply_vec<32, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
+    case 1: k_apply_vec<1, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
+    case 2: k_apply_vec<2, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
+    case 4: k_apply_vec<4, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
+    case 8: k_apply_vec<8, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
+    case 16: k_apply_vec<16, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
+    default: k_apply_vec<32, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, idx, coeff, values, target ); break;
     }
+}
+
+template <bool F32>
+void launch_vec( int R, int64_t n_tgt, int32_t const *idx, void const *coeff,
+                 double const *values, double *target, cudaStream_t s )
+{
+    constexpr int EPL = apply_epl<F32>();
+    int const epl = R >= EPL ? EPL : 4;
+    int const L = R / epl;
+    unsigned const blocks = (unsigned)( ( n_tgt * L + 255 ) / 256 );
+    if ( epl == EPL )
+        launch_vec_epl<EPL, F32>( L, blocks, n_tgt, idx, coeff, values, target, s );
+    else
+        launch_vec_epl<4, F32>( L, blocks, n_tgt, idx, coeff, values, target, s );
     check_launch( "k_apply_vec" );
 }
 
@@ -205,9 +233,9 @@ void apply_csr( int64_t n_tgt, int32_t const *offset, int32_t const *idx, double
          uniform_row / 4 <= 32 )
     {
         if ( f32 )
-            launch_vec<true>( uniform_row / 4, n_tgt, idx, coeff, values, target, s );
+            launch_vec<true>( uniform_row, n_tgt, idx, coeff, values, target, s );
         else
-            launch_vec<false>( uniform_row / 4, n_tgt, idx, coeff, values, target, s );
+            launch_vec<false>( uniform_row, n_tgt, idx, coeff, values, target, s );
         return;
     }
     int const len = uniform_row > 0 ? uniform_row : mean_row;
