@@ -26,7 +26,7 @@ EXPORTED = [
     "dtk_mls_batch_get_csr", "dtk_mls_batch_destroy", "dtk_mls_batch_get_stage_times", "dtk_last_error", "dtk_status_string",
     "dtk_kernel_launch_count", "dtk_svd_pinv_noalloc", "dtk_mls_apply_multi", "dtk_nn_create",
     "dtk_nn_apply", "dtk_nn_apply_multi", "dtk_nn_get_indices", "dtk_nn_destroy",
-    "dtk_mls_export_size", "dtk_mls_export", "dtk_mls_import",
+    "dtk_mls_export_size", "dtk_mls_export", "dtk_mls_import", "dtk_release_cached_memory",
 ]
 
 
@@ -73,6 +73,7 @@ def _declare(L):
     L.dtk_mls_get_search_times.argtypes = [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.dtk_mls_get_rotation_count.argtypes = [_vp, C.POINTER(_i64), C.POINTER(_i64)]
     L.dtk_kernel_launch_count.argtypes = []
+    L.dtk_release_cached_memory.argtypes = []
     L.dtk_mls_destroy.argtypes = [_vp]
     L.dtk_knn_search.argtypes = [_vp, _i64, _i64, _i64, _vp, _i64, _i64, _i64, C.c_int32, _vp, _vp, _vp]
     L.dtk_svd_pinv.argtypes = [C.c_int32, _i64, _vp, _vp, C.POINTER(_i64), _vp]

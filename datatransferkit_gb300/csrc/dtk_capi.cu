@@ -11,6 +11,7 @@
 
 #include <cmath>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -29,6 +30,36 @@ long long &launch_counter()
 {
     static long long n = 0;
     return n;
+}
+
+namespace
+{
+std::mutex g_pool_mutex;
+std::vector<cudaMemPool_t> g_pools; // per device, created on first use
+} // namespace
+
+cudaMemPool_t device_pool()
+{
+    int dev = 0;
+    DTK_CUDA_OR_THROW( cudaGetDevice( &dev ) );
+    std::lock_guard<std::mutex> lock( g_pool_mutex );
+    if ( g_pools.size() <= (size_t)dev )
+        g_pools.resize( dev + 1, nullptr );
+    if ( !g_pools[dev] )
+    {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        DTK_CUDA_OR_THROW( cudaMemPoolCreate( &pool, &props ) );
+        size_t free_b = 0, total_b = 0;
+        DTK_CUDA_OR_THROW( cudaMemGetInfo( &free_b, &total_b ) );
+        unsigned long long keep = total_b / 8;
+        DTK_CUDA_OR_THROW( cudaMemPoolSetAttribute( pool, cudaMemPoolAttrReleaseThreshold, &keep ) );
+        g_pools[dev] = pool;
+    }
+    return g_pools[dev];
 }
 
 __global__ void k_fill_uniform_offsets( int32_t *offset, int64_t n_tgt, int row )
@@ -371,6 +402,16 @@ dtk_status dtk_mls_get_rotation_count( dtk_mls_handle h, int64_t *rotations,
 }
 
 int64_t dtk_kernel_launch_count( void ) { return launch_counter(); }
+
+dtk_status dtk_release_cached_memory( void )
+{
+    return guarded( [&] {
+        std::lock_guard<std::mutex> lock( g_pool_mutex );
+        for ( cudaMemPool_t pool : g_pools )
+            if ( pool )
+                DTK_CUDA_OR_THROW( cudaMemPoolTrimTo( pool, 0 ) );
+    } );
+}
 
 dtk_status dtk_mls_destroy( dtk_mls_handle h )
 {

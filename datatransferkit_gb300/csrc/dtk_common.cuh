@@ -85,7 +85,13 @@ inline void validate_points( double const *p, int64_t n, int64_t ps, int64_t ds,
                           std::string( what ) + " strides are zero" );
 }
 
-// Stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync).
+// The library's stream-ordered memory pool on the current device: freed
+// blocks stay cached across synchronizations up to 1/8 of the device's
+// memory (the default pool returns them at every synchronization, and the
+// next create pays to map them again); dtk_release_cached_memory trims it.
+cudaMemPool_t device_pool();
+
+// Stream-ordered device buffer from the library's pool (cudaFreeAsync frees).
 template <class T>
 struct DeviceBuffer
 {
@@ -116,7 +122,7 @@ struct DeviceBuffer
         stream = s;
         n = count;
         if ( count )
-            DTK_CUDA_OR_THROW( cudaMallocAsync( (void **)&ptr, count * sizeof( T ), s ) );
+            DTK_CUDA_OR_THROW( cudaMallocFromPoolAsync( (void **)&ptr, count * sizeof( T ), device_pool(), s ) );
     }
     void release()
     {

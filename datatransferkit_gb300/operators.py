@@ -489,6 +489,14 @@ def kernel_launch_count() -> int:
     return int(lib().dtk_kernel_launch_count())
 
 
+def release_cached_memory() -> None:
+    """Return the device memory cached in the library's pools to the driver
+    (memory that live operators own stays); the pools keep freed blocks, up
+    to 1/8 of a device's memory, so that repeated setups need not map memory
+    again."""
+    check(lib().dtk_release_cached_memory())
+
+
 def knn_search(source_points: torch.Tensor, target_points: torch.Tensor, k: int, stream=None):
     """(offset, indices) of the k nearest sources per target by (d2, index)."""
     src = _check_points(source_points, "source_points")

@@ -159,6 +159,14 @@ dtk_status dtk_mls_get_rotation_count(dtk_mls_handle h, int64_t *rotations,
  * (diagnostics; not a reference interface). */
 int64_t dtk_kernel_launch_count(void);
 
+/* Device memory: the library allocates its handles' buffers and its scratch
+ * in its own stream-ordered pool, one per device, which keeps freed blocks
+ * cached across synchronizations (up to 1/8 of the device's memory) so that
+ * repeated setups do not map memory again.  This returns the cached blocks
+ * of every device's pool to the driver; memory that live handles own stays.
+ * No counterpart in the reference (Kokkos manages its own memory). */
+dtk_status dtk_release_cached_memory(void);
+
 dtk_status dtk_mls_destroy(dtk_mls_handle h);
 
 /* ---- search only (the ArborX query the constructor runs,
