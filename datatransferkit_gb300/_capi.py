@@ -27,6 +27,7 @@ EXPORTED = [
     "dtk_kernel_launch_count", "dtk_svd_pinv_noalloc", "dtk_mls_apply_multi", "dtk_nn_create",
     "dtk_nn_apply", "dtk_nn_apply_multi", "dtk_nn_get_indices", "dtk_nn_destroy",
     "dtk_mls_export_size", "dtk_mls_export", "dtk_mls_import", "dtk_release_cached_memory",
+    "dtk_mls_transfer_host",
 ]
 
 
@@ -74,6 +75,8 @@ def _declare(L):
     L.dtk_mls_get_rotation_count.argtypes = [_vp, C.POINTER(_i64), C.POINTER(_i64)]
     L.dtk_kernel_launch_count.argtypes = []
     L.dtk_release_cached_memory.argtypes = []
+    L.dtk_mls_transfer_host.argtypes = [C.POINTER(Options), _vp, _i64, _vp, _i64, _vp, _vp, _vp,
+                                        C.POINTER(_vp)]
     L.dtk_mls_destroy.argtypes = [_vp]
     L.dtk_knn_search.argtypes = [_vp, _i64, _i64, _i64, _vp, _i64, _i64, _i64, C.c_int32, _vp, _vp, _vp]
     L.dtk_svd_pinv.argtypes = [C.c_int32, _i64, _vp, _vp, C.POINTER(_i64), _vp]

@@ -122,6 +122,157 @@ Geometry check_options( dtk_mls_options const *o )
 
 using namespace dtk;
 
+namespace dtk
+{
+// The create's work on stream s, for validated points; the targets are read
+// only after `tgt_ready` (when not null) has fired.  Returns the handle.
+std::unique_ptr<dtk_mls_s> create_impl( Geometry const &g, dtk_mls_options const *opts, PointsView sv,
+                                        PointsView tv, cudaStream_t s, cudaEvent_t tgt_ready )
+{
+    int64_t const n_src = sv.n, n_tgt = tv.n;
+    auto h = new dtk_mls_s();
+    std::unique_ptr<dtk_mls_s> guard( h );
+    h->opts = *opts;
+    h->n_src = n_src;
+    h->n_tgt = n_tgt;
+    h->m = g.m;
+    if ( opts->keep_points )
+    {
+        if ( tgt_ready )
+            DTK_CUDA_OR_THROW( cudaStreamWaitEvent( s, tgt_ready, 0 ) );
+        // packed n x 3 copies for the coordinate adjoint
+        h->src_copy.allocate( 3 * n_src, s );
+        h->tgt_copy.allocate( std::max<int64_t>( 1, 3 * n_tgt ), s );
+        k_pack_points<<<(unsigned)( ( n_src + 255 ) / 256 ), 256, 0, s>>>( sv, h->src_copy.get() );
+        check_launch( "k_pack_points" );
+        if ( n_tgt )
+        {
+            k_pack_points<<<(unsigned)( ( n_tgt + 255 ) / 256 ), 256, 0, s>>>( tv, h->tgt_copy.get() );
+            check_launch( "k_pack_points" );
+        }
+    }
+
+    cudaEvent_t ev[4];
+    for ( auto &e : ev )
+        DTK_CUDA_OR_THROW( cudaEventCreate( &e ) );
+    struct EvGuard
+    {
+        cudaEvent_t *e;
+        ~EvGuard()
+        {
+            for ( int i = 0; i < 4; ++i )
+                cudaEventDestroy( e[i] );
+        }
+    } evg{ev};
+    DeviceBuffer<unsigned> status( 1, s );
+    DeviceBuffer<unsigned long long> counters( 3, s );
+    DTK_CUDA_OR_THROW( cudaMemsetAsync( status.get(), 0, sizeof( unsigned ), s ) );
+    DTK_CUDA_OR_THROW( cudaMemsetAsync( counters.get(), 0, 3 * sizeof( unsigned long long ), s ) );
+    DTK_CUDA_OR_THROW( cudaEventRecord( ev[0], s ) );
+
+    // --- search (ArborX tree + query, def.hpp:114-129) ---
+    Lbvh tree;
+    build_lbvh( sv, tree, status.get(), s );
+    if ( tgt_ready ) // the targets arrive while the tree is built
+        DTK_CUDA_OR_THROW( cudaStreamWaitEvent( s, tgt_ready, 0 ) );
+    sort_queries( tree, tv, h->order, s );
+    DTK_CUDA_OR_THROW( cudaEventRecord( ev[3], s ) );
+    h->offset.allocate( n_tgt + 1, s );
+    if ( !g.radius_mode )
+    {
+        int const row = (int)std::min<int64_t>( g.k, n_src );
+        DTK_REQUIRE_OR_THROW( n_tgt * (int64_t)row <= INT32_MAX,
+                              "n_targets * k exceeds int32 CSR offsets" );
+        h->uniform_row = row;
+        h->mean_row = row;
+        h->nnz = n_tgt * (int64_t)row;
+        k_fill_uniform_offsets<<<(unsigned)( ( n_tgt + 256 ) / 256 ), 256, 0, s>>>(
+            h->offset.get(), n_tgt, row );
+        check_launch( "k_fill_uniform_offsets" );
+        h->idx.allocate( std::max<int64_t>( 1, h->nnz ), s );
+        knn_query( tree, tv, h->order.get(), g.k, GroupArgs{}, h->offset.get(), h->idx.get(), status.get(), s );
+    }
+    else
+    {
+        DeviceBuffer<int64_t> counts( std::max<int64_t>( 1, n_tgt ), s ),
+            offs( n_tgt + 1, s );
+        radius_count( tree, tv, h->order.get(), g.opts.radius, GroupArgs{}, counts.get(), status.get(), s );
+        exclusive_scan_i64( counts.get(), offs.get(), n_tgt, s );
+        int64_t total = 0;
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( &total, offs.get() + n_tgt, sizeof( int64_t ),
+                                            cudaMemcpyDeviceToHost, s ) );
+        DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+        DTK_REQUIRE_OR_THROW( total <= INT32_MAX, "neighbour count exceeds int32 CSR offsets" );
+        h->nnz = total;
+        h->mean_row = n_tgt ? (int)( ( total + n_tgt - 1 ) / n_tgt ) : 0;
+        k_narrow_offsets<<<(unsigned)( ( n_tgt + 256 ) / 256 ), 256, 0, s>>>( offs.get(),
+                                                                              h->offset.get(), n_tgt );
+        check_launch( "k_narrow_offsets" );
+        h->idx.allocate( std::max<int64_t>( 1, total ), s );
+        radius_fill( tree, tv, h->order.get(), g.opts.radius, GroupArgs{}, h->offset.get(), h->idx.get(),
+                     status.get(), s );
+    }
+    DTK_CUDA_OR_THROW( cudaEventRecord( ev[1], s ) );
+
+    // --- setup numerics (def.hpp:136-185) ---
+    SetupArgs a{};
+    a.src = sv;
+    a.tgt = tv;
+    a.offset = h->offset.get();
+    a.idx = h->idx.get();
+    a.order = h->order.get();
+    a.n_tgt = n_tgt;
+    a.rbf = g.opts.rbf;
+    a.basis = g.opts.basis;
+    a.rows_sorted = !g.radius_mode;
+    a.underdetermined = counters.get();
+    a.rotations = counters.get() + 1;
+    a.rotations32 = counters.get() + 2;
+    a.status = status.get();
+    if ( g.opts.precision == DTK_FP64 )
+    {
+        h->coeff64.allocate( std::max<int64_t>( 1, h->nnz ), s );
+        a.coeff64 = h->coeff64.get();
+    }
+    else
+    {
+        h->coeff32.allocate( std::max<int64_t>( 1, h->nnz ), s );
+        a.coeff32 = h->coeff32.get();
+    }
+    if ( g.radius_mode )
+        // radius rows are uneven (0 to thousands of entries): the split
+        // setup with 8 or 32 lanes per target by row length
+        run_setup_plan( a, g.opts.precision, nullptr, nullptr, nullptr, true, s );
+    else if ( g.opts.precision == DTK_FP64 )
+        setup_fp64( a, s );
+    else
+        setup_mixed( a, s );
+    DTK_CUDA_OR_THROW( cudaEventRecord( ev[2], s ) );
+
+    unsigned st = 0;
+    unsigned long long cnt[3] = {0, 0, 0};
+    DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, status.get(), sizeof( unsigned ),
+                                        cudaMemcpyDeviceToHost, s ) );
+    DTK_CUDA_OR_THROW( cudaMemcpyAsync( cnt, counters.get(), sizeof( cnt ),
+                                        cudaMemcpyDeviceToHost, s ) );
+    // Release the tree and scratch before returning (stream ordered).
+    tree = Lbvh();
+    DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+    if ( st & DEV_TIMEOUT )
+        throw Error{DTK_ERR_TIMEOUT, "a Jacobi iteration hit its iteration cap"};
+    if ( st )
+        throw Error{DTK_ERR_INTERNAL, "search traversal reported an internal error"};
+    h->underdetermined = (int64_t)cnt[0];
+    h->rotations = (int64_t)cnt[1];
+    h->rotations32 = (int64_t)cnt[2];
+    DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->search_ms, ev[0], ev[1] ) );
+    DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->setup_ms, ev[1], ev[2] ) );
+    DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->build_ms, ev[0], ev[3] ) );
+    DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->query_ms, ev[3], ev[1] ) );
+    return guard;
+}
+} // namespace dtk
+
 extern "C" {
 
 void dtk_mls_default_options( dtk_mls_options *o )
@@ -168,144 +319,9 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
         // DTK_CHECK( !search_tree.empty() ), DTK_MovingLeastSquaresOperator_def.hpp:116
         DTK_REQUIRE_OR_THROW( n_src > 0, "the source point cloud is empty" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
-        auto h = new dtk_mls_s();
-        std::unique_ptr<dtk_mls_s> guard( h );
-        h->opts = *opts;
-        h->n_src = n_src;
-        h->n_tgt = n_tgt;
-        h->m = g.m;
         PointsView const sv{src, n_src, src_pt_stride, src_dim_stride};
         PointsView const tv{tgt, n_tgt, tgt_pt_stride, tgt_dim_stride};
-        if ( opts->keep_points )
-        {
-            // packed n x 3 copies for the coordinate adjoint
-            h->src_copy.allocate( 3 * n_src, s );
-            h->tgt_copy.allocate( std::max<int64_t>( 1, 3 * n_tgt ), s );
-            k_pack_points<<<(unsigned)( ( n_src + 255 ) / 256 ), 256, 0, s>>>( sv, h->src_copy.get() );
-            check_launch( "k_pack_points" );
-            if ( n_tgt )
-            {
-                k_pack_points<<<(unsigned)( ( n_tgt + 255 ) / 256 ), 256, 0, s>>>( tv, h->tgt_copy.get() );
-                check_launch( "k_pack_points" );
-            }
-        }
-
-        cudaEvent_t ev[4];
-        for ( auto &e : ev )
-            DTK_CUDA_OR_THROW( cudaEventCreate( &e ) );
-        struct EvGuard
-        {
-            cudaEvent_t *e;
-            ~EvGuard()
-            {
-                for ( int i = 0; i < 4; ++i )
-                    cudaEventDestroy( e[i] );
-            }
-        } evg{ev};
-        DeviceBuffer<unsigned> status( 1, s );
-        DeviceBuffer<unsigned long long> counters( 3, s );
-        DTK_CUDA_OR_THROW( cudaMemsetAsync( status.get(), 0, sizeof( unsigned ), s ) );
-        DTK_CUDA_OR_THROW( cudaMemsetAsync( counters.get(), 0, 3 * sizeof( unsigned long long ), s ) );
-        DTK_CUDA_OR_THROW( cudaEventRecord( ev[0], s ) );
-
-        // --- search (ArborX tree + query, def.hpp:114-129) ---
-        Lbvh tree;
-        build_lbvh( sv, tree, status.get(), s );
-        sort_queries( tree, tv, h->order, s );
-        DTK_CUDA_OR_THROW( cudaEventRecord( ev[3], s ) );
-        h->offset.allocate( n_tgt + 1, s );
-        if ( !g.radius_mode )
-        {
-            int const row = (int)std::min<int64_t>( g.k, n_src );
-            DTK_REQUIRE_OR_THROW( n_tgt * (int64_t)row <= INT32_MAX,
-                                  "n_targets * k exceeds int32 CSR offsets" );
-            h->uniform_row = row;
-            h->mean_row = row;
-            h->nnz = n_tgt * (int64_t)row;
-            k_fill_uniform_offsets<<<(unsigned)( ( n_tgt + 256 ) / 256 ), 256, 0, s>>>(
-                h->offset.get(), n_tgt, row );
-            check_launch( "k_fill_uniform_offsets" );
-            h->idx.allocate( std::max<int64_t>( 1, h->nnz ), s );
-            knn_query( tree, tv, h->order.get(), g.k, GroupArgs{}, h->offset.get(), h->idx.get(), status.get(), s );
-        }
-        else
-        {
-            DeviceBuffer<int64_t> counts( std::max<int64_t>( 1, n_tgt ), s ),
-                offs( n_tgt + 1, s );
-            radius_count( tree, tv, h->order.get(), g.opts.radius, GroupArgs{}, counts.get(), status.get(), s );
-            exclusive_scan_i64( counts.get(), offs.get(), n_tgt, s );
-            int64_t total = 0;
-            DTK_CUDA_OR_THROW( cudaMemcpyAsync( &total, offs.get() + n_tgt, sizeof( int64_t ),
-                                                cudaMemcpyDeviceToHost, s ) );
-            DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
-            DTK_REQUIRE_OR_THROW( total <= INT32_MAX, "neighbour count exceeds int32 CSR offsets" );
-            h->nnz = total;
-            h->mean_row = n_tgt ? (int)( ( total + n_tgt - 1 ) / n_tgt ) : 0;
-            k_narrow_offsets<<<(unsigned)( ( n_tgt + 256 ) / 256 ), 256, 0, s>>>( offs.get(),
-                                                                                  h->offset.get(), n_tgt );
-            check_launch( "k_narrow_offsets" );
-            h->idx.allocate( std::max<int64_t>( 1, total ), s );
-            radius_fill( tree, tv, h->order.get(), g.opts.radius, GroupArgs{}, h->offset.get(), h->idx.get(),
-                         status.get(), s );
-        }
-        DTK_CUDA_OR_THROW( cudaEventRecord( ev[1], s ) );
-
-        // --- setup numerics (def.hpp:136-185) ---
-        SetupArgs a{};
-        a.src = sv;
-        a.tgt = tv;
-        a.offset = h->offset.get();
-        a.idx = h->idx.get();
-        a.order = h->order.get();
-        a.n_tgt = n_tgt;
-        a.rbf = g.opts.rbf;
-        a.basis = g.opts.basis;
-        a.rows_sorted = !g.radius_mode;
-        a.underdetermined = counters.get();
-        a.rotations = counters.get() + 1;
-        a.rotations32 = counters.get() + 2;
-        a.status = status.get();
-        if ( g.opts.precision == DTK_FP64 )
-        {
-            h->coeff64.allocate( std::max<int64_t>( 1, h->nnz ), s );
-            a.coeff64 = h->coeff64.get();
-        }
-        else
-        {
-            h->coeff32.allocate( std::max<int64_t>( 1, h->nnz ), s );
-            a.coeff32 = h->coeff32.get();
-        }
-        if ( g.radius_mode )
-            // radius rows are uneven (0 to thousands of entries): the split
-            // setup with 8 or 32 lanes per target by row length
-            run_setup_plan( a, g.opts.precision, nullptr, nullptr, nullptr, true, s );
-        else if ( g.opts.precision == DTK_FP64 )
-            setup_fp64( a, s );
-        else
-            setup_mixed( a, s );
-        DTK_CUDA_OR_THROW( cudaEventRecord( ev[2], s ) );
-
-        unsigned st = 0;
-        unsigned long long cnt[3] = {0, 0, 0};
-        DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, status.get(), sizeof( unsigned ),
-                                            cudaMemcpyDeviceToHost, s ) );
-        DTK_CUDA_OR_THROW( cudaMemcpyAsync( cnt, counters.get(), sizeof( cnt ),
-                                            cudaMemcpyDeviceToHost, s ) );
-        // Release the tree and scratch before returning (stream ordered).
-        tree = Lbvh();
-        DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
-        if ( st & DEV_TIMEOUT )
-            throw Error{DTK_ERR_TIMEOUT, "a Jacobi iteration hit its iteration cap"};
-        if ( st )
-            throw Error{DTK_ERR_INTERNAL, "search traversal reported an internal error"};
-        h->underdetermined = (int64_t)cnt[0];
-        h->rotations = (int64_t)cnt[1];
-        h->rotations32 = (int64_t)cnt[2];
-        DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->search_ms, ev[0], ev[1] ) );
-        DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->setup_ms, ev[1], ev[2] ) );
-        DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->build_ms, ev[0], ev[3] ) );
-        DTK_CUDA_OR_THROW( cudaEventElapsedTime( &h->query_ms, ev[3], ev[1] ) );
-        *out = guard.release();
+        *out = create_impl( g, opts, sv, tv, s, nullptr ).release();
     } );
 }
 
@@ -324,6 +340,97 @@ dtk_status dtk_mls_apply( dtk_mls_handle h, const double *source_values, int64_t
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
         apply_csr( h->n_tgt, h->offset.get(), h->idx.get(), h->coeff64.get(), h->coeff32.get(),
                    h->uniform_row, h->mean_row, source_values, target_values, s );
+    } );
+}
+
+dtk_status dtk_mls_transfer_host( const dtk_mls_options *opts, const double *src_host, int64_t n_src,
+                                  const double *tgt_host, int64_t n_tgt, const double *values_host,
+                                  double *target_values_host, dtk_stream_t stream_, dtk_mls_handle *out )
+{
+    return guarded( [&] {
+        if ( out )
+            *out = nullptr;
+        Geometry const g = check_options( opts );
+        validate_points( src_host, n_src, 3, 1, "source points" );
+        validate_points( tgt_host, n_tgt, 3, 1, "target points" );
+        DTK_REQUIRE_OR_THROW( n_src > 0, "the source point cloud is empty" );
+        DTK_REQUIRE_OR_THROW( values_host != nullptr, "source values are null" );
+        DTK_REQUIRE_OR_THROW( n_tgt == 0 || target_values_host != nullptr, "target values are null" );
+        cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        // the side stream carries the target and value copies in and the
+        // result slices out
+        struct Side
+        {
+            cudaStream_t s2 = nullptr;
+            std::vector<cudaEvent_t> ev;
+            ~Side()
+            {
+                for ( cudaEvent_t e : ev )
+                    cudaEventDestroy( e );
+                if ( s2 )
+                    cudaStreamDestroy( s2 );
+            }
+            cudaEvent_t event()
+            {
+                cudaEvent_t e = nullptr;
+                DTK_CUDA_OR_THROW( cudaEventCreateWithFlags( &e, cudaEventDisableTiming ) );
+                ev.push_back( e );
+                return e;
+            }
+        } side;
+        DTK_CUDA_OR_THROW( cudaStreamCreateWithFlags( &side.s2, cudaStreamNonBlocking ) );
+        DeviceBuffer<double> d_src( 3 * n_src, s ), d_tgt( std::max<int64_t>( 1, 3 * n_tgt ), s ),
+            d_vals( n_src, s ), d_out( std::max<int64_t>( 1, n_tgt ), s );
+        cudaEvent_t const allocated = side.event(), tgt_ready = side.event(), vals_ready = side.event();
+        DTK_CUDA_OR_THROW( cudaEventRecord( allocated, s ) );
+        DTK_CUDA_OR_THROW( cudaStreamWaitEvent( side.s2, allocated, 0 ) );
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( d_src.get(), src_host, 3 * n_src * sizeof( double ),
+                                            cudaMemcpyHostToDevice, s ) );
+        if ( n_tgt )
+            DTK_CUDA_OR_THROW( cudaMemcpyAsync( d_tgt.get(), tgt_host, 3 * n_tgt * sizeof( double ),
+                                                cudaMemcpyHostToDevice, side.s2 ) );
+        DTK_CUDA_OR_THROW( cudaEventRecord( tgt_ready, side.s2 ) );
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( d_vals.get(), values_host, n_src * sizeof( double ),
+                                            cudaMemcpyHostToDevice, side.s2 ) );
+        DTK_CUDA_OR_THROW( cudaEventRecord( vals_ready, side.s2 ) );
+        PointsView const sv{d_src.get(), n_src, 3, 1};
+        PointsView const tv{d_tgt.get(), n_tgt, 3, 1};
+        std::unique_ptr<dtk_mls_s> h = create_impl( g, opts, sv, tv, s, tgt_ready );
+        DTK_CUDA_OR_THROW( cudaStreamWaitEvent( s, vals_ready, 0 ) );
+        // the apply in row slices; each slice's results go back while the
+        // next one computes
+        int64_t const slices = n_tgt >= ( int64_t( 1 ) << 20 ) ? 8 : 1;
+        int64_t const per = ( n_tgt + slices - 1 ) / std::max<int64_t>( 1, slices );
+        int const R = h->uniform_row;
+        for ( int64_t r0 = 0; r0 < n_tgt; r0 += per )
+        {
+            int64_t const r1 = std::min( n_tgt, r0 + per );
+            if ( R > 0 ) // uniform rows: offset[i] = i R also indexes the shifted slice
+                apply_csr( r1 - r0, h->offset.get(), h->idx.get() + r0 * R,
+                           h->coeff64.get() ? h->coeff64.get() + r0 * R : nullptr,
+                           h->coeff32.get() ? h->coeff32.get() + r0 * R : nullptr, R, h->mean_row,
+                           d_vals.get(), d_out.get() + r0, s );
+            else // absolute offsets into the whole arrays
+                apply_csr( r1 - r0, h->offset.get() + r0, h->idx.get(), h->coeff64.get(), h->coeff32.get(), 0,
+                           h->mean_row, d_vals.get(), d_out.get() + r0, s );
+            cudaEvent_t const done = side.event();
+            DTK_CUDA_OR_THROW( cudaEventRecord( done, s ) );
+            DTK_CUDA_OR_THROW( cudaStreamWaitEvent( side.s2, done, 0 ) );
+            DTK_CUDA_OR_THROW( cudaMemcpyAsync( target_values_host + r0, d_out.get() + r0,
+                                                ( r1 - r0 ) * sizeof( double ), cudaMemcpyDeviceToHost,
+                                                side.s2 ) );
+        }
+        // the buffers are freed on s: after the last copy out
+        cudaEvent_t const copied = side.event();
+        DTK_CUDA_OR_THROW( cudaEventRecord( copied, side.s2 ) );
+        DTK_CUDA_OR_THROW( cudaStreamWaitEvent( s, copied, 0 ) );
+        d_src = DeviceBuffer<double>();
+        d_tgt = DeviceBuffer<double>();
+        d_vals = DeviceBuffer<double>();
+        d_out = DeviceBuffer<double>();
+        DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+        if ( out )
+            *out = h.release();
     } );
 }
 

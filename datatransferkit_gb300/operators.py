@@ -178,6 +178,50 @@ class MovingLeastSquaresOperator(PointCloudOperator):
         self.n_source_points = int(src.shape[0])
         self.n_target_points = int(tgt.shape[0])
 
+    @classmethod
+    def transfer_host(cls, comm, source_points, target_points, source_values, target_values,
+                      rbf=None, basis=None, *, k: int | None = None, radius: float | None = None,
+                      precision="fp64", keep: bool = False, stream=None):
+        """Setup and one apply from HOST tensors (float64, contiguous: points
+        (n, 3), values (n,)), with the copies overlapping the work (pinned
+        tensors for asynchronous copies); writes ``target_values`` in place.
+        Returns the operator when ``keep`` (for further device applies)."""
+        basis = basis or MultivariatePolynomialBasis(Linear, 3)
+        rbf = rbf or Wendland(0)
+        for t, what, shape in ((source_points, "source_points", 2), (target_points, "target_points", 2),
+                               (source_values, "source_values", 1), (target_values, "target_values", 1)):
+            if not isinstance(t, torch.Tensor) or t.is_cuda or t.dtype != torch.float64:
+                raise _capi.InvalidArgument(1, f"{what} must be a float64 host tensor")
+            if t.dim() != shape or not t.is_contiguous():
+                raise _capi.InvalidArgument(1, f"{what} must be contiguous of rank {shape}")
+        if source_points.shape[1] != 3 or target_points.shape[1] != 3 or basis.dim != 3:
+            raise _capi.InvalidArgument(1, "source_points.extent(1) == 3")
+        if source_values.shape[0] != source_points.shape[0]:
+            raise _capi.InvalidArgument(1, "source_values.extent(0) == n_source_points")
+        if target_values.shape[0] != target_points.shape[0]:
+            raise _capi.InvalidArgument(1, "target_values.extent(0) == n_target_points")
+        o = Options()
+        lib().dtk_mls_default_options(C.byref(o))
+        o.rbf = rbf.id
+        o.basis = basis.id
+        o.k = 0 if k is None else int(k)
+        o.radius = 0.0 if radius is None else float(radius)
+        o.precision = _PRECISIONS[precision]
+        o.comm_size = _comm_size(comm)
+        h = C.c_void_p()
+        check(lib().dtk_mls_transfer_host(C.byref(o), source_points.data_ptr(), source_points.shape[0],
+                                          target_points.data_ptr(), target_points.shape[0],
+                                          source_values.data_ptr(), target_values.data_ptr(),
+                                          _stream(stream), C.byref(h) if keep else None))
+        if not keep:
+            return None
+        op = cls.__new__(cls)
+        op.polynomial_basis, op.radial_basis_function = basis, rbf
+        op.options, op._h, op._stream = o, h, stream
+        op.n_source_points = int(source_points.shape[0])
+        op.n_target_points = int(target_points.shape[0])
+        return op
+
     # -- reference API ------------------------------------------------------
     def apply(self, source_values: torch.Tensor, target_values: torch.Tensor, stream=None) -> None:
         """target_values = T source_values; rank-1 fields, or rank-2 (n, n_comp) fields

@@ -155,6 +155,25 @@ dtk_status dtk_mls_get_search_times(dtk_mls_handle h, float *build_ms,
 dtk_status dtk_mls_get_rotation_count(dtk_mls_handle h, int64_t *rotations,
                                       int64_t *rotations_fp32);
 
+/* Setup and apply in one call with HOST buffers (the constructor followed by
+ * one apply, for callers whose points and values live in host memory):
+ * src_host n_src x 3 and tgt_host n_tgt x 3 row-major points, values_host
+ * n_src source values in, target_values_host n_tgt values out.  The copies
+ * overlap the work: the targets and the values travel on a second stream
+ * while the tree is built, and the results come back in row slices while the
+ * apply finishes the rest.  The copies are asynchronous only from pinned
+ * host memory (cudaHostAlloc / cudaHostRegister); from pageable memory the
+ * results are the same.  Synchronous: returns after the results are in host
+ * memory.  When `out` is not NULL it receives the operator (for further
+ * applies on device buffers; destroy it with dtk_mls_destroy).  No
+ * counterpart in the reference (its operator takes device Views). */
+dtk_status dtk_mls_transfer_host(const dtk_mls_options *opts,
+                                 const double *src_host, int64_t n_src,
+                                 const double *tgt_host, int64_t n_tgt,
+                                 const double *values_host,
+                                 double *target_values_host,
+                                 dtk_stream_t stream, dtk_mls_handle *out);
+
 /* Running count of the kernels this library has launched in the process
  * (diagnostics; not a reference interface). */
 int64_t dtk_kernel_launch_count(void);
