@@ -327,13 +327,15 @@ void radix_sort_pairs( uint32_t *keys, uint32_t *values, int64_t n, int bits,
 struct Lbvh
 {
     int64_t n = 0;        // points
-    int64_t n_leaves = 0; // ceil(n / 32)
+    int64_t n_leaves = 0; // leaves: the Morton cells of at most 32 points
     double lo[3], hi[3];  // scene bounds (host copy)
     DeviceBuffer<double> sx, sy, sz;  // Morton-sorted coordinates
     DeviceBuffer<float> fx, fy, fz;   // the same, centred on the scene box, FP32
     DeviceBuffer<uint32_t> codes;     // Morton codes in sorted order
     DeviceBuffer<uint32_t> grp;       // group (problem) of each sorted point; empty if ungrouped
     DeviceBuffer<uint32_t> perm;      // sorted position -> original index
+    DeviceBuffer<int32_t> leaf_start; // first sorted position of each leaf, then n (n_leaves + 1)
+    DeviceBuffer<int32_t> leaf_of;    // leaf of each sorted position
     DeviceBuffer<float4> nodes;       // 4 float4 per binary internal node (released after the collapse)
     DeviceBuffer<float4> wide;        // 24 float4 per 8-wide node (the queries' tree)
     int64_t n_wide = 0;

@@ -238,25 +238,91 @@ __global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double cons
 }
 
 // ---------------------------------------------------------------------------
+// Leaves: the Morton cells of at most LEAF points.  Splitting the bit trie of
+// the sorted keys one bit at a time until a cell holds <= LEAF points keeps
+// every leaf inside one cell (compact boxes; a fixed bucket of 32 consecutive
+// points straddles cell boundaries and spans far more space): at 1M uniform
+// points, 44k leaves of 22.6 points on average, and a query ball meets 12 of
+// them instead of 22 buckets.
+// ---------------------------------------------------------------------------
+// Common-prefix length of the sorted keys of points j and j + 1 (key = group
+// << 32 | Morton code; equal keys are ranked by position, below every key bit,
+// as in the tree over the leaves).
+__device__ __forceinline__ unsigned long long point_key( uint32_t const *codes, uint32_t const *grp,
+                                                         int64_t p )
+{
+    unsigned long long k = codes[p];
+    if ( grp )
+        k |= (unsigned long long)grp[p] << 32;
+    return k;
+}
+
+__global__ void k_point_delta( uint32_t const *codes, uint32_t const *grp, int64_t n, int *dlt )
+{
+    int64_t const j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( j >= n - 1 )
+        return;
+    unsigned long long const a = point_key( codes, grp, j ), b = point_key( codes, grp, j + 1 );
+    dlt[j] = a != b ? __clzll( a ^ b ) : 64 + __clzll( (unsigned long long)( j ^ ( j + 1 ) ) );
+}
+
+// Position i (0 < i < n) starts a leaf when the smallest cell holding points
+// i - 1 and i has more than LEAF points: the points of that cell are the run
+// of adjacent pairs around (i - 1, i) whose common prefix is at least
+// dlt[i - 1], so the test counts at most LEAF pairs.  Position 0 starts the
+// first leaf.
+__global__ void k_leaf_flags( int const *dlt, int64_t n, int64_t *flag )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i >= n )
+        return;
+    if ( i == 0 )
+    {
+        flag[0] = 1;
+        return;
+    }
+    int const L = dlt[i - 1];
+    int run = 1;
+    for ( int64_t j = i - 2; j >= 0 && run < LEAF && dlt[j] >= L; --j )
+        ++run;
+    for ( int64_t j = i; j < n - 1 && run < LEAF && dlt[j] >= L; ++j )
+        ++run;
+    flag[i] = run >= LEAF ? 1 : 0;
+}
+
+// leaf_of[i] and leaf_start[] from the exclusive scan of the flags.
+__global__ void k_leaf_index( int64_t const *flag, int64_t const *scan, int64_t n, int32_t *leaf_of,
+                              int32_t *leaf_start )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i >= n )
+        return;
+    int64_t const leaf = scan[i] + flag[i] - 1;
+    leaf_of[i] = (int32_t)leaf;
+    if ( flag[i] )
+        leaf_start[scan[i]] = (int32_t)i;
+    if ( i == n - 1 )
+        leaf_start[leaf + 1] = (int32_t)n;
+}
+
+// ---------------------------------------------------------------------------
 // Karras hierarchy over leaf keys.
 // ---------------------------------------------------------------------------
 // Leaf key: (group of the leaf's first point, its Morton code); groups are
 // the problems of a batch (absent for a single operator).
 __device__ __forceinline__ unsigned long long leaf_key( uint32_t const *codes, uint32_t const *grp,
-                                                        int64_t leaf )
+                                                        int32_t const *leaf_start, int64_t leaf )
 {
-    unsigned long long k = codes[leaf * LEAF];
-    if ( grp )
-        k |= (unsigned long long)grp[leaf * LEAF] << 32;
-    return k;
+    return point_key( codes, grp, leaf_start[leaf] );
 }
 
-__device__ __forceinline__ int delta( uint32_t const *codes, uint32_t const *grp, int64_t nl,
-                                      int64_t i, int64_t j )
+__device__ __forceinline__ int delta( uint32_t const *codes, uint32_t const *grp, int32_t const *leaf_start,
+                                      int64_t nl, int64_t i, int64_t j )
 {
     if ( j < 0 || j >= nl )
         return -1;
-    unsigned long long const ki = leaf_key( codes, grp, i ), kj = leaf_key( codes, grp, j );
+    unsigned long long const ki = leaf_key( codes, grp, leaf_start, i ),
+                             kj = leaf_key( codes, grp, leaf_start, j );
     if ( ki != kj )
         return __clzll( ki ^ kj );
     // equal leaf keys: ranks by leaf index, always above any 64-bit key prefix
@@ -266,30 +332,31 @@ __device__ __forceinline__ int delta( uint32_t const *codes, uint32_t const *grp
 // Internal node i covers leaves [lo[i], hi[i]]; its left child covers
 // [lo, gamma] and its right child [gamma + 1, hi], gamma being the index of
 // the left child (leaf or internal, Karras 2012).
-__global__ void k_karras( uint32_t const *codes, uint32_t const *grp, int64_t nl, int *left,
+__global__ void k_karras( uint32_t const *codes, uint32_t const *grp, int32_t const *leaf_start, int64_t nl,
+                          int *left,
                           int *right, int *parent_node, int *parent_leaf, int *range_lo,
                           int *range_hi )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i >= nl - 1 )
         return;
-    int const d = ( delta( codes, grp, nl, i, i + 1 ) - delta( codes, grp, nl, i, i - 1 ) ) >= 0 ? 1 : -1;
-    int const dmin = delta( codes, grp, nl, i, i - d );
+    int const d = ( delta( codes, grp, leaf_start, nl, i, i + 1 ) - delta( codes, grp, leaf_start, nl, i, i - 1 ) ) >= 0 ? 1 : -1;
+    int const dmin = delta( codes, grp, leaf_start, nl, i, i - d );
     int64_t lmax = 2;
-    while ( delta( codes, grp, nl, i, i + lmax * d ) > dmin )
+    while ( delta( codes, grp, leaf_start, nl, i, i + lmax * d ) > dmin )
         lmax <<= 1;
     int64_t l = 0;
     for ( int64_t t = lmax >> 1; t >= 1; t >>= 1 )
-        if ( delta( codes, grp, nl, i, i + ( l + t ) * d ) > dmin )
+        if ( delta( codes, grp, leaf_start, nl, i, i + ( l + t ) * d ) > dmin )
             l += t;
     int64_t const j = i + l * d;
-    int const dnode = delta( codes, grp, nl, i, j );
+    int const dnode = delta( codes, grp, leaf_start, nl, i, j );
     int64_t s = 0;
     int64_t t = l;
     do
     {
         t = ( t + 1 ) >> 1;
-        if ( delta( codes, grp, nl, i, i + ( s + t ) * d ) > dnode )
+        if ( delta( codes, grp, leaf_start, nl, i, i + ( s + t ) * d ) > dnode )
             s += t;
     } while ( t > 1 );
     int64_t const gamma = i + s * d + min( d, 0 );
@@ -356,7 +423,7 @@ __device__ __forceinline__ Box load_child_box( float4 const *nodes, int parent, 
 // One thread per leaf: leaf box, then walk up; the second child to arrive at
 // a node computes its box and continues.
 __global__ void k_refit( double const *sx, double const *sy, double const *sz,
-                         double const *scene, int64_t n, int64_t nl, int const *left,
+                         double const *scene, int32_t const *leaf_start, int64_t nl, int const *left,
                          int const *right,
                          int const *parent_node, int const *parent_leaf, float4 *nodes,
                          unsigned *flags, float4 *root_box, unsigned *status )
@@ -364,10 +431,10 @@ __global__ void k_refit( double const *sx, double const *sy, double const *sz,
     int64_t const leaf = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( leaf >= nl )
         return;
-    double lo[3] = {sx[leaf * LEAF], sy[leaf * LEAF], sz[leaf * LEAF]};
+    int64_t const begin = leaf_start[leaf], end = leaf_start[leaf + 1];
+    double lo[3] = {sx[begin], sy[begin], sz[begin]};
     double hi[3] = {lo[0], lo[1], lo[2]};
-    int64_t const end = min( n, ( leaf + 1 ) * (int64_t)LEAF );
-    for ( int64_t p = leaf * LEAF + 1; p < end; ++p )
+    for ( int64_t p = begin + 1; p < end; ++p )
     {
         double const c[3] = {sx[p], sy[p], sz[p]};
 #pragma unroll
@@ -613,6 +680,7 @@ struct TreeView
     double const *sx, *sy, *sz;
     float const *fx, *fy, *fz;
     uint32_t const *codes, *perm;
+    int32_t const *leaf_start, *leaf_of;
     float4 const *wide; // 8-wide nodes (24 float4 each)
     double const *scene;
     int64_t n, nl, nw;
@@ -757,8 +825,8 @@ __device__ __forceinline__ Range query_range( TreeView const &tr, GroupView cons
     r.g = GROUPED ? (int)gv.tgt_grp[qi] : 0;
     r.ps = GROUPED ? gv.src_off[r.g] : 0;
     r.pe = GROUPED ? gv.src_off[r.g + 1] : tr.n;
-    r.lps = (int)( r.ps / LEAF );
-    r.lpe = r.pe > r.ps ? (int)( ( r.pe - 1 ) / LEAF ) : -1;
+    r.lps = GROUPED && r.pe > r.ps ? tr.leaf_of[r.ps] : 0;
+    r.lpe = GROUPED ? ( r.pe > r.ps ? tr.leaf_of[r.pe - 1] : -1 ) : (int)tr.nl - 1;
     return r;
 }
 
@@ -924,8 +992,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         kp = -1;
     }
     // the list's starting members by leaf and lane: a leaf screens them out
-    int seed_leaf = kp >= 0 ? kp / LEAF : -1;
-    unsigned seed_bit = kp >= 0 ? 1u << ( kp % LEAF ) : 0u;
+    int seed_leaf = kp >= 0 ? tr.leaf_of[kp] : -1;
+    unsigned seed_bit = kp >= 0 ? 1u << ( kp - tr.leaf_start[seed_leaf] ) : 0u;
     // speculative bound (seeded queries with full rows): boxes and points
     // beyond it are skipped as if the list were already that tight
     float spec = seeded && row == k ? next_spec : __int_as_float( 0x7f800000 );
@@ -1001,10 +1069,11 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     // bound cannot beat or tie it (screen_threshold keeps all the others);
     // the survivors queue for exact keys.
     auto process_leaf = [&]( int leaf ) {
-        int64_t const p = (int64_t)leaf * LEAF + lane;
+        int64_t const p = (int64_t)tr.leaf_start[leaf] + lane;
         bool surv = false;
         unsigned const seen = __reduce_or_sync( FULL, seed_leaf == leaf ? seed_bit : 0u );
-        if ( ( GROUPED ? p >= rg.ps : true ) && p < rg.pe && !( ( seen >> lane ) & 1u ) )
+        if ( ( GROUPED ? p >= rg.ps && p < rg.pe : true ) && p < tr.leaf_start[leaf + 1] &&
+             !( ( seen >> lane ) & 1u ) )
         {
             float const dx = __ldg( tr.fx + p ) - q.tf[0];
             float const dy = __ldg( tr.fy + p ) - q.tf[1];
@@ -1134,8 +1203,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         if ( !( spec < __int_as_float( 0x7f800000 ) ) ||
              bd <= (unsigned long long)__double_as_longlong( __dmul_rd( (double)spec, 1.0 - 0x1p-40 ) ) )
             break;
-        seed_leaf = kp >= 0 ? kp / LEAF : -1;
-        seed_bit = kp >= 0 ? 1u << ( kp % LEAF ) : 0u;
+        seed_leaf = kp >= 0 ? tr.leaf_of[kp] : -1;
+        seed_bit = kp >= 0 ? 1u << ( kp - tr.leaf_start[seed_leaf] ) : 0u;
         spec = __int_as_float( 0x7f800000 );
         bound_f = prune_threshold( bd );
         screen_f = screen_threshold( bound_f, q.err );
@@ -1177,9 +1246,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     int64_t const out_end = FILL ? offset[qi + 1] : 0;
 
     auto process_leaf = [&]( int leaf ) {
-        int64_t const p = (int64_t)leaf * LEAF + lane;
+        int64_t const p = (int64_t)tr.leaf_start[leaf] + lane;
         bool hit = false, unsure = false;
-        if ( ( GROUPED ? p >= rg.ps : true ) && p < rg.pe )
+        if ( ( GROUPED ? p >= rg.ps && p < rg.pe : true ) && p < tr.leaf_start[leaf + 1] )
         {
             float lo, hi;
             d2_bounds( tr, q, p, lo, hi );
@@ -1274,7 +1343,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
 TreeView view_of( Lbvh const &t )
 {
     return TreeView{t.sx.get(), t.sy.get(), t.sz.get(), t.fx.get(), t.fy.get(), t.fz.get(),
-                    t.codes.get(), t.perm.get(), t.wide.get(), t.scene.get(), t.n, t.n_leaves, t.n_wide};
+                    t.codes.get(), t.perm.get(), t.leaf_start.get(), t.leaf_of.get(), t.wide.get(),
+                    t.scene.get(), t.n, t.n_leaves, t.n_wide};
 }
 
 unsigned blocks_for( int64_t n, int threads )
@@ -1289,8 +1359,7 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
 {
     int64_t const n = src.n;
     tree.n = n;
-    tree.n_leaves = ( n + LEAF - 1 ) / LEAF;
-    int64_t const nl = tree.n_leaves;
+    int64_t nl = 0; // known after the sort
     tree.scene.allocate( 17, s );
     int const nb = std::max( 1, std::min<int>( 4 * num_sms(), (int)( ( n + BND_THREADS - 1 ) / BND_THREADS ) ) );
     DeviceBuffer<unsigned long long> partial( 6 * nb, s );
@@ -1320,6 +1389,30 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
         check_launch( "k_morton_of" );
     }
 
+    // leaves: the Morton cells of at most LEAF points (their count is needed
+    // on the host to size the tree)
+    {
+        DeviceBuffer<int> dlt( std::max<int64_t>( 1, n - 1 ), s );
+        DeviceBuffer<int64_t> lflag( n, s ), lscan( n + 1, s );
+        if ( n > 1 )
+        {
+            k_point_delta<<<blocks_for( n - 1, 256 ), 256, 0, s>>>( tree.codes.get(), tree.grp.get(), n,
+                                                                    dlt.get() );
+            check_launch( "k_point_delta" );
+        }
+        k_leaf_flags<<<blocks_for( n, 256 ), 256, 0, s>>>( dlt.get(), n, lflag.get() );
+        check_launch( "k_leaf_flags" );
+        exclusive_scan_i64( lflag.get(), lscan.get(), n, s );
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( &nl, lscan.get() + n, sizeof( int64_t ), cudaMemcpyDeviceToHost, s ) );
+        DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+        tree.leaf_start.allocate( nl + 1, s );
+        tree.leaf_of.allocate( n, s );
+        k_leaf_index<<<blocks_for( n, 256 ), 256, 0, s>>>( lflag.get(), lscan.get(), n, tree.leaf_of.get(),
+                                                           tree.leaf_start.get() );
+        check_launch( "k_leaf_index" );
+    }
+    tree.n_leaves = nl;
+
     tree.sx.allocate( n, s );
     tree.sy.allocate( n, s );
     tree.sz.allocate( n, s );
@@ -1341,7 +1434,8 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
     DTK_CUDA_OR_THROW( cudaMemsetAsync( flags.get(), 0, flags.n * sizeof( unsigned ), s ) );
     if ( ni > 0 )
     {
-        k_karras<<<blocks_for( ni, 256 ), 256, 0, s>>>( tree.codes.get(), tree.grp.get(), nl, left.get(),
+        k_karras<<<blocks_for( ni, 256 ), 256, 0, s>>>( tree.codes.get(), tree.grp.get(), tree.leaf_start.get(),
+                                                          nl, left.get(),
                                                           right.get(), parent_node.get(), parent_leaf.get(),
                                                           range_lo.get(), range_hi.get() );
         check_launch( "k_karras" );
@@ -1350,7 +1444,7 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
         check_launch( "k_pack_children" );
     }
     k_refit<<<blocks_for( nl, 128 ), 128, 0, s>>>( tree.sx.get(), tree.sy.get(), tree.sz.get(),
-                                                     tree.scene.get(), n, nl,
+                                                     tree.scene.get(), tree.leaf_start.get(), nl,
                                                      left.get(), right.get(), parent_node.get(),
                                                      parent_leaf.get(), tree.nodes.get(), flags.get(),
                                                      tree.root_box.get(), status );
