@@ -508,9 +508,10 @@ __global__ void k_pack_children( int64_t n_internal, int const *left, int const 
 // are its descendants three levels down (or the leaves met on the way), in
 // binary left-to-right order, so child leaf ranges ascend.  Child slot c of
 // wide node w is 3 float4 at wide[24 w + 3 c]: (lo.x, lo.y, lo.z, hi.x),
-// (hi.y, hi.z, ref, -), (range_lo, range_hi, -, -), with ref >= 0 a wide
-// node, ref < 0 the leaf ~ref, and WIDE_EMPTY an unused slot (box lo = +inf,
-// hi = -inf, so its lower bound is +inf).
+// (hi.y, hi.z, ref, end), (range_lo, range_hi, -, -), with ref >= 0 a wide
+// node, ref < 0 a leaf of the sorted positions [~ref, end), and WIDE_EMPTY
+// an unused slot (box lo = +inf, hi = -inf, so its lower bound is +inf);
+// range_lo/hi are the leaf indices the child covers.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void load_node( float4 const *nodes, int node, float *l_lo,
                                            float *l_hi, float *r_lo, float *r_hi, int &lc,
@@ -544,7 +545,7 @@ constexpr int WIDE_EMPTY = INT_MIN;
 // Child slot c of wide node `node`: its box, ref and (RANGE) leaf range.
 template <bool RANGE>
 __device__ __forceinline__ void load_wide( float4 const *wide, int node, int c, float *lo, float *hi,
-                                           int &ref, int &rlo, int &rhi )
+                                           int &ref, int &end, int &rlo, int &rhi )
 {
     float4 const *p = wide + 24 * (int64_t)node + 3 * c;
     float4 const a = __ldg( p ), b = __ldg( p + 1 );
@@ -555,6 +556,7 @@ __device__ __forceinline__ void load_wide( float4 const *wide, int node, int c, 
     hi[1] = b.x;
     hi[2] = b.y;
     ref = __float_as_int( b.z );
+    end = __float_as_int( b.w );
     if ( RANGE )
     {
         float4 const e = __ldg( p + 2 );
@@ -584,7 +586,7 @@ __global__ void k_depth_flags( int64_t ni, int const *parent_node, int64_t *flag
 }
 
 __global__ void k_collapse( int64_t ni, float4 const *nodes, int64_t const *flag, int64_t const *widx,
-                            float4 *wide )
+                            int32_t const *leaf_start, float4 *wide )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i >= ni || !flag[i] )
@@ -650,9 +652,11 @@ __global__ void k_collapse( int64_t ni, float4 const *nodes, int64_t const *flag
     {
         if ( c < cnt )
         {
-            int const r = ref[c] >= 0 ? (int)widx[ref[c]] : ref[c];
+            // a leaf child carries its first and end positions
+            int const r = ref[c] >= 0 ? (int)widx[ref[c]] : ~leaf_start[~ref[c]];
+            int const end = ref[c] >= 0 ? 0 : leaf_start[~ref[c] + 1];
             out[3 * c] = make_float4( box[c].lo[0], box[c].lo[1], box[c].lo[2], box[c].hi[0] );
-            out[3 * c + 1] = make_float4( box[c].hi[1], box[c].hi[2], __int_as_float( r ), 0.f );
+            out[3 * c + 1] = make_float4( box[c].hi[1], box[c].hi[2], __int_as_float( r ), __int_as_float( end ) );
             out[3 * c + 2] = make_float4( __int_as_float( rlo[c] ), __int_as_float( rhi[c] ), 0.f, 0.f );
         }
         else
@@ -992,8 +996,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         kp = -1;
     }
     // the list's starting members by leaf and lane: a leaf screens them out
-    int seed_leaf = kp >= 0 ? tr.leaf_of[kp] : -1;
-    unsigned seed_bit = kp >= 0 ? 1u << ( kp - tr.leaf_start[seed_leaf] ) : 0u;
+    // (a leaf is named by its first position)
+    int seed_leaf = kp >= 0 ? tr.leaf_start[tr.leaf_of[kp]] : -1;
+    unsigned seed_bit = kp >= 0 ? 1u << ( kp - seed_leaf ) : 0u;
     // speculative bound (seeded queries with full rows): boxes and points
     // beyond it are skipped as if the list were already that tight
     float spec = seeded && row == k ? next_spec : __int_as_float( 0x7f800000 );
@@ -1068,12 +1073,11 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     // FP32 screen of a leaf: a source whose FP32 lower bound exceeds the
     // bound cannot beat or tie it (screen_threshold keeps all the others);
     // the survivors queue for exact keys.
-    auto process_leaf = [&]( int leaf ) {
-        int64_t const p = (int64_t)tr.leaf_start[leaf] + lane;
+    auto process_leaf = [&]( int start, int end ) {
+        int64_t const p = (int64_t)start + lane;
         bool surv = false;
-        unsigned const seen = __reduce_or_sync( FULL, seed_leaf == leaf ? seed_bit : 0u );
-        if ( ( GROUPED ? p >= rg.ps && p < rg.pe : true ) && p < tr.leaf_start[leaf + 1] &&
-             !( ( seen >> lane ) & 1u ) )
+        unsigned const seen = __reduce_or_sync( FULL, seed_leaf == start ? seed_bit : 0u );
+        if ( ( GROUPED ? p >= rg.ps && p < rg.pe : true ) && p < end && !( ( seen >> lane ) & 1u ) )
         {
             float const dx = __ldg( tr.fx + p ) - q.tf[0];
             float const dy = __ldg( tr.fy + p ) - q.tf[1];
@@ -1097,7 +1101,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     {
         if ( tr.nl == 1 )
         {
-            process_leaf( 0 );
+            process_leaf( 0, (int)tr.n );
         }
         else
         {
@@ -1121,13 +1125,13 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                     break;
                 }
                 float lb = __int_as_float( 0x7f800000 );
-                int ref = WIDE_EMPTY;
+                int ref = WIDE_EMPTY, lend = 0;
                 bool ok = false;
                 if ( node >= 0 )
                 {
                     float lo[3], hi[3];
                     int rlo = 0, rhi = 0;
-                    load_wide<GROUPED>( tr.wide, node, slot, lo, hi, ref, rlo, rhi );
+                    load_wide<GROUPED>( tr.wide, node, slot, lo, hi, ref, lend, rlo, rhi );
                     lb = box_lb( lo, hi, q.qlo, q.qhi );
                     ok = ref != WIDE_EMPTY && ( GROUPED ? !( rhi < rg.lps || rlo > rg.lpe ) : true );
                 }
@@ -1153,8 +1157,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                     int const from = __ffs( m ) - 1;
                     float const lbr = __shfl_sync( FULL, lb, from );
                     int const lref = __shfl_sync( FULL, ref, from );
+                    int const le = __shfl_sync( FULL, lend, from );
                     if ( lbr <= bound_f )
-                        process_leaf( ~lref );
+                        process_leaf( ~lref, le );
                 }
                 // the next nodes: entry j from the top (lane j) is taken when it
                 // still passes the bound, up to P of them; the others above the
@@ -1203,8 +1208,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         if ( !( spec < __int_as_float( 0x7f800000 ) ) ||
              bd <= (unsigned long long)__double_as_longlong( __dmul_rd( (double)spec, 1.0 - 0x1p-40 ) ) )
             break;
-        seed_leaf = kp >= 0 ? tr.leaf_of[kp] : -1;
-        seed_bit = kp >= 0 ? 1u << ( kp - tr.leaf_start[seed_leaf] ) : 0u;
+        seed_leaf = kp >= 0 ? tr.leaf_start[tr.leaf_of[kp]] : -1;
+        seed_bit = kp >= 0 ? 1u << ( kp - seed_leaf ) : 0u;
         spec = __int_as_float( 0x7f800000 );
         bound_f = prune_threshold( bd );
         screen_f = screen_threshold( bound_f, q.err );
@@ -1245,10 +1250,10 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
     int64_t out = FILL ? offset[qi] : 0;
     int64_t const out_end = FILL ? offset[qi + 1] : 0;
 
-    auto process_leaf = [&]( int leaf ) {
-        int64_t const p = (int64_t)tr.leaf_start[leaf] + lane;
+    auto process_leaf = [&]( int start, int end ) {
+        int64_t const p = (int64_t)start + lane;
         bool hit = false, unsure = false;
-        if ( ( GROUPED ? p >= rg.ps && p < rg.pe : true ) && p < tr.leaf_start[leaf + 1] )
+        if ( ( GROUPED ? p >= rg.ps && p < rg.pe : true ) && p < end )
         {
             float lo, hi;
             d2_bounds( tr, q, p, lo, hi );
@@ -1276,7 +1281,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
 
     if ( tr.nl == 1 )
     {
-        process_leaf( 0 );
+        process_leaf( 0, (int)tr.n );
     }
     else
     {
@@ -1298,12 +1303,12 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
                 break;
             }
             bool cand = false;
-            int ref = WIDE_EMPTY;
+            int ref = WIDE_EMPTY, lend = 0;
             if ( node >= 0 )
             {
                 float lo[3], hi[3];
                 int rlo = 0, rhi = 0;
-                load_wide<GROUPED>( tr.wide, node, slot, lo, hi, ref, rlo, rhi );
+                load_wide<GROUPED>( tr.wide, node, slot, lo, hi, ref, lend, rlo, rhi );
                 cand = ref != WIDE_EMPTY && box_lb( lo, hi, q.qlo, q.qhi ) <= bound_f &&
                        ( GROUPED ? !( rhi < rg.lps || rlo > rg.lpe ) : true );
             }
@@ -1321,8 +1326,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32 )
             __syncwarp();
             for ( unsigned m = ml; m; m &= m - 1 )
             {
-                int const lref = __shfl_sync( FULL, ref, __ffs( m ) - 1 );
-                process_leaf( ~lref );
+                int const from = __ffs( m ) - 1;
+                int const lref = __shfl_sync( FULL, ref, from );
+                process_leaf( ~lref, __shfl_sync( FULL, lend, from ) );
             }
             if ( sp == 0 )
                 break;
@@ -1462,7 +1468,7 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
         tree.n_wide = nw;
         tree.wide.allocate( 24 * std::max<int64_t>( 1, nw ), s );
         k_collapse<<<blocks_for( ni, 128 ), 128, 0, s>>>( ni, tree.nodes.get(), flag.get(), widx.get(),
-                                                           tree.wide.get() );
+                                                           tree.leaf_start.get(), tree.wide.get() );
         check_launch( "k_collapse" );
     }
     tree.nodes = DeviceBuffer<float4>(); // the queries use the wide nodes
