@@ -3,7 +3,8 @@
 // Radix sort: 8-bit digits; per pass a per-tile histogram kernel, a scan of
 // the digit-major (digit, tile) count table, and a stable scatter that ranks
 // equal digits with __match_any_sync inside each warp and a shared-memory
-// prefix across the 8 warps of a 256-thread block.
+// prefix across the 8 warps of a 256-thread block, reorders the tile by digit
+// in shared memory and writes it out in digit runs.
 #include "dtk_common.cuh"
 
 #include <algorithm>
@@ -142,26 +143,61 @@ __global__ void __launch_bounds__( RS_THREADS )
     hist[(int64_t)threadIdx.x * n_tiles + blockIdx.x] = s_hist[threadIdx.x];
 }
 
+// Stable scatter of one tile: the ranks of equal digits come from
+// __match_any_sync inside each warp, a shared-memory prefix across the 8
+// warps and a running count across the tile's rounds; the tile is first
+// reordered by digit in shared memory, then written out in that order, so
+// that consecutive threads write consecutive positions of a digit's run
+// (coalesced) instead of one element per digit bucket per round.
 __global__ void __launch_bounds__( RS_THREADS )
     k_radix_scatter( uint32_t const *keys, uint32_t const *vals, uint32_t *keys_out,
                      uint32_t *vals_out, int64_t n, int shift, int64_t n_tiles,
                      int64_t const *offsets )
 {
-    __shared__ int64_t s_base[256];
+    __shared__ int64_t s_base[256];      // global position of the tile's first element of each digit
+    __shared__ unsigned s_start[256];    // tile position of the first element of each digit
+    __shared__ unsigned s_run[256];      // elements of each digit placed so far
     __shared__ unsigned s_wcount[RS_WARPS][256];
+    __shared__ uint32_t s_key[RS_TILE], s_val[RS_TILE];
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    s_base[tid] = offsets[(int64_t)tid * n_tiles + blockIdx.x];
-    unsigned const lt_mask = ( 1u << lane ) - 1u;
     int64_t const base = (int64_t)blockIdx.x * RS_TILE;
+    int64_t const rem = n - base;
+    int const count = rem < RS_TILE ? (int)rem : RS_TILE;
+    s_base[tid] = offsets[(int64_t)tid * n_tiles + blockIdx.x];
+    s_run[tid] = 0;
+    // tile-local digit starts: the tile's counts from consecutive global offsets
+    {
+        int64_t const next = blockIdx.x + 1 < n_tiles ? offsets[(int64_t)tid * n_tiles + blockIdx.x + 1]
+                                                      : offsets[(int64_t)( tid + 1 ) * n_tiles];
+        unsigned const cnt = (unsigned)( next - s_base[tid] );
+        // exclusive scan of the 256 counts (one per thread)
+        unsigned incl = cnt;
+#pragma unroll
+        for ( int o = 1; o < 32; o <<= 1 )
+        {
+            unsigned const v = __shfl_up_sync( 0xffffffffu, incl, o );
+            if ( lane >= o )
+                incl += v;
+        }
+        if ( lane == 31 )
+            s_wcount[0][warp] = incl;
+        __syncthreads();
+        unsigned wpre = 0;
+        for ( int w = 0; w < warp; ++w )
+            wpre += s_wcount[0][w];
+        s_start[tid] = wpre + incl - cnt;
+    }
+    unsigned const lt_mask = ( 1u << lane ) - 1u;
     for ( int r = 0; r < RS_ROUNDS; ++r )
     {
+        __syncthreads();
 #pragma unroll
         for ( int w = 0; w < RS_WARPS; ++w )
             s_wcount[w][tid] = 0;
         __syncthreads();
-        int64_t const e = base + r * RS_THREADS + tid;
-        bool const valid = e < n;
-        uint32_t const key = valid ? keys[e] : 0u;
+        int const t = r * RS_THREADS + tid;
+        bool const valid = t < count;
+        uint32_t const key = valid ? keys[base + t] : 0u;
         unsigned const digit = valid ? ( ( key >> shift ) & 255u ) : 256u;
         unsigned const peers = __match_any_sync( 0xffffffffu, digit );
         unsigned const rank = __popc( peers & lt_mask );
@@ -170,19 +206,27 @@ __global__ void __launch_bounds__( RS_THREADS )
         __syncthreads();
         if ( valid )
         {
-            int64_t pos = s_base[digit] + rank;
+            unsigned pos = s_start[digit] + s_run[digit] + rank;
             for ( int w = 0; w < warp; ++w )
                 pos += s_wcount[w][digit];
-            keys_out[pos] = key;
-            vals_out[pos] = vals[e];
+            s_key[pos] = key;
+            s_val[pos] = vals[base + t];
         }
         __syncthreads();
         unsigned add = 0;
 #pragma unroll
         for ( int w = 0; w < RS_WARPS; ++w )
             add += s_wcount[w][tid];
-        s_base[tid] += add;
-        __syncthreads();
+        s_run[tid] += add;
+    }
+    __syncthreads();
+    for ( int i = tid; i < count; i += RS_THREADS )
+    {
+        uint32_t const key = s_key[i];
+        unsigned const digit = ( key >> shift ) & 255u;
+        int64_t const pos = s_base[digit] + ( i - s_start[digit] );
+        keys_out[pos] = key;
+        vals_out[pos] = s_val[i];
     }
 }
 
