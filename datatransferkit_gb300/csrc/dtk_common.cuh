@@ -338,6 +338,7 @@ struct Lbvh
     DeviceBuffer<int32_t> leaf_of;    // leaf of each sorted position
     DeviceBuffer<float4> nodes;       // 4 float4 per binary internal node (released after the collapse)
     DeviceBuffer<float4> wide;        // 24 float4 per 8-wide node (the queries' tree)
+    DeviceBuffer<float4> wide_cell;   // per wide node: its Morton cell as a box (lo + parent, hi), inset
     int64_t n_wide = 0;
     DeviceBuffer<float4> root_box;    // box of the whole tree (2 float4)
     DeviceBuffer<double> scene;       // lo[3], Morton scale[3], hi[3], centre[3], bound S, FP32 lo/scale

@@ -585,6 +585,58 @@ __global__ void k_depth_flags( int64_t ni, int const *parent_node, int64_t *flag
     flag[i] = d % 3 == 0 ? 1 : 0;
 }
 
+__device__ __forceinline__ uint32_t compact10( uint32_t v )
+{
+    v &= 0x09249249u;
+    v = ( v ^ ( v >> 2 ) ) & 0x030C30C3u;
+    v = ( v ^ ( v >> 4 ) ) & 0x0300F00Fu;
+    v = ( v ^ ( v >> 8 ) ) & 0x030000FFu;
+    v = ( v ^ ( v >> 16 ) ) & 0x000003FFu;
+    return v;
+}
+
+// The Morton cell of each wide node (binary node i at a depth divisible by 3)
+// as a box in the scene-centred FP32 frame, and its parent wide node.  Every
+// point of the node lies in the cell of the common prefix of its first and
+// last leaves' first codes (the leaves are cells).  The box is inset by a
+// margin of 2^-18 (|c| + S + extent), which covers the FP32 rounding of the
+// Morton quantization; a side at the end of the quantized range is open (no
+// source lies beyond the scene box).  wide_cell[2 w] = (lo, parent),
+// wide_cell[2 w + 1] = (hi, -).
+__global__ void k_wide_cells( int64_t ni, int64_t const *flag, int64_t const *widx, int const *parent_node,
+                              int const *range_lo, int const *range_hi, int32_t const *leaf_start,
+                              uint32_t const *codes, double const *scene, float4 *wide_cell )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i >= ni || !flag[i] )
+        return;
+    uint32_t const c1 = codes[leaf_start[range_lo[i]]], c2 = codes[leaf_start[range_hi[i]]];
+    int const len = c1 == c2 ? 30 : __clz( c1 ^ c2 ) - 2;
+    double const ext = fmax( scene[6] - scene[0], fmax( scene[7] - scene[1], scene[8] - scene[2] ) );
+    double const cmax = fmax( fabs( scene[9] ), fmax( fabs( scene[10] ), fabs( scene[11] ) ) );
+    double const mg = ldexp( cmax + scene[12] + ext, -18 );
+    float lo[3], hi[3];
+#pragma unroll
+    for ( int a = 0; a < 3; ++a )
+    {
+        int const nb = len > a ? ( len - a + 2 ) / 3 : 0; // fixed bits of axis a
+        uint32_t const q = compact10( c1 >> ( 2 - a ) );
+        uint32_t const qmin = nb ? ( q >> ( 10 - nb ) ) << ( 10 - nb ) : 0u;
+        uint32_t const qmax = qmin + ( 1u << ( 10 - nb ) ) - 1u;
+        double const scale = scene[3 + a], c = scene[9 + a];
+        double const dlo = ( qmin == 0u || scale == 0.0 ) ? -INFINITY : scene[a] + qmin / scale - c + mg;
+        double const dhi = ( qmax >= 1023u || scale == 0.0 ) ? INFINITY : scene[a] + ( qmax + 1 ) / scale - c - mg;
+        lo[a] = __double2float_ru( dlo );
+        hi[a] = __double2float_rd( dhi );
+    }
+    int p = (int)i;
+    for ( int t = 0; t < 3 && p != 0; ++t )
+        p = parent_node[p];
+    int const parent = i == 0 ? -1 : (int)widx[p];
+    wide_cell[2 * widx[i]] = make_float4( lo[0], lo[1], lo[2], __int_as_float( parent ) );
+    wide_cell[2 * widx[i] + 1] = make_float4( hi[0], hi[1], hi[2], 0.f );
+}
+
 __global__ void k_collapse( int64_t ni, float4 const *nodes, int64_t const *flag, int64_t const *widx,
                             int32_t const *leaf_start, float4 *wide )
 {
@@ -686,6 +738,7 @@ struct TreeView
     uint32_t const *codes, *perm;
     int32_t const *leaf_start, *leaf_of;
     float4 const *wide; // 8-wide nodes (24 float4 each)
+    float4 const *wide_cell; // per wide node: its Morton cell (lo + parent, hi)
     double const *scene;
     int64_t n, nl, nw;
 };
@@ -913,11 +966,14 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     __shared__ int s_queue[Q_WARPS][QUEUE];
     __shared__ Query s_query[Q_WARPS];
     __shared__ int s_pop[Q_WARPS][NODE_GROUPS];
+    __shared__ int s_entry[Q_WARPS]; // the wide node the previous query started from
     int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     int64_t const w0 = ( blockIdx.x * (int64_t)Q_WARPS + wib ) * seq;
     if ( w0 >= tgt.n )
         return;
     unsigned const lt_mask = ( 1u << lane ) - 1u;
+    if ( lane == 0 )
+        s_entry[wib] = 0;
     // the list of the previous query (its sorted positions kp and indices ki)
     // seeds the next one: Morton-consecutive queries share most neighbours
     int prev_g = -1, prev_row = 0;
@@ -1113,7 +1169,45 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
             // entries (at least one), so its children fit on the stack.
             int sp = 0;
             int const grp = lane >> 3, slot = lane & 7;
-            int node = grp == 0 ? 0 : -1;
+            // Start node: every point within the speculative bound lies in the
+            // subtree of a wide node whose Morton cell holds the ball of that
+            // radius (the cell's points are the subtree's), so the search may
+            // start there; the proof after the search covers the bound, and a
+            // second pass starts from the root.  The previous query's start
+            // node is the first guess: up while its cell misses the ball, then
+            // down while one internal child's cell holds it.  (Ungrouped trees:
+            // the keys of a batch tree carry the problem above the code.)
+            int start = 0;
+            if ( !GROUPED && spec < __int_as_float( 0x7f800000 ) )
+            {
+                float const R = __fadd_ru( __fsqrt_ru( spec ), q.err );
+                auto holds = [&]( int w ) {
+                    float4 const lo = __ldg( tr.wide_cell + 2 * (int64_t)w ),
+                                 hi = __ldg( tr.wide_cell + 2 * (int64_t)w + 1 );
+                    return q.tf[0] - R > lo.x && q.tf[1] - R > lo.y && q.tf[2] - R > lo.z &&
+                           q.tf[0] + R < hi.x && q.tf[1] + R < hi.y && q.tf[2] + R < hi.z;
+                };
+                int e = s_entry[wib];
+                for ( int64_t g = 0; e > 0 && g < tr.nw && !holds( e ); ++g )
+                    e = __float_as_int( __ldg( tr.wide_cell + 2 * (int64_t)e ).w );
+                if ( e < 0 )
+                    e = 0;
+                for ( int64_t g = 0; g < tr.nw; ++g )
+                {
+                    int cref = -1;
+                    if ( lane < WIDE )
+                        cref = __float_as_int( __ldg( tr.wide + 24 * (int64_t)e + 3 * lane + 1 ).z );
+                    unsigned const m = __ballot_sync( FULL, lane < WIDE && cref >= 0 && holds( cref ) );
+                    if ( !m )
+                        break;
+                    e = __shfl_sync( FULL, cref, __ffs( m ) - 1 );
+                }
+                __syncwarp();
+                if ( lane == 0 )
+                    s_entry[wib] = e;
+                start = e;
+            }
+            int node = grp == 0 ? start : -1;
             // every step enters at least one wide node, and every wide node is
             // entered at most once
             for ( int64_t guard = 0;; ++guard )
@@ -1350,7 +1444,7 @@ TreeView view_of( Lbvh const &t )
 {
     return TreeView{t.sx.get(), t.sy.get(), t.sz.get(), t.fx.get(), t.fy.get(), t.fz.get(),
                     t.codes.get(), t.perm.get(), t.leaf_start.get(), t.leaf_of.get(), t.wide.get(),
-                    t.scene.get(), t.n, t.n_leaves, t.n_wide};
+                    t.wide_cell.get(), t.scene.get(), t.n, t.n_leaves, t.n_wide};
 }
 
 unsigned blocks_for( int64_t n, int threads )
@@ -1470,6 +1564,12 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
         k_collapse<<<blocks_for( ni, 128 ), 128, 0, s>>>( ni, tree.nodes.get(), flag.get(), widx.get(),
                                                            tree.leaf_start.get(), tree.wide.get() );
         check_launch( "k_collapse" );
+        tree.wide_cell.allocate( 2 * std::max<int64_t>( 1, nw ), s );
+        k_wide_cells<<<blocks_for( ni, 256 ), 256, 0, s>>>( ni, flag.get(), widx.get(), parent_node.get(),
+                                                              range_lo.get(), range_hi.get(), tree.leaf_start.get(),
+                                                              tree.codes.get(), tree.scene.get(),
+                                                              tree.wide_cell.get() );
+        check_launch( "k_wide_cells" );
     }
     tree.nodes = DeviceBuffer<float4>(); // the queries use the wide nodes
 }
