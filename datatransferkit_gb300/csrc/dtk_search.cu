@@ -759,12 +759,30 @@ __device__ __forceinline__ float box_lb( float const *lo, float const *hi,
 }
 
 // Upper FP32 threshold for pruning against an FP64 bound (2^-20 margin).
+// A non-negative double (its bits) rounded up to a float on the integer pipe
+// (the conversion instruction runs on the FP64 pipe, the scarcest on GB300):
+// the exponent rebiased, the mantissa cut to 23 bits and incremented when
+// anything was cut (a carry moves to the next binade, or to +inf); +inf for
+// +inf, NaN and values above FLT_MAX.  Results below the normal range take
+// the conversion instruction (distances that small are rare).
+__device__ __forceinline__ float ru_float_of( unsigned long long b )
+{
+    if ( b >= 0x7ff0000000000000ull )
+        return __int_as_float( 0x7f800000 );
+    int const fe = (int)( b >> 52 ) - 1023 + 127;
+    if ( fe >= 255 )
+        return __int_as_float( 0x7f800000 );
+    if ( fe <= 0 )
+        return __double2float_ru( __longlong_as_double( (long long)b ) );
+    uint32_t const bits = ( (uint32_t)fe << 23 ) | (uint32_t)( ( b >> 29 ) & 0x7fffffu );
+    return __uint_as_float( bits + ( ( b & 0x1fffffffull ) != 0 ? 1u : 0u ) );
+}
+
 __device__ __forceinline__ float prune_threshold( unsigned long long bound_bits )
 {
     if ( bound_bits >= 0x7ff0000000000000ull )
         return __int_as_float( 0x7f800000 ); // +inf (list not full): prune nothing
-    float const f = __double2float_ru( __longlong_as_double( (long long)bound_bits ) );
-    return __fmul_ru( f, 1.0f + 9.5367431640625e-07f );
+    return __fmul_ru( ru_float_of( bound_bits ), 1.0f + 9.5367431640625e-07f );
 }
 
 __device__ __forceinline__ bool key_less( unsigned long long ad, int ai,
@@ -921,6 +939,41 @@ __device__ __forceinline__ Query make_query( TreeView const &tr, PointsView cons
     return q;
 }
 
+// The same from a precomputed FP32 centred position tf = fl32(t - c) (the
+// FP64 subtraction and conversion are done once per target by
+// k_query_frame, off the search's FP64 pipe).
+__device__ __forceinline__ Query make_query_from( TreeView const &tr, PointsView const &tgt, int64_t qi,
+                                                  float4 tfv )
+{
+    Query q;
+    q.tx = tgt( qi, 0 );
+    q.ty = tgt( qi, 1 );
+    q.tz = tgt( qi, 2 );
+    float const tf[3] = {tfv.x, tfv.y, tfv.z};
+    float tmax = 0.f;
+#pragma unroll
+    for ( int d = 0; d < 3; ++d )
+    {
+        q.tf[d] = tf[d];
+        q.qlo[d] = nextafterf( tf[d], -INFINITY );
+        q.qhi[d] = nextafterf( tf[d], INFINITY );
+        tmax = fmaxf( tmax, fmaxf( fabsf( q.qlo[d] ), fabsf( q.qhi[d] ) ) );
+    }
+    q.err = ( reinterpret_cast<float const *>( tr.scene + 13 )[6] + tmax ) * 2.384185791015625e-07f; // 2^-22
+    return q;
+}
+
+// tf = fl32(t - c) of the w-th query in processing order.
+__global__ void k_query_frame( PointsView tgt, uint32_t const *order, double const *scene, float4 *qf )
+{
+    int64_t const w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( w >= tgt.n )
+        return;
+    int64_t const qi = order ? (int64_t)order[w] : w;
+    qf[w] = make_float4( __double2float_rn( tgt( qi, 0 ) - scene[9] ), __double2float_rn( tgt( qi, 1 ) - scene[10] ),
+                         __double2float_rn( tgt( qi, 2 ) - scene[11] ), 0.f );
+}
+
 // FP32 bounds lo <= d2(p, t) <= hi for sorted source p (centred FP32 copy).
 __device__ __forceinline__ void d2_bounds( TreeView const &tr, Query const &q, int64_t p,
                                            float &lo, float &hi )
@@ -958,7 +1011,8 @@ constexpr float SPEC_GROWTH = 1.25f; // speculative k-th squared distance over t
 
 template <bool GROUPED>
 __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
-    k_knn( TreeView tr, PointsView tgt, uint32_t const *order, int k_all, int seq, GroupView gv,
+    k_knn( TreeView tr, PointsView tgt, uint32_t const *order, float4 const *qframe, int k_all, int seq,
+           GroupView gv,
            int32_t const *offset, int32_t *idx_out, unsigned *status )
 {
     __shared__ int s_stack[Q_WARPS][STACK];
@@ -997,7 +1051,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     // the query waits in shared memory: registers limit how many warps an
     // SM holds, and values there can be re-read instead of spilled
     {
-        Query const qv = make_query( tr, tgt, qi );
+        Query const qv = make_query_from( tr, tgt, qi, __ldg( qframe + w ) );
         if ( lane == 0 )
             s_query[wib] = qv;
     }
@@ -1296,11 +1350,11 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         // Proof: a skipped box or point had an FP32 lower bound above spec,
         // so its exact squared distance exceeds spec and its FP64 key (a few
         // ulps off the exact value) exceeds spec (1 - 2^-40); a k-th key at
-        // or below that loses nothing.  d2 >= 0, so the bits of doubles
-        // compare as integers.
+        // or below spec (1 - 2^-20) (tested as its FP32 round-up against the
+        // round-down product) loses nothing.
         unsigned long long const bd = __shfl_sync( FULL, kd, k - 1 );
         if ( !( spec < __int_as_float( 0x7f800000 ) ) ||
-             bd <= (unsigned long long)__double_as_longlong( __dmul_rd( (double)spec, 1.0 - 0x1p-40 ) ) )
+             ru_float_of( bd ) <= __fmul_rd( spec, 1.0f - 9.5367431640625e-07f ) )
             break;
         seed_leaf = kp >= 0 ? tr.leaf_start[tr.leaf_of[kp]] : -1;
         seed_bit = kp >= 0 ? 1u << ( kp - seed_leaf ) : 0u;
@@ -1610,12 +1664,15 @@ void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
     while ( seq > 1 && ( tgt.n + seq - 1 ) / seq < 4 * resident )
         seq /= 2;
     unsigned const blocks = blocks_for( ( tgt.n + seq - 1 ) / seq, Q_WARPS );
+    DeviceBuffer<float4> qframe( tgt.n, s );
+    k_query_frame<<<blocks_for( tgt.n, 256 ), 256, 0, s>>>( tgt, order, tree.scene.get(), qframe.get() );
+    check_launch( "k_query_frame" );
     if ( groups.tgt_grp )
-        k_knn<true><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, k, seq, gv, offset, idx,
-                                                     status );
+        k_knn<true><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, qframe.get(), k, seq, gv,
+                                                     offset, idx, status );
     else
-        k_knn<false><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, k, seq, gv, offset, idx,
-                                                      status );
+        k_knn<false><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, qframe.get(), k, seq, gv,
+                                                      offset, idx, status );
     check_launch( "k_knn" );
 }
 
