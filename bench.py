@@ -634,14 +634,15 @@ def run_ours(args, rank, world, local_rank):
         "accuracy_vs_fp64_oracle": acc,
         "stages_ms": {"search": search_ms, "setup": setup_ms,
                       "apply": ms_mixed - search_ms - setup_ms},
-        "roofline": {"bound": "hbm", "kernel": "k_knn (8-wide BVH, warp per query)",
+        "roofline": {"bound": "hbm", "kernel": "k_knn (Morton-cell 8-wide BVH, warp per query)",
                      "achieved": q_gbs, "peak": hbm, "unit": "GB/s", "frac": q_gbs / hbm,
                      "peak_source": hbm_src, "traffic": (traffic_q * n_tgt) if traffic_q else None,
                      "algorithmic_bytes": q_bytes, "launch_ms": query_ms,
                      "note": ("the dominant kernel of a mixed step; algorithmic bytes = N_t (24 + 4k + 4) "
-                              "+ N_s (24 + 12 + 4); measured traffic matches them (no re-reads) and the "
-                              "kernel is instruction-issue bound (69% of issue slots, profiles/k_knn_1m.md), "
-                              "not HBM bound")},
+                              "+ N_s (24 + 12 + 4); the measured traffic above them is register spills "
+                              "evicted from L2 (32 registers at full occupancy); the kernel is bound by "
+                              "instruction issue and L2 latency (78% of issue slots, profiles/k_knn_1m.md), "
+                              "not by HBM")},
         "roofline_stages": {
             "search_build_ms": build_ms,
             "query": {"bound": "hbm", "achieved": q_gbs, "peak": hbm, "unit": "GB/s",
