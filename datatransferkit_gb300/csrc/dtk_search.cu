@@ -192,12 +192,12 @@ __global__ void k_bounds_final( unsigned long long const *partial, int nblocks,
 }
 
 __global__ void k_morton( PointsView p, double const *scene, uint32_t *codes,
-                          uint32_t *ids )
+                          uint32_t *ids, int drop = 0 )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i < p.n )
     {
-        codes[i] = morton3( p( i, 0 ), p( i, 1 ), p( i, 2 ), scene );
+        codes[i] = morton3( p( i, 0 ), p( i, 1 ), p( i, 2 ), scene ) >> drop;
         ids[i] = (uint32_t)i;
     }
 }
@@ -1636,9 +1636,11 @@ void sort_queries( Lbvh const &tree, PointsView tgt, DeviceBuffer<uint32_t> &ord
     if ( n == 0 )
         return;
     DeviceBuffer<uint32_t> codes( n, s );
-    k_morton<<<blocks_for( n, 256 ), 256, 0, s>>>( tgt, tree.scene.get(), codes.get(), order.get() );
+    // the queries' order needs only the top 24 bits of their codes (a 256^3
+    // grid): three radix passes instead of four
+    k_morton<<<blocks_for( n, 256 ), 256, 0, s>>>( tgt, tree.scene.get(), codes.get(), order.get(), 6 );
     check_launch( "k_morton(targets)" );
-    radix_sort_pairs( codes.get(), order.get(), n, 30, s );
+    radix_sort_pairs( codes.get(), order.get(), n, 24, s );
     if ( group )
     {
         k_group_of<<<blocks_for( n, 256 ), 256, 0, s>>>( group, order.get(), n, codes.get() );
