@@ -110,6 +110,22 @@ def test_knn_near_ties_resolved_exactly():
         assert np.array_equal(gpu_knn(src, tgt, k)[1], cpu.knn(src, tgt, k)[1]), k
 
 
+def test_knn_deep_and_degenerate_trees():
+    # the leaves are Morton cells of at most 32 points: runs of identical codes
+    # (split by position), a geometric sequence (a deep key trie), a cluster
+    # of extent 1e-9 inside a unit cloud, and targets on, near and far from all
+    rng = np.random.default_rng(14)
+    geo = np.zeros((400, 3))
+    geo[:, 0] = 2.0 ** -np.arange(400) * 0.9
+    dup = np.concatenate([np.tile([[0.3, 0.3, 0.3]], (700, 1)), np.tile([[0.7, 0.2, 0.9]], (45, 1))])
+    tiny = 0.5 + 1e-9 * rng.random((300, 3))
+    src = np.concatenate([geo, dup, tiny, rng.random((6000, 3))])
+    tgt = np.concatenate([src[::37], [[0.3, 0.3, 0.3], [0.5, 0.5, 0.5], [0.0, 0.0, 0.0], [3.0, -2.0, 0.5]],
+                          rng.random((500, 3))])
+    for k in (1, 7, 32):
+        assert np.array_equal(gpu_knn(src, tgt, k)[1], cpu.knn(src, tgt, k)[1]), k
+
+
 def test_radius_sets_bit_exact():
     src = syn.gaussian_mixture(20000, 11)
     tgt = syn.uniform_points(3000, 12)
