@@ -3,13 +3,15 @@
 // Replaces the ArborX tree and query the MLS constructor runs
 // (packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:114-129).
 //
-// Build: scene box -> 30-bit Morton codes -> stable radix sort (codes, ids)
-// -> Morton-sorted FP64 coordinates (SoA, plus FP32 copies centred on the
-// scene) -> leaf buckets of 32 consecutive points -> Karras (2012) binary
-// radix tree over the leaf keys (first code of each leaf, ties broken by leaf
+// Build: scene box -> 30-bit Morton codes (FP32 quantization) -> stable
+// radix sort (codes, ids) -> Morton-sorted FP64 coordinates (SoA, plus FP32
+// copies centred on the scene) -> leaves: the Morton cells of at most 32
+// points (the key trie split one bit at a time) -> Karras (2012) binary radix
+// tree over the leaf keys (first code of each leaf, ties broken by leaf
 // index) -> bottom-up refit of FP32 boxes rounded outward -> collapse into an
 // 8-wide BVH (three binary levels per wide node), so that 8 lanes test the 8
-// children of a node at once.
+// children of a node at once; each wide node also keeps its Morton cell (an
+// inset FP32 box) and its parent.
 //
 // kNN query: a warp runs up to 64 Morton-consecutive targets one after the
 // other; the k best (d2, index) keys sit one per lane, sorted across lanes.
@@ -19,17 +21,20 @@
 // are screened out of their leaves (a warp OR-reduction of a per-leaf lane
 // mask), so no source enters the list twice.  A seeded target also prunes
 // with a speculative bound, 1.25 times the previous target's k-th squared
-// distance; when the search ends with a k-th key above it, a second pass
-// (with the whole list screened out and the list's own bound) finds what it
-// skipped.  A box is pruned only when its FP32 round-down lower bound
-// exceeds the round-up bound with a 2^-20 relative margin, and a leaf point
-// only when its FP32 lower bound (with a rigorous rounding bound) does, so no
-// point whose FP64 distance could tie or beat the bound is skipped.  The
-// survivors get exact FP64 keys 32 at a time and are merged into the list as
-// a batch (bitonic sort, merge against the reversed candidates, bitonic
-// clean).  Distances of points are exact FP64 with separately rounded
-// operations: (dx*dx + dy*dy) + dz*dz.  Keys compare as integers (d2 >= 0,
-// so its IEEE bits are monotone), lexicographic with the source index.
+// distance, and starts at the deepest wide node whose cell holds the ball of
+// that radius; when the search ends with a k-th key above the bound, a
+// second pass (from the root, with the whole list screened out and the
+// list's own bound) finds what it skipped.  A box is pruned only when its
+// FP32 round-down lower bound exceeds the round-up bound with a 2^-20
+// relative margin, and a leaf point only when its FP32 lower bound (with a
+// rigorous rounding bound) does, so no point whose FP64 distance could tie or
+// beat the bound is skipped.  The survivors get exact FP64 keys 32 at a time
+// and are merged into the list as a batch (bitonic sort, merge against the
+// reversed candidates, bitonic clean; the networks run on 32-bit keys and
+// fall back to exact ones on a collision).  Distances of points are exact
+// FP64 with separately rounded operations: (dx*dx + dy*dy) + dz*dz.  Keys
+// compare as integers (d2 >= 0, so its IEEE bits are monotone),
+// lexicographic with the source index.
 #include "dtk_common.cuh"
 
 #include <climits>
