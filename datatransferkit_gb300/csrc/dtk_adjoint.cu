@@ -640,6 +640,10 @@ extern "C" dtk_status dtk_mls_apply_adjoint( dtk_mls_handle h, const double *cot
             DTK_REQUIRE_OR_THROW( h->src_copy.get() != nullptr,
                                   "the coordinate adjoint needs a handle created with keep_points" );
         }
+        require_device_memory( h->n_tgt ? cot : nullptr, "cot" );
+        require_device_memory( grad_values, "grad_values" );
+        require_device_memory( source_values, "source_values" );
+        require_device_memory( grad_coords, "grad_coords" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
         build_transpose_for( h, s );
         DeviceBuffer<unsigned> status( 1, s );

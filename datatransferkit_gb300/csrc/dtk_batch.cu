@@ -433,6 +433,8 @@ dtk_status dtk_mls_batch_create( int32_t n_problems, const dtk_mls_options *opts
         int64_t const n_src = src_offsets[n_problems], n_tgt = tgt_offsets[n_problems];
         DTK_REQUIRE_OR_THROW( n_src <= INT32_MAX && n_tgt < INT32_MAX, "too many points" );
         DTK_REQUIRE_OR_THROW( src != nullptr && ( n_tgt == 0 || tgt != nullptr ), "null points" );
+        require_device_memory( src, "source points" );
+        require_device_memory( n_tgt ? tgt : nullptr, "target points" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
         auto h = std::make_unique<dtk_mls_batch_s>();
         h->n_problems = n_problems;
@@ -606,6 +608,8 @@ dtk_status dtk_mls_batch_apply( dtk_mls_batch_handle h, const double *src_values
         DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
         DTK_REQUIRE_OR_THROW( src_values != nullptr && ( h->n_tgt == 0 || tgt_values != nullptr ),
                               "null values" );
+        require_device_memory( src_values, "src_values" );
+        require_device_memory( tgt_values, "tgt_values" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
         if ( !h->tuned )
             h->tune( src_values, tgt_values, s );

@@ -337,6 +337,8 @@ dtk_status dtk_mls_apply( dtk_mls_handle h, const double *source_values, int64_t
                               "target_values.extent(0) == n_target_points" );
         DTK_REQUIRE_OR_THROW( h->n_src == 0 || source_values != nullptr, "source_values is null" );
         DTK_REQUIRE_OR_THROW( h->n_tgt == 0 || target_values != nullptr, "target_values is null" );
+        require_device_memory( source_values, "source_values" );
+        require_device_memory( target_values, "target_values" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
         apply_csr( h->n_tgt, h->offset.get(), h->idx.get(), h->coeff64.get(), h->coeff32.get(),
                    h->uniform_row, h->mean_row, source_values, target_values, s );
@@ -351,8 +353,8 @@ dtk_status dtk_mls_transfer_host( const dtk_mls_options *opts, const double *src
         if ( out )
             *out = nullptr;
         Geometry const g = check_options( opts );
-        validate_points( src_host, n_src, 3, 1, "source points" );
-        validate_points( tgt_host, n_tgt, 3, 1, "target points" );
+        validate_points( src_host, n_src, 3, 1, "source points", true );
+        validate_points( tgt_host, n_tgt, 3, 1, "target points", true );
         DTK_REQUIRE_OR_THROW( n_src > 0, "the source point cloud is empty" );
         DTK_REQUIRE_OR_THROW( values_host != nullptr, "source values are null" );
         DTK_REQUIRE_OR_THROW( n_tgt == 0 || target_values_host != nullptr, "target values are null" );

@@ -52,6 +52,8 @@ FieldView field_in( double const *p, int64_t n, int64_t n_comp, int64_t ps, int6
     DTK_REQUIRE_OR_THROW( n == 0 || p != nullptr, std::string( what ) + " is null" );
     DTK_REQUIRE_OR_THROW( n <= 1 || ps != 0, std::string( what ) + ": zero point stride" );
     DTK_REQUIRE_OR_THROW( n_comp == 1 || cs != 0, std::string( what ) + ": zero component stride" );
+    if ( n > 0 )
+        require_device_memory( p, what );
     return FieldView{p, nullptr, n, n_comp, ps, cs};
 }
 
