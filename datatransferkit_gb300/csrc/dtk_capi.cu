@@ -318,6 +318,8 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
         validate_points( tgt, n_tgt, tgt_pt_stride, tgt_dim_stride, "target points" );
         // DTK_CHECK( !search_tree.empty() ), DTK_MovingLeastSquaresOperator_def.hpp:116
         DTK_REQUIRE_OR_THROW( n_src > 0, "the source point cloud is empty" );
+        require_device_memory( src, "source points" );
+        require_device_memory( n_tgt ? tgt : nullptr, "target points" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
         PointsView const sv{src, n_src, src_pt_stride, src_dim_stride};
         PointsView const tv{tgt, n_tgt, tgt_pt_stride, tgt_dim_stride};
@@ -353,8 +355,8 @@ dtk_status dtk_mls_transfer_host( const dtk_mls_options *opts, const double *src
         if ( out )
             *out = nullptr;
         Geometry const g = check_options( opts );
-        validate_points( src_host, n_src, 3, 1, "source points", true );
-        validate_points( tgt_host, n_tgt, 3, 1, "target points", true );
+        validate_points( src_host, n_src, 3, 1, "source points" );
+        validate_points( tgt_host, n_tgt, 3, 1, "target points" );
         DTK_REQUIRE_OR_THROW( n_src > 0, "the source point cloud is empty" );
         DTK_REQUIRE_OR_THROW( values_host != nullptr, "source values are null" );
         DTK_REQUIRE_OR_THROW( n_tgt == 0 || target_values_host != nullptr, "target values are null" );
@@ -543,6 +545,10 @@ dtk_status dtk_knn_search( const double *src, int64_t n_src, int64_t src_pt_stri
         int const row = (int)std::min<int64_t>( k, n_src );
         DTK_REQUIRE_OR_THROW( n_tgt * (int64_t)row <= INT32_MAX, "n_targets * k exceeds int32" );
         DTK_REQUIRE_OR_THROW( n_tgt * (int64_t)row == 0 || indices != nullptr, "indices is null" );
+        require_device_memory( src, "source points" );
+        require_device_memory( n_tgt ? tgt : nullptr, "target points" );
+        require_device_memory( offset, "offset" );
+        require_device_memory( n_tgt * (int64_t)row ? indices : nullptr, "indices" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
         PointsView const sv{src, n_src, src_pt_stride, src_dim_stride};
         PointsView const tv{tgt, n_tgt, tgt_pt_stride, tgt_dim_stride};

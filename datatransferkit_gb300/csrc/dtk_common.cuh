@@ -83,10 +83,13 @@ inline void require_device_memory( void const *p, char const *what )
     if ( !p )
         return;
     cudaPointerAttributes a{};
-    if ( cudaPointerGetAttributes( &a, p ) != cudaSuccess )
+    cudaError_t const e = cudaPointerGetAttributes( &a, p );
+    if ( e != cudaSuccess )
     {
         cudaGetLastError();
-        throw Error{DTK_ERR_INVALID_ARG, std::string( what ) + " is not a pointer CUDA can use"};
+        if ( e == cudaErrorInvalidValue )
+            throw Error{DTK_ERR_INVALID_ARG, std::string( what ) + " is not a pointer CUDA can use"};
+        throw Error{DTK_ERR_CUDA, std::string( what ) + ": " + cudaGetErrorString( e )};
     }
     if ( a.type == cudaMemoryTypeUnregistered )
         throw Error{DTK_ERR_INVALID_ARG, std::string( what ) +
@@ -94,18 +97,15 @@ inline void require_device_memory( void const *p, char const *what )
                                              "(host buffers go through dtk_mls_transfer_host)"};
 }
 
-// Point-cloud arguments of an entry point: count, pointer and strides; device
-// memory unless `host`.
-inline void validate_points( double const *p, int64_t n, int64_t ps, int64_t ds, char const *what,
-                             bool host = false )
+// Point-cloud arguments of an entry point: count, pointer and strides (the
+// entry points check device memory after every argument check).
+inline void validate_points( double const *p, int64_t n, int64_t ps, int64_t ds, char const *what )
 {
     DTK_REQUIRE_OR_THROW( n >= 0, std::string( what ) + " count is negative" );
     DTK_REQUIRE_OR_THROW( n == 0 || p != nullptr, std::string( what ) + " pointer is null" );
     DTK_REQUIRE_OR_THROW( n <= INT32_MAX, std::string( what ) + " count exceeds int32 indices" );
     DTK_REQUIRE_OR_THROW( n == 0 || ( ps != 0 || n == 1 ) && ds != 0,
                           std::string( what ) + " strides are zero" );
-    if ( !host && n > 0 )
-        require_device_memory( p, what );
 }
 
 // The library's stream-ordered memory pool on the current device: freed

@@ -77,6 +77,8 @@ dtk_status dtk_nn_create( const double *src, int64_t n_src, int64_t src_pt_strid
         validate_points( tgt, n_tgt, tgt_pt_stride, tgt_dim_stride, "target points" );
         // DTK_CHECK( !search_tree.empty() ), DTK_NearestNeighborOperator_def.hpp:43
         DTK_REQUIRE_OR_THROW( n_src > 0, "the source point cloud is empty" );
+        require_device_memory( src, "source points" );
+        require_device_memory( n_tgt ? tgt : nullptr, "target points" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
         auto h = std::make_unique<dtk_nn_s>();
         h->n_src = n_src;
