@@ -484,9 +484,8 @@ dtk_status dtk_mls_batch_create( int32_t n_problems, const dtk_mls_options *opts
 
         // --- search over all problems at once ---
         Lbvh tree;
-        build_lbvh( sv, tree, status.get(), s, src_grp.get(), n_problems );
         DeviceBuffer<uint32_t> order;
-        sort_queries( tree, tv, order, s, tgt_grp.get(), n_problems );
+        build_tree_and_order( sv, tv, tree, order, status.get(), s, src_grp.get(), tgt_grp.get(), n_problems );
         GroupArgs ga;
         ga.src_off = d_src_off.get();
         ga.tgt_grp = tgt_grp.get();

@@ -172,10 +172,9 @@ std::unique_ptr<dtk_mls_s> create_impl( Geometry const &g, dtk_mls_options const
 
     // --- search (ArborX tree + query, def.hpp:114-129) ---
     Lbvh tree;
-    build_lbvh( sv, tree, status.get(), s );
-    if ( tgt_ready ) // the targets arrive while the tree is built
-        DTK_CUDA_OR_THROW( cudaStreamWaitEvent( s, tgt_ready, 0 ) );
-    sort_queries( tree, tv, h->order, s );
+    // (the targets may still be arriving: the query order waits for them on
+    // its own stream while the tree is built)
+    build_tree_and_order( sv, tv, tree, h->order, status.get(), s, nullptr, nullptr, 0, tgt_ready );
     DTK_CUDA_OR_THROW( cudaEventRecord( ev[3], s ) );
     h->offset.allocate( n_tgt + 1, s );
     if ( !g.radius_mode )
@@ -557,9 +556,8 @@ dtk_status dtk_knn_search( const double *src, int64_t n_src, int64_t src_pt_stri
         k_fill_uniform_offsets<<<(unsigned)( ( n_tgt + 256 ) / 256 ), 256, 0, s>>>( offset, n_tgt, row );
         check_launch( "k_fill_uniform_offsets" );
         Lbvh tree;
-        build_lbvh( sv, tree, status.get(), s );
         DeviceBuffer<uint32_t> order;
-        sort_queries( tree, tv, order, s );
+        build_tree_and_order( sv, tv, tree, order, status.get(), s );
         knn_query( tree, tv, order.get(), k, GroupArgs{}, offset, indices, status.get(), s );
         unsigned st = 0;
         DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, status.get(), sizeof( unsigned ),

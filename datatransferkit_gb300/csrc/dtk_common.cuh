@@ -7,6 +7,7 @@
 #include <climits>
 #include <cstdint>
 #include <exception>
+#include <functional>
 #include <new>
 #include <string>
 
@@ -369,13 +370,26 @@ struct Lbvh
 
 // group (optional, per input point) makes the order problem-major: the
 // points of group g then occupy one contiguous range of sorted positions.
+// after_scene (optional) runs on the host once the scene box is enqueued on
+// s (tree.scene), before the rest of the build.
 void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
-                 uint32_t const *group = nullptr, int64_t n_groups = 0 );
+                 uint32_t const *group = nullptr, int64_t n_groups = 0,
+                 std::function<void()> const &after_scene = nullptr );
 
 // Morton order of query points (sorted query ids) using the tree's scene box;
-// with groups, problem-major and Morton within each problem.
+// with groups, problem-major and Morton within each problem.  An order buffer
+// already holding max(1, tgt.n) entries is used as it is.
 void sort_queries( Lbvh const &tree, PointsView tgt, DeviceBuffer<uint32_t> &order,
                    cudaStream_t s, uint32_t const *group = nullptr, int64_t n_groups = 0 );
+
+// The tree over src on s and, on a second stream as soon as the scene box is
+// known, the order of the queries, concurrently with the rest of the build;
+// s waits for the order before this returns.
+// (tgt_ready, when not null, is an event the query points wait for.)
+void build_tree_and_order( PointsView src, PointsView tgt, Lbvh &tree, DeviceBuffer<uint32_t> &order,
+                           unsigned *status, cudaStream_t s, uint32_t const *src_group = nullptr,
+                           uint32_t const *tgt_group = nullptr, int64_t n_groups = 0,
+                           cudaEvent_t tgt_ready = nullptr );
 
 // Problems of a batch, all optional (null: one problem over all sources,
 // uniform k / radius): per group the sorted-position range of its sources,

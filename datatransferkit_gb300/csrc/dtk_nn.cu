@@ -94,9 +94,8 @@ dtk_status dtk_nn_create( const double *src, int64_t n_src, int64_t src_pt_strid
             k_iota_offsets<<<(unsigned)( ( n_tgt + 256 ) / 256 ), 256, 0, s>>>( offset.get(), n_tgt );
             check_launch( "k_iota_offsets" );
             Lbvh tree;
-            build_lbvh( sv, tree, status.get(), s );
             DeviceBuffer<uint32_t> order;
-            sort_queries( tree, tv, order, s );
+            build_tree_and_order( sv, tv, tree, order, status.get(), s );
             knn_query( tree, tv, order.get(), 1, GroupArgs{}, offset.get(), h->idx.get(), status.get(), s );
             unsigned st = 0;
             DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, status.get(), sizeof( st ), cudaMemcpyDeviceToHost, s ) );

@@ -40,6 +40,7 @@
 #include <climits>
 
 #include <algorithm>
+#include <functional>
 #include <vector>
 
 namespace dtk
@@ -1514,7 +1515,7 @@ unsigned blocks_for( int64_t n, int threads )
 } // namespace
 
 void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
-                 uint32_t const *group, int64_t n_groups )
+                 uint32_t const *group, int64_t n_groups, std::function<void()> const &after_scene )
 {
     int64_t const n = src.n;
     tree.n = n;
@@ -1526,6 +1527,8 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
     check_launch( "k_bounds_partial" );
     k_bounds_final<<<1, 32, 0, s>>>( partial.get(), nb, tree.scene.get() );
     check_launch( "k_bounds_final" );
+    if ( after_scene )
+        after_scene();
 
     tree.codes.allocate( n, s );
     tree.perm.allocate( n, s );
@@ -1637,7 +1640,8 @@ void sort_queries( Lbvh const &tree, PointsView tgt, DeviceBuffer<uint32_t> &ord
                    cudaStream_t s, uint32_t const *group, int64_t n_groups )
 {
     int64_t const n = tgt.n;
-    order.allocate( std::max<int64_t>( 1, n ), s );
+    if ( order.n < (size_t)std::max<int64_t>( 1, n ) )
+        order.allocate( std::max<int64_t>( 1, n ), s );
     if ( n == 0 )
         return;
     DeviceBuffer<uint32_t> codes( n, s );
@@ -1655,6 +1659,39 @@ void sort_queries( Lbvh const &tree, PointsView tgt, DeviceBuffer<uint32_t> &ord
             ++bits;
         radix_sort_pairs( codes.get(), order.get(), n, ( bits + 7 ) / 8 * 8, s );
     }
+}
+
+void build_tree_and_order( PointsView src, PointsView tgt, Lbvh &tree, DeviceBuffer<uint32_t> &order,
+                           unsigned *status, cudaStream_t s, uint32_t const *src_group,
+                           uint32_t const *tgt_group, int64_t n_groups, cudaEvent_t tgt_ready )
+{
+    struct Side
+    {
+        cudaStream_t s2 = nullptr;
+        cudaEvent_t scene = nullptr, done = nullptr;
+        ~Side()
+        {
+            if ( scene )
+                cudaEventDestroy( scene );
+            if ( done )
+                cudaEventDestroy( done );
+            if ( s2 )
+                cudaStreamDestroy( s2 );
+        }
+    } side;
+    DTK_CUDA_OR_THROW( cudaStreamCreateWithFlags( &side.s2, cudaStreamNonBlocking ) );
+    DTK_CUDA_OR_THROW( cudaEventCreateWithFlags( &side.scene, cudaEventDisableTiming ) );
+    DTK_CUDA_OR_THROW( cudaEventCreateWithFlags( &side.done, cudaEventDisableTiming ) );
+    order.allocate( std::max<int64_t>( 1, tgt.n ), s ); // owned by s, filled on the side stream
+    build_lbvh( src, tree, status, s, src_group, n_groups, [&] {
+        DTK_CUDA_OR_THROW( cudaEventRecord( side.scene, s ) );
+        DTK_CUDA_OR_THROW( cudaStreamWaitEvent( side.s2, side.scene, 0 ) );
+        if ( tgt_ready )
+            DTK_CUDA_OR_THROW( cudaStreamWaitEvent( side.s2, tgt_ready, 0 ) );
+        sort_queries( tree, tgt, order, side.s2, tgt_group, n_groups );
+        DTK_CUDA_OR_THROW( cudaEventRecord( side.done, side.s2 ) );
+    } );
+    DTK_CUDA_OR_THROW( cudaStreamWaitEvent( s, side.done, 0 ) );
 }
 
 void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
