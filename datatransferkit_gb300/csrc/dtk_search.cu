@@ -52,13 +52,14 @@ constexpr int LEAF = 32;
 constexpr int STACK = 256; // wide-node stack entries per warp
 constexpr int NODE_GROUPS = 4; // wide nodes a kNN warp tests per step (8 lanes each)
 static_assert( NODE_GROUPS * 8 == 32, "one lane per child slot" );
-constexpr int Q_WARPS = 4; // warps per block in the query kernels
+constexpr int Q_WARPS = 8; // warps per block in the kNN query kernel
+constexpr int R_WARPS = 4; // warps per block in the radius query kernel
 constexpr int Q_SEQ = 64;  // most consecutive kNN queries per warp (each seeds the next)
-// kNN blocks per SM: 16 blocks of 4 warps (all 64 warp slots) cap the kernel
+// kNN blocks per SM: 8 blocks of 8 warps (all 64 warp slots) cap the kernel
 // at 32 registers, with the query in shared memory; the values spilled cost
-// less than the warps gained (8M-point query: 39.0 ms at 8 blocks, 34.5 ms
-// at 16)
-constexpr int KNN_BLOCKS_PER_SM = 16;
+// less than the warps gained (8M-point query, 4-warp blocks: 39.0 ms at 8
+// blocks, 34.5 ms at 16; 8-warp blocks are 1% faster again)
+constexpr int KNN_BLOCKS_PER_SM = 8;
 constexpr unsigned FULL = 0xffffffffu;
 constexpr unsigned long long KEY_INF = 0xffffffffffffffffull;
 
@@ -1384,13 +1385,13 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
 // every source whose bound interval lies clear of r^2 (2^-20 margins), and
 // only the rest pay for an FP64 distance.
 template <bool FILL, bool GROUPED>
-__global__ void __launch_bounds__( Q_WARPS * 32 )
+__global__ void __launch_bounds__( R_WARPS * 32 )
     k_radius( TreeView tr, PointsView tgt, uint32_t const *order, double r_all, GroupView gv,
               int64_t *counts, int32_t const *offset, int32_t *idx_out, unsigned *status )
 {
-    __shared__ int s_stack[Q_WARPS][STACK];
+    __shared__ int s_stack[R_WARPS][STACK];
     int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    int64_t const w = blockIdx.x * (int64_t)Q_WARPS + wib;
+    int64_t const w = blockIdx.x * (int64_t)R_WARPS + wib;
     if ( w >= tgt.n )
         return;
     int64_t const qi = order ? (int64_t)order[w] : w;
@@ -1727,10 +1728,10 @@ void radius_count( Lbvh const &tree, PointsView tgt, uint32_t const *order, doub
         return;
     GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
     if ( groups.tgt_grp )
-        k_radius<false, true><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
+        k_radius<false, true><<<blocks_for( tgt.n, R_WARPS ), R_WARPS * 32, 0, s>>>(
             view_of( tree ), tgt, order, r, gv, counts, nullptr, nullptr, status );
     else
-        k_radius<false, false><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
+        k_radius<false, false><<<blocks_for( tgt.n, R_WARPS ), R_WARPS * 32, 0, s>>>(
             view_of( tree ), tgt, order, r, gv, counts, nullptr, nullptr, status );
     check_launch( "k_radius(count)" );
 }
@@ -1743,10 +1744,10 @@ void radius_fill( Lbvh const &tree, PointsView tgt, uint32_t const *order, doubl
         return;
     GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
     if ( groups.tgt_grp )
-        k_radius<true, true><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
+        k_radius<true, true><<<blocks_for( tgt.n, R_WARPS ), R_WARPS * 32, 0, s>>>(
             view_of( tree ), tgt, order, r, gv, nullptr, offset, idx, status );
     else
-        k_radius<true, false><<<blocks_for( tgt.n, Q_WARPS ), Q_WARPS * 32, 0, s>>>(
+        k_radius<true, false><<<blocks_for( tgt.n, R_WARPS ), R_WARPS * 32, 0, s>>>(
             view_of( tree ), tgt, order, r, gv, nullptr, offset, idx, status );
     check_launch( "k_radius(fill)" );
 }
