@@ -52,14 +52,15 @@ constexpr int LEAF = 32;
 constexpr int STACK = 256; // wide-node stack entries per warp
 constexpr int NODE_GROUPS = 4; // wide nodes a kNN warp tests per step (8 lanes each)
 static_assert( NODE_GROUPS * 8 == 32, "one lane per child slot" );
-constexpr int Q_WARPS = 8; // warps per block in the kNN query kernel
+constexpr int Q_WARPS = 16; // warps per block in the kNN query kernel
 constexpr int R_WARPS = 4; // warps per block in the radius query kernel
 constexpr int Q_SEQ = 64;  // most consecutive kNN queries per warp (each seeds the next)
-// kNN blocks per SM: 8 blocks of 8 warps (all 64 warp slots) cap the kernel
+// kNN blocks per SM: 4 blocks of 16 warps (all 64 warp slots) cap the kernel
 // at 32 registers, with the query in shared memory; the values spilled cost
 // less than the warps gained (8M-point query, 4-warp blocks: 39.0 ms at 8
-// blocks, 34.5 ms at 16; 8-warp blocks are 1% faster again)
-constexpr int KNN_BLOCKS_PER_SM = 8;
+// blocks, 34.5 ms at 16; then 8-, 16- and 32-warp blocks: 22.0, 21.4 and
+// 21.7 ms)
+constexpr int KNN_BLOCKS_PER_SM = 4;
 constexpr unsigned FULL = 0xffffffffu;
 constexpr unsigned long long KEY_INF = 0xffffffffffffffffull;
 
