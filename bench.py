@@ -641,7 +641,7 @@ def run_ours(args, rank, world, local_rank):
                      "note": ("the dominant kernel of a mixed step; algorithmic bytes = N_t (24 + 4k + 4) "
                               "+ N_s (24 + 12 + 4); the measured traffic above them is register spills "
                               "evicted from L2 (32 registers at full occupancy); the kernel is bound by "
-                              "instruction issue and L2 latency (78% of issue slots, profiles/k_knn_1m.md), "
+                              "instruction issue and L2 latency (81% of issue slots, profiles/k_knn_1m.md), "
                               "not by HBM")},
         "roofline_stages": {
             "search_build_ms": build_ms,
