@@ -49,12 +49,13 @@ namespace
 {
 
 constexpr int LEAF = 32;
-constexpr int STACK = 256; // wide-node stack entries per warp
+constexpr int STACK = 256; // wide-node stack entries per warp (radius search)
+constexpr int K_STACK = 192; // the same for the kNN search
 constexpr int NODE_GROUPS = 4; // wide nodes a kNN warp tests per step (8 lanes each)
 static_assert( NODE_GROUPS * 8 == 32, "one lane per child slot" );
 constexpr int Q_WARPS = 16; // warps per block in the kNN query kernel
 constexpr int R_WARPS = 4; // warps per block in the radius query kernel
-constexpr int Q_SEQ = 64;  // most consecutive kNN queries per warp (each seeds the next)
+constexpr int Q_SEQ = 48;  // most consecutive kNN queries per warp (each seeds the next)
 // kNN blocks per SM: 4 blocks of 16 warps (all 64 warp slots) cap the kernel
 // at 32 registers, with the query in shared memory; the values spilled cost
 // less than the warps gained (8M-point query, 4-warp blocks: 39.0 ms at 8
@@ -1017,25 +1018,58 @@ __device__ __forceinline__ float screen_threshold( float b, float err )
 constexpr int QUEUE = 64;
 constexpr float SPEC_GROWTH = 1.25f; // speculative k-th squared distance over the previous query's
 
+// Queries go to warps in chunks of Morton-consecutive queries (each query
+// seeds the next): n_big chunks of seq queries, then chunks of seq / 2 up to
+// the end, so that the warps finish close together.  A warp takes the next
+// chunk from a counter as soon as it is done with one.
+struct KnnChunks
+{
+    int seq;
+    int64_t n_big;
+    unsigned *next;
+};
+
+__device__ __forceinline__ void chunk_range( KnnChunks const &ch, unsigned c, int64_t &w0, int64_t &len )
+{
+    if ( c < ch.n_big )
+    {
+        w0 = (int64_t)c * ch.seq;
+        len = ch.seq;
+    }
+    else
+    {
+        int const tail = ch.seq > 1 ? ch.seq / 2 : 1;
+        w0 = ch.n_big * ch.seq + ( (int64_t)c - ch.n_big ) * tail;
+        len = tail;
+    }
+}
+
 template <bool GROUPED>
 __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
-    k_knn( TreeView tr, PointsView tgt, uint32_t const *order, float4 const *qframe, int k_all, int seq,
+    k_knn( TreeView tr, PointsView tgt, uint32_t const *order, float4 const *qframe, int k_all, KnnChunks ch,
            GroupView gv,
            int32_t const *offset, int32_t *idx_out, unsigned *status )
 {
-    __shared__ int s_stack[Q_WARPS][STACK];
-    __shared__ float s_lb[Q_WARPS][STACK];
+    // the stack of wide nodes to enter: small, to leave most of the SM's L1
+    // to the tree and the points
+    __shared__ int s_stack[Q_WARPS][K_STACK];
     __shared__ int s_queue[Q_WARPS][QUEUE];
     __shared__ Query s_query[Q_WARPS];
-    __shared__ int s_pop[Q_WARPS][NODE_GROUPS];
     __shared__ int s_entry[Q_WARPS]; // the wide node the previous query started from
     int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    int64_t const w0 = ( blockIdx.x * (int64_t)Q_WARPS + wib ) * seq;
-    if ( w0 >= tgt.n )
-        return;
     unsigned const lt_mask = ( 1u << lane ) - 1u;
     if ( lane == 0 )
         s_entry[wib] = 0;
+    for ( ;; )
+    {
+    unsigned c = 0;
+    if ( lane == 0 )
+        c = atomicAdd( ch.next, 1u );
+    c = __shfl_sync( FULL, c, 0 );
+    int64_t w0, len;
+    chunk_range( ch, c, w0, len );
+    if ( w0 >= tgt.n )
+        return;
     // the list of the previous query (its sorted positions kp and indices ki)
     // seeds the next one: Morton-consecutive queries share most neighbours
     int prev_g = -1, prev_row = 0;
@@ -1044,7 +1078,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     float next_spec = __int_as_float( 0x7f800000 );
     unsigned long long kd = KEY_INF;
     int ki = 0x7fffffff, kp = -1;
-    for ( int64_t w = w0; w < w0 + seq && w < tgt.n; ++w )
+    for ( int64_t w = w0; w < w0 + len && w < tgt.n; ++w )
     {
     int64_t const qi = order ? (int64_t)order[w] : w;
     Range const rg = query_range<GROUPED>( tr, gv, qi );
@@ -1226,8 +1260,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
             // Wide-node traversal, up to NODE_GROUPS nodes a step: lane group g
             // (lanes 8g .. 8g+7) tests the 8 children of its node; leaf children
             // are screened in lane order, internal children go on the stack in
-            // lane order, and the next step takes the top entries that still
-            // pass the current bound.  A step takes at most (STACK - sp) / 7
+            // lane order, and the next step takes the top entries.  A step
+            // takes at most (K_STACK - sp) / 7
             // entries (at least one), so its children fit on the stack.
             int sp = 0;
             int const grp = lane >> 3, slot = lane & 7;
@@ -1295,13 +1329,12 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                 unsigned const ml = __ballot_sync( FULL, cand && ref < 0 );
                 unsigned const mi = __ballot_sync( FULL, cand && ref >= 0 );
                 int const n_int = __popc( mi );
-                if ( sp + n_int <= STACK )
+                if ( sp + n_int <= K_STACK )
                 {
                     if ( cand && ref >= 0 )
                     {
                         int const pos = sp + __popc( mi & lt_mask );
                         s_stack[wib][pos] = ref;
-                        s_lb[wib][pos] = lb;
                     }
                     sp += n_int;
                 }
@@ -1317,40 +1350,18 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                     if ( lbr <= bound_f )
                         process_leaf( ~lref, le );
                 }
-                // the next nodes: entry j from the top (lane j) is taken when it
-                // still passes the bound, up to P of them; the others above the
-                // last one taken are dropped
-                int const P = sp <= STACK - NODE_GROUPS * ( WIDE - 1 )
+                // the next nodes: the top P entries (a node is pushed only when
+                // its box passes the bound; the bound tightens rarely during a
+                // search, and a node's children are tested against it again)
+                int const P = sp <= K_STACK - NODE_GROUPS * ( WIDE - 1 )
                                   ? NODE_GROUPS
-                                  : max( 1, ( STACK - sp ) / ( WIDE - 1 ) );
-                int taken = 0;
-                while ( sp > 0 )
-                {
-                    int const avail = sp < 32 ? sp : 32;
-                    int e_node = 0;
-                    bool pass = false;
-                    if ( lane < avail )
-                    {
-                        e_node = s_stack[wib][sp - 1 - lane];
-                        pass = s_lb[wib][sp - 1 - lane] <= bound_f;
-                    }
-                    unsigned const v0 = __ballot_sync( FULL, pass );
-                    // the passing entry of rank r (from the top) goes to group r
-                    int const rank = __popc( v0 & lt_mask );
-                    if ( pass && rank < P )
-                        s_pop[wib][rank] = e_node;
-                    int const nv = __popc( v0 );
-                    taken = nv < P ? nv : P;
-                    // one past the P-th entry taken, or all that were examined
-                    unsigned const last = __ballot_sync( FULL, pass && rank == P - 1 );
-                    sp -= last ? __ffs( last ) : avail;
-                    if ( taken > 0 )
-                        break;
-                }
-                __syncwarp();
+                                  : max( 1, ( K_STACK - sp ) / ( WIDE - 1 ) );
+                int const taken = sp < P ? sp : P;
                 if ( taken == 0 )
                     break;
-                node = grp < taken ? s_pop[wib][grp] : -1;
+                node = grp < taken ? s_stack[wib][sp - 1 - grp] : -1;
+                sp -= taken;
+                __syncwarp();
             }
         }
         if ( qn > 0 )
@@ -1376,6 +1387,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     prev_row = row;
     next_spec = __fmul_ru( prune_threshold( __shfl_sync( FULL, kd, k - 1 ) ), SPEC_GROWTH );
     __syncwarp();
+    }
     }
 }
 
@@ -1703,21 +1715,30 @@ void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
     if ( tgt.n == 0 || tree.n == 0 || ( k == 0 && !groups.k ) )
         return;
     GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
-    // queries per warp: up to Q_SEQ, fewer when that leaves under four waves
-    // of resident warps
+    // chunk length: up to Q_SEQ queries, fewer when that leaves under four
+    // chunks per resident warp; the last chunk per resident warp is cut in
+    // two halves
     int seq = Q_SEQ;
     int64_t const resident = (int64_t)num_sms() * KNN_BLOCKS_PER_SM * Q_WARPS;
     while ( seq > 1 && ( tgt.n + seq - 1 ) / seq < 4 * resident )
         seq /= 2;
-    unsigned const blocks = blocks_for( ( tgt.n + seq - 1 ) / seq, Q_WARPS );
+    int64_t const tail_q = resident * seq;
+    int64_t const n_big = tgt.n > tail_q ? ( tgt.n - tail_q ) / seq : 0;
+    int const tail = seq > 1 ? seq / 2 : 1;
+    int64_t const n_chunks = n_big + ( tgt.n - n_big * seq + tail - 1 ) / tail;
+    int64_t const warps = n_chunks < resident ? n_chunks : resident;
+    unsigned const blocks = blocks_for( warps, Q_WARPS );
+    DeviceBuffer<unsigned> next( 1, s );
+    DTK_CUDA_OR_THROW( cudaMemsetAsync( next.get(), 0, sizeof( unsigned ), s ) );
+    KnnChunks const ch{seq, n_big, next.get()};
     DeviceBuffer<float4> qframe( tgt.n, s );
     k_query_frame<<<blocks_for( tgt.n, 256 ), 256, 0, s>>>( tgt, order, tree.scene.get(), qframe.get() );
     check_launch( "k_query_frame" );
     if ( groups.tgt_grp )
-        k_knn<true><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, qframe.get(), k, seq, gv,
+        k_knn<true><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, qframe.get(), k, ch, gv,
                                                      offset, idx, status );
     else
-        k_knn<false><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, qframe.get(), k, seq, gv,
+        k_knn<false><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, qframe.get(), k, ch, gv,
                                                       offset, idx, status );
     check_launch( "k_knn" );
 }
