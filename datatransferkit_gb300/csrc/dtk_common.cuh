@@ -361,7 +361,8 @@ struct Lbvh
     DeviceBuffer<int32_t> leaf_start; // first sorted position of each leaf, then n (n_leaves + 1)
     DeviceBuffer<int32_t> leaf_of;    // leaf of each sorted position
     DeviceBuffer<float4> nodes;       // 4 float4 per binary internal node (released after the collapse)
-    DeviceBuffer<float4> wide;        // 24 float4 per 8-wide node (the queries' tree)
+    DeviceBuffer<float4> wide;        // 16 float4 per 8-wide node (the queries' tree)
+    DeviceBuffer<int2> wide_range;    // 8 leaf ranges per wide node (trees over several problems)
     DeviceBuffer<float4> wide_cell;   // per wide node: its Morton cell as a box (lo + parent, hi), inset
     int64_t n_wide = 0;
     DeviceBuffer<float4> root_box;    // box of the whole tree (2 float4)

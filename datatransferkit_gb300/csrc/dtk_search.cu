@@ -552,11 +552,13 @@ constexpr int WIDE = 8;
 constexpr int WIDE_EMPTY = INT_MIN;
 
 // Child slot c of wide node `node`: its box, ref and (RANGE) leaf range.
+// A node is 8 x 32 bytes (one sector a child); the leaf ranges, needed only
+// by trees over several problems, are a separate array.
 template <bool RANGE>
-__device__ __forceinline__ void load_wide( float4 const *wide, int node, int c, float *lo, float *hi,
-                                           int &ref, int &end, int &rlo, int &rhi )
+__device__ __forceinline__ void load_wide( float4 const *wide, int2 const *wide_range, int node, int c,
+                                           float *lo, float *hi, int &ref, int &end, int &rlo, int &rhi )
 {
-    float4 const *p = wide + 24 * (int64_t)node + 3 * c;
+    float4 const *p = wide + 16 * (int64_t)node + 2 * c;
     float4 const a = __ldg( p ), b = __ldg( p + 1 );
     lo[0] = a.x;
     lo[1] = a.y;
@@ -568,9 +570,9 @@ __device__ __forceinline__ void load_wide( float4 const *wide, int node, int c, 
     end = __float_as_int( b.w );
     if ( RANGE )
     {
-        float4 const e = __ldg( p + 2 );
-        rlo = __float_as_int( e.x );
-        rhi = __float_as_int( e.y );
+        int2 const e = __ldg( wide_range + 8 * (int64_t)node + c );
+        rlo = e.x;
+        rhi = e.y;
     }
 }
 
@@ -647,7 +649,7 @@ __global__ void k_wide_cells( int64_t ni, int64_t const *flag, int64_t const *wi
 }
 
 __global__ void k_collapse( int64_t ni, float4 const *nodes, int64_t const *flag, int64_t const *widx,
-                            int32_t const *leaf_start, float4 *wide )
+                            int32_t const *leaf_start, float4 *wide, int2 *wide_range )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i >= ni || !flag[i] )
@@ -708,7 +710,8 @@ __global__ void k_collapse( int64_t ni, float4 const *nodes, int64_t const *flag
         }
         cnt = n2;
     }
-    float4 *out = wide + 24 * widx[i];
+    float4 *out = wide + 16 * widx[i];
+    int2 *out_range = wide_range + 8 * widx[i];
     for ( int c = 0; c < WIDE; ++c )
     {
         if ( c < cnt )
@@ -716,15 +719,15 @@ __global__ void k_collapse( int64_t ni, float4 const *nodes, int64_t const *flag
             // a leaf child carries its first and end positions
             int const r = ref[c] >= 0 ? (int)widx[ref[c]] : ~leaf_start[~ref[c]];
             int const end = ref[c] >= 0 ? 0 : leaf_start[~ref[c] + 1];
-            out[3 * c] = make_float4( box[c].lo[0], box[c].lo[1], box[c].lo[2], box[c].hi[0] );
-            out[3 * c + 1] = make_float4( box[c].hi[1], box[c].hi[2], __int_as_float( r ), __int_as_float( end ) );
-            out[3 * c + 2] = make_float4( __int_as_float( rlo[c] ), __int_as_float( rhi[c] ), 0.f, 0.f );
+            out[2 * c] = make_float4( box[c].lo[0], box[c].lo[1], box[c].lo[2], box[c].hi[0] );
+            out[2 * c + 1] = make_float4( box[c].hi[1], box[c].hi[2], __int_as_float( r ), __int_as_float( end ) );
+            out_range[c] = make_int2( rlo[c], rhi[c] );
         }
         else
         {
-            out[3 * c] = make_float4( INFINITY, INFINITY, INFINITY, -INFINITY );
-            out[3 * c + 1] = make_float4( -INFINITY, -INFINITY, __int_as_float( WIDE_EMPTY ), 0.f );
-            out[3 * c + 2] = make_float4( __int_as_float( 1 ), __int_as_float( 0 ), 0.f, 0.f );
+            out[2 * c] = make_float4( INFINITY, INFINITY, INFINITY, -INFINITY );
+            out[2 * c + 1] = make_float4( -INFINITY, -INFINITY, __int_as_float( WIDE_EMPTY ), 0.f );
+            out_range[c] = make_int2( 1, 0 );
         }
     }
 }
@@ -746,7 +749,8 @@ struct TreeView
     float const *fx, *fy, *fz;
     uint32_t const *codes, *perm;
     int32_t const *leaf_start, *leaf_of;
-    float4 const *wide; // 8-wide nodes (24 float4 each)
+    float4 const *wide; // 8-wide nodes (16 float4 each)
+    int2 const *wide_range; // per wide node: its children's leaf ranges (8 int2)
     float4 const *wide_cell; // per wide node: its Morton cell (lo + parent, hi)
     double const *scene;
     int64_t n, nl, nw;
@@ -1292,7 +1296,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                 {
                     int cref = -1;
                     if ( lane < WIDE )
-                        cref = __float_as_int( __ldg( tr.wide + 24 * (int64_t)e + 3 * lane + 1 ).z );
+                        cref = __float_as_int( __ldg( tr.wide + 16 * (int64_t)e + 2 * lane + 1 ).z );
                     unsigned const m = __ballot_sync( FULL, lane < WIDE && cref >= 0 && holds( cref ) );
                     if ( !m )
                         break;
@@ -1321,7 +1325,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                 {
                     float lo[3], hi[3];
                     int rlo = 0, rhi = 0;
-                    load_wide<GROUPED>( tr.wide, node, slot, lo, hi, ref, lend, rlo, rhi );
+                    load_wide<GROUPED>( tr.wide, tr.wide_range, node, slot, lo, hi, ref, lend, rlo, rhi );
                     lb = box_lb( lo, hi, q.qlo, q.qhi );
                     ok = ref != WIDE_EMPTY && ( GROUPED ? !( rhi < rg.lps || rlo > rg.lpe ) : true );
                 }
@@ -1476,7 +1480,7 @@ __global__ void __launch_bounds__( R_WARPS * 32 )
             {
                 float lo[3], hi[3];
                 int rlo = 0, rhi = 0;
-                load_wide<GROUPED>( tr.wide, node, slot, lo, hi, ref, lend, rlo, rhi );
+                load_wide<GROUPED>( tr.wide, tr.wide_range, node, slot, lo, hi, ref, lend, rlo, rhi );
                 cand = ref != WIDE_EMPTY && box_lb( lo, hi, q.qlo, q.qhi ) <= bound_f &&
                        ( GROUPED ? !( rhi < rg.lps || rlo > rg.lpe ) : true );
             }
@@ -1518,7 +1522,7 @@ TreeView view_of( Lbvh const &t )
 {
     return TreeView{t.sx.get(), t.sy.get(), t.sz.get(), t.fx.get(), t.fy.get(), t.fz.get(),
                     t.codes.get(), t.perm.get(), t.leaf_start.get(), t.leaf_of.get(), t.wide.get(),
-                    t.wide_cell.get(), t.scene.get(), t.n, t.n_leaves, t.n_wide};
+                    t.wide_range.get(), t.wide_cell.get(), t.scene.get(), t.n, t.n_leaves, t.n_wide};
 }
 
 unsigned blocks_for( int64_t n, int threads )
@@ -1636,9 +1640,11 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
         DTK_CUDA_OR_THROW( cudaMemcpyAsync( &nw, widx.get() + ni, sizeof( int64_t ), cudaMemcpyDeviceToHost, s ) );
         DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
         tree.n_wide = nw;
-        tree.wide.allocate( 24 * std::max<int64_t>( 1, nw ), s );
+        tree.wide.allocate( 16 * std::max<int64_t>( 1, nw ), s );
+        tree.wide_range.allocate( 8 * std::max<int64_t>( 1, nw ), s );
         k_collapse<<<blocks_for( ni, 128 ), 128, 0, s>>>( ni, tree.nodes.get(), flag.get(), widx.get(),
-                                                           tree.leaf_start.get(), tree.wide.get() );
+                                                           tree.leaf_start.get(), tree.wide.get(),
+                                                           tree.wide_range.get() );
         check_launch( "k_collapse" );
         tree.wide_cell.allocate( 2 * std::max<int64_t>( 1, nw ), s );
         k_wide_cells<<<blocks_for( ni, 256 ), 256, 0, s>>>( ni, flag.get(), widx.get(), parent_node.get(),
