@@ -384,11 +384,13 @@ dtk_status dtk_mls_transfer_host( const dtk_mls_options *opts, const double *src
         DTK_CUDA_OR_THROW( cudaStreamCreateWithFlags( &side.s2, cudaStreamNonBlocking ) );
         DeviceBuffer<double> d_src( 3 * n_src, s ), d_tgt( std::max<int64_t>( 1, 3 * n_tgt ), s ),
             d_vals( n_src, s ), d_out( std::max<int64_t>( 1, n_tgt ), s );
-        cudaEvent_t const allocated = side.event(), tgt_ready = side.event(), vals_ready = side.event();
-        DTK_CUDA_OR_THROW( cudaEventRecord( allocated, s ) );
-        DTK_CUDA_OR_THROW( cudaStreamWaitEvent( side.s2, allocated, 0 ) );
+        cudaEvent_t const src_in = side.event(), tgt_ready = side.event(), vals_ready = side.event();
         DTK_CUDA_OR_THROW( cudaMemcpyAsync( d_src.get(), src_host, 3 * n_src * sizeof( double ),
                                             cudaMemcpyHostToDevice, s ) );
+        // the targets and values follow the sources over the host link (the
+        // tree build needs only the sources; the later copies overlap it)
+        DTK_CUDA_OR_THROW( cudaEventRecord( src_in, s ) );
+        DTK_CUDA_OR_THROW( cudaStreamWaitEvent( side.s2, src_in, 0 ) );
         if ( n_tgt )
             DTK_CUDA_OR_THROW( cudaMemcpyAsync( d_tgt.get(), tgt_host, 3 * n_tgt * sizeof( double ),
                                                 cudaMemcpyHostToDevice, side.s2 ) );
