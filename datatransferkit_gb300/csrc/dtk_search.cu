@@ -229,8 +229,7 @@ __global__ void k_morton_of( PointsView p, uint32_t const *perm, double const *s
 }
 
 __global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double const *scene,
-                                 double *sx, double *sy, double *sz, float *fx, float *fy,
-                                 float *fz )
+                                 double *sx, double *sy, double *sz, float4 *f4 )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i < p.n )
@@ -240,9 +239,7 @@ __global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double cons
         sx[i] = x;
         sy[i] = y;
         sz[i] = z;
-        fx[i] = (float)( x - scene[9] );
-        fy[i] = (float)( y - scene[10] );
-        fz[i] = (float)( z - scene[11] );
+        f4[i] = make_float4( (float)( x - scene[9] ), (float)( y - scene[10] ), (float)( z - scene[11] ), 0.f );
     }
 }
 
@@ -746,7 +743,7 @@ struct GroupView
 struct TreeView
 {
     double const *sx, *sy, *sz;
-    float const *fx, *fy, *fz;
+    float4 const *f4; // centred FP32 coordinates (x, y, z, 0): one load a point
     uint32_t const *codes, *perm;
     int32_t const *leaf_start, *leaf_of;
     float4 const *wide; // 8-wide nodes (16 float4 each)
@@ -991,9 +988,10 @@ __global__ void k_query_frame( PointsView tgt, uint32_t const *order, double con
 __device__ __forceinline__ void d2_bounds( TreeView const &tr, Query const &q, int64_t p,
                                            float &lo, float &hi )
 {
-    float const dx = __ldg( tr.fx + p ) - q.tf[0];
-    float const dy = __ldg( tr.fy + p ) - q.tf[1];
-    float const dz = __ldg( tr.fz + p ) - q.tf[2];
+    float4 const f = __ldg( tr.f4 + p );
+    float const dx = f.x - q.tf[0];
+    float const dy = f.y - q.tf[1];
+    float const dz = f.z - q.tf[2];
     float const d2 = fmaf( dz, dz, fmaf( dy, dy, dx * dx ) );
     float const spread = q.err * ( 4.f * ( fabsf( dx ) + fabsf( dy ) + fabsf( dz ) ) + 3.f * q.err ) +
                          d2 * 9.5367431640625e-07f;
@@ -1235,9 +1233,10 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         unsigned const seen = __reduce_or_sync( FULL, seed_leaf == start ? seed_bit : 0u );
         if ( ( GROUPED ? p >= rg.ps && p < rg.pe : true ) && p < end && !( ( seen >> lane ) & 1u ) )
         {
-            float const dx = __ldg( tr.fx + p ) - q.tf[0];
-            float const dy = __ldg( tr.fy + p ) - q.tf[1];
-            float const dz = __ldg( tr.fz + p ) - q.tf[2];
+            float4 const f = __ldg( tr.f4 + p );
+            float const dx = f.x - q.tf[0];
+            float const dy = f.y - q.tf[1];
+            float const dz = f.z - q.tf[2];
             surv = fmaf( dz, dz, fmaf( dy, dy, dx * dx ) ) <= screen_f;
         }
         unsigned const m = __ballot_sync( FULL, surv );
@@ -1520,7 +1519,7 @@ __global__ void __launch_bounds__( R_WARPS * 32 )
 
 TreeView view_of( Lbvh const &t )
 {
-    return TreeView{t.sx.get(), t.sy.get(), t.sz.get(), t.fx.get(), t.fy.get(), t.fz.get(),
+    return TreeView{t.sx.get(), t.sy.get(), t.sz.get(), t.f4.get(),
                     t.codes.get(), t.perm.get(), t.leaf_start.get(), t.leaf_of.get(), t.wide.get(),
                     t.wide_range.get(), t.wide_cell.get(), t.scene.get(), t.n, t.n_leaves, t.n_wide};
 }
@@ -1596,12 +1595,10 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
     tree.sx.allocate( n, s );
     tree.sy.allocate( n, s );
     tree.sz.allocate( n, s );
-    tree.fx.allocate( n, s );
-    tree.fy.allocate( n, s );
-    tree.fz.allocate( n, s );
+    tree.f4.allocate( n, s );
     k_gather_sorted<<<blocks_for( n, 256 ), 256, 0, s>>>( src, tree.perm.get(), tree.scene.get(),
                                                             tree.sx.get(), tree.sy.get(), tree.sz.get(),
-                                                            tree.fx.get(), tree.fy.get(), tree.fz.get() );
+                                                            tree.f4.get() );
     check_launch( "k_gather_sorted" );
 
     int64_t const ni = std::max<int64_t>( 0, nl - 1 );
