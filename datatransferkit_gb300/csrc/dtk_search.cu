@@ -229,16 +229,15 @@ __global__ void k_morton_of( PointsView p, uint32_t const *perm, double const *s
 }
 
 __global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double const *scene,
-                                 double *sx, double *sy, double *sz, float4 *f4 )
+                                 double2 *s2, float4 *f4 )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i < p.n )
     {
         int64_t const o = perm[i];
         double const x = p( o, 0 ), y = p( o, 1 ), z = p( o, 2 );
-        sx[i] = x;
-        sy[i] = y;
-        sz[i] = z;
+        s2[2 * i] = make_double2( x, y );
+        s2[2 * i + 1] = make_double2( z, __longlong_as_double( o ) );
         f4[i] = make_float4( (float)( x - scene[9] ), (float)( y - scene[10] ), (float)( z - scene[11] ), 0.f );
     }
 }
@@ -428,7 +427,7 @@ __device__ __forceinline__ Box load_child_box( float4 const *nodes, int parent, 
 
 // One thread per leaf: leaf box, then walk up; the second child to arrive at
 // a node computes its box and continues.
-__global__ void k_refit( double const *sx, double const *sy, double const *sz,
+__global__ void k_refit( double2 const *s2,
                          double const *scene, int32_t const *leaf_start, int64_t nl, int const *left,
                          int const *right,
                          int const *parent_node, int const *parent_leaf, float4 *nodes,
@@ -438,11 +437,11 @@ __global__ void k_refit( double const *sx, double const *sy, double const *sz,
     if ( leaf >= nl )
         return;
     int64_t const begin = leaf_start[leaf], end = leaf_start[leaf + 1];
-    double lo[3] = {sx[begin], sy[begin], sz[begin]};
+    double lo[3] = {s2[2 * begin].x, s2[2 * begin].y, s2[2 * begin + 1].x};
     double hi[3] = {lo[0], lo[1], lo[2]};
     for ( int64_t p = begin + 1; p < end; ++p )
     {
-        double const c[3] = {sx[p], sy[p], sz[p]};
+        double const c[3] = {s2[2 * p].x, s2[2 * p].y, s2[2 * p + 1].x};
 #pragma unroll
         for ( int d = 0; d < 3; ++d )
         {
@@ -742,7 +741,7 @@ struct GroupView
 
 struct TreeView
 {
-    double const *sx, *sy, *sz;
+    double2 const *s2; // Morton-sorted FP64 points: (x, y), (z, original index bits)
     float4 const *f4; // centred FP32 coordinates (x, y, z, 0): one load a point
     uint32_t const *codes, *perm;
     int32_t const *leaf_start, *leaf_of;
@@ -984,6 +983,14 @@ __global__ void k_query_frame( PointsView tgt, uint32_t const *order, double con
                          __double2float_rn( tgt( qi, 2 ) - scene[11] ), 0.f );
 }
 
+// Sorted source p: the FP64 squared distance to the query (the exact key)
+// and the source's original index (its bits in .y); two 16-byte loads.
+__device__ __forceinline__ double2 sorted_dist2( TreeView const &tr, int64_t p, Query const &q )
+{
+    double2 const a = __ldg( tr.s2 + 2 * p ), b = __ldg( tr.s2 + 2 * p + 1 );
+    return make_double2( dist2_rn( a.x, a.y, b.x, q.tx, q.ty, q.tz ), b.y );
+}
+
 // FP32 bounds lo <= d2(p, t) <= hi for sorted source p (centred FP32 copy).
 __device__ __forceinline__ void d2_bounds( TreeView const &tr, Query const &q, int64_t p,
                                            float &lo, float &hi )
@@ -1109,7 +1116,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         // row hold entries that insertions shifted out: cleared)
         if ( lane < row )
             kd = (unsigned long long)__double_as_longlong(
-                dist2_rn( __ldg( tr.sx + kp ), __ldg( tr.sy + kp ), __ldg( tr.sz + kp ), q.tx, q.ty, q.tz ) );
+                sorted_dist2( tr, kp, q ).x );
         else
         {
             kd = KEY_INF;
@@ -1135,9 +1142,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         if ( lane < W )
         {
             int64_t const p = s0 + lane;
-            kd = (unsigned long long)__double_as_longlong(
-                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), q.tx, q.ty, q.tz ) );
-            ki = (int)__ldg( tr.perm + p );
+            double2 const e = sorted_dist2( tr, p, q );
+            kd = (unsigned long long)__double_as_longlong( e.x );
+            ki = (int)__double_as_longlong( e.y );
             kp = (int)p;
         }
     }
@@ -1172,9 +1179,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         int ci = 0x7fffffff, cp = -1;
         if ( p >= 0 )
         {
-            cd = (unsigned long long)__double_as_longlong(
-                dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ), q.tx, q.ty, q.tz ) );
-            ci = (int)__ldg( tr.perm + p );
+            double2 const e = sorted_dist2( tr, p, q );
+            cd = (unsigned long long)__double_as_longlong( e.x );
+            ci = (int)__double_as_longlong( e.y );
             cp = p;
         }
         // the list's k-th key, the bound a candidate must beat
@@ -1433,8 +1440,7 @@ __global__ void __launch_bounds__( R_WARPS * 32 )
         }
         if ( __any_sync( FULL, unsure ) && unsure )
         {
-            double const d2 = dist2_rn( __ldg( tr.sx + p ), __ldg( tr.sy + p ), __ldg( tr.sz + p ),
-                                        q.tx, q.ty, q.tz );
+            double const d2 = sorted_dist2( tr, p, q ).x;
             hit = __dsqrt_rn( d2 ) <= r;
         }
         unsigned const b = __ballot_sync( FULL, hit );
@@ -1519,7 +1525,7 @@ __global__ void __launch_bounds__( R_WARPS * 32 )
 
 TreeView view_of( Lbvh const &t )
 {
-    return TreeView{t.sx.get(), t.sy.get(), t.sz.get(), t.f4.get(),
+    return TreeView{t.s2.get(), t.f4.get(),
                     t.codes.get(), t.perm.get(), t.leaf_start.get(), t.leaf_of.get(), t.wide.get(),
                     t.wide_range.get(), t.wide_cell.get(), t.scene.get(), t.n, t.n_leaves, t.n_wide};
 }
@@ -1592,13 +1598,10 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
     }
     tree.n_leaves = nl;
 
-    tree.sx.allocate( n, s );
-    tree.sy.allocate( n, s );
-    tree.sz.allocate( n, s );
+    tree.s2.allocate( 2 * n, s );
     tree.f4.allocate( n, s );
     k_gather_sorted<<<blocks_for( n, 256 ), 256, 0, s>>>( src, tree.perm.get(), tree.scene.get(),
-                                                            tree.sx.get(), tree.sy.get(), tree.sz.get(),
-                                                            tree.f4.get() );
+                                                            tree.s2.get(), tree.f4.get() );
     check_launch( "k_gather_sorted" );
 
     int64_t const ni = std::max<int64_t>( 0, nl - 1 );
@@ -1620,7 +1623,7 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
                                                                  range_hi.get(), tree.nodes.get() );
         check_launch( "k_pack_children" );
     }
-    k_refit<<<blocks_for( nl, 128 ), 128, 0, s>>>( tree.sx.get(), tree.sy.get(), tree.sz.get(),
+    k_refit<<<blocks_for( nl, 128 ), 128, 0, s>>>( tree.s2.get(),
                                                      tree.scene.get(), tree.leaf_start.get(), nl,
                                                      left.get(), right.get(), parent_node.get(),
                                                      parent_leaf.get(), tree.nodes.get(), flags.get(),
