@@ -354,7 +354,7 @@ struct Lbvh
     int64_t n_leaves = 0; // leaves: the Morton cells of at most 32 points
     double lo[3], hi[3];  // scene bounds (host copy)
     DeviceBuffer<double2> s2;         // Morton-sorted coordinates: (x, y), (z, original index bits)
-    DeviceBuffer<float4> f4;          // the same, centred on the scene box, FP32 (x, y, z, 0)
+    DeviceBuffer<float4> f4;          // the same, centred on the scene box, FP32 (x, y, z), and the leaf's first position
     DeviceBuffer<uint32_t> codes;     // Morton codes in sorted order
     DeviceBuffer<uint32_t> grp;       // group (problem) of each sorted point; empty if ungrouped
     DeviceBuffer<uint32_t> perm;      // sorted position -> original index

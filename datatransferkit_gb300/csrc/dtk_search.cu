@@ -229,7 +229,7 @@ __global__ void k_morton_of( PointsView p, uint32_t const *perm, double const *s
 }
 
 __global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double const *scene,
-                                 double2 *s2, float4 *f4 )
+                                 int32_t const *leaf_of, int32_t const *leaf_start, double2 *s2, float4 *f4 )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i < p.n )
@@ -238,7 +238,8 @@ __global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double cons
         double const x = p( o, 0 ), y = p( o, 1 ), z = p( o, 2 );
         s2[2 * i] = make_double2( x, y );
         s2[2 * i + 1] = make_double2( z, __longlong_as_double( o ) );
-        f4[i] = make_float4( (float)( x - scene[9] ), (float)( y - scene[10] ), (float)( z - scene[11] ), 0.f );
+        f4[i] = make_float4( (float)( x - scene[9] ), (float)( y - scene[10] ), (float)( z - scene[11] ),
+                             __int_as_float( leaf_start[leaf_of[i]] ) );
     }
 }
 
@@ -742,7 +743,7 @@ struct GroupView
 struct TreeView
 {
     double2 const *s2; // Morton-sorted FP64 points: (x, y), (z, original index bits)
-    float4 const *f4; // centred FP32 coordinates (x, y, z, 0): one load a point
+    float4 const *f4; // centred FP32 coordinates (x, y, z) and the first position of the point's leaf
     uint32_t const *codes, *perm;
     int32_t const *leaf_start, *leaf_of;
     float4 const *wide; // 8-wide nodes (16 float4 each)
@@ -983,6 +984,12 @@ __global__ void k_query_frame( PointsView tgt, uint32_t const *order, double con
                          __double2float_rn( tgt( qi, 2 ) - scene[11] ), 0.f );
 }
 
+// First sorted position of the leaf of sorted source p.
+__device__ __forceinline__ int leaf_first( TreeView const &tr, int64_t p )
+{
+    return __float_as_int( __ldg( reinterpret_cast<float const *>( tr.f4 + p ) + 3 ) );
+}
+
 // Sorted source p: the FP64 squared distance to the query (the exact key)
 // and the source's original index (its bits in .y); two 16-byte loads.
 __device__ __forceinline__ double2 sorted_dist2( TreeView const &tr, int64_t p, Query const &q )
@@ -1158,7 +1165,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     }
     // the list's starting members by leaf and lane: a leaf screens them out
     // (a leaf is named by its first position)
-    int seed_leaf = kp >= 0 ? tr.leaf_start[tr.leaf_of[kp]] : -1;
+    int seed_leaf = kp >= 0 ? leaf_first( tr, kp ) : -1;
     unsigned seed_bit = kp >= 0 ? 1u << ( kp - seed_leaf ) : 0u;
     // speculative bound (seeded queries with full rows): boxes and points
     // beyond it are skipped as if the list were already that tight
@@ -1385,7 +1392,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         if ( !( spec < __int_as_float( 0x7f800000 ) ) ||
              ru_float_of( bd ) <= __fmul_rd( spec, 1.0f - 9.5367431640625e-07f ) )
             break;
-        seed_leaf = kp >= 0 ? tr.leaf_start[tr.leaf_of[kp]] : -1;
+        seed_leaf = kp >= 0 ? leaf_first( tr, kp ) : -1;
         seed_bit = kp >= 0 ? 1u << ( kp - seed_leaf ) : 0u;
         spec = __int_as_float( 0x7f800000 );
         bound_f = prune_threshold( bd );
@@ -1601,6 +1608,7 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
     tree.s2.allocate( 2 * n, s );
     tree.f4.allocate( n, s );
     k_gather_sorted<<<blocks_for( n, 256 ), 256, 0, s>>>( src, tree.perm.get(), tree.scene.get(),
+                                                            tree.leaf_of.get(), tree.leaf_start.get(),
                                                             tree.s2.get(), tree.f4.get() );
     check_launch( "k_gather_sorted" );
 
