@@ -926,14 +926,13 @@ struct Query
     float err;
 };
 
-__device__ __forceinline__ Query make_query( TreeView const &tr, PointsView const &tgt,
-                                             int64_t qi )
+__device__ __forceinline__ Query make_query( double const *scene, PointsView const &tgt, int64_t qi )
 {
     Query q;
     q.tx = tgt( qi, 0 );
     q.ty = tgt( qi, 1 );
     q.tz = tgt( qi, 2 );
-    double const tc[3] = {q.tx - tr.scene[9], q.ty - tr.scene[10], q.tz - tr.scene[11]};
+    double const tc[3] = {q.tx - scene[9], q.ty - scene[10], q.tz - scene[11]};
     float tmax = 0.f;
 #pragma unroll
     for ( int d = 0; d < 3; ++d )
@@ -945,43 +944,21 @@ __device__ __forceinline__ Query make_query( TreeView const &tr, PointsView cons
         q.qhi[d] = nextafterf( q.tf[d], INFINITY );
         tmax = fmaxf( tmax, fmaxf( fabsf( q.qlo[d] ), fabsf( q.qhi[d] ) ) );
     }
-    q.err = ( reinterpret_cast<float const *>( tr.scene + 13 )[6] + tmax ) * 2.384185791015625e-07f; // 2^-22
+    q.err = ( reinterpret_cast<float const *>( scene + 13 )[6] + tmax ) * 2.384185791015625e-07f; // 2^-22
     return q;
 }
 
-// The same from a precomputed FP32 centred position tf = fl32(t - c) (the
-// FP64 subtraction and conversion are done once per target by
-// k_query_frame, off the search's FP64 pipe).
-__device__ __forceinline__ Query make_query_from( TreeView const &tr, PointsView const &tgt, int64_t qi,
-                                                  float4 tfv )
-{
-    Query q;
-    q.tx = tgt( qi, 0 );
-    q.ty = tgt( qi, 1 );
-    q.tz = tgt( qi, 2 );
-    float const tf[3] = {tfv.x, tfv.y, tfv.z};
-    float tmax = 0.f;
-#pragma unroll
-    for ( int d = 0; d < 3; ++d )
-    {
-        q.tf[d] = tf[d];
-        q.qlo[d] = nextafterf( tf[d], -INFINITY );
-        q.qhi[d] = nextafterf( tf[d], INFINITY );
-        tmax = fmaxf( tmax, fmaxf( fabsf( q.qlo[d] ), fabsf( q.qhi[d] ) ) );
-    }
-    q.err = ( reinterpret_cast<float const *>( tr.scene + 13 )[6] + tmax ) * 2.384185791015625e-07f; // 2^-22
-    return q;
-}
-
-// tf = fl32(t - c) of the w-th query in processing order.
-__global__ void k_query_frame( PointsView tgt, uint32_t const *order, double const *scene, float4 *qf )
+// The w-th query in processing order, prepared once per target (the FP64
+// subtractions and conversions off the search's FP64 pipe, the interval's
+// round-ups off its issue slots): the search copies the 64-byte record into
+// shared memory with one coalesced load.
+static_assert( sizeof( Query ) == 64, "a query record is 16 words" );
+__global__ void k_query_frame( PointsView tgt, uint32_t const *order, double const *scene, Query *qrec )
 {
     int64_t const w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( w >= tgt.n )
         return;
-    int64_t const qi = order ? (int64_t)order[w] : w;
-    qf[w] = make_float4( __double2float_rn( tgt( qi, 0 ) - scene[9] ), __double2float_rn( tgt( qi, 1 ) - scene[10] ),
-                         __double2float_rn( tgt( qi, 2 ) - scene[11] ), 0.f );
+    qrec[w] = make_query( scene, tgt, order ? (int64_t)order[w] : w );
 }
 
 // First sorted position of the leaf of sorted source p.
@@ -1062,7 +1039,7 @@ __device__ __forceinline__ void chunk_range( KnnChunks const &ch, unsigned c, in
 
 template <bool GROUPED>
 __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
-    k_knn( TreeView tr, PointsView tgt, uint32_t const *order, float4 const *qframe, int k_all, KnnChunks ch,
+    k_knn( TreeView tr, PointsView tgt, uint32_t const *order, Query const *qrec, int k_all, KnnChunks ch,
            GroupView gv,
            int32_t const *offset, int32_t *idx_out, unsigned *status )
 {
@@ -1108,11 +1085,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     }
     // the query waits in shared memory: registers limit how many warps an
     // SM holds, and values there can be re-read instead of spilled
-    {
-        Query const qv = make_query_from( tr, tgt, qi, __ldg( qframe + w ) );
-        if ( lane == 0 )
-            s_query[wib] = qv;
-    }
+    if ( lane < 16 )
+        reinterpret_cast<uint32_t *>( &s_query[wib] )[lane] =
+            __ldg( reinterpret_cast<uint32_t const *>( qrec + w ) + lane );
     __syncwarp();
     Query const &q = s_query[wib];
     bool const seeded = prev_row == row && ( !GROUPED || prev_g == rg.g );
@@ -1173,6 +1148,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     float bound_f = fminf( prune_threshold( __shfl_sync( FULL, kd, k - 1 ) ), spec );
     float screen_f = screen_threshold( bound_f, q.err ); // the leaf screen's bound
     int qn = 0; // queued survivors (warp-uniform)
+    float kth_ru = __int_as_float( 0x7f800000 ); // the final k-th key rounded up to FP32
 
     // Exact FP64 keys for up to 32 queued sources, merged into the list as a
     // batch: the candidates below the bound are sorted (bitonic) and merged
@@ -1389,8 +1365,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         // or below spec (1 - 2^-20) (tested as its FP32 round-up against the
         // round-down product) loses nothing.
         unsigned long long const bd = __shfl_sync( FULL, kd, k - 1 );
-        if ( !( spec < __int_as_float( 0x7f800000 ) ) ||
-             ru_float_of( bd ) <= __fmul_rd( spec, 1.0f - 9.5367431640625e-07f ) )
+        kth_ru = ru_float_of( bd );
+        if ( !( spec < __int_as_float( 0x7f800000 ) ) || kth_ru <= __fmul_rd( spec, 1.0f - 9.5367431640625e-07f ) )
             break;
         seed_leaf = kp >= 0 ? leaf_first( tr, kp ) : -1;
         seed_bit = kp >= 0 ? 1u << ( kp - seed_leaf ) : 0u;
@@ -1402,7 +1378,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         idx_out[offset[qi] + lane] = ki;
     prev_g = rg.g;
     prev_row = row;
-    next_spec = __fmul_ru( prune_threshold( __shfl_sync( FULL, kd, k - 1 ) ), SPEC_GROWTH );
+    next_spec = __fmul_ru( __fmul_ru( kth_ru, 1.0f + 9.5367431640625e-07f ), SPEC_GROWTH ); // prune_threshold
     __syncwarp();
     }
     }
@@ -1427,7 +1403,7 @@ __global__ void __launch_bounds__( R_WARPS * 32 )
     int64_t const qi = order ? (int64_t)order[w] : w;
     Range const rg = query_range<GROUPED>( tr, gv, qi );
     double const r = GROUPED ? gv.r[rg.g] : r_all;
-    Query const q = make_query( tr, tgt, qi );
+    Query const q = make_query( tr.scene, tgt, qi );
     double const r2 = __dmul_ru( r, r );
     float const bound_f = prune_threshold( (unsigned long long)__double_as_longlong( r2 ) );
     float const in_f = __fmul_rd( __double2float_rd( __dmul_rd( r, r ) ), 1.0f - 9.5367431640625e-07f );
@@ -1745,14 +1721,14 @@ void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
     DeviceBuffer<unsigned> next( 1, s );
     DTK_CUDA_OR_THROW( cudaMemsetAsync( next.get(), 0, sizeof( unsigned ), s ) );
     KnnChunks const ch{seq, n_big, next.get()};
-    DeviceBuffer<float4> qframe( tgt.n, s );
-    k_query_frame<<<blocks_for( tgt.n, 256 ), 256, 0, s>>>( tgt, order, tree.scene.get(), qframe.get() );
+    DeviceBuffer<Query> qrec( tgt.n, s );
+    k_query_frame<<<blocks_for( tgt.n, 256 ), 256, 0, s>>>( tgt, order, tree.scene.get(), qrec.get() );
     check_launch( "k_query_frame" );
     if ( groups.tgt_grp )
-        k_knn<true><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, qframe.get(), k, ch, gv,
+        k_knn<true><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, qrec.get(), k, ch, gv,
                                                      offset, idx, status );
     else
-        k_knn<false><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, qframe.get(), k, ch, gv,
+        k_knn<false><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, qrec.get(), k, ch, gv,
                                                       offset, idx, status );
     check_launch( "k_knn" );
 }
