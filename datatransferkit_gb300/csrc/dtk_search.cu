@@ -1155,7 +1155,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     // with the list (elementwise minimum against the reversed candidates, then
     // a bitonic clean), keeping the k smallest (d2, index).  No candidate is
     // in the list already: the list's starting members are screened out.
-    auto flush = [&]( int count ) {
+    auto flush = [&]( int count, bool last ) {
         int const p = lane < count ? s_queue[wib][lane] : -1;
         __syncwarp();
         unsigned long long cd = KEY_INF;
@@ -1202,6 +1202,13 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                 kp = -1;
             }
         }
+        // (the pass's last merge: the proof reads the list itself, and a
+        // second pass sets its own bounds)
+        if ( last )
+        {
+            qn = 0;
+            return;
+        }
         bound_f = fminf( prune_threshold( __shfl_sync( FULL, kd, k - 1 ) ), spec );
         screen_f = screen_threshold( bound_f, q.err );
         // move the remaining queue entries to the front
@@ -1235,7 +1242,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         __syncwarp();
         qn += __popc( m );
         if ( qn >= 32 )
-            flush( 32 );
+            flush( 32, false );
     };
 
     // A pass searches the tree; a second one follows only when the
@@ -1358,7 +1365,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
             }
         }
         if ( qn > 0 )
-            flush( qn );
+            flush( qn, true );
         // Proof: a skipped box or point had an FP32 lower bound above spec,
         // so its exact squared distance exceeds spec and its FP64 key (a few
         // ulps off the exact value) exceeds spec (1 - 2^-40); a k-th key at
