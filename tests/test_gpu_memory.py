@@ -37,7 +37,11 @@ def test_pool_caches_then_releases():
     dtk.release_cached_memory()
     free2 = free_bytes()
     assert free2 > free1 + 100 * MB
-    assert free2 > free0 - 64 * MB  # only the live operator's buffers remain
+    # only the live operator's buffers remain: its small allocations may sit
+    # in (and keep mapped) one block the pool carved for a larger transient
+    # buffer of the first setup (the 64 MB of query records at 1M targets);
+    # the first operator's CSR alone is 384 MB
+    assert free2 > free0 - 128 * MB
     y = torch.empty(1000, dtype=torch.float64, device="cuda")
     keep.apply(vals[:1000], y)  # still usable after the release
     assert torch.isfinite(y).all()
