@@ -4,8 +4,9 @@
 // (packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:114-129).
 //
 // Build: scene box -> 30-bit Morton codes (FP32 quantization) -> stable
-// radix sort (codes, ids) -> Morton-sorted FP64 coordinates (SoA, plus FP32
-// copies centred on the scene) -> leaves: the Morton cells of at most 32
+// radix sort (codes, ids) -> Morton-sorted FP64 coordinates (packed with the
+// original index, plus FP32 copies centred on the scene with each point's
+// leaf start) -> leaves: the Morton cells of at most 32
 // points (the key trie split one bit at a time) -> Karras (2012) binary radix
 // tree over the leaf keys (first code of each leaf, ties broken by leaf
 // index) -> bottom-up refit of FP32 boxes rounded outward -> collapse into an
@@ -13,9 +14,10 @@
 // children of a node at once; each wide node also keeps its Morton cell (an
 // inset FP32 box) and its parent.
 //
-// kNN query: a warp runs up to 64 Morton-consecutive targets one after the
-// other; the k best (d2, index) keys sit one per lane, sorted across lanes.
-// The first target of a warp starts from the 32 Morton-sorted sources around
+// kNN query: a warp runs chunks of 48 Morton-consecutive targets one after
+// the other, taking the next chunk from a counter; the k best (d2, index)
+// keys sit one per lane, sorted across lanes.
+// The first target of a chunk starts from the 32 Morton-sorted sources around
 // its code, every later one from the previous target's final list re-keyed
 // for it (neighbouring targets share most neighbours).  The starting members
 // are screened out of their leaves (a warp OR-reduction of a per-leaf lane
@@ -55,7 +57,7 @@ constexpr int NODE_GROUPS = 4; // wide nodes a kNN warp tests per step (8 lanes 
 static_assert( NODE_GROUPS * 8 == 32, "one lane per child slot" );
 constexpr int Q_WARPS = 16; // warps per block in the kNN query kernel
 constexpr int R_WARPS = 4; // warps per block in the radius query kernel
-constexpr int Q_SEQ = 48;  // most consecutive kNN queries per warp (each seeds the next)
+constexpr int Q_SEQ = 48;  // kNN queries per chunk, run in order by one warp (each seeds the next)
 // kNN blocks per SM: 4 blocks of 16 warps (all 64 warp slots) cap the kernel
 // at 32 registers, with the query in shared memory; the values spilled cost
 // less than the warps gained (8M-point query, 4-warp blocks: 39.0 ms at 8
