@@ -365,6 +365,7 @@ struct Lbvh
     DeviceBuffer<int2> wide_range;    // 8 leaf ranges per wide node (trees over several problems)
     DeviceBuffer<float4> wide_cell;   // per wide node: its Morton cell as a box (lo + parent, hi), inset
     int64_t n_wide = 0;
+    int wide_levels = 0;              // the deepest wide node's level (root 0)
     DeviceBuffer<float4> root_box;    // box of the whole tree (2 float4)
     DeviceBuffer<double> scene;       // lo[3], Morton scale[3], hi[3], centre[3], bound S, FP32 lo/scale
 };

@@ -52,7 +52,7 @@ namespace
 
 constexpr int LEAF = 32;
 constexpr int STACK = 256; // wide-node stack entries per warp (radius search)
-constexpr int K_STACK = 192; // the same for the kNN search
+constexpr int K_STACK = 256; // the same for the kNN search
 constexpr int NODE_GROUPS = 4; // wide nodes a kNN warp tests per step (8 lanes each)
 static_assert( NODE_GROUPS * 8 == 32, "one lane per child slot" );
 constexpr int Q_WARPS = 16; // warps per block in the kNN query kernel
@@ -575,7 +575,10 @@ __device__ __forceinline__ void load_wide( float4 const *wide, int2 const *wide_
     }
 }
 
-__global__ void k_depth_flags( int64_t ni, int const *parent_node, int64_t *flag, unsigned *status )
+// Wide nodes: the binary nodes at depths 0, 3, 6, ...; max_depth gets the
+// largest binary depth (the wide levels bound the traversal stacks).
+__global__ void k_depth_flags( int64_t ni, int const *parent_node, int64_t *flag, unsigned *max_depth,
+                               unsigned *status )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i >= ni )
@@ -593,6 +596,10 @@ __global__ void k_depth_flags( int64_t ni, int const *parent_node, int64_t *flag
         }
     }
     flag[i] = d % 3 == 0 ? 1 : 0;
+    unsigned const m = __activemask();
+    unsigned const dm = __reduce_max_sync( m, (unsigned)d );
+    if ( ( threadIdx.x & 31 ) == __ffs( m ) - 1 )
+        atomicMax( max_depth, dm );
 }
 
 __device__ __forceinline__ uint32_t compact10( uint32_t v )
@@ -753,6 +760,7 @@ struct TreeView
     float4 const *wide_cell; // per wide node: its Morton cell (lo + parent, hi)
     double const *scene;
     int64_t n, nl, nw;
+    int levels; // the deepest wide node's level (the root's is 0)
 };
 
 // FP32 lower bound of the squared distance between any point of [lo, hi]
@@ -1263,7 +1271,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
             // (lanes 8g .. 8g+7) tests the 8 children of its node; leaf children
             // are screened in lane order, internal children go on the stack in
             // lane order, and the next step takes the top entries.  A step
-            // takes at most (K_STACK - sp) / 7
+            // takes four nodes only while a depth-first descent after them
+            // fits, else one
             // entries (at least one), so its children fit on the stack.
             int sp = 0;
             int const grp = lane >> 3, slot = lane & 7;
@@ -1354,10 +1363,13 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                 }
                 // the next nodes: the top P entries (a node is pushed only when
                 // its box passes the bound; the bound tightens rarely during a
-                // search, and a node's children are tested against it again)
-                int const P = sp <= K_STACK - NODE_GROUPS * ( WIDE - 1 )
-                                  ? NODE_GROUPS
-                                  : max( 1, ( K_STACK - sp ) / ( WIDE - 1 ) );
+                // search, and a node's children are tested against it again).
+                // Four only while the stack has room for their children and
+                // for a depth-first descent below them (one node a step adds
+                // at most 7 entries a level), else one: the stack holds at
+                // most 7 entries per wide level on top of what a four-node
+                // step left, so it cannot overflow while 7 levels + 1 fit.
+                int const P = sp + ( NODE_GROUPS + tr.levels ) * ( WIDE - 1 ) <= K_STACK ? NODE_GROUPS : 1;
                 int const taken = sp < P ? sp : P;
                 if ( taken == 0 )
                     break;
@@ -1501,8 +1513,9 @@ __global__ void __launch_bounds__( R_WARPS * 32 )
             }
             if ( sp == 0 )
                 break;
-            int const room = ( STACK - sp ) / ( WIDE - 1 );
-            int const P = room >= NODE_GROUPS ? NODE_GROUPS : ( room > 0 ? room : 1 );
+            // four nodes only while a depth-first descent after them fits
+            // (as in the kNN traversal), else one
+            int const P = sp + ( NODE_GROUPS + tr.levels ) * ( WIDE - 1 ) <= STACK ? NODE_GROUPS : 1;
             int const take = P < sp ? P : sp;
             node = grp < take ? s_stack[wib][sp - 1 - grp] : -1;
             sp -= take;
@@ -1519,7 +1532,8 @@ TreeView view_of( Lbvh const &t )
 {
     return TreeView{t.s2.get(), t.f4.get(),
                     t.codes.get(), t.perm.get(), t.leaf_start.get(), t.leaf_of.get(), t.wide.get(),
-                    t.wide_range.get(), t.wide_cell.get(), t.scene.get(), t.n, t.n_leaves, t.n_wide};
+                    t.wide_range.get(), t.wide_cell.get(), t.scene.get(), t.n, t.n_leaves, t.n_wide,
+                    t.wide_levels};
 }
 
 unsigned blocks_for( int64_t n, int threads )
@@ -1626,13 +1640,19 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
     if ( ni > 0 )
     {
         DeviceBuffer<int64_t> flag( ni, s ), widx( ni + 1, s );
-        k_depth_flags<<<blocks_for( ni, 256 ), 256, 0, s>>>( ni, parent_node.get(), flag.get(), status );
+        DeviceBuffer<unsigned> max_depth( 1, s );
+        DTK_CUDA_OR_THROW( cudaMemsetAsync( max_depth.get(), 0, sizeof( unsigned ), s ) );
+        k_depth_flags<<<blocks_for( ni, 256 ), 256, 0, s>>>( ni, parent_node.get(), flag.get(), max_depth.get(),
+                                                             status );
         check_launch( "k_depth_flags" );
         exclusive_scan_i64( flag.get(), widx.get(), ni, s );
         int64_t nw = 0;
+        unsigned depth = 0;
         DTK_CUDA_OR_THROW( cudaMemcpyAsync( &nw, widx.get() + ni, sizeof( int64_t ), cudaMemcpyDeviceToHost, s ) );
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( &depth, max_depth.get(), sizeof( unsigned ), cudaMemcpyDeviceToHost, s ) );
         DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
         tree.n_wide = nw;
+        tree.wide_levels = (int)( depth / 3 );
         tree.wide.allocate( 16 * std::max<int64_t>( 1, nw ), s );
         tree.wide_range.allocate( 8 * std::max<int64_t>( 1, nw ), s );
         k_collapse<<<blocks_for( ni, 128 ), 128, 0, s>>>( ni, tree.nodes.get(), flag.get(), widx.get(),
