@@ -51,8 +51,7 @@ namespace
 {
 
 constexpr int LEAF = 32;
-constexpr int STACK = 256; // wide-node stack entries per warp (radius search)
-constexpr int K_STACK = 256; // the same for the kNN search
+constexpr int STACK = 256; // wide-node stack entries per warp (kNN and radius search)
 constexpr int NODE_GROUPS = 4; // wide nodes a kNN warp tests per step (8 lanes each)
 static_assert( NODE_GROUPS * 8 == 32, "one lane per child slot" );
 constexpr int Q_WARPS = 16; // warps per block in the kNN query kernel
@@ -1055,7 +1054,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
 {
     // the stack of wide nodes to enter: small, to leave most of the SM's L1
     // to the tree and the points
-    __shared__ int s_stack[Q_WARPS][K_STACK];
+    __shared__ int s_stack[Q_WARPS][STACK];
     __shared__ int s_queue[Q_WARPS][QUEUE];
     __shared__ Query s_query[Q_WARPS];
     __shared__ int s_entry[Q_WARPS]; // the wide node the previous query started from
@@ -1340,7 +1339,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                 unsigned const ml = __ballot_sync( FULL, cand && ref < 0 );
                 unsigned const mi = __ballot_sync( FULL, cand && ref >= 0 );
                 int const n_int = __popc( mi );
-                if ( sp + n_int <= K_STACK )
+                if ( sp + n_int <= STACK )
                 {
                     if ( cand && ref >= 0 )
                     {
@@ -1369,7 +1368,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
                 // at most 7 entries a level), else one: the stack holds at
                 // most 7 entries per wide level on top of what a four-node
                 // step left, so it cannot overflow while 7 levels + 1 fit.
-                int const P = sp + ( NODE_GROUPS + tr.levels ) * ( WIDE - 1 ) <= K_STACK ? NODE_GROUPS : 1;
+                int const P = sp + ( NODE_GROUPS + tr.levels ) * ( WIDE - 1 ) <= STACK ? NODE_GROUPS : 1;
                 int const taken = sp < P ? sp : P;
                 if ( taken == 0 )
                     break;
