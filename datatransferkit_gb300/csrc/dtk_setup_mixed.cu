@@ -64,59 +64,6 @@ __device__ __forceinline__ float weight32( int rbf, float x, float y, float z )
     return rbf_eval<float>( rbf, sqrtf( x * x + y * y + z * z ) );
 }
 
-// Refinement and coefficients shared by both paths: a += M (e0 - A a) with
-// the FP64 residual over the neighbours, `steps` times, then
-// c_j = phi_j (P_j . a) stored in FP32.  `pinv32(v, y)` applies M in FP32.
-template <int M, class Scaled, class Pinv>
-__device__ __forceinline__ void refine_and_store( int len, int rbf, int steps, Scaled const &scaled,
-                                                  Pinv const &pinv32, double *a, float *coeff_row )
-{
-    for ( int step = 0; step < steps; ++step )
-    {
-        double r[M];
-#pragma unroll
-        for ( int q = 0; q < M; ++q )
-            r[q] = q == 0 ? 1.0 : 0.0;
-        for ( int j = 0; j < len; ++j )
-        {
-            float x, y, z;
-            scaled( j, x, y, z );
-            double P[M];
-            basis_eval<M, double>( (double)x, (double)y, (double)z, P );
-            double const phi = (double)weight32( rbf, x, y, z );
-            double dot = 0.0;
-#pragma unroll
-            for ( int q = 0; q < M; ++q )
-                dot = fma( P[q], a[q], dot );
-            double const w = phi * dot;
-#pragma unroll
-            for ( int q = 0; q < M; ++q )
-                r[q] = fma( -w, P[q], r[q] );
-        }
-        float rf[M], d[M];
-#pragma unroll
-        for ( int q = 0; q < M; ++q )
-            rf[q] = (float)r[q];
-        pinv32( rf, d );
-#pragma unroll
-        for ( int q = 0; q < M; ++q )
-            a[q] += (double)d[q];
-    }
-    for ( int j = 0; j < len; ++j )
-    {
-        float x, y, z;
-        scaled( j, x, y, z );
-        double P[M];
-        basis_eval<M, double>( (double)x, (double)y, (double)z, P );
-        float const phi = weight32( rbf, x, y, z );
-        double dot = 0.0;
-#pragma unroll
-        for ( int q = 0; q < M; ++q )
-            dot = fma( P[q], a[q], dot );
-        coeff_row[j] = (float)( dot * (double)phi );
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Double-float arithmetic on the FP32 pipe (GB300's FP64 rate is 1/58 of its
 // FP32 rate): a value is an unevaluated sum hi + lo of two floats.  TwoSum
