@@ -549,7 +549,7 @@ dtk_status dtk_knn_search( const double *src, int64_t n_src, int64_t src_pt_stri
         require_device_memory( src, "source points" );
         require_device_memory( n_tgt ? tgt : nullptr, "target points" );
         require_device_memory( offset, "offset" );
-        require_device_memory( n_tgt * (int64_t)row ? indices : nullptr, "indices" );
+        require_device_memory( n_tgt * (int64_t)row != 0 ? indices : nullptr, "indices" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
         PointsView const sv{src, n_src, src_pt_stride, src_dim_stride};
         PointsView const tv{tgt, n_tgt, tgt_pt_stride, tgt_dim_stride};
