@@ -2,7 +2,6 @@
 overlap the work and the apply runs in row slices, so the results must equal
 the device operator's bit for bit; kNN (uniform rows) and radius rows
 (offset-addressed slices), both forms, pinned and pageable buffers."""
-import numpy as np
 import pytest
 import torch
 
