@@ -80,6 +80,30 @@ def test_apply_and_queries_reject_null_handle(dtk_lib):
     assert dtk_lib.dtk_mls_destroy(None) == 0
 
 
+HANDLE_ENTRIES = ("dtk_mls_apply", "dtk_mls_apply_adjoint", "dtk_mls_apply_multi", "dtk_mls_get_csr",
+                  "dtk_mls_get_sizes", "dtk_mls_underdetermined_count", "dtk_mls_get_stage_times",
+                  "dtk_mls_get_search_times", "dtk_mls_get_rotation_count", "dtk_mls_export_size",
+                  "dtk_mls_export", "dtk_nn_apply", "dtk_nn_apply_multi", "dtk_nn_get_indices",
+                  "dtk_mls_batch_apply", "dtk_mls_batch_get_csr", "dtk_mls_batch_get_stage_times")
+CREATE_ENTRIES = ("dtk_mls_import", "dtk_mls_transfer_host", "dtk_nn_create", "dtk_knn_search",
+                  "dtk_mls_batch_create", "dtk_svd_pinv_noalloc")
+
+
+def _null_args(fn):
+    return [0 if t in (C.c_int64, C.c_int32, C.c_int) else None for t in fn.argtypes]
+
+
+def test_every_entry_rejects_null_arguments(dtk_lib):
+    # a null handle (or null inputs) is DTK_ERR_INVALID_ARG with a message,
+    # decided before any device call; destroying a null handle is a no-op
+    for name in HANDLE_ENTRIES + CREATE_ENTRIES:
+        fn = getattr(dtk_lib, name)
+        assert fn(*_null_args(fn)) == 1, name
+        assert dtk_lib.dtk_last_error().startswith(b"DTK_REQUIRE"), name
+    for name in ("dtk_mls_destroy", "dtk_nn_destroy", "dtk_mls_batch_destroy"):
+        assert getattr(dtk_lib, name)(None) == 0, name
+
+
 def test_svd_rejects_bad_sizes(dtk_lib):
     assert dtk_lib.dtk_svd_pinv(0, 1, 1, 1, None, None) == 1
     assert dtk_lib.dtk_svd_pinv(65, 1, 1, 1, None, None) == 1
