@@ -6,25 +6,33 @@ configuration the headline metric is quoted on.  One step = one operator
 setup (search, weights, moments, pseudo-inverse, coefficients) plus one
 apply over all targets.  ``value`` is targets/s of the mixed FP32/FP64 form
 with inputs resident in HBM; the plain FP64 form (the reference algorithm) is
-timed on the same inputs and reported beside it, with the relative L2 error
-of both against the FP64 CPU oracle on a sample of targets.  ``e2e`` is the
-same metric through the public host-buffer call (``transfer_host``, the C
-entry ``dtk_mls_transfer_host``): the H2D copies of the points and the source
-field from pinned memory and the D2H copy of the target field are inside the
-timed region, overlapped with the work as that call does.
+timed on the same inputs and reported beside it (``fp64_form``,
+``mixed_over_fp64``), with the relative L2 error of both against the FP64 CPU
+oracle on every target and the neighbour rows compared with the oracle's
+(``accuracy``).  ``e2e`` is the same metric through the public host-buffer
+call (``transfer_host``, the C entry ``dtk_mls_transfer_host``): the H2D
+copies of the points and the source field from pinned memory and the D2H copy
+of the target field are inside the timed region, overlapped with the work as
+that call does.  ``cpu_baseline`` is that oracle run, timed: the CPU
+restatement of the reference on all host threads over the whole workload.
 
 At N=1 the line also carries ``rows``: short measurements (CUDA events,
-one warm-up, three steps) of the other workloads of the path -- the FP64
-form at 2M points with neighbour rows checked against the oracle, the
-256-problem batched radius transfer, and the 1M-point adjoint.
+one warm-up, three steps) of the other workloads of the path -- the plain
+10k transfer, the FP64 form at 2M points with every neighbour row and value
+checked against the oracle, the 256-problem batched radius transfer, and the
+1M-point adjoint.  ``--detail FILE`` writes the full record (notes, stage
+splits, per-problem errors) beside the one-line summary.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Multi-GPU (torchrun, one process per GPU): targets shard across ranks
-(each rank its own 8M-target shard, seeds 7 + rank) with the sources
-replicated; no data-path collective ("scaling": "weak").  Timing takes the
-max over ranks.  ``--impl reference`` times the CPU restatement of the
-reference algorithm (the oracle, all host threads) on a bounded sample.
+Multi-GPU (torchrun, one process per GPU): one shared target set of N x 8M
+points U[0,1]^3 (seed 7) is cut into N Morton-ordered slices
+(``sharding.target_shard``), one per rank, with the sources replicated; each
+rank builds its own tree and operator, with no data-path collective
+("scaling": "weak": 8M targets per GPU at every N).  Timing takes the max
+over ranks.  ``--impl reference`` times the CPU restatement of the reference
+algorithm (the oracle, all host threads) on the whole workload of one rank
+every step.
 """
 from __future__ import annotations
 
@@ -62,7 +70,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="mixed_8m", choices=sorted(set(WORKLOADS) | set(ROW_WORKLOADS)))
-    ap.add_argument("--sample", type=int, default=20000, help="targets in the CPU/oracle sample")
+    ap.add_argument("--sample", type=int, default=20000,
+                    help="targets of the CPU sample behind the per-target extrapolation")
+    ap.add_argument("--oracle-targets", type=int, default=0,
+                    help="targets checked against the oracle (0 = all)")
+    ap.add_argument("--detail", default="", help="write the full record to this JSON file")
     ap.add_argument("--no-rows", action="store_true",
                     help="skip the side measurements of the other workloads")
     ap.add_argument("--profile-only", action="store_true",
@@ -70,12 +82,28 @@ def parse():
     return ap.parse_args()
 
 
-def make_inputs(name, rank=0):
+def make_inputs(name, rank=0, world=1):
+    """Sources (replicated) and this rank's targets: its Morton-ordered slice
+    of one shared set of world x n_tgt targets (the whole set when world = 1)."""
     from datatransferkit_gb300 import synthetic as syn
+    from datatransferkit_gb300.sharding import target_shard
     n_src, n_tgt, s_seed, t_seed, rbf, basis, k = WORKLOADS[name]
     src = syn.uniform_points(n_src, s_seed)
-    tgt = syn.jittered_grid(126, t_seed + rank) if n_tgt is None else syn.uniform_points(n_tgt, t_seed + rank)
+    if n_tgt is None:
+        tgt = syn.jittered_grid(126, t_seed)
+    else:
+        tgt = syn.uniform_points(n_tgt * world, t_seed)
+        if world > 1:
+            tgt = np.ascontiguousarray(tgt[target_shard(tgt, rank, world)])
     return src, tgt, rbf, basis, k
+
+
+def config_of(name, n_src, n_tgt_per_rank):
+    """The workload's config, the same keys and values in both arms."""
+    _, _, _, _, rbf, basis, k = WORKLOADS[name]
+    return {"workload": name, "n_sources": int(n_src), "n_targets_per_gpu": int(n_tgt_per_rank),
+            "basis": {1: "Linear3", 2: "Quadratic3"}[basis], "rbf": RBF_NAMES[rbf], "k": k,
+            "l2_flush": f"inputs larger than L2 ({n_src * 24 / 1e6:.0f} MB of source coordinates)"}
 
 
 # ---------------------------------------------------------------------------
@@ -221,18 +249,30 @@ def hbm_peak():
 
 
 # ---------------------------------------------------------------------------
-# CPU oracle timing (bounded sample)
+# CPU oracle: the whole workload, timed
 # ---------------------------------------------------------------------------
-def cpu_oracle_run(src, tgt, vals, rbf, basis, k, sample):
-    """Time the FP64 CPU oracle (all host threads) on a sample of the targets.
-
-    The index build over all sources is timed on its own (warm, best of two),
-    the per-target work (kNN query, setup, apply) on `sample` targets; the
-    returned value extrapolates to the full target set:
-    n_targets / (t_build + n_targets * t_per_target).
-    """
+def cpu_oracle_full(src, tgt, rbf, basis, k, fields):
+    """The FP64 CPU oracle (all host threads) over every target: index build
+    and kNN query, setup, and one apply per field.  Timed from the search to
+    the first apply (one setup + apply, the GPU step's work)."""
     from oracle import cpu
     threads = cpu.max_threads()
+    t0 = time.perf_counter()
+    off, idx, _ = cpu.knn(src, tgt, k)
+    t1 = time.perf_counter()
+    coeff, _, _, under = cpu.mls_coefficients(src, tgt, off, idx, rbf, basis)
+    ys = [cpu.apply(off, idx, coeff, fields[0])]
+    t2 = time.perf_counter()
+    ys += [cpu.apply(off, idx, coeff, f) for f in fields[1:]]
+    return dict(seconds=t2 - t0, search_s=t1 - t0, setup_apply_s=t2 - t1, threads=threads,
+                offset=off, idx=idx, ys=ys, underdetermined=under)
+
+
+def cpu_oracle_extrapolated(src, tgt, vals, rbf, basis, k, sample):
+    """The per-target extrapolation kept beside the full run: the index build
+    over all sources (warm, best of two) plus `sample` targets' kNN query,
+    setup and apply, scaled to the whole target set."""
+    from oracle import cpu
     sub = tgt[:sample]
     cpu.knn(src[:1000], tgt[:10], k)  # load and warm the library
     t_build = float("inf")
@@ -245,42 +285,42 @@ def cpu_oracle_run(src, tgt, vals, rbf, basis, k, sample):
     t_knn = time.perf_counter() - t0
     t0 = time.perf_counter()
     coeff, _, _, _ = cpu.mls_coefficients(src, sub, off, idx, rbf, basis)
-    y = cpu.apply(off, idx, coeff, vals)
+    cpu.apply(off, idx, coeff, vals)
     t_setup = time.perf_counter() - t0
     per_target = (max(t_knn - t_build, 0.0) + t_setup) / len(sub)
-    n_full = len(tgt)
-    value = n_full / (t_build + n_full * per_target)
-    return dict(value=value, threads=threads, t_build=t_build, t_knn=t_knn, t_setup=t_setup,
-                y=y, sample=len(sub))
+    return len(tgt) / (t_build + len(tgt) * per_target)
 
 
 # ---------------------------------------------------------------------------
-# reference arm
+# reference arm: the CPU restatement of the reference, the whole workload per step
 # ---------------------------------------------------------------------------
 def run_reference(args, rank, world):
     if rank != 0:
         return
     from datatransferkit_gb300 import synthetic as syn
-    src, tgt, rbf, basis, k = make_inputs(args.workload)
+    src, tgt, rbf, basis, k = make_inputs(args.workload, 0, world)
     vals = syn.smooth_field(src)
-    times, last = [], None
+    secs, last = [], None
     for it in range(args.warmup + args.steps):
-        r = cpu_oracle_run(src, tgt, vals, rbf, basis, k, args.sample)
+        r = cpu_oracle_full(src, tgt, rbf, basis, k, [vals])
         if it >= args.warmup:
-            times.append(r["value"])
+            secs.append(r["seconds"])
         last = r
-    value = float(np.median(times))
+        del r
+    mean_s = float(np.mean(secs))
+    value = len(tgt) / mean_s
+    extrap = cpu_oracle_extrapolated(src, tgt, vals, rbf, basis, k, args.sample)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": len(tgt) / value * 1e3, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": mean_s * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded U[0,1]^3 clouds)",
-        "config": {"workload": args.workload, "n_sources": len(src), "n_targets": len(tgt),
-                   "basis": "Quadratic3", "rbf": RBF_NAMES[rbf], "k": k},
+        "config": config_of(args.workload, len(src), len(tgt)),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": last["threads"], "kind": "port",
-                         "sample": (f"full {len(src)}-source grid index build + {last['sample']} "
-                                    f"of {len(tgt)} targets (kNN, setup, apply), extrapolated "
-                                    "to the full target set")},
+                         "sample": (f"every step the whole workload: {len(src)}-source index build, "
+                                    f"kNN, FP64 setup and apply of all {len(tgt)} targets"),
+                         "stage_s": {"search": last["search_s"], "setup_apply": last["setup_apply_s"]},
+                         "extrapolated_from_sample": {"value": extrap, "sample_targets": args.sample}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -302,10 +342,38 @@ def _event_time(torch, stream, fn, steps, warmup):
     return e0.elapsed_time(e1) / steps
 
 
-def row_fp64_2m(torch, dtk, syn, dev, stream, sample, profile_only=False):
+def row_plain_10k(torch, dtk, syn, dev, stream):
+    """Plain transfer: 10k / 10k U[0,1]^3 (seeds 1, 2), Quadratic3, Wendland<2>,
+    k = 20, FP64; rows and values against the oracle, and the approximation
+    error against f at the targets."""
+    from oracle import cpu as ocpu
+    src, tgt = syn.uniform_points(10_000, 1), syn.uniform_points(10_000, 2)
+    vals = syn.smooth_field(src)
+    s_d, t_d, v_d = (torch.from_numpy(a).to(dev) for a in (src, tgt, vals))
+    out = torch.empty(len(tgt), dtype=torch.float64, device=dev)
+    W2, Q = dtk.Wendland(2), dtk.MultivariatePolynomialBasis(dtk.Quadratic, 3)
+    holder = {}
+
+    def step():
+        holder["op"] = dtk.MovingLeastSquaresOperator(None, s_d, t_d, W2, Q, k=20, precision="fp64")
+        holder["op"].apply(v_d, out)
+
+    ms = _event_time(torch, stream, step, 3, 1)
+    ref = ocpu.mls_transfer(src, tgt, vals, 1, 2, k=20)
+    y = out.cpu().numpy()
+    _, idx, _ = holder["op"].csr()
+    f_t = syn.smooth_field(tgt)
+    return {"value": len(tgt) / (ms / 1e3), "ms": ms,
+            "rows_bit_exact": bool(np.array_equal(idx.cpu().numpy(), ref["idx"])),
+            "rel_l2_vs_oracle": float(np.linalg.norm(y - ref["target"]) / np.linalg.norm(ref["target"])),
+            "rel_l2_vs_f": float(np.linalg.norm(y - f_t) / np.linalg.norm(f_t))}
+
+
+def row_fp64_2m(torch, dtk, syn, dev, stream, n_check=0, profile_only=False):
     """Plain FP64 form at scale: 2M U[0,1]^3 sources, 2M targets on a jittered
-    126^3 grid, Quadratic3, Wendland<2>, k = 32; neighbour rows of a target
-    sample compared bit-exact with the oracle, values by relative L2."""
+    126^3 grid, Quadratic3, Wendland<2>, k = 32; every neighbour row compared
+    with the oracle's and every value by relative L2 (n_check > 0: the first
+    n_check targets only)."""
     from oracle import cpu as ocpu
     src, tgt, rbf, basis_id, k = make_inputs("fp64_2m")
     vals = syn.smooth_field(src)
@@ -324,19 +392,17 @@ def row_fp64_2m(torch, dtk, syn, dev, stream, sample, profile_only=False):
         return {"profile_only": True, "workload": "fp64_2m", "ms_per_step": ms}
     op = dtk.MovingLeastSquaresOperator(None, s_d, t_d, W2, Q, k=k, precision="fp64")
     op.apply(v_d, out)
-    off, idx, _ = op.csr()
-    sub = tgt[:sample]
-    o_off, o_idx, _ = ocpu.knn(src, sub, k)
-    coeff, _, _, _ = ocpu.mls_coefficients(src, sub, o_off, o_idx, rbf, basis_id)
-    y_ref = ocpu.apply(o_off, o_idx, coeff, vals)
-    y = out[:sample].cpu().numpy()
-    return {"workload": "2M U[0,1]^3 sources, 126^3 jittered-grid targets, Quadratic3, Wendland<2>, k=32, FP64",
-            "value": len(tgt) / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+    _, idx, _ = op.csr()
+    sub = tgt if n_check <= 0 else tgt[:n_check]
+    r = cpu_oracle_full(src, sub, rbf, basis_id, k, [vals])
+    y = out[: len(sub)].cpu().numpy()
+    y_ref = r["ys"][0]
+    return {"value": len(tgt) / (ms / 1e3), "ms": ms,
             "stages_ms": {"search": float(np.mean([t[0] for t in ops[1:]])),
                           "setup": float(np.mean([t[1] for t in ops[1:]]))},
-            "neighbours_bit_exact_sample": bool(np.array_equal(idx[: len(o_idx)].cpu().numpy(), o_idx)),
-            "rel_l2_vs_oracle_sample": float(np.linalg.norm(y - y_ref) / np.linalg.norm(y_ref)),
-            "sample_targets": int(sample)}
+            "rows_checked": len(sub),
+            "rows_bit_exact": bool(np.array_equal(idx[: len(r["idx"])].cpu().numpy(), r["idx"])),
+            "rel_l2_vs_oracle": float(np.linalg.norm(y - y_ref) / np.linalg.norm(y_ref))}
 
 
 def row_batch(torch, dtk, syn, dev, stream, n_problems=256, profile_only=False):
@@ -385,17 +451,16 @@ def row_batch(torch, dtk, syn, dev, stream, n_problems=256, profile_only=False):
         _, spread = ocpu.rounding_spread(pr["src"], pr["tgt"], ref["offset"], ref["idx"], 1, pr["basis"], f,
                                          ref["coeff"])
         yp = y[b.target_offsets[p]:b.target_offsets[p + 1]]
-        errs[f"problem_{p}_n{sizes[p]}"] = {
+        errs[f"p{p}_n{sizes[p]}"] = {
             "rel_l2": float(np.linalg.norm(yp - ref["target"]) / max(np.linalg.norm(ref["target"]), 1e-300)),
             "oracle_spread": float(spread)}
-    return {"workload": f"{n_problems} problems, log-uniform 1e3..1e5 points, Gaussian-mixture sources, radius 0.05, "
-                        "Linear3/Quadratic3 alternating, Wendland<2>, FP64",
-            "value": n_tgt / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
-            "n_sources": int(sum(sizes)), "n_targets": int(n_tgt), "nnz": int(off[-1]),
-            "row_length": {"mean": float(rows.mean()), "p50": float(np.percentile(rows, 50)),
-                           "p99": float(np.percentile(rows, 99)), "max": int(rows.max())},
+    return {"value": n_tgt / (ms / 1e3), "ms": ms, "n_targets": int(n_tgt), "nnz": int(off[-1]),
+            "stages_ms": dict(zip(("search", "setup", "host"), b.stage_times_ms)),
             "apply_ms": {"graph": ms_graph, "direct": ms_direct},
-            "rel_l2_vs_oracle": errs}
+            "rel_l2_vs_oracle": errs,
+            "detail": {"row_length": {"mean": float(rows.mean()), "p50": float(np.percentile(rows, 50)),
+                                      "p99": float(np.percentile(rows, 99)), "max": int(rows.max())},
+                       "n_sources": int(sum(sizes))}}
 
 
 def row_adjoint_1m(torch, dtk, syn, dev, stream, profile_only=False):
@@ -423,8 +488,7 @@ def row_adjoint_1m(torch, dtk, syn, dev, stream, profile_only=False):
     op = holder["op"]
     ms_adj = _event_time(torch, stream, lambda: op.apply_adjoint(y - g_d, f_d, coords=True), 3, 1)
     ms_adj_v = _event_time(torch, stream, lambda: op.apply_adjoint(y - g_d), 5, 1)
-    return {"workload": "1M/1M U[0,1]^3, Quadratic3, Wendland<2>, k=32, FP64, L=1/2||Tf-g||^2",
-            "value": len(tgt) / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+    return {"value": len(tgt) / (ms / 1e3), "ms": ms,
             "adjoint_ms": {"values_and_coords": ms_adj, "values_only": ms_adj_v}}
 
 
@@ -438,7 +502,7 @@ def run_row_workload(args):
     stream = torch.cuda.current_stream(dev)
     po = args.profile_only
     if args.workload == "fp64_2m":
-        r = row_fp64_2m(torch, dtk, syn, dev, stream, args.sample, po)
+        r = row_fp64_2m(torch, dtk, syn, dev, stream, args.oracle_targets, po)
     elif args.workload.startswith("batch_"):
         r = row_batch(torch, dtk, syn, dev, stream, int(args.workload.split("_")[1]), po)
     else:
@@ -451,12 +515,13 @@ def run_rows(args, dev, stream):
     import datatransferkit_gb300 as dtk
     from datatransferkit_gb300 import synthetic as syn
     rows = {}
-    for name, fn in (("fp64_2m", lambda: row_fp64_2m(torch, dtk, syn, dev, stream, args.sample)),
+    for name, fn in (("plain_10k", lambda: row_plain_10k(torch, dtk, syn, dev, stream)),
+                     ("fp64_2m", lambda: row_fp64_2m(torch, dtk, syn, dev, stream, args.oracle_targets)),
                      ("batch_256", lambda: row_batch(torch, dtk, syn, dev, stream)),
                      ("adjoint_1m", lambda: row_adjoint_1m(torch, dtk, syn, dev, stream))):
         t0 = time.perf_counter()
         rows[name] = fn()
-        rows[name]["wall_s"] = time.perf_counter() - t0
+        rows[name]["wall_s"] = round(time.perf_counter() - t0, 1)
         torch.cuda.empty_cache()
     return rows
 
@@ -471,7 +536,7 @@ def run_ours(args, rank, world, local_rank):
 
     dev = torch.device("cuda", local_rank)
     torch.cuda.set_device(dev)
-    src, tgt, rbf, basis_id, k = make_inputs(args.workload, rank)
+    src, tgt, rbf, basis_id, k = make_inputs(args.workload, rank, world)
     vals = syn.smooth_field(src)
     front = syn.front_field(src)
     RBF = {1: dtk.Wendland(2), 2: dtk.Wendland(4)}[rbf]
@@ -533,31 +598,6 @@ def run_ours(args, rank, world, local_rank):
                               "workload": args.workload}), flush=True)
         return
 
-    # -- accuracy vs the FP64 oracle on a sample of targets ----------------------
-    acc = {}
-    cpu = None
-    if rank == 0:
-        cpu = cpu_oracle_run(src, tgt, vals, rbf, basis_id, k, args.sample)
-    for name, field in (("smooth", vals), ("front", front)):
-        f_d = torch.from_numpy(field).to(dev)
-        res = {}
-        for prec in ("mixed", "fp64"):
-            op = dtk.MovingLeastSquaresOperator(None, s_d, t_d, RBF, BASIS, k=k, precision=prec)
-            op.apply(f_d, out)
-            res[prec] = out[: args.sample].cpu().numpy()
-            if prec == "fp64":
-                off, idx, _ = op.csr()
-        if rank == 0:
-            from oracle import cpu as ocpu
-            sub = tgt[: args.sample]
-            o_off, o_idx, _ = ocpu.knn(src, sub, k)
-            same = np.array_equal(idx[: len(o_idx)].cpu().numpy(), o_idx)
-            coeff, _, _, _ = ocpu.mls_coefficients(src, sub, o_off, o_idx, rbf, basis_id)
-            y_ref = ocpu.apply(o_off, o_idx, coeff, field)
-            nrm = np.linalg.norm(y_ref)
-            acc[name] = {prec: float(np.linalg.norm(res[prec] - y_ref) / nrm) for prec in res}
-            acc["neighbours_bit_exact"] = bool(same)
-
     # -- e2e through the public API with host buffers -----------------------------
     src_h = torch.from_numpy(src).pin_memory()
     tgt_h = torch.from_numpy(tgt).pin_memory()
@@ -581,6 +621,34 @@ def run_ours(args, rank, world, local_rank):
     barrier()
     ms_e2e = max_over_ranks(e0.elapsed_time(e1) / args.steps)
 
+    # -- both forms against the FP64 oracle: every target (rank 0's shard) --------
+    acc, cpu = {}, None
+    n_chk = n_tgt if args.oracle_targets <= 0 else min(n_tgt, args.oracle_targets)
+    res = {}
+    for name, field in (("smooth", vals), ("front", front)):
+        f_d = torch.from_numpy(field).to(dev)
+        for prec in ("mixed", "fp64"):
+            op = dtk.MovingLeastSquaresOperator(None, s_d, t_d, RBF, BASIS, k=k, precision=prec)
+            op.apply(f_d, out)
+            res[name, prec] = out[:n_chk].cpu().numpy()
+            if prec == "fp64" and name == "smooth":
+                idx_gpu = op.csr()[1][: n_chk * k].cpu().numpy()
+            del op
+        del f_d
+    if rank == 0:
+        cpu = cpu_oracle_full(src, tgt[:n_chk], rbf, basis_id, k, [vals, front])
+        for j, name in enumerate(("smooth", "front")):
+            y_ref = cpu["ys"][j]
+            nrm = np.linalg.norm(y_ref)
+            acc[name] = {prec: float(np.linalg.norm(res[name, prec] - y_ref) / nrm)
+                         for prec in ("mixed", "fp64")}
+        acc["neighbour_rows_bit_exact"] = bool(np.array_equal(idx_gpu, cpu["idx"]))
+        acc["targets_checked"] = int(n_chk)
+        cpu_value = n_chk / cpu["seconds"]
+        cpu_extrap = cpu_oracle_extrapolated(src, tgt, vals, rbf, basis_id, k, args.sample)
+        del cpu["ys"], cpu["idx"], cpu["offset"]
+    del res
+
     rows = run_rows(args, dev, stream) if (world == 1 and not args.no_rows) else None
 
     if rank != 0:
@@ -597,10 +665,17 @@ def run_ours(args, rank, world, local_rank):
     hbm, hbm_src = hbm_peak()
     traffic_pt = read_profile_traffic("setup_mixed_traffic.txt", "bytes_per_target")
     traffic_q = read_profile_traffic("knn_traffic.txt", "bytes_per_query")
+    instr_q = read_profile_traffic("knn_traffic.txt", "warp_instructions_per_query")
     # kNN query launch, algorithmic bytes: per query the FP64 point, k indices
     # out and the offset; per source its FP64 + FP32 sorted copies and its index
     q_bytes = n_tgt * (24 + 4 * k + 4) + len(src) * (24 + 12 + 4)
     q_gbs = q_bytes / (query_ms / 1e3) / 1e9
+    # the issue ruler: warp instructions (ncu count per query) over the SMs'
+    # issue rate, one warp instruction per cycle per scheduler at the sampled clock
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    clk_mhz = clocks.get("sm_mhz") or 2070.0
+    issue_peak = n_sm * 4 * clk_mhz * 1e6
+    issue_frac = (instr_q * n_tgt / (query_ms / 1e3) / issue_peak) if instr_q else None
     # apply alone (CUDA events on the launching stream, inputs resident)
     op_m = dtk.MovingLeastSquaresOperator(None, s_d, t_d, RBF, BASIS, k=k, precision="mixed")
     apply_ms = _event_time(torch, stream, lambda: op_m.apply(v_d, out), 10, 3)
@@ -620,53 +695,60 @@ def run_ours(args, rank, world, local_rank):
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded U[0,1]^3 clouds)",
-        "config": {"workload": args.workload, "n_sources": len(src), "n_targets_per_gpu": n_tgt,
-                   "basis": "Quadratic3", "rbf": RBF_NAMES[rbf], "k": k, "form": "mixed",
-                   "l2_flush": "inputs larger than L2 (192 MB coordinates per cloud)"},
-        "fp64_form": {"value": total_targets / (ms_fp64 / 1e3), "ms_per_step": ms_fp64,
-                      "setup_ms": setup64_ms,
-                      "setup_fp64_tflops": flops64 / (setup64_ms / 1e3) / 1e12,
-                      "setup_fp64_frac_of_dgemm": flops64 / (setup64_ms / 1e3) / 1e12 / peak64},
+        "config": config_of(args.workload, len(src), n_tgt),
+        "form": "mixed",
+        "fp64_form": {"value": total_targets / (ms_fp64 / 1e3), "ms_per_step": ms_fp64},
         "mixed_over_fp64": ms_fp64 / ms_mixed,
-        "rotations_per_target": {
-            "mixed_fp32": float(np.mean([r[2] for r in rec_mixed])) / n_tgt,
-            "fp64_form": rot_fp64_form / n_tgt},
-        "accuracy_vs_fp64_oracle": acc,
-        "stages_ms": {"search": search_ms, "setup": setup_ms,
-                      "apply": ms_mixed - search_ms - setup_ms},
-        "roofline": {"bound": "hbm", "kernel": "k_knn (Morton-cell 8-wide BVH, warp per query)",
-                     "achieved": q_gbs, "peak": hbm, "unit": "GB/s", "frac": q_gbs / hbm,
-                     "peak_source": hbm_src, "traffic": (traffic_q * n_tgt) if traffic_q else None,
-                     "algorithmic_bytes": q_bytes, "launch_ms": query_ms,
-                     "note": ("the dominant kernel of a mixed step; algorithmic bytes = N_t (24 + 4k + 4) "
-                              "+ N_s (24 + 12 + 4); the measured traffic above them is register spills "
-                              "evicted from L2 (32 registers at full occupancy); the kernel is bound by "
-                              "instruction issue and L2 latency (81% of issue slots, profiles/k_knn_1m.md), "
-                              "not by HBM")},
+        "accuracy": acc,
+        "e2e": {"value": total_targets / (ms_e2e / 1e3), "unit": UNIT,
+                "h2d_bytes_per_step": int(src_h.numel() * 8 + tgt_h.numel() * 8 + val_h.numel() * 8),
+                "d2h_bytes_per_step": int(out_h.numel() * 8)},
+        "roofline": {"bound": "hbm", "kernel": "k_knn", "achieved": q_gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": q_gbs / hbm, "traffic": (traffic_q * n_tgt) if traffic_q else None,
+                     "launch_ms": query_ms, "issue_frac": issue_frac},
+        "cpu_baseline": ({"value": cpu_value, "unit": UNIT, "cores": cpu["threads"], "kind": "port",
+                          "sample": f"whole workload, all {n_chk} targets, timed"} if cpu else None),
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "stages_ms": {"build": build_ms, "query": query_ms, "setup": setup_ms,
+                      "apply": ms_mixed - search_ms - setup_ms, "fp64_setup": setup64_ms},
+    }
+    if rows is not None:
+        line["rows"] = {name: {k2: v for k2, v in r.items() if k2 not in ("detail", "stages_ms")}
+                        for name, r in rows.items()}
+    detail = dict(line)
+    detail.update({
+        "roofline_detail": {
+            "peak_source": hbm_src, "algorithmic_bytes": q_bytes,
+            "note": ("the dominant kernel of a mixed step; algorithmic bytes = N_t (24 + 4k + 4) "
+                     "+ N_s (24 + 12 + 4); traffic = the ncu DRAM bytes per query of profiles/knn_traffic.txt "
+                     "x N_t; issue_frac = ncu warp instructions per query x N_t / launch time / "
+                     "(SMs x 4 schedulers x sampled SM clock)")},
         "roofline_stages": {
-            "search_build_ms": build_ms,
             "query": {"bound": "hbm", "achieved": q_gbs, "peak": hbm, "unit": "GB/s",
-                      "frac": q_gbs / hbm, "ms": query_ms},
+                      "frac": q_gbs / hbm, "ms": query_ms, "issue_frac": issue_frac},
             "setup": {"bound": "fp32", "kernel": "k_setup_mixed<10>", "achieved": achieved,
                       "peak": peak, "unit": "T FP32 ops/s (FMA = 1)", "frac": achieved / peak, "ms": setup_ms,
                       "peak_source": "measured cuBLAS SGEMM 8192^3 (no TF32) in this run, FMA/s",
                       "traffic": (traffic_pt * n_tgt) if traffic_pt else None},
-            "apply": {"bound": "hbm", "kernel": "k_apply_vec<8,1>", "achieved": a_gbs, "peak": hbm,
+            "apply": {"bound": "hbm", "kernel": "k_apply_vec", "achieved": a_gbs, "peak": hbm,
                       "unit": "GB/s", "frac": a_gbs / hbm, "ms": apply_ms},
             "time_weighted_frac": combined},
-        "e2e": {"value": total_targets / (ms_e2e / 1e3), "unit": UNIT,
-                "h2d_bytes_per_step": int(src_h.numel() * 8 + tgt_h.numel() * 8 + val_h.numel() * 8),
-                "d2h_bytes_per_step": int(out_h.numel() * 8)},
-        "gpu_launches": int(launches),
-        "clocks": clocks,
-    }
-    if rows is not None:
-        line["rows"] = rows
-    if cpu is not None:
-        line["cpu_baseline"] = {
-            "value": cpu["value"], "unit": UNIT, "cores": cpu["threads"], "kind": "port",
-            "sample": (f"full {len(src)}-source grid index build + {cpu['sample']} of {n_tgt} "
-                       "targets (kNN, FP64 setup, apply), extrapolated to the full target set")}
+        "fp64_form_detail": {"setup_ms": setup64_ms,
+                             "setup_fp64_tflops": flops64 / (setup64_ms / 1e3) / 1e12,
+                             "setup_fp64_frac_of_dgemm": flops64 / (setup64_ms / 1e3) / 1e12 / peak64,
+                             "dgemm_tflops": peak64, "clocks": clocks64},
+        "rotations_per_target": {
+            "mixed_fp32": float(np.mean([r[2] for r in rec_mixed])) / n_tgt,
+            "fp64_form": rot_fp64_form / n_tgt},
+        "cpu_detail": ({"seconds": cpu["seconds"], "search_s": cpu["search_s"],
+                        "setup_apply_s": cpu["setup_apply_s"],
+                        "extrapolated_from_sample": {"value": cpu_extrap, "sample_targets": args.sample}}
+                       if cpu else None),
+        "rows": rows,
+    })
+    if args.detail:
+        Path(args.detail).write_text(json.dumps(detail, indent=1))
     print(json.dumps(line), flush=True)
 
 

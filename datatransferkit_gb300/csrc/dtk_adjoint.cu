@@ -570,14 +570,7 @@ void launch_adjoint_entries( dtk_mls_s const *h, double const *values, double co
     check_launch( "k_adjoint_fast" );
     size_t const smem = ( 2 * NU * sizeof( double ) + M * M * sizeof( double ) +
                           M * M * sizeof( float ) ) * AB;
-    static bool configured = false;
-    if ( !configured )
-    {
-        DTK_CUDA_OR_THROW( cudaFuncSetAttribute( k_adjoint_entries<M>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem ) );
-        configured = true;
-    }
+    ensure_dynamic_smem( k_adjoint_entries<M>, smem );
     int64_t const want = ( h->n_tgt + AB - 1 ) / AB;
     unsigned const blocks = (unsigned)std::max<int64_t>( 1, std::min<int64_t>( want, 4 * num_sms() ) );
     k_adjoint_entries<M><<<blocks, AB, smem, s>>>( h->src_copy.get(), h->tgt_copy.get(), h->offset.get(),
@@ -645,6 +638,7 @@ extern "C" dtk_status dtk_mls_apply_adjoint( dtk_mls_handle h, const double *cot
         require_device_memory( source_values, "source_values" );
         require_device_memory( grad_coords, "grad_coords" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        TouchOnExit const touch{&h->life, s};
         build_transpose_for( h, s );
         DeviceBuffer<unsigned> status( 1, s );
         DTK_CUDA_OR_THROW( cudaMemsetAsync( status.get(), 0, sizeof( unsigned ), s ) );

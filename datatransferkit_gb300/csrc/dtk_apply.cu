@@ -1,7 +1,7 @@
 // MLS apply: CSR gather-SpMV (sm_103a).
 //
 // Replaces MovingLeastSquaresOperator::apply
-// (packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:188-208):
+// (packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:121-141):
 // the single-rank fetch (a gather of source values into per-neighbour
 // order, DTK_DetailsNearestNeighborOperatorImpl.hpp:152-192), computeTargetValues
 // (DTK_DetailsMovingLeastSquaresOperatorImpl.hpp:49-70) and the deep_copy fuse

@@ -237,6 +237,11 @@ using namespace dtk;
 
 struct dtk_mls_batch_s
 {
+    HandleLife life;
+    explicit dtk_mls_batch_s( cudaStream_t home )
+        : life( home )
+    {
+    }
     int32_t n_problems = 0;
     int precision = DTK_FP64;
     int64_t n_src = 0, n_tgt = 0, nnz = 0;
@@ -261,6 +266,7 @@ struct dtk_mls_batch_s
 
     ~dtk_mls_batch_s()
     {
+        life.retire( offset, idx, coeff64, coeff32, rows, tasks );
         if ( exec )
             cudaGraphExecDestroy( exec );
         if ( graph )
@@ -436,7 +442,8 @@ dtk_status dtk_mls_batch_create( int32_t n_problems, const dtk_mls_options *opts
         require_device_memory( src, "source points" );
         require_device_memory( n_tgt ? tgt : nullptr, "target points" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
-        auto h = std::make_unique<dtk_mls_batch_s>();
+        auto h = std::make_unique<dtk_mls_batch_s>( s );
+        TouchOnExit const touch{&h->life, s};
         h->n_problems = n_problems;
         h->precision = precision;
         h->n_src = n_src;
@@ -610,6 +617,7 @@ dtk_status dtk_mls_batch_apply( dtk_mls_batch_handle h, const double *src_values
         require_device_memory( src_values, "src_values" );
         require_device_memory( tgt_values, "tgt_values" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        TouchOnExit const touch{&h->life, s};
         if ( !h->tuned )
             h->tune( src_values, tgt_values, s );
         if ( !use_graph )

@@ -9,7 +9,9 @@
 #include "dtk_common.cuh"
 #include "dtk_handle.cuh"
 
+#include <atomic>
 #include <cmath>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -60,6 +62,58 @@ cudaMemPool_t device_pool()
         g_pools[dev] = pool;
     }
     return g_pools[dev];
+}
+
+namespace
+{
+std::mutex g_attr_mutex;
+std::map<std::pair<int, void const *>, size_t> g_smem_set; // (device, kernel) -> bytes set
+std::vector<int> g_sms;                                    // per device, 0 = not queried
+} // namespace
+
+namespace
+{
+std::atomic<int64_t> g_jacobi_cap{0}, g_traversal_cap{0};
+}
+
+unsigned long long jacobi_cap( int m )
+{
+    int64_t const c = g_jacobi_cap.load( std::memory_order_relaxed );
+    return c > 0 ? (unsigned long long)c : 200ull * m * m + 2000ull;
+}
+
+int64_t traversal_cap( int64_t wide_nodes )
+{
+    int64_t const c = g_traversal_cap.load( std::memory_order_relaxed );
+    return c > 0 && c < wide_nodes ? c : wide_nodes;
+}
+
+int num_sms()
+{
+    int dev = 0;
+    DTK_CUDA_OR_THROW( cudaGetDevice( &dev ) );
+    std::lock_guard<std::mutex> lock( g_attr_mutex );
+    if ( g_sms.size() <= (size_t)dev )
+        g_sms.resize( dev + 1, 0 );
+    if ( !g_sms[dev] )
+    {
+        int sms = 0;
+        DTK_CUDA_OR_THROW( cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev ) );
+        g_sms[dev] = sms > 0 ? sms : 1;
+    }
+    return g_sms[dev];
+}
+
+void set_dynamic_smem( void const *kernel, size_t bytes )
+{
+    int dev = 0;
+    DTK_CUDA_OR_THROW( cudaGetDevice( &dev ) );
+    std::lock_guard<std::mutex> lock( g_attr_mutex );
+    size_t &done = g_smem_set[{dev, kernel}];
+    if ( done >= bytes )
+        return;
+    DTK_CUDA_OR_THROW( cudaFuncSetAttribute( kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes ) );
+    done = bytes;
 }
 
 __global__ void k_fill_uniform_offsets( int32_t *offset, int64_t n_tgt, int row )
@@ -130,8 +184,9 @@ std::unique_ptr<dtk_mls_s> create_impl( Geometry const &g, dtk_mls_options const
                                         PointsView tv, cudaStream_t s, cudaEvent_t tgt_ready )
 {
     int64_t const n_src = sv.n, n_tgt = tv.n;
-    auto h = new dtk_mls_s();
+    auto h = new dtk_mls_s( s );
     std::unique_ptr<dtk_mls_s> guard( h );
+    TouchOnExit const touch{&h->life, s};
     h->opts = *opts;
     h->n_src = n_src;
     h->n_tgt = n_tgt;
@@ -170,7 +225,7 @@ std::unique_ptr<dtk_mls_s> create_impl( Geometry const &g, dtk_mls_options const
     DTK_CUDA_OR_THROW( cudaMemsetAsync( counters.get(), 0, 3 * sizeof( unsigned long long ), s ) );
     DTK_CUDA_OR_THROW( cudaEventRecord( ev[0], s ) );
 
-    // --- search (ArborX tree + query, def.hpp:114-129) ---
+    // --- search (ArborX tree + query, _def.hpp:47-62) ---
     Lbvh tree;
     // (the targets may still be arriving: the query order waits for them on
     // its own stream while the tree is built)
@@ -258,7 +313,7 @@ std::unique_ptr<dtk_mls_s> create_impl( Geometry const &g, dtk_mls_options const
     tree = Lbvh();
     DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
     if ( st & DEV_TIMEOUT )
-        throw Error{DTK_ERR_TIMEOUT, "a Jacobi iteration hit its iteration cap"};
+        throw Error{DTK_ERR_TIMEOUT, "a bounded device loop (Jacobi rotations or tree traversal) hit its cap"};
     if ( st )
         throw Error{DTK_ERR_INTERNAL, "search traversal reported an internal error"};
     h->underdetermined = (int64_t)cnt[0];
@@ -285,6 +340,16 @@ void dtk_mls_default_options( dtk_mls_options *o )
     o->radius = 0.0;
     o->comm_size = 1;
     o->keep_points = 0;
+}
+
+dtk_status dtk_set_loop_caps( int64_t jacobi_rotations, int64_t traversal_steps )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( jacobi_rotations >= 0 && traversal_steps >= 0, "caps must be >= 0" );
+        DTK_REQUIRE_OR_THROW( jacobi_rotations <= UINT32_MAX, "Jacobi cap exceeds 2^32 - 1" );
+        g_jacobi_cap.store( jacobi_rotations, std::memory_order_relaxed );
+        g_traversal_cap.store( traversal_steps, std::memory_order_relaxed );
+    } );
 }
 
 const char *dtk_last_error( void ) { return g_error.c_str(); }
@@ -315,7 +380,7 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
         Geometry const g = check_options( opts );
         validate_points( src, n_src, src_pt_stride, src_dim_stride, "source points" );
         validate_points( tgt, n_tgt, tgt_pt_stride, tgt_dim_stride, "target points" );
-        // DTK_CHECK( !search_tree.empty() ), DTK_MovingLeastSquaresOperator_def.hpp:116
+        // DTK_CHECK( !search_tree.empty() ), DTK_MovingLeastSquaresOperator_def.hpp:49
         DTK_REQUIRE_OR_THROW( n_src > 0, "the source point cloud is empty" );
         require_device_memory( src, "source points" );
         require_device_memory( n_tgt ? tgt : nullptr, "target points" );
@@ -331,7 +396,7 @@ dtk_status dtk_mls_apply( dtk_mls_handle h, const double *source_values, int64_t
 {
     return guarded( [&] {
         DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
-        // DTK_REQUIRE at DTK_MovingLeastSquaresOperator_def.hpp:196-197
+        // DTK_REQUIRE at DTK_MovingLeastSquaresOperator_def.hpp:129-130
         DTK_REQUIRE_OR_THROW( n_source_values == h->n_src,
                               "source_values.extent(0) == n_source_points" );
         DTK_REQUIRE_OR_THROW( n_target_values == h->n_tgt,
@@ -341,6 +406,7 @@ dtk_status dtk_mls_apply( dtk_mls_handle h, const double *source_values, int64_t
         require_device_memory( source_values, "source_values" );
         require_device_memory( target_values, "target_values" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        TouchOnExit const touch{&h->life, s};
         apply_csr( h->n_tgt, h->offset.get(), h->idx.get(), h->coeff64.get(), h->coeff32.get(),
                    h->uniform_row, h->mean_row, source_values, target_values, s );
     } );
@@ -401,6 +467,7 @@ dtk_status dtk_mls_transfer_host( const dtk_mls_options *opts, const double *src
         PointsView const sv{d_src.get(), n_src, 3, 1};
         PointsView const tv{d_tgt.get(), n_tgt, 3, 1};
         std::unique_ptr<dtk_mls_s> h = create_impl( g, opts, sv, tv, s, tgt_ready );
+        TouchOnExit const touch{&h->life, s};
         DTK_CUDA_OR_THROW( cudaStreamWaitEvent( s, vals_ready, 0 ) );
         // the apply in row slices; each slice's results go back while the
         // next one computes
@@ -515,6 +582,11 @@ dtk_status dtk_mls_get_rotation_count( dtk_mls_handle h, int64_t *rotations,
 
 int64_t dtk_kernel_launch_count( void ) { return launch_counter(); }
 
+dtk_status dtk_stream_synchronize( dtk_stream_t stream )
+{
+    return guarded( [&] { DTK_CUDA_OR_THROW( cudaStreamSynchronize( reinterpret_cast<cudaStream_t>( stream ) ) ); } );
+}
+
 dtk_status dtk_release_cached_memory( void )
 {
     return guarded( [&] {
@@ -566,6 +638,8 @@ dtk_status dtk_knn_search( const double *src, int64_t n_src, int64_t src_pt_stri
                                             cudaMemcpyDeviceToHost, s ) );
         tree = Lbvh();
         DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+        if ( st & DEV_TIMEOUT )
+            throw Error{DTK_ERR_TIMEOUT, "a bounded device loop (tree traversal) hit its cap"};
         if ( st )
             throw Error{DTK_ERR_INTERNAL, "search traversal reported an internal error"};
     } );
@@ -578,6 +652,11 @@ dtk_status dtk_svd_pinv( int32_t n, int64_t count, const double *a, double *pinv
         DTK_REQUIRE_OR_THROW( n >= 1 && n <= 64, "matrix size must be in [1, 64]" );
         DTK_REQUIRE_OR_THROW( count >= 0, "count is negative" );
         DTK_REQUIRE_OR_THROW( count == 0 || ( a && pinv ), "null matrix pointer" );
+        if ( count )
+        {
+            require_device_memory( a, "a" );
+            require_device_memory( pinv, "pinv" );
+        }
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
         DeviceBuffer<unsigned> status( 1, s );
         DeviceBuffer<unsigned long long> under( 1, s );
@@ -590,7 +669,7 @@ dtk_status dtk_svd_pinv( int32_t n, int64_t count, const double *a, double *pinv
         DTK_CUDA_OR_THROW( cudaMemcpyAsync( &u, under.get(), sizeof( u ), cudaMemcpyDeviceToHost, s ) );
         DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
         if ( st & DEV_TIMEOUT )
-            throw Error{DTK_ERR_TIMEOUT, "a Jacobi iteration hit its iteration cap"};
+            throw Error{DTK_ERR_TIMEOUT, "a bounded device loop (Jacobi rotations or tree traversal) hit its cap"};
         if ( underdetermined )
             *underdetermined = (int64_t)u;
     } );

@@ -158,6 +158,52 @@ struct DeviceBuffer
     T *get() const { return ptr; }
 };
 
+// Lifetime of a handle's device buffers: the stream they were allocated on
+// (the create call's; it must stay valid until the handle is destroyed) and
+// an event recorded on a call's stream after the work of every call that
+// uses them (TouchOnExit).  At destroy the home stream waits for that event
+// and the buffers are freed there, so a call queued on another stream never
+// races the free, and the home stream's next allocations reuse the blocks.
+struct HandleLife
+{
+    cudaStream_t home = nullptr;
+    cudaEvent_t last_use = nullptr;
+    explicit HandleLife( cudaStream_t s )
+        : home( s )
+    {
+        DTK_CUDA_OR_THROW( cudaEventCreateWithFlags( &last_use, cudaEventDisableTiming ) );
+    }
+    HandleLife( HandleLife const & ) = delete;
+    HandleLife &operator=( HandleLife const & ) = delete;
+    ~HandleLife()
+    {
+        if ( last_use )
+            cudaEventDestroy( last_use );
+    }
+    void touch( cudaStream_t s ) { cudaEventRecord( last_use, s ); }
+    // Moves the buffers' frees to the home stream, behind last_use (called
+    // from a handle's destructor, which does not throw).
+    template <class... Buffers>
+    void retire( Buffers &...buffers ) noexcept
+    {
+        cudaStreamWaitEvent( home, last_use, 0 );
+        ( ( buffers.stream = home ), ... );
+    }
+};
+
+// Records the handle's last-use event on the call's stream when the entry
+// point returns or throws, so that its buffers outlive the work it queued.
+struct TouchOnExit
+{
+    HandleLife *life;
+    cudaStream_t s;
+    ~TouchOnExit()
+    {
+        if ( life )
+            life->touch( s );
+    }
+};
+
 // Running count of this library's kernel launches (diagnostics).
 long long &launch_counter();
 
@@ -170,19 +216,25 @@ inline void check_launch( char const *what )
         throw Error{DTK_ERR_CUDA, std::string( what ) + ": " + cudaGetErrorString( e )};
 }
 
-inline int num_sms()
+// SM count of the current device (cached per device).
+int num_sms();
+
+// Raises a kernel's dynamic shared-memory limit to `bytes` on the current
+// device.  The attribute is per device, so it is set once per (device,
+// kernel) and again whenever a larger size is asked for; thread-safe.
+void set_dynamic_smem( void const *kernel, size_t bytes );
+template <class K>
+inline void ensure_dynamic_smem( K *kernel, size_t bytes )
 {
-    static int sms = 0;
-    if ( !sms )
-    {
-        int dev = 0;
-        cudaGetDevice( &dev );
-        cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev );
-        if ( sms <= 0 )
-            sms = 152;
-    }
-    return sms;
+    set_dynamic_smem( reinterpret_cast<void const *>( kernel ), bytes );
 }
+
+// Caps of the bounded device loops (dtk_set_loop_caps; 0 = built in):
+// Jacobi rotations per moment matrix of size m (built in: 200 m^2 + 2000)
+// and tree-traversal steps per query (built in: the tree's wide-node count,
+// which a search never exceeds).
+unsigned long long jacobi_cap( int m );
+int64_t traversal_cap( int64_t wide_nodes );
 
 inline int basis_size( int basis )
 {
@@ -194,8 +246,17 @@ enum : unsigned
 {
     DEV_TIMEOUT = 1u,
     DEV_STACK_OVERFLOW = 2u,
-    DEV_BAD_INDEX = 4u
+    DEV_BAD_INDEX = 4u,
+    DEV_NONFINITE_SOURCE = 8u, // a source coordinate is NaN or infinite
+    DEV_NONFINITE_TARGET = 16u // a target coordinate is NaN or infinite
 };
+
+// NaN or infinite: all exponent bits set (integer pipe).
+__device__ __forceinline__ bool nonfinite_bits( double v )
+{
+    return ( (unsigned long long)__double_as_longlong( v ) & 0x7ff0000000000000ull ) ==
+           0x7ff0000000000000ull;
+}
 
 // ---------------------------------------------------------------------------
 // Device math shared by the kernels.
@@ -292,7 +353,7 @@ __device__ __forceinline__ double rbf_deriv( int rbf, double x )
 }
 
 // Polynomial basis in 3-D, order 1, x, y, z, x^2, xy, xz, y^2, yz, z^2
-// (DTK_MultivariatePolynomialBasis.hpp:249-276).
+// (DTK_MultivariatePolynomialBasis.hpp:98-125).
 template <int M, class T>
 __device__ __forceinline__ void basis_eval( T x, T y, T z, T *p )
 {
@@ -381,13 +442,18 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
 // Morton order of query points (sorted query ids) using the tree's scene box;
 // with groups, problem-major and Morton within each problem.  An order buffer
 // already holding max(1, tgt.n) entries is used as it is.
+// (status, when not null, receives DEV_NONFINITE_TARGET for a target with a
+// NaN or infinite coordinate.)
 void sort_queries( Lbvh const &tree, PointsView tgt, DeviceBuffer<uint32_t> &order,
-                   cudaStream_t s, uint32_t const *group = nullptr, int64_t n_groups = 0 );
+                   cudaStream_t s, uint32_t const *group = nullptr, int64_t n_groups = 0,
+                   unsigned *status = nullptr );
 
 // The tree over src on s and, on a second stream as soon as the scene box is
 // known, the order of the queries, concurrently with the rest of the build;
 // s waits for the order before this returns.
 // (tgt_ready, when not null, is an event the query points wait for.)
+// A NaN or infinite coordinate in either cloud is DTK_ERR_INVALID_ARG,
+// thrown here before any search (one synchronisation of s).
 void build_tree_and_order( PointsView src, PointsView tgt, Lbvh &tree, DeviceBuffer<uint32_t> &order,
                            unsigned *status, cudaStream_t s, uint32_t const *src_group = nullptr,
                            uint32_t const *tgt_group = nullptr, int64_t n_groups = 0,

@@ -11,7 +11,12 @@
 
 struct dtk_mls_s
 {
+    dtk::HandleLife life; // first: its event outlives the buffers' frees
     dtk_mls_options opts;
+    explicit dtk_mls_s( cudaStream_t home )
+        : life( home )
+    {
+    }
     int64_t n_src = 0, n_tgt = 0, nnz = 0;
     int m = 0;
     int uniform_row = 0; // > 0 for kNN rows
@@ -28,4 +33,6 @@ struct dtk_mls_s
     int64_t rotations = 0, rotations32 = 0;
     float search_ms = 0.f, setup_ms = 0.f;
     float build_ms = 0.f, query_ms = 0.f; // the search split: tree build + query sort, kNN/radius queries
+
+    ~dtk_mls_s() { life.retire( offset, idx, coeff64, coeff32, order, src_copy, tgt_copy, t_offset, t_entry ); }
 };

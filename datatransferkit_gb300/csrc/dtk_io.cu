@@ -103,6 +103,7 @@ dtk_status dtk_mls_export( dtk_mls_handle h, void *host_buffer, int64_t bytes, d
         std::memcpy( p + 40, o, 16 );
         std::memcpy( p + 56, &h->opts.radius, 8 );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        TouchOnExit const touch{&h->life, s};
         int64_t at = HEADER;
         DTK_CUDA_OR_THROW( cudaMemcpyAsync( p + at, h->offset.get(), 4 * ( h->n_tgt + 1 ),
                                             cudaMemcpyDeviceToHost, s ) );
@@ -148,7 +149,8 @@ dtk_status dtk_mls_import( const void *host_buffer, int64_t bytes, dtk_stream_t 
         uint64_t sum;
         std::memcpy( &sum, p + need - 8, 8 );
         DTK_REQUIRE_OR_THROW( checksum( p, need - 8 ) == sum, "product checksum mismatch" );
-        auto h = std::make_unique<dtk_mls_s>();
+        cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        auto h = std::make_unique<dtk_mls_s>( s );
         dtk_mls_default_options( &h->opts );
         int32_t o[4];
         std::memcpy( o, p + 40, 16 );
@@ -181,7 +183,7 @@ dtk_status dtk_mls_import( const void *host_buffer, int64_t bytes, dtk_stream_t 
         }
         h->uniform_row = uniform ? (int)row : 0;
         h->mean_row = n_tgt ? (int)( ( nnz + n_tgt - 1 ) / n_tgt ) : 0;
-        cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        TouchOnExit const touch{&h->life, s};
         h->offset.allocate( n_tgt + 1, s );
         h->idx.allocate( std::max<int64_t>( 1, nnz ), s );
         DTK_CUDA_OR_THROW( cudaMemcpyAsync( h->offset.get(), off.data(), 4 * ( n_tgt + 1 ), cudaMemcpyHostToDevice, s ) );

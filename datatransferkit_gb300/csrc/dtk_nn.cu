@@ -19,8 +19,14 @@
 
 struct dtk_nn_s
 {
+    dtk::HandleLife life;
     int64_t n_src = 0, n_tgt = 0;
     dtk::DeviceBuffer<int32_t> idx; // nearest source of every target
+    explicit dtk_nn_s( cudaStream_t home )
+        : life( home )
+    {
+    }
+    ~dtk_nn_s() { life.retire( idx ); }
 };
 
 namespace dtk
@@ -75,12 +81,13 @@ dtk_status dtk_nn_create( const double *src, int64_t n_src, int64_t src_pt_strid
             throw Error{DTK_ERR_UNSUPPORTED, "only single-rank operators (MPI_COMM_SELF)"};
         validate_points( src, n_src, src_pt_stride, src_dim_stride, "source points" );
         validate_points( tgt, n_tgt, tgt_pt_stride, tgt_dim_stride, "target points" );
-        // DTK_CHECK( !search_tree.empty() ), DTK_NearestNeighborOperator_def.hpp:43
+        // DTK_CHECK( !search_tree.empty() ), DTK_NearestNeighborOperator_def.hpp:44
         DTK_REQUIRE_OR_THROW( n_src > 0, "the source point cloud is empty" );
         require_device_memory( src, "source points" );
         require_device_memory( n_tgt ? tgt : nullptr, "target points" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
-        auto h = std::make_unique<dtk_nn_s>();
+        auto h = std::make_unique<dtk_nn_s>( s );
+        TouchOnExit const touch{&h->life, s};
         h->n_src = n_src;
         h->n_tgt = n_tgt;
         h->idx.allocate( std::max<int64_t>( 1, n_tgt ), s );
@@ -101,6 +108,8 @@ dtk_status dtk_nn_create( const double *src, int64_t n_src, int64_t src_pt_strid
             DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, status.get(), sizeof( st ), cudaMemcpyDeviceToHost, s ) );
             tree = Lbvh();
             DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+            if ( st & DEV_TIMEOUT )
+                throw Error{DTK_ERR_TIMEOUT, "a bounded device loop (tree traversal) hit its cap"};
             if ( st )
                 throw Error{DTK_ERR_INTERNAL, "search traversal reported an internal error"};
         }
@@ -122,7 +131,7 @@ dtk_status dtk_nn_apply_multi( dtk_nn_handle h, const double *source_values, int
 {
     return guarded( [&] {
         DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
-        // DTK_REQUIRE at DTK_NearestNeighborOperator_def.hpp:73-74
+        // DTK_REQUIRE at DTK_NearestNeighborOperator_def.hpp:79-80
         DTK_REQUIRE_OR_THROW( n_target_values == h->n_tgt, "_indices.extent(0) == target_values.extent(0)" );
         DTK_REQUIRE_OR_THROW( n_source_values == h->n_src, "_size == source_values.extent(0)" );
         FieldView const in = field_in( source_values, h->n_src, n_comp, src_pt_stride, src_comp_stride,
@@ -133,6 +142,7 @@ dtk_status dtk_nn_apply_multi( dtk_nn_handle h, const double *source_values, int
         if ( h->n_tgt == 0 )
             return;
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        TouchOnExit const touch{&h->life, s};
         int64_t const n = h->n_tgt * n_comp;
         k_gather<<<(unsigned)( ( n + 255 ) / 256 ), 256, 0, s>>>( h->n_tgt, h->idx.get(), in, out );
         check_launch( "k_gather" );
@@ -162,7 +172,7 @@ dtk_status dtk_mls_apply_multi( dtk_mls_handle h, const double *source_values, i
 {
     return guarded( [&] {
         DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
-        // DTK_REQUIRE at DTK_MovingLeastSquaresOperator_def.hpp:196-197, per component
+        // DTK_REQUIRE at DTK_MovingLeastSquaresOperator_def.hpp:129-130, per component
         DTK_REQUIRE_OR_THROW( n_source_values == h->n_src, "source_values.extent(0) == n_source_points" );
         DTK_REQUIRE_OR_THROW( n_target_values == h->n_tgt, "target_values.extent(0) == n_target_points" );
         FieldView const in = field_in( source_values, h->n_src, n_comp, src_pt_stride, src_comp_stride,
@@ -171,6 +181,7 @@ dtk_status dtk_mls_apply_multi( dtk_mls_handle h, const double *source_values, i
                                   "target_values" );
         out.wbase = target_values;
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        TouchOnExit const touch{&h->life, s};
         apply_csr_multi( h->n_tgt, h->offset.get(), h->idx.get(), h->coeff64.get(), h->coeff32.get(), in,
                          out, s );
     } );

@@ -1,7 +1,7 @@
 // Linear BVH and warp-cooperative kNN / radius search (sm_103a).
 //
 // Replaces the ArborX tree and query the MLS constructor runs
-// (packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:114-129).
+// (packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:47-62).
 //
 // Build: scene box -> 30-bit Morton codes (FP32 quantization) -> stable
 // radix sort (codes, ids) -> Morton-sorted FP64 coordinates (packed with the
@@ -117,17 +117,22 @@ __device__ __forceinline__ double double_of( unsigned long long o )
 constexpr int BND_THREADS = 256;
 
 __global__ void __launch_bounds__( BND_THREADS )
-    k_bounds_partial( PointsView p, unsigned long long *partial )
+    k_bounds_partial( PointsView p, unsigned long long *partial, unsigned *status )
 {
     unsigned long long mn[3] = {KEY_INF, KEY_INF, KEY_INF}, mx[3] = {0, 0, 0};
+    bool bad = false;
     for ( int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < p.n;
           i += (int64_t)gridDim.x * blockDim.x )
         for ( int d = 0; d < 3; ++d )
         {
-            unsigned long long const o = ord_of( p( i, d ) );
+            double const v = p( i, d );
+            bad |= nonfinite_bits( v );
+            unsigned long long const o = ord_of( v );
             mn[d] = min( mn[d], o );
             mx[d] = max( mx[d], o );
         }
+    if ( bad )
+        atomicOr( status, DEV_NONFINITE_SOURCE );
     __shared__ unsigned long long s[6][BND_THREADS / 32];
     int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for ( int d = 0; d < 3; ++d )
@@ -201,14 +206,20 @@ __global__ void k_bounds_final( unsigned long long const *partial, int nblocks,
     }
 }
 
+// (bad_flag: when not null, a point with a NaN or infinite coordinate sets
+// DEV_NONFINITE_TARGET there; codes of such points are clamped, never out of
+// range)
 __global__ void k_morton( PointsView p, double const *scene, uint32_t *codes,
-                          uint32_t *ids, int drop = 0 )
+                          uint32_t *ids, int drop = 0, unsigned *bad_flag = nullptr )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i < p.n )
     {
-        codes[i] = morton3( p( i, 0 ), p( i, 1 ), p( i, 2 ), scene ) >> drop;
+        double const x = p( i, 0 ), y = p( i, 1 ), z = p( i, 2 );
+        codes[i] = morton3( x, y, z, scene ) >> drop;
         ids[i] = (uint32_t)i;
+        if ( bad_flag && ( nonfinite_bits( x ) || nonfinite_bits( y ) || nonfinite_bits( z ) ) )
+            atomicOr( bad_flag, DEV_NONFINITE_TARGET );
     }
 }
 
@@ -760,6 +771,7 @@ struct TreeView
     double const *scene;
     int64_t n, nl, nw;
     int levels; // the deepest wide node's level (the root's is 0)
+    int64_t step_cap; // traversal steps a query may take (<= nw, the most it needs)
 };
 
 // FP32 lower bound of the squared distance between any point of [lo, hi]
@@ -1318,7 +1330,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
             // entered at most once
             for ( int64_t guard = 0;; ++guard )
             {
-                if ( guard >= tr.nw )
+                if ( guard >= tr.step_cap )
                 {
                     if ( lane == 0 )
                         atomicOr( status, DEV_TIMEOUT );
@@ -1476,7 +1488,7 @@ __global__ void __launch_bounds__( R_WARPS * 32 )
         // entered at most once
         for ( int64_t guard = 0;; ++guard )
         {
-            if ( guard >= tr.nw )
+            if ( guard >= tr.step_cap )
             {
                 if ( lane == 0 )
                     atomicOr( status, DEV_TIMEOUT );
@@ -1532,7 +1544,7 @@ TreeView view_of( Lbvh const &t )
     return TreeView{t.s2.get(), t.f4.get(),
                     t.codes.get(), t.perm.get(), t.leaf_start.get(), t.leaf_of.get(), t.wide.get(),
                     t.wide_range.get(), t.wide_cell.get(), t.scene.get(), t.n, t.n_leaves, t.n_wide,
-                    t.wide_levels};
+                    t.wide_levels, traversal_cap( t.n_wide )};
 }
 
 unsigned blocks_for( int64_t n, int threads )
@@ -1551,7 +1563,7 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
     tree.scene.allocate( 17, s );
     int const nb = std::max( 1, std::min<int>( 4 * num_sms(), (int)( ( n + BND_THREADS - 1 ) / BND_THREADS ) ) );
     DeviceBuffer<unsigned long long> partial( 6 * nb, s );
-    k_bounds_partial<<<nb, BND_THREADS, 0, s>>>( src, partial.get() );
+    k_bounds_partial<<<nb, BND_THREADS, 0, s>>>( src, partial.get(), status );
     check_launch( "k_bounds_partial" );
     k_bounds_final<<<1, 32, 0, s>>>( partial.get(), nb, tree.scene.get() );
     check_launch( "k_bounds_final" );
@@ -1669,7 +1681,7 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
 }
 
 void sort_queries( Lbvh const &tree, PointsView tgt, DeviceBuffer<uint32_t> &order,
-                   cudaStream_t s, uint32_t const *group, int64_t n_groups )
+                   cudaStream_t s, uint32_t const *group, int64_t n_groups, unsigned *status )
 {
     int64_t const n = tgt.n;
     if ( order.n < (size_t)std::max<int64_t>( 1, n ) )
@@ -1679,7 +1691,8 @@ void sort_queries( Lbvh const &tree, PointsView tgt, DeviceBuffer<uint32_t> &ord
     DeviceBuffer<uint32_t> codes( n, s );
     // the queries' order needs only the top 24 bits of their codes (a 256^3
     // grid): three radix passes instead of four
-    k_morton<<<blocks_for( n, 256 ), 256, 0, s>>>( tgt, tree.scene.get(), codes.get(), order.get(), 6 );
+    k_morton<<<blocks_for( n, 256 ), 256, 0, s>>>( tgt, tree.scene.get(), codes.get(), order.get(), 6,
+                                                     status );
     check_launch( "k_morton(targets)" );
     radix_sort_pairs( codes.get(), order.get(), n, 24, s );
     if ( group )
@@ -1720,10 +1733,20 @@ void build_tree_and_order( PointsView src, PointsView tgt, Lbvh &tree, DeviceBuf
         DTK_CUDA_OR_THROW( cudaStreamWaitEvent( side.s2, side.scene, 0 ) );
         if ( tgt_ready )
             DTK_CUDA_OR_THROW( cudaStreamWaitEvent( side.s2, tgt_ready, 0 ) );
-        sort_queries( tree, tgt, order, side.s2, tgt_group, n_groups );
+        sort_queries( tree, tgt, order, side.s2, tgt_group, n_groups, status );
         DTK_CUDA_OR_THROW( cudaEventRecord( side.done, side.s2 ) );
     } );
     DTK_CUDA_OR_THROW( cudaStreamWaitEvent( s, side.done, 0 ) );
+    // Points with a NaN or infinite coordinate were flagged by the passes
+    // that read them (scene bounds, target Morton codes), whose results stay
+    // in range either way; no search runs on them.
+    unsigned st = 0;
+    DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, status, sizeof( st ), cudaMemcpyDeviceToHost, s ) );
+    DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+    if ( st & DEV_NONFINITE_SOURCE )
+        throw Error{DTK_ERR_INVALID_ARG, "DTK_REQUIRE: source point coordinates must be finite"};
+    if ( st & DEV_NONFINITE_TARGET )
+        throw Error{DTK_ERR_INVALID_ARG, "DTK_REQUIRE: target point coordinates must be finite"};
 }
 
 void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,

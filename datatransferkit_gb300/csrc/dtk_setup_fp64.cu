@@ -265,7 +265,7 @@ __global__ void __launch_bounds__( SETUP_BLOCK )
     k_setup_fp64( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
                   uint32_t const *order, int64_t n_tgt, int rbf, bool rows_sorted,
                   double *coeff, unsigned long long *under_count,
-                  unsigned long long *rot_count, unsigned *status )
+                  unsigned long long *rot_count, unsigned *status, unsigned jcap )
 {
     extern __shared__ double smem[];
     Smem<M> s{smem, smem + M * M * SETUP_BLOCK, smem + 2 * M * M * SETUP_BLOCK, (int)threadIdx.x};
@@ -345,7 +345,7 @@ __global__ void __launch_bounds__( SETUP_BLOCK )
             }
         }
         double row0[M];
-        dropped = jacobi_row0<M>( s, row0, iters, 200u * M * M + 2000u, status );
+        dropped = jacobi_row0<M>( s, row0, iters, jcap, status );
 
         // computePolynomialCoefficients: c_k = phi_k * (row0 . P_k)
         for ( int j = 0; j < len; ++j )
@@ -384,7 +384,8 @@ __global__ void __launch_bounds__( SETUP_BLOCK )
 // General-n SVDFunctor (one thread per matrix, E/U/V in a global work area):
 // the batched pseudo-inverse kernel of DTK_DetailsSVDImpl.hpp:197-302.
 __global__ void k_svd_general( int n, int64_t count, double const *a, double *pinv,
-                               double *work, unsigned long long *under, unsigned *status )
+                               double *work, unsigned long long *under, unsigned *status,
+                               unsigned long long cap )
 {
     int64_t const mid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( mid >= count )
@@ -401,7 +402,6 @@ __global__ void k_svd_general( int n, int64_t count, double const *a, double *pi
             V[i * n + j] = i == j ? 1.0 : 0.0;
         }
     double const tol = DBL_EPSILON;
-    unsigned long long const cap = 200ull * nn + 2000ull;
     unsigned long long it = 0;
     while ( true )
     {
@@ -578,7 +578,7 @@ __global__ void __launch_bounds__( 128 )
 template <int M>
 __global__ void __launch_bounds__( SETUP_BLOCK )
     k_split_jacobi( int64_t n, double *work, unsigned long long *under_count,
-                    unsigned long long *rot_count, unsigned *status )
+                    unsigned long long *rot_count, unsigned *status, unsigned jcap )
 {
     constexpr int NU = M * ( M + 1 ) / 2;
     constexpr int STRIDE = NU + 1 + M;
@@ -604,7 +604,7 @@ __global__ void __launch_bounds__( SETUP_BLOCK )
             s.v( a ) = a == 0 ? 1.0 : 0.0;
         }
         double row0[M];
-        dropped = jacobi_row0<M>( s, row0, iters, 200u * M * M + 2000u, status );
+        dropped = jacobi_row0<M>( s, row0, iters, jcap, status );
         for ( int a = 0; a < M; ++a )
             rec[NU + 1 + a] = row0[a];
     }
@@ -678,15 +678,9 @@ void launch_split( SetupArgs const &a, int32_t const *targets, int64_t n, cudaSt
                                                     work.get(), a.status );
     check_launch( "k_split_moments" );
     size_t const smem = ( 2 * M * M + M ) * SETUP_BLOCK * sizeof( double );
-    static bool configured = false;
-    if ( !configured )
-    {
-        DTK_CUDA_OR_THROW( cudaFuncSetAttribute( k_split_jacobi<M>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem ) );
-        configured = true;
-    }
+    ensure_dynamic_smem( k_split_jacobi<M>, smem );
     k_split_jacobi<M><<<(unsigned)( ( n + SETUP_BLOCK - 1 ) / SETUP_BLOCK ), SETUP_BLOCK, smem, s>>>(
-        n, work.get(), a.underdetermined, a.rotations, a.status );
+        n, work.get(), a.underdetermined, a.rotations, a.status, (unsigned)jacobi_cap( M ) );
     check_launch( "k_split_jacobi" );
     k_split_coeffs<M, G><<<gblocks, 128, 0, s>>>( a.src, a.tgt, a.offset, a.idx, targets, n, a.rbf,
                                                    work.get(), a.coeff64, a.coeff32 );
@@ -714,18 +708,12 @@ template <int M>
 void launch_fp64( SetupArgs const &a, cudaStream_t s )
 {
     size_t const smem = ( 2 * M * M + M ) * SETUP_BLOCK * sizeof( double );
-    static bool configured = false;
-    if ( !configured )
-    {
-        DTK_CUDA_OR_THROW( cudaFuncSetAttribute( k_setup_fp64<M>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem ) );
-        configured = true;
-    }
+    ensure_dynamic_smem( k_setup_fp64<M>, smem );
     unsigned const blocks = (unsigned)( ( a.n_tgt + SETUP_BLOCK - 1 ) / SETUP_BLOCK );
     k_setup_fp64<M><<<blocks, SETUP_BLOCK, smem, s>>>( a.src, a.tgt, a.offset, a.idx, a.order,
                                                         a.n_tgt, a.rbf, a.rows_sorted, a.coeff64,
-                                                        a.underdetermined, a.rotations, a.status );
+                                                        a.underdetermined, a.rotations, a.status,
+                                                        (unsigned)jacobi_cap( M ) );
     check_launch( "k_setup_fp64" );
 }
 
@@ -765,7 +753,7 @@ void svd_pinv_batched_work( int n, int64_t count, double const *a, double *pinv,
     if ( count == 0 )
         return;
     unsigned const blocks = (unsigned)( ( count + 63 ) / 64 );
-    k_svd_general<<<blocks, 64, 0, s>>>( n, count, a, pinv, work, underdetermined, status );
+    k_svd_general<<<blocks, 64, 0, s>>>( n, count, a, pinv, work, underdetermined, status, jacobi_cap( n ) );
     check_launch( "k_svd_general" );
 }
 
@@ -776,7 +764,8 @@ void svd_pinv_batched( int n, int64_t count, double const *a, double *pinv,
         return;
     DeviceBuffer<double> work( 3 * (size_t)n * n * count, s );
     unsigned const blocks = (unsigned)( ( count + 63 ) / 64 );
-    k_svd_general<<<blocks, 64, 0, s>>>( n, count, a, pinv, work.get(), underdetermined, status );
+    k_svd_general<<<blocks, 64, 0, s>>>( n, count, a, pinv, work.get(), underdetermined, status,
+                                         jacobi_cap( n ) );
     check_launch( "k_svd_general" );
 }
 

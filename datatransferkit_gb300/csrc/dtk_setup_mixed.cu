@@ -698,14 +698,7 @@ void launch_mixed( SetupArgs const &a, cudaStream_t s )
     check_launch( "k_setup_mixed" );
     // the listed targets (count known only on the device): persistent blocks
     size_t const smem = ( (size_t)M * ( M + 1 ) / 2 + (size_t)M * M ) * sizeof( float ) * MB;
-    static bool configured = false;
-    if ( !configured )
-    {
-        DTK_CUDA_OR_THROW( cudaFuncSetAttribute( k_setup_mixed_eig<M>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem ) );
-        configured = true;
-    }
+    ensure_dynamic_smem( k_setup_mixed_eig<M>, smem );
     int64_t const want = ( a.n_tgt + MB - 1 ) / MB;
     unsigned const blocks = (unsigned)std::max<int64_t>( 1, std::min<int64_t>( want, 8 * num_sms() ) );
     k_setup_mixed_eig<M><<<blocks, MB, smem, s>>>( a.src, a.tgt, a.offset, a.idx, list.get(), count.get(),

@@ -5,7 +5,7 @@ Mirrors (paths inside the DataTransferKit project):
   MovingLeastSquaresOperator<Device, RBF, Basis>
         constructor (setup) / apply          DTK_MovingLeastSquaresOperator_decl.hpp:36-63
   Wendland<k>, Wu<k>, Buhmann<k>             DTK_CompactlySupportedRadialBasisFunctions.hpp:42-147
-  MultivariatePolynomialBasis<Basis, DIM>    DTK_MultivariatePolynomialBasis.hpp:178-238
+  MultivariatePolynomialBasis<Basis, DIM>    DTK_MultivariatePolynomialBasis.hpp:79-92
 
 Arrays are CUDA tensors (device memory, the analogue of Kokkos Views in a
 CUDA memory space): points float64 of shape (n, 3) with any strides
@@ -155,7 +155,7 @@ class MovingLeastSquaresOperator(PointCloudOperator):
         src = _check_points(source_points, "source_points")
         tgt = _check_points(target_points, "target_points")
         # DTK_REQUIRE(source dim == target dim), DTK_REQUIRE(dim == 3):
-        # DTK_MovingLeastSquaresOperator_def.hpp:106-109
+        # DTK_MovingLeastSquaresOperator_def.hpp:39-42
         if src.shape[1] != tgt.shape[1]:
             raise _capi.InvalidArgument(1, "source_points.extent(1) == target_points.extent(1)")
         if src.shape[1] != 3 or self.polynomial_basis.dim != 3:

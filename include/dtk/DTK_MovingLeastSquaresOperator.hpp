@@ -10,7 +10,7 @@
  *   Wendland<k>, Wu<k>, Buhmann<k>, RadialBasisFunction<RBF>
  *       packages/Meshfree/src/DTK_CompactlySupportedRadialBasisFunctions.hpp:22-147
  *   Constant / Linear / Quadratic, MultivariatePolynomialBasis<Basis, DIM>
- *       packages/Meshfree/src/DTK_MultivariatePolynomialBasis.hpp:178-304
+ *       packages/Meshfree/src/DTK_MultivariatePolynomialBasis.hpp:79-125
  *   DataTransferKitException (DTK_REQUIRE failures)
  *       packages/Utils/src/DTK_DBC.hpp:36-89
  *
@@ -18,6 +18,13 @@
  * a Kokkos::View in a CUDA memory space satisfies this, as does the small
  * DataTransferKit::DeviceView below.  Points are rank-2 (n x 3) views of
  * double in either layout; values are rank-1 contiguous views of double.
+ * PointCloudOperator<DeviceType>::apply is virtual over the reference's own
+ * value views, Kokkos::View<double const *, DeviceType> and
+ * Kokkos::View<double *, DeviceType>, when <Kokkos_Core.hpp> is included
+ * before this header, and over DeviceView otherwise.
+ * apply returns after the target values are written, like the reference's
+ * apply, which ends in Kokkos::deep_copy (DTK_MovingLeastSquaresOperator_def.hpp:140);
+ * MlsOptions::asynchronous leaves it queued on the operator's stream instead.
  * The communicator must have one rank (MPI_COMM_SELF): with <mpi.h>
  * included first its size is checked, otherwise any communicator value is
  * taken as one rank.
@@ -275,15 +282,33 @@ struct DeviceView
     std::ptrdiff_t stride( int d ) const { return d == 0 ? s0 : s1; }
 };
 
-/* Extensions to the reference constructor: neighbours, radius search and
- * the precision form (defaults reproduce the reference: k = basis size,
- * kNN, FP64). */
+// The value views of the virtual PointCloudOperator::apply: the reference's
+// (DTK_PointCloudOperator.hpp:34-36) when Kokkos is included first, the
+// DeviceView stand-ins otherwise.
+#if defined( KOKKOS_VERSION )
+template <typename DeviceType>
+using SourceValuesView = Kokkos::View<double const *, DeviceType>;
+template <typename DeviceType>
+using TargetValuesView = Kokkos::View<double *, DeviceType>;
+#else
+template <typename DeviceType>
+using SourceValuesView = DeviceView<double const>;
+template <typename DeviceType>
+using TargetValuesView = DeviceView<double>;
+#endif
+
+/* Extensions to the reference constructor: neighbours, radius search, the
+ * precision form, the stream (it must outlive the operator, whose buffers
+ * are freed on it), and whether apply may return before its results are
+ * written (defaults reproduce the reference: k = basis size, kNN, FP64,
+ * synchronous apply). */
 struct MlsOptions
 {
     int k = 0;
     double radius = 0.0;
     int precision = DTK_FP64;
     dtk_stream_t stream = nullptr;
+    bool asynchronous = false;
 };
 
 namespace Details
@@ -308,8 +333,8 @@ class PointCloudOperator
 {
   public:
     virtual ~PointCloudOperator() = default;
-    virtual void apply( DeviceView<double const> source_values,
-                        DeviceView<double> target_values ) const = 0;
+    virtual void apply( SourceValuesView<DeviceType> source_values,
+                        TargetValuesView<DeviceType> target_values ) const = 0;
 };
 
 template <typename DeviceType, typename CompactlySupportedRadialBasisFunction = Wendland<0>,
@@ -328,9 +353,10 @@ class MovingLeastSquaresOperator : public PointCloudOperator<DeviceType>
         : _n_source_points( source_points.extent( 0 ) )
         , _n_target_points( target_points.extent( 0 ) )
         , _stream( ext.stream )
+        , _asynchronous( ext.asynchronous )
     {
         // DTK_REQUIRE(source dim == target dim), DTK_REQUIRE(dim == 3):
-        // DTK_MovingLeastSquaresOperator_def.hpp:106-109
+        // DTK_MovingLeastSquaresOperator_def.hpp:39-42
         if ( source_points.extent( 1 ) != target_points.extent( 1 ) )
             throw DataTransferKitException(
                 "DTK_REQUIRE( source_points.extent_int( 1 ) == target_points.extent_int( 1 ) )" );
@@ -357,7 +383,7 @@ class MovingLeastSquaresOperator : public PointCloudOperator<DeviceType>
     template <typename SourceValues, typename TargetValues>
     void apply_values( SourceValues const &source_values, TargetValues const &target_values ) const
     {
-        // DTK_REQUIRE at DTK_MovingLeastSquaresOperator_def.hpp:196-197
+        // DTK_REQUIRE at DTK_MovingLeastSquaresOperator_def.hpp:129-130
         if ( (std::size_t)source_values.extent( 0 ) != _n_source_points )
             throw DataTransferKitException(
                 "DTK_REQUIRE( source_values.extent( 0 ) == _n_source_points )" );
@@ -370,17 +396,19 @@ class MovingLeastSquaresOperator : public PointCloudOperator<DeviceType>
                                        const_cast<double *>( reinterpret_cast<double const *>(
                                            target_values.data() ) ),
                                        (int64_t)target_values.extent( 0 ), _stream ) );
+        if ( !_asynchronous ) // the reference's deep_copy fences
+            Details::check( dtk_stream_synchronize( _stream ) );
     }
 
-    void apply( DeviceView<double const> source_values,
-                DeviceView<double> target_values ) const override
+    void apply( SourceValuesView<DeviceType> source_values,
+                TargetValuesView<DeviceType> target_values ) const override
     {
         apply_values( source_values, target_values );
     }
 
-    // apply(source_values, target_values) for any view type (Kokkos::View).
+    // apply(source_values, target_values) for any other view type.
     template <typename SourceValues, typename TargetValues,
-              typename = std::enable_if_t<!std::is_same<SourceValues, DeviceView<double const>>::value>>
+              typename = std::enable_if_t<!std::is_same<SourceValues, SourceValuesView<DeviceType>>::value>>
     void apply( SourceValues const &source_values, TargetValues const &target_values ) const
     {
         apply_values( source_values, target_values );
@@ -401,6 +429,8 @@ class MovingLeastSquaresOperator : public PointCloudOperator<DeviceType>
             const_cast<double *>( reinterpret_cast<double const *>( target_values.data() ) ),
             (int64_t)target_values.extent( 0 ), (int64_t)target_values.stride( 0 ),
             (int64_t)target_values.stride( 1 ), _stream ) );
+        if ( !_asynchronous )
+            Details::check( dtk_stream_synchronize( _stream ) );
     }
     int64_t underdetermined() const
     {
@@ -413,6 +443,7 @@ class MovingLeastSquaresOperator : public PointCloudOperator<DeviceType>
   private:
     std::size_t _n_source_points, _n_target_points;
     dtk_stream_t _stream;
+    bool _asynchronous;
     std::shared_ptr<struct dtk_mls_s> _handle;
 };
 

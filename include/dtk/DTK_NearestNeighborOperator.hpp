@@ -5,9 +5,11 @@
  * Mirrors (paths inside the DataTransferKit project):
  *   DataTransferKit::NearestNeighborOperator<DeviceType>
  *       packages/Meshfree/src/DTK_NearestNeighborOperator_decl.hpp:27-49
- *       packages/Meshfree/src/DTK_NearestNeighborOperator_def.hpp:23-81
+ *       packages/Meshfree/src/DTK_NearestNeighborOperator_def.hpp:23-86
  *
- * Views, communicator and exceptions as in DTK_MovingLeastSquaresOperator.hpp.
+ * Views, communicator, exceptions and the synchronous apply (the reference's
+ * ends in Kokkos::deep_copy, DTK_NearestNeighborOperator_def.hpp:85) as in
+ * DTK_MovingLeastSquaresOperator.hpp.
  * The nearest source of a target is the smallest (d^2, source index): ties
  * go to the smaller source index.
  */
@@ -28,10 +30,11 @@ class NearestNeighborOperator : public PointCloudOperator<DeviceType>
 
     template <typename Comm, typename SourceView, typename TargetView>
     NearestNeighborOperator( Comm comm, SourceView const &source_points, TargetView const &target_points,
-                             dtk_stream_t stream = nullptr )
+                             dtk_stream_t stream = nullptr, bool asynchronous = false )
         : _size( source_points.extent( 0 ) )
         , _n_target_points( target_points.extent( 0 ) )
         , _stream( stream )
+        , _asynchronous( asynchronous )
     {
         dtk_nn_handle h = nullptr;
         Details::check( dtk_nn_create(
@@ -46,7 +49,7 @@ class NearestNeighborOperator : public PointCloudOperator<DeviceType>
     template <typename SourceValues, typename TargetValues>
     void apply_values( SourceValues const &source_values, TargetValues const &target_values ) const
     {
-        // DTK_REQUIRE at DTK_NearestNeighborOperator_def.hpp:73-74
+        // DTK_REQUIRE at DTK_NearestNeighborOperator_def.hpp:79-80
         if ( (std::size_t)target_values.extent( 0 ) != _n_target_points )
             throw DataTransferKitException( "DTK_REQUIRE( _indices.extent( 0 ) == target_values.extent( 0 ) )" );
         if ( (std::size_t)source_values.extent( 0 ) != _size )
@@ -58,17 +61,20 @@ class NearestNeighborOperator : public PointCloudOperator<DeviceType>
             const_cast<double *>( reinterpret_cast<double const *>( target_values.data() ) ),
             (int64_t)target_values.extent( 0 ), (int64_t)target_values.stride( 0 ),
             (int64_t)target_values.stride( 1 ), _stream ) );
+        if ( !_asynchronous )
+            Details::check( dtk_stream_synchronize( _stream ) );
     }
 
-    void apply( DeviceView<double const> source_values, DeviceView<double> target_values ) const override
+    void apply( SourceValuesView<DeviceType> source_values,
+                TargetValuesView<DeviceType> target_values ) const override
     {
         apply_values( source_values, target_values );
     }
 
-    // apply(source_values, target_values) for any view type (Kokkos::View),
-    // rank 1 or rank 2 (the reference's fetch handles both).
+    // apply(source_values, target_values) for any other view type, rank 1
+    // or rank 2 (the reference's fetch handles both).
     template <typename SourceValues, typename TargetValues,
-              typename = std::enable_if_t<!std::is_same<SourceValues, DeviceView<double const>>::value>>
+              typename = std::enable_if_t<!std::is_same<SourceValues, SourceValuesView<DeviceType>>::value>>
     void apply( SourceValues const &source_values, TargetValues const &target_values ) const
     {
         apply_values( source_values, target_values );
@@ -79,6 +85,7 @@ class NearestNeighborOperator : public PointCloudOperator<DeviceType>
   private:
     std::size_t _size, _n_target_points;
     dtk_stream_t _stream;
+    bool _asynchronous;
     std::shared_ptr<struct dtk_nn_s> _handle;
 };
 

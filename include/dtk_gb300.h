@@ -8,14 +8,18 @@
  * handle owns the operator's CSR product (offset, indices, coefficients).
  * Calls on one handle are ordered on the stream they are given and are not
  * re-entrant.  `stream` is a cudaStream_t (NULL = legacy default stream).
+ * A handle's buffers live on the stream its create call was given: that
+ * stream must stay valid until the handle is destroyed, where the buffers
+ * are freed on it behind the work of the handle's last call (on whichever
+ * stream that call was given).
  *
  * Reference interface replaced (paths inside the DataTransferKit project):
  *   DataTransferKit::MovingLeastSquaresOperator<DeviceType, RBF, Basis>
  *     packages/Meshfree/src/DTK_MovingLeastSquaresOperator_decl.hpp:36-63
  *   its constructor (setup: search, weights, moments, pseudo-inverse,
- *   coefficients)  DTK_MovingLeastSquaresOperator_def.hpp:91-186
+ *   coefficients)  DTK_MovingLeastSquaresOperator_def.hpp:24-119
  *   apply(source_values, target_values)
- *                   DTK_MovingLeastSquaresOperator_def.hpp:188-208
+ *                   DTK_MovingLeastSquaresOperator_def.hpp:121-141
  */
 #ifndef DTK_GB300_H
 #define DTK_GB300_H
@@ -54,7 +58,7 @@ typedef enum
     DTK_BUHMANN4 = 8
 } dtk_rbf;
 
-/* MultivariatePolynomialBasis<., 3>: DTK_MultivariatePolynomialBasis.hpp:249-276 */
+/* MultivariatePolynomialBasis<., 3>: DTK_MultivariatePolynomialBasis.hpp:98-125 */
 typedef enum
 {
     DTK_CONSTANT3 = 0, /* m = 1  */
@@ -90,10 +94,12 @@ typedef struct
  * Wendland<0>, Linear3, k = basis size, FP64, comm_size 1, keep_points 0. */
 void dtk_mls_default_options(dtk_mls_options *opts);
 
-/* Setup.  Replaces the constructor, DTK_MovingLeastSquaresOperator_def.hpp:91-186.
+/* Setup.  Replaces the constructor, DTK_MovingLeastSquaresOperator_def.hpp:24-119.
  * src / tgt: n x 3 coordinates, element (i, d) at ptr[i*pt_stride + d*dim_stride]
  * (doubles; LayoutRight: (3, 1); LayoutLeft: (1, n)).  Preconditions as the
  * reference: dimension 3 (implied), n_src > 0 (DTK_CHECK(!tree.empty())).
+ * A NaN or infinite coordinate in either cloud is DTK_ERR_INVALID_ARG,
+ * detected before the search runs.
  * Returns when the product is complete (the reference fences). */
 dtk_status dtk_mls_create(const dtk_mls_options *opts, const double *src,
                           int64_t n_src, int64_t src_pt_stride,
@@ -103,10 +109,11 @@ dtk_status dtk_mls_create(const dtk_mls_options *opts, const double *src,
                           dtk_mls_handle *out);
 
 /* apply: target_values[i] = sum_j coeff_j * source_values[idx_j].
- * Replaces MovingLeastSquaresOperator::apply, DTK_MovingLeastSquaresOperator_def.hpp:188-208,
+ * Replaces MovingLeastSquaresOperator::apply, DTK_MovingLeastSquaresOperator_def.hpp:121-141,
  * with its preconditions n_source_values == n_src and n_target_values ==
- * n_tgt (DTK_REQUIRE at :196-197).  Writes every target value; enqueued on
- * `stream`, asynchronous. */
+ * n_tgt (DTK_REQUIRE at :129-130).  Writes every target value; enqueued on
+ * `stream`, asynchronous (the reference's apply fences: follow with
+ * dtk_stream_synchronize for that behaviour, as the C++ drop-in does). */
 dtk_status dtk_mls_apply(dtk_mls_handle h, const double *source_values,
                          int64_t n_source_values, double *target_values,
                          int64_t n_target_values, dtk_stream_t stream);
@@ -174,6 +181,12 @@ dtk_status dtk_mls_transfer_host(const dtk_mls_options *opts,
                                  double *target_values_host,
                                  dtk_stream_t stream, dtk_mls_handle *out);
 
+/* Blocks the calling host thread until the work queued on `stream` is done
+ * (the fence the reference's apply ends with, Kokkos::deep_copy at
+ * DTK_MovingLeastSquaresOperator_def.hpp:140; the C++ drop-in's apply calls
+ * it).  An error of that work is DTK_ERR_CUDA. */
+dtk_status dtk_stream_synchronize(dtk_stream_t stream);
+
 /* Running count of the kernels this library has launched in the process
  * (diagnostics; not a reference interface). */
 int64_t dtk_kernel_launch_count(void);
@@ -182,14 +195,15 @@ int64_t dtk_kernel_launch_count(void);
  * in its own stream-ordered pool, one per device, which keeps freed blocks
  * cached across synchronizations (up to 1/8 of the device's memory) so that
  * repeated setups do not map memory again.  This returns the cached blocks
- * of every device's pool to the driver; memory that live handles own stays.
+ * of every device's pool to the driver; memory that live handles own stays,
+ * and so does memory whose free is still queued behind work on a stream.
  * No counterpart in the reference (Kokkos manages its own memory). */
 dtk_status dtk_release_cached_memory(void);
 
 dtk_status dtk_mls_destroy(dtk_mls_handle h);
 
 /* ---- search only (the ArborX query the constructor runs,
- *      DTK_MovingLeastSquaresOperator_def.hpp:114-129) ----
+ *      DTK_MovingLeastSquaresOperator_def.hpp:47-62) ----
  * kNN: row i = the min(k, n_src) nearest sources by (d2, index), ascending,
  * d2 = (dx*dx + dy*dy) + dz*dz in FP64 with separately rounded operations.
  * offset must hold n_tgt+1 and indices n_tgt*min(k, n_src) entries. */
@@ -230,11 +244,11 @@ dtk_status dtk_mls_apply_multi(dtk_mls_handle h, const double *source_values,
                                dtk_stream_t stream);
 
 /* ---- NearestNeighborOperator (DTK_NearestNeighborOperator_decl.hpp:27-49) ----
- * create (DTK_NearestNeighborOperator_def.hpp:23-66): the nearest source of
+ * create (DTK_NearestNeighborOperator_def.hpp:23-71): the nearest source of
  * every target, (d^2, index) order (ties to the smaller source index);
  * comm_size > 1 -> DTK_ERR_UNSUPPORTED; an empty source cloud ->
  * DTK_ERR_INVALID_ARG (the reference's DTK_CHECK(!search_tree.empty())).
- * apply (:68-81): target_values[i] = source_values[nearest(i)]; the
+ * apply (:73-86): target_values[i] = source_values[nearest(i)]; the
  * DTK_REQUIREs on the extents -> DTK_ERR_INVALID_ARG.  Device pointers. */
 typedef struct dtk_nn_s *dtk_nn_handle;
 dtk_status dtk_nn_create(const double *src, int64_t n_src, int64_t src_pt_stride,
@@ -309,6 +323,17 @@ dtk_status dtk_mls_batch_destroy(dtk_mls_batch_handle h);
  * host time the create call spent planning (bucketing targets, binning rows). */
 dtk_status dtk_mls_batch_get_stage_times(dtk_mls_batch_handle h, float *search_ms,
                                          float *setup_ms, float *host_ms);
+
+/* Caps of the bounded device loops, for tests and diagnostics (no
+ * counterpart in the reference): Jacobi rotations per moment matrix (FP64
+ * setup, split setup, batched pseudo-inverse) and tree-traversal steps per
+ * query (kNN and radius search), for the calls made after it in this
+ * process.  A loop that reaches its cap stops, sets a status bit, and the
+ * call returns DTK_ERR_TIMEOUT with the device context intact, so a test can
+ * drive the caps to exhaustion on an ordinary input.  0 restores the built-in
+ * caps: 200 m^2 + 2000 rotations, and the tree's node count in steps (more
+ * than a search takes).  Negative values -> DTK_ERR_INVALID_ARG. */
+dtk_status dtk_set_loop_caps(int64_t jacobi_rotations, int64_t traversal_steps);
 
 /* Last error message of the calling host thread (never NULL). */
 const char *dtk_last_error(void);

@@ -9,8 +9,9 @@
 * ``_ref/libdtk_ref.so``: the reference's own MLS numerics headers compiled
   where they lie in the DataTransferKit tree against the project-written API
   shim in ``ref_shim/`` plus ``ref_driver.cpp``.  Built only when the
-  reference sources are present (``DTK_REFERENCE_ROOT``, default
-  ``/root/reference``); it never travels as source and never ships.
+  reference sources are present (``DTK_REFERENCE_ROOT``, else a
+  ``reference`` directory beside this repository); it never travels as
+  source and never ships.
 
 Both use portable flags only (no -march), so results agree between x86-64
 and aarch64 hosts.
@@ -35,7 +36,9 @@ COMMON = ["-O3", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
 
 
 def reference_root() -> Path:
-    return Path(os.environ.get("DTK_REFERENCE_ROOT", "/root/reference"))
+    """DTK_REFERENCE_ROOT, else the DataTransferKit tree beside this repository."""
+    env = os.environ.get("DTK_REFERENCE_ROOT")
+    return Path(env) if env else HERE.parent.parent / "reference"
 
 
 def _stale(out: Path, deps) -> bool:

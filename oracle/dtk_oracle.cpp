@@ -7,11 +7,11 @@
 // so that every product and sum is rounded separately on every host.
 //
 // Reference files restated (paths inside the DataTransferKit project):
-//   packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:91-208
+//   packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:24-141
 //   packages/Meshfree/src/DTK_DetailsMovingLeastSquaresOperatorImpl.hpp:49-336
 //   packages/Meshfree/src/DTK_DetailsSVDImpl.hpp:29-302
 //   packages/Meshfree/src/DTK_CompactlySupportedRadialBasisFunctions.hpp:22-147
-//   packages/Meshfree/src/DTK_MultivariatePolynomialBasis.hpp:249-304
+//   packages/Meshfree/src/DTK_MultivariatePolynomialBasis.hpp:98-125
 #include "dtk_oracle.h"
 
 #include <algorithm>
@@ -135,7 +135,7 @@ inline double rbf_deriv( int rbf, double x )
 }
 
 // ---------------------------------------------------------------------------
-// Polynomial bases in 3-D: DTK_MultivariatePolynomialBasis.hpp:249-276.
+// Polynomial bases in 3-D: DTK_MultivariatePolynomialBasis.hpp:98-125.
 // basis id 0 = Constant (m=1), 1 = Linear (m=4), 2 = Quadratic (m=10).
 // ---------------------------------------------------------------------------
 inline int basis_size( int basis )
@@ -558,7 +558,7 @@ struct RowScratch
 };
 
 // Stages of MovingLeastSquaresOperator setup for one target row, in the
-// reference order (DTK_MovingLeastSquaresOperator_def.hpp:133-185).
+// reference order (DTK_MovingLeastSquaresOperator_def.hpp:64-118).
 // Returns the rank-deficiency flag; fills coeff[0..len) and row0[0..m).
 int mls_row( double const *src, double const *t, int32_t const *idx, int len,
              int rbf, int basis, RowScratch &w, double *coeff, double *radius_out,

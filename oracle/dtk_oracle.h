@@ -6,13 +6,13 @@
  * in the product (datatransferkit_gb300/, include/) links, loads or calls it.
  *
  * It restates, in plain FP64 C++ with OpenMP over targets, the algorithm of
- *   packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:91-208
+ *   packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:24-141
  *   packages/Meshfree/src/DTK_DetailsMovingLeastSquaresOperatorImpl.hpp:49-336
  *   packages/Meshfree/src/DTK_DetailsSVDImpl.hpp:29-302
  *   packages/Meshfree/src/DTK_CompactlySupportedRadialBasisFunctions.hpp:22-147
- *   packages/Meshfree/src/DTK_MultivariatePolynomialBasis.hpp:249-304
+ *   packages/Meshfree/src/DTK_MultivariatePolynomialBasis.hpp:98-125
  * and the neighbour contract of the (un-vendored) ArborX nearest / radius
- * queries used at DTK_MovingLeastSquaresOperator_def.hpp:114-127:
+ * queries used at DTK_MovingLeastSquaresOperator_def.hpp:47-60:
  *   row i = the min(k, n_src) smallest (d2, source index) pairs in
  *   lexicographic order, ascending, d2 = (dx*dx + dy*dy) + dz*dz with
  *   dx = s.x - t.x, every operation rounded separately (no FMA).

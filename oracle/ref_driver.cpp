@@ -6,7 +6,7 @@
 // shipped, never linked by the product.
 //
 // The driver follows the stage order of
-// packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:133-185 from
+// packages/Meshfree/src/DTK_MovingLeastSquaresOperator_def.hpp:64-118 from
 // the fetch onwards.  The ArborX search is not vendored, so the (offset,
 // indices) connectivity is an input (the oracle's exact kNN), and the
 // single-rank fetch is the gather points(j, :) = source(indices(j), :).
@@ -155,7 +155,7 @@ int dtk_ref_apply( int64_t n_tgt, int32_t const *offset, int32_t const *idx,
     return 0;
 }
 
-// SVDFunctor over count n x n matrices (tstSVD.cpp:240-273 usage).
+// SVDFunctor over count n x n matrices (tstSVD.cpp:67-100 usage).
 int64_t dtk_ref_svd_pinv( int n, int64_t count, double const *a, double *pinv )
 {
     Kokkos::View<double *, DeviceType> m( "matrices", count * n * n ),

@@ -5,8 +5,17 @@
 //   tstMeshfreeOperatorsSimpleProblem.cpp:113-147 (corner_cases)
 //   tstNearestNeighborOperator.cpp:85-273 (unique_source_point,
 //     structured_clouds, mixed_clouds) on one rank
-// plus a LayoutLeft input, a rank-2 field and the DTK_REQUIRE error convention.
+// plus a LayoutLeft input, a rank-2 field, the DTK_REQUIRE error convention,
+// and apply called through PointCloudOperator<DeviceType>& with the
+// operator's stream non-blocking, its result read on another stream with no
+// other synchronisation (apply returns complete, as the reference's does).
+// Built twice: plain, and with -DDTK_FAKE_KOKKOS, where the virtual apply
+// takes Kokkos::View<double const *, DeviceType> / Kokkos::View<double *,
+// DeviceType> (a test stand-in for Kokkos, tests/cpp/fake_kokkos.hpp).
 // Prints "PASS <n>" on success; exits non-zero on the first failure.
+#ifdef DTK_FAKE_KOKKOS
+#include "fake_kokkos.hpp"
+#endif
 #include <dtk/DTK_MovingLeastSquaresOperator.hpp>
 #include <dtk/DTK_NearestNeighborOperator.hpp>
 
@@ -18,6 +27,7 @@
 #include <cstdlib>
 #include <functional>
 #include <random>
+#include <type_traits>
 #include <vector>
 
 using namespace DataTransferKit;
@@ -260,8 +270,80 @@ void run_nearest()
     }
 }
 
+// apply through the base class, with the reference's value view types
+void run_polymorphic()
+{
+#ifdef DTK_FAKE_KOKKOS
+    using SrcV = Kokkos::View<double const *, CudaDevice>;
+    using TgtV = Kokkos::View<double *, CudaDevice>;
+    auto src_view = []( Buf &b ) { return SrcV( b.d, b.n ); };
+    auto tgt_view = []( Buf &b ) { return TgtV( b.d, b.n ); };
+#else
+    using SrcV = DeviceView<double const>;
+    using TgtV = DeviceView<double>;
+    auto src_view = []( Buf &b ) {
+        SrcV v;
+        v.ptr = b.d;
+        v.n0 = b.n;
+        return v;
+    };
+    auto tgt_view = []( Buf &b ) { return out( b ); };
+#endif
+    static_assert( std::is_same<SrcV, SourceValuesView<CudaDevice>>::value, "reference value views" );
+    static_assert( std::is_same<TgtV, TargetValuesView<CudaDevice>>::value, "reference value views" );
+    cudaStream_t s = nullptr, reader = nullptr;
+    cudaStreamCreateWithFlags( &s, cudaStreamNonBlocking );
+    cudaStreamCreateWithFlags( &reader, cudaStreamNonBlocking );
+    auto f = poly( 10 );
+    std::mt19937_64 g( 11 );
+    std::uniform_real_distribution<double> u( 0., 1. );
+    std::vector<Pt> src, tgt;
+    for ( int i = 0; i < 200000; ++i )
+        src.push_back( {u( g ), u( g ), u( g )} );
+    for ( int i = 0; i < 50000; ++i )
+        tgt.push_back( {0.1 + 0.8 * u( g ), 0.1 + 0.8 * u( g ), 0.1 + 0.8 * u( g )} );
+    Buf bs( 3 * src.size() ), bt( 3 * tgt.size() ), bv( src.size() ), bo( tgt.size() );
+    std::vector<double> sv;
+    for ( auto &p : src )
+        sv.push_back( f( p ) );
+    values( bv, sv );
+    // (the operators live in this scope: the stream they were created on
+    // must outlive them)
+    {
+        MlsOptions ext;
+        ext.k = 32;
+        ext.stream = reinterpret_cast<dtk_stream_t>( s );
+        using Op = MovingLeastSquaresOperator<CudaDevice, Wendland<2>, MultivariatePolynomialBasis<Quadratic, 3>>;
+        Op op( 0, points( bs, src ), points( bt, tgt ), ext );
+        PointCloudOperator<CudaDevice> const &base = op;
+        for ( int rep = 0; rep < 3; ++rep )
+        {
+            cudaMemsetAsync( bo.d, 0xff, bo.n * 8, s ); // NaN, queued on the operator's stream
+            base.apply( src_view( bv ), tgt_view( bo ) );
+            std::vector<double> y( tgt.size() );
+            cudaMemcpyAsync( y.data(), bo.d, y.size() * 8, cudaMemcpyDeviceToHost, reader );
+            cudaStreamSynchronize( reader );
+            for ( std::size_t i = 0; i < tgt.size(); ++i )
+                CHECK( std::abs( y[i] - f( tgt[i] ) ) <= 1e-9 * std::max( 1.0, std::abs( f( tgt[i] ) ) ) );
+        }
+        using NN = NearestNeighborOperator<CudaDevice>;
+        NN nn( 0, points( bs, src ), points( bt, tgt ), reinterpret_cast<dtk_stream_t>( s ) );
+        PointCloudOperator<CudaDevice> const &nbase = nn;
+        cudaMemsetAsync( bo.d, 0xff, bo.n * 8, s );
+        nbase.apply( src_view( bv ), tgt_view( bo ) );
+        std::vector<double> y( tgt.size() );
+        cudaMemcpyAsync( y.data(), bo.d, y.size() * 8, cudaMemcpyDeviceToHost, reader );
+        cudaStreamSynchronize( reader );
+        for ( std::size_t i = 0; i < tgt.size(); ++i )
+            CHECK( std::isfinite( y[i] ) );
+    }
+    cudaStreamDestroy( s );
+    cudaStreamDestroy( reader );
+}
+
 int main()
 {
+    run_polymorphic();
     run_nearest();
     run_basis<MultivariatePolynomialBasis<Constant, 3>>();
     run_basis<MultivariatePolynomialBasis<Linear, 3>>();

@@ -62,7 +62,7 @@ def main():
     mls_case("uniform_w2_q_k20", src, tgt, syn.smooth_field(src), 1, 2, 20)
     mls_case("uniform_w4_q_k32", src, tgt, syn.smooth_field(src), 2, 2, 32)
     mls_case("uniform_w0_l_k4", src, tgt, syn.smooth_field(src), 0, 1, 4)
-    # SVD known answers (tstSVD.cpp:240-323 layouts, own seeded inputs)
+    # SVD known answers (tstSVD.cpp:67-150 layouts, own seeded inputs)
     rng = np.random.default_rng(13)
     full = rng.uniform(-1000, 1000, (10, 32, 32))
     pf, uf = ref.svd_pinv(full)

@@ -109,6 +109,14 @@ def test_svd_rejects_bad_sizes(dtk_lib):
     assert dtk_lib.dtk_svd_pinv(65, 1, 1, 1, None, None) == 1
 
 
+def test_noalloc_rejects_counts_whose_work_size_would_overflow(dtk_lib):
+    # 3 n^2 count overflows int64 for these counts: the bound on count comes
+    # first, so they are refused before any device call
+    for n, count in ((64, (1 << 63) // 8), (64, (1 << 63) - 1), (1, (1 << 62))):
+        assert dtk_lib.dtk_svd_pinv_noalloc(n, count, 1, 1, None, None) == 1
+        assert b"static work area" in dtk_lib.dtk_last_error()
+
+
 def test_status_strings(dtk_lib):
     for s, name in [(0, b"DTK_OK"), (1, b"DTK_ERR_INVALID_ARG"), (5, b"DTK_ERR_TIMEOUT")]:
         assert dtk_lib.dtk_status_string(s) == name

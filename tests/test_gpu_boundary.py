@@ -41,3 +41,17 @@ def test_pageable_host_pointers_are_refused():
     y = torch.empty(10, dtype=torch.float64, device="cuda")
     op.apply(torch.ones(100, dtype=torch.float64, device="cuda"), y)
     assert torch.equal(pin_o, y.cpu())
+
+
+def test_svd_entry_points_refuse_pageable_host_matrices():
+    L = _capi.lib()
+    host = np.eye(4).reshape(1, 4, 4).copy()
+    out = np.zeros_like(host)
+    dev = torch.from_numpy(host).cuda()
+    dev_out = torch.empty_like(dev)
+    for fn in ("dtk_svd_pinv", "dtk_svd_pinv_noalloc"):
+        f = getattr(L, fn)
+        assert f(4, 1, host.ctypes.data, dev_out.data_ptr(), None, None) == INVALID_ARG, fn
+        assert b"a is host memory" in L.dtk_last_error(), fn
+        assert f(4, 1, dev.data_ptr(), out.ctypes.data, None, None) == INVALID_ARG, fn
+        assert b"pinv is host memory" in L.dtk_last_error(), fn

@@ -1,5 +1,5 @@
 """The batched Jacobi pseudo-inverse kernel on the reference's SVD tests
-(tstSVD.cpp:240-323) and the golden pseudo-inverses of the reference code."""
+(tstSVD.cpp:67-150) and the golden pseudo-inverses of the reference code."""
 from pathlib import Path
 
 import numpy as np

@@ -4,9 +4,9 @@ Ported from packages/Meshfree/test (paths inside the DataTransferKit project):
   tstMeshfreeOperators.cpp:130-448           same_npoints_and_basis, grid, line,
                                               single_point_in_radius
   tstMeshfreeOperatorsSimpleProblem.cpp:113-147  corner_cases
-  tstSVD.cpp:240-323                          full_rank, rank_deficient
+  tstSVD.cpp:67-150                          full_rank, rank_deficient
   tstCompactlySupportedRadialBasisFunctions.cpp:52-108  polynomial_rbf, wrap_rbf
-  tstMultivariatePolynomialBasis.cpp:185-215  3D basis values
+  tstMultivariatePolynomialBasis.cpp:60-84  3D basis values
   tstNearestNeighborOperator.cpp:141-273      k = 1 on structured / mixed clouds
 Inputs come from the project's own seeded generators (std::default_random_engine
 is implementation-defined); the properties checked and tolerances are the
