@@ -244,7 +244,10 @@ std::unique_ptr<dtk_mls_s> create_impl( Geometry const &g, dtk_mls_options const
             h->offset.get(), n_tgt, row );
         check_launch( "k_fill_uniform_offsets" );
         h->idx.allocate( std::max<int64_t>( 1, h->nnz ), s );
-        knn_query( tree, tv, h->order.get(), g.k, GroupArgs{}, h->offset.get(), h->idx.get(), status.get(), s );
+        if ( apply_sorted_supported( row ) )
+            h->pos.allocate( std::max<int64_t>( 1, h->nnz ), s );
+        knn_query( tree, tv, h->order.get(), g.k, GroupArgs{}, h->offset.get(), h->idx.get(), status.get(), s,
+                   h->pos.get() );
     }
     else
     {
@@ -279,6 +282,11 @@ std::unique_ptr<dtk_mls_s> create_impl( Geometry const &g, dtk_mls_options const
     a.rbf = g.opts.rbf;
     a.basis = g.opts.basis;
     a.rows_sorted = !g.radius_mode;
+    if ( h->pos.get() )
+    {
+        a.pos = h->pos.get();
+        a.s2 = tree.s2.get();
+    }
     a.underdetermined = counters.get();
     a.rotations = counters.get() + 1;
     a.rotations32 = counters.get() + 2;
@@ -309,7 +317,10 @@ std::unique_ptr<dtk_mls_s> create_impl( Geometry const &g, dtk_mls_options const
                                         cudaMemcpyDeviceToHost, s ) );
     DTK_CUDA_OR_THROW( cudaMemcpyAsync( cnt, counters.get(), sizeof( cnt ),
                                         cudaMemcpyDeviceToHost, s ) );
-    // Release the tree and scratch before returning (stream ordered).
+    // The apply's position -> index map stays; the rest of the tree and the
+    // scratch are released before returning (stream ordered).
+    if ( h->pos.get() )
+        h->perm = std::move( tree.perm );
     tree = Lbvh();
     DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
     if ( st & DEV_TIMEOUT )
@@ -407,8 +418,16 @@ dtk_status dtk_mls_apply( dtk_mls_handle h, const double *source_values, int64_t
         require_device_memory( target_values, "target_values" );
         cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
         TouchOnExit const touch{&h->life, s};
-        apply_csr( h->n_tgt, h->offset.get(), h->idx.get(), h->coeff64.get(), h->coeff32.get(),
-                   h->uniform_row, h->mean_row, source_values, target_values, s );
+        // uniform rows: by sorted position when the search left them; the
+        // mixed form always (its double-float sum), by index otherwise
+        bool const by_pos = h->pos.get() && h->perm.get();
+        if ( apply_sorted_supported( h->uniform_row ) && ( by_pos || h->coeff32.get() ) )
+            apply_sorted( h->n_tgt, h->uniform_row, by_pos ? h->pos.get() : h->idx.get(), h->coeff64.get(),
+                          h->coeff32.get(), h->n_src, by_pos ? h->perm.get() : nullptr, source_values,
+                          target_values, s );
+        else
+            apply_csr( h->n_tgt, h->offset.get(), h->idx.get(), h->coeff64.get(), h->coeff32.get(),
+                       h->uniform_row, h->mean_row, source_values, target_values, s );
     } );
 }
 
@@ -474,10 +493,17 @@ dtk_status dtk_mls_transfer_host( const dtk_mls_options *opts, const double *src
         int64_t const slices = n_tgt >= ( int64_t( 1 ) << 20 ) ? 8 : 1;
         int64_t const per = ( n_tgt + slices - 1 ) / std::max<int64_t>( 1, slices );
         int const R = h->uniform_row;
+        bool const by_pos = h->pos.get() && h->perm.get();
+        SortedValues sorted;
+        if ( by_pos )
+            sorted = permute_values( n_src, h->perm.get(), d_vals.get(), h->coeff32.get() != nullptr, s );
         for ( int64_t r0 = 0; r0 < n_tgt; r0 += per )
         {
             int64_t const r1 = std::min( n_tgt, r0 + per );
-            if ( R > 0 ) // uniform rows: offset[i] = i R also indexes the shifted slice
+            if ( by_pos )
+                apply_pos( r1 - r0, R, h->pos.get() + r0 * R, h->coeff64.get() ? h->coeff64.get() + r0 * R : nullptr,
+                           h->coeff32.get() ? h->coeff32.get() + r0 * R : nullptr, sorted, d_out.get() + r0, s );
+            else if ( R > 0 ) // uniform rows: offset[i] = i R also indexes the shifted slice
                 apply_csr( r1 - r0, h->offset.get(), h->idx.get() + r0 * R,
                            h->coeff64.get() ? h->coeff64.get() + r0 * R : nullptr,
                            h->coeff32.get() ? h->coeff32.get() + r0 * R : nullptr, R, h->mean_row,
@@ -500,6 +526,7 @@ dtk_status dtk_mls_transfer_host( const dtk_mls_options *opts, const double *src
         d_tgt = DeviceBuffer<double>();
         d_vals = DeviceBuffer<double>();
         d_out = DeviceBuffer<double>();
+        sorted = SortedValues();
         DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
         if ( out )
             *out = h.release();

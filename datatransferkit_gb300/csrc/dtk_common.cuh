@@ -395,6 +395,38 @@ struct PointsView
     }
 };
 
+// The neighbours of CSR entries: from the tree's Morton-sorted FP64 copy by
+// sorted position when pos is set (consecutive targets' neighbours are then
+// close in memory), else from the caller's points by original index.  Both
+// give the same coordinates.
+struct Neighbours
+{
+    PointsView src;
+    int32_t const *idx;
+    int32_t const *pos;
+    double2 const *s2;
+    // the entry's reference (position or index) for a bounds check against src.n
+    __device__ __forceinline__ int32_t ref( int64_t e ) const { return pos ? pos[e] : idx[e]; }
+    __device__ __forceinline__ void xyz( int64_t e, double &x, double &y, double &z ) const
+    {
+        if ( pos )
+        {
+            int64_t const p = pos[e];
+            double2 const a = __ldg( s2 + 2 * p ), b = __ldg( s2 + 2 * p + 1 );
+            x = a.x;
+            y = a.y;
+            z = b.x;
+        }
+        else
+        {
+            int64_t const sj = idx[e];
+            x = src( sj, 0 );
+            y = src( sj, 1 );
+            z = src( sj, 2 );
+        }
+    }
+};
+
 // ---------------------------------------------------------------------------
 // Internal library API shared between translation units.
 // ---------------------------------------------------------------------------
@@ -470,10 +502,12 @@ struct GroupArgs
     double const *r = nullptr;
 };
 
-// kNN: writes each row at offset[target] (ascending (d2, index)).
+// kNN: writes each row at offset[target] (ascending (d2, index)): the
+// sources' original indices in idx and, when pos is not null, their sorted
+// positions in the tree (tree.perm maps a position to its index).
 void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
                 GroupArgs const &groups, int32_t const *offset, int32_t *idx, unsigned *status,
-                cudaStream_t s );
+                cudaStream_t s, int32_t *pos = nullptr );
 
 // Radius: count pass (counts[n_tgt]) and fill pass given offsets.
 void radius_count( Lbvh const &tree, PointsView tgt, uint32_t const *order, double r,
@@ -492,6 +526,12 @@ struct SetupArgs
     int64_t n_tgt;
     int rbf, basis;
     bool rows_sorted;     // rows ascending by distance (kNN)
+    // when set: the neighbours' sorted positions (parallel to idx) and the
+    // tree's Morton-sorted FP64 points, (x, y), (z, index bits) per position;
+    // the kernels gather the neighbours from there (the same values as
+    // src(idx), in the order the search walked them)
+    int32_t const *pos = nullptr;
+    double2 const *s2 = nullptr;
     double *coeff64;      // FP64 form output
     float *coeff32;       // mixed form output
     unsigned long long *underdetermined;
@@ -535,6 +575,23 @@ void apply_csr_multi( int64_t n_tgt, int32_t const *offset, int32_t const *idx, 
 void apply_csr( int64_t n_tgt, int32_t const *offset, int32_t const *idx,
                 double const *coeff64, float const *coeff32, int uniform_row, int mean_row,
                 double const *values, double *target, cudaStream_t s );
+// Uniform rows over sorted positions: the values are permuted into the
+// tree's order (perm: sorted position -> index) and gathered by position.
+bool apply_sorted_supported( int uniform_row );
+struct SortedValues
+{
+    DeviceBuffer<double> v64; // FP64 form
+    DeviceBuffer<float2> v32; // mixed form: (hi, lo) = (fl32(v), fl32(v - hi))
+};
+// (perm null: the values in their own order, for entries that hold indices)
+SortedValues permute_values( int64_t n_src, uint32_t const *perm, double const *values, bool f32,
+                             cudaStream_t s );
+// n_rows uniform rows starting at pos / coeff (a slice of the operator's)
+void apply_pos( int64_t n_rows, int uniform_row, int32_t const *pos, double const *coeff64, float const *coeff32,
+                SortedValues const &v, double *target, cudaStream_t s );
+void apply_sorted( int64_t n_tgt, int uniform_row, int32_t const *pos, double const *coeff64,
+                   float const *coeff32, int64_t n_src, uint32_t const *perm, double const *values,
+                   double *target, cudaStream_t s );
 
 // Adjoint kernels.
 struct AdjointArgs

@@ -25,6 +25,10 @@ struct dtk_mls_s
     dtk::DeviceBuffer<double> coeff64;
     dtk::DeviceBuffer<float> coeff32;
     dtk::DeviceBuffer<uint32_t> order;            // Morton order of targets
+    // kNN operators: the entries' sorted positions in the source tree
+    // (parallel to idx) and the tree's position -> index map, for the apply
+    dtk::DeviceBuffer<int32_t> pos;
+    dtk::DeviceBuffer<uint32_t> perm;
     dtk::DeviceBuffer<double> src_copy, tgt_copy; // packed n x 3 (keep_points)
     // transpose of the CSR (source -> its entries, ascending), built on the
     // first adjoint call
@@ -34,5 +38,8 @@ struct dtk_mls_s
     float search_ms = 0.f, setup_ms = 0.f;
     float build_ms = 0.f, query_ms = 0.f; // the search split: tree build + query sort, kNN/radius queries
 
-    ~dtk_mls_s() { life.retire( offset, idx, coeff64, coeff32, order, src_copy, tgt_copy, t_offset, t_entry ); }
+    ~dtk_mls_s()
+    {
+        life.retire( offset, idx, coeff64, coeff32, order, pos, perm, src_copy, tgt_copy, t_offset, t_entry );
+    }
 };

@@ -1062,7 +1062,7 @@ template <bool GROUPED>
 __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     k_knn( TreeView tr, PointsView tgt, uint32_t const *order, Query const *qrec, int k_all, KnnChunks ch,
            GroupView gv,
-           int32_t const *offset, int32_t *idx_out, unsigned *status )
+           int32_t const *offset, int32_t *idx_out, int32_t *pos_out, unsigned *status )
 {
     // the stack of wide nodes to enter: small, to leave most of the SM's L1
     // to the tree and the points
@@ -1407,7 +1407,12 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         screen_f = screen_threshold( bound_f, q.err );
     }
     if ( lane < row )
-        idx_out[offset[qi] + lane] = ki;
+    {
+        int64_t const o = offset[qi] + lane;
+        idx_out[o] = ki;
+        if ( pos_out )
+            pos_out[o] = kp;
+    }
     prev_g = rg.g;
     prev_row = row;
     next_spec = __fmul_ru( __fmul_ru( kth_ru, 1.0f + 9.5367431640625e-07f ), SPEC_GROWTH ); // prune_threshold
@@ -1751,7 +1756,7 @@ void build_tree_and_order( PointsView src, PointsView tgt, Lbvh &tree, DeviceBuf
 
 void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
                 GroupArgs const &groups, int32_t const *offset, int32_t *idx, unsigned *status,
-                cudaStream_t s )
+                cudaStream_t s, int32_t *pos )
 {
     if ( tgt.n == 0 || tree.n == 0 || ( k == 0 && !groups.k ) )
         return;
@@ -1777,10 +1782,10 @@ void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
     check_launch( "k_query_frame" );
     if ( groups.tgt_grp )
         k_knn<true><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, qrec.get(), k, ch, gv,
-                                                     offset, idx, status );
+                                                     offset, idx, pos, status );
     else
         k_knn<false><<<blocks, Q_WARPS * 32, 0, s>>>( view_of( tree ), tgt, order, qrec.get(), k, ch, gv,
-                                                      offset, idx, status );
+                                                      offset, idx, pos, status );
     check_launch( "k_knn" );
 }
 

@@ -262,7 +262,7 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
 
 template <int M>
 __global__ void __launch_bounds__( SETUP_BLOCK )
-    k_setup_fp64( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
+    k_setup_fp64( Neighbours nb, PointsView tgt, int32_t const *offset,
                   uint32_t const *order, int64_t n_tgt, int rbf, bool rows_sorted,
                   double *coeff, unsigned long long *under_count,
                   unsigned long long *rot_count, unsigned *status, unsigned jcap )
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__( SETUP_BLOCK )
         int64_t const b = offset[i];
         int len = offset[i + 1] - (int)b;
         for ( int j = 0; j < len; ++j )
-            if ( (uint32_t)idx[b + j] >= (uint64_t)src.n )
+            if ( (uint32_t)nb.ref( b + j ) >= (uint64_t)nb.src.n )
             {
                 atomicOr( status, DEV_BAD_INDEX );
                 len = 0;
@@ -290,8 +290,9 @@ __global__ void __launch_bounds__( SETUP_BLOCK )
         double d2max = 0.0;
         for ( int j = rows_sorted ? max( 0, len - 1 ) : 0; j < len; ++j )
         {
-            int64_t const sj = idx[b + j];
-            d2max = fmax( d2max, dist2_rn( src( sj, 0 ), src( sj, 1 ), src( sj, 2 ), tx, ty, tz ) );
+            double sx, sy, sz;
+            nb.xyz( b + j, sx, sy, sz );
+            d2max = fmax( d2max, dist2_rn( sx, sy, sz, tx, ty, tz ) );
         }
         double distance = 10. * DBL_EPSILON;
         double const dmax = __dsqrt_rn( d2max );
@@ -306,9 +307,9 @@ __global__ void __launch_bounds__( SETUP_BLOCK )
             A[a] = 0.0;
         for ( int j = 0; j < len; ++j )
         {
-            int64_t const sj = idx[b + j];
-            double const x = __dsub_rn( src( sj, 0 ), tx ), y = __dsub_rn( src( sj, 1 ), ty ),
-                         z = __dsub_rn( src( sj, 2 ), tz );
+            double sx, sy, sz;
+            nb.xyz( b + j, sx, sy, sz );
+            double const x = __dsub_rn( sx, tx ), y = __dsub_rn( sy, ty ), z = __dsub_rn( sz, tz );
             double P[M];
             basis_eval<M>( x, y, z, P );
             double const dist =
@@ -350,9 +351,9 @@ __global__ void __launch_bounds__( SETUP_BLOCK )
         // computePolynomialCoefficients: c_k = phi_k * (row0 . P_k)
         for ( int j = 0; j < len; ++j )
         {
-            int64_t const sj = idx[b + j];
-            double const x = __dsub_rn( src( sj, 0 ), tx ), y = __dsub_rn( src( sj, 1 ), ty ),
-                         z = __dsub_rn( src( sj, 2 ), tz );
+            double sx, sy, sz;
+            nb.xyz( b + j, sx, sy, sz );
+            double const x = __dsub_rn( sx, tx ), y = __dsub_rn( sy, ty ), z = __dsub_rn( sz, tz );
             double P[M];
             basis_eval<M>( x, y, z, P );
             double const dist =
@@ -710,7 +711,8 @@ void launch_fp64( SetupArgs const &a, cudaStream_t s )
     size_t const smem = ( 2 * M * M + M ) * SETUP_BLOCK * sizeof( double );
     ensure_dynamic_smem( k_setup_fp64<M>, smem );
     unsigned const blocks = (unsigned)( ( a.n_tgt + SETUP_BLOCK - 1 ) / SETUP_BLOCK );
-    k_setup_fp64<M><<<blocks, SETUP_BLOCK, smem, s>>>( a.src, a.tgt, a.offset, a.idx, a.order,
+    Neighbours const nb{a.src, a.idx, a.pos, a.s2};
+    k_setup_fp64<M><<<blocks, SETUP_BLOCK, smem, s>>>( nb, a.tgt, a.offset, a.order,
                                                         a.n_tgt, a.rbf, a.rows_sorted, a.coeff64,
                                                         a.underdetermined, a.rotations, a.status,
                                                         (unsigned)jacobi_cap( M ) );

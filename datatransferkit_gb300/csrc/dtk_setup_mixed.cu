@@ -204,18 +204,29 @@ __device__ __forceinline__ void refine_and_store_df( int len, int rbf, int steps
 }
 
 // Sources as double-floats: hi = fl32(v), lo = fl32(v - hi), (hi, lo) per
-// coordinate, 3 float2 per point in the caller's point order.
-__global__ void k_split_points( PointsView p, float2 *out )
+// coordinate, 3 float2 per point: in the tree's sorted order (s2 set: the
+// neighbours are then addressed by sorted position) or in the caller's.
+__global__ void k_split_points( PointsView p, double2 const *s2, float2 *out )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i >= p.n )
         return;
+    double v[3];
+    if ( s2 )
+    {
+        double2 const a = s2[2 * i], b = s2[2 * i + 1];
+        v[0] = a.x;
+        v[1] = a.y;
+        v[2] = b.x;
+    }
+    else
+        for ( int d = 0; d < 3; ++d )
+            v[d] = p( i, d );
 #pragma unroll
     for ( int d = 0; d < 3; ++d )
     {
-        double const v = p( i, d );
-        float const hi = __double2float_rn( v );
-        out[3 * i + d] = make_float2( hi, __double2float_rn( v - (double)hi ) );
+        float const hi = __double2float_rn( v[d] );
+        out[3 * i + d] = make_float2( hi, __double2float_rn( v[d] - (double)hi ) );
     }
 }
 
@@ -232,8 +243,8 @@ constexpr int ROW_PITCH = 33; // staged rows: [axis][neighbour][target lane], 33
 
 template <int M>
 __global__ void __launch_bounds__( SMX, 16 )
-    k_setup_mixed( PointsView src, float2 const *__restrict__ split, PointsView tgt, int32_t const *offset,
-                   int32_t const *idx, uint32_t const *order, int64_t n_tgt, int rbf, bool rows_sorted,
+    k_setup_mixed( Neighbours nb, float2 const *__restrict__ split, PointsView tgt, int32_t const *offset,
+                   uint32_t const *order, int64_t n_tgt, int rbf, bool rows_sorted,
                    float *coeff, int32_t *list, unsigned *count, unsigned *status )
 {
     constexpr int NU = M * ( M + 1 ) / 2;
@@ -261,16 +272,8 @@ __global__ void __launch_bounds__( SMX, 16 )
     // sorted rows: the farthest neighbour (the last) sets the support radius;
     // its FP64 coordinates are fetched now, to arrive during the staging
     double fx = 0.0, fy = 0.0, fz = 0.0;
-    if ( rows_sorted && len > 0 )
-    {
-        uint32_t const sj = (uint32_t)idx[b + len - 1];
-        if ( sj < (uint64_t)src.n )
-        {
-            fx = src( sj, 0 );
-            fy = src( sj, 1 );
-            fz = src( sj, 2 );
-        }
-    }
+    if ( rows_sorted && len > 0 && (uint32_t)nb.ref( b + len - 1 ) < (uint64_t)nb.src.n )
+        nb.xyz( b + len - 1, fx, fy, fz );
     {
         // the target as double-floats; (sh - th) is exact for nearby points
         // (Sterbenz)
@@ -297,8 +300,8 @@ __global__ void __launch_bounds__( SMX, 16 )
             bool bad = false;
             if ( lane < lt )
             {
-                uint32_t const sj = (uint32_t)idx[bt + lane];
-                if ( sj >= (uint64_t)src.n )
+                uint32_t const sj = (uint32_t)nb.ref( bt + lane );
+                if ( sj >= (uint64_t)nb.src.n )
                     bad = true;
                 else
                 {
@@ -325,8 +328,9 @@ __global__ void __launch_bounds__( SMX, 16 )
         double d2max = rows_sorted && len > 0 ? dist2_rn( fx, fy, fz, tx, ty, tz ) : 0.0;
         for ( int j = 0; !rows_sorted && j < len; ++j )
         {
-            int64_t const sj = idx[b + j];
-            d2max = fmax( d2max, dist2_rn( src( sj, 0 ), src( sj, 1 ), src( sj, 2 ), tx, ty, tz ) );
+            double sx, sy, sz;
+            nb.xyz( b + j, sx, sy, sz );
+            d2max = fmax( d2max, dist2_rn( sx, sy, sz, tx, ty, tz ) );
         }
         double distance = 10. * DBL_EPSILON;
         double const dmax = __dsqrt_rn( d2max );
@@ -690,10 +694,12 @@ void launch_mixed( SetupArgs const &a, cudaStream_t s )
     DeviceBuffer<unsigned> count( 1, s );
     DTK_CUDA_OR_THROW( cudaMemsetAsync( count.get(), 0, sizeof( unsigned ), s ) );
     DeviceBuffer<float2> split( 3 * a.src.n, s );
-    k_split_points<<<(unsigned)( ( a.src.n + 255 ) / 256 ), 256, 0, s>>>( a.src, split.get() );
+    k_split_points<<<(unsigned)( ( a.src.n + 255 ) / 256 ), 256, 0, s>>>( a.src, a.pos ? a.s2 : nullptr,
+                                                                          split.get() );
     check_launch( "k_split_points" );
+    Neighbours const nb{a.src, a.idx, a.pos, a.s2};
     k_setup_mixed<M><<<(unsigned)( ( a.n_tgt + SMX - 1 ) / SMX ), SMX, 0, s>>>(
-        a.src, split.get(), a.tgt, a.offset, a.idx, a.order, a.n_tgt, a.rbf, a.rows_sorted, a.coeff32,
+        nb, split.get(), a.tgt, a.offset, a.order, a.n_tgt, a.rbf, a.rows_sorted, a.coeff32,
         list.get(), count.get(), a.status );
     check_launch( "k_setup_mixed" );
     // the listed targets (count known only on the device): persistent blocks

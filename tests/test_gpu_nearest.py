@@ -5,7 +5,9 @@ cases on one rank, and the k = 1 search against the oracle), and rank-2
 Nearest indices are bit-exact against the oracle's k = 1 search (ties to the
 smaller source index).  Values: the reference's 1e-14 relative checks.
 Rank-2 MLS applies: each component within 1e-14 of sum_j |c_j v_j| of the
-rank-1 apply of that column (two summation orders of one row)."""
+rank-1 apply of that column (two summation orders of one row) in the FP64
+form; within 2^-40 in the mixed form, whose rank-1 apply sums in double-float
+arithmetic on the FP32 pipe (a 2^-48 unit per term, up to 32 terms)."""
 import numpy as np
 import pytest
 import torch
@@ -106,7 +108,8 @@ def test_rank2_fields_mls(precision, n_comp):
     for v in (dev(vals), dev(vals.T.copy()).t()):
         out = torch.empty((len(tgt), n_comp), dtype=torch.float64, device="cuda")
         op.apply(v, out)
-        assert np.all(np.abs(out.cpu().numpy() - ref) <= 1e-14 * mag + 1e-300)
+        tol = 1e-14 if precision == "fp64" else 2.0 ** -40
+        assert np.all(np.abs(out.cpu().numpy() - ref) <= tol * mag + 1e-300)
 
 
 def test_preconditions():
