@@ -173,7 +173,10 @@ bool is_pow2( int v ) { return v > 0 && ( v & ( v - 1 ) ) == 0; }
 // fl32(v - hi)) and sums c_j (hi_j + lo_j) in double-float arithmetic on the
 // FP32 pipe (TwoProd / TwoSum, the compensated scheme of the mixed setup):
 // the FP32 coefficients are the only rounding left, as with an FP64 sum.
-// The FP64 form permutes the doubles and sums with FP64 FMAs.
+// The FP64 form permutes the doubles and sums with FP64 FMAs.  Rows go in
+// the targets' Morton order when the operator has it, so that consecutive
+// rows share most of their neighbours' values in L1 (0.70 -> 0.59 ms for 8M
+// rows of 32; 16 entries a lane instead of 8 was 1.26 ms, 4 no different).
 // ---------------------------------------------------------------------------
 namespace
 {
@@ -224,11 +227,12 @@ __device__ __forceinline__ void df_axpy( float c, float2 v, float &s, float &cs 
 template <int L, int EPL, bool F32>
 __global__ void __launch_bounds__( 256 )
     k_apply_pos( int64_t n_tgt, int32_t const *__restrict__ pos, void const *__restrict__ coeff,
-                 void const *__restrict__ sorted, double *__restrict__ target )
+                 void const *__restrict__ sorted, double *__restrict__ target, uint32_t const *__restrict__ order )
 {
     constexpr int R = EPL * L;
     int64_t const gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    int64_t const row = gt / L;
+    int64_t const row0 = gt / L;
+    int64_t const row = ( order && row0 < n_tgt ) ? (int64_t)__ldg( order + row0 ) : row0;
     int const sub = (int)( gt % L );
     if constexpr ( F32 )
     {
@@ -287,16 +291,16 @@ __global__ void __launch_bounds__( 256 )
 
 template <int EPL, bool F32>
 void launch_pos_epl( int L, unsigned blocks, int64_t n_tgt, int32_t const *pos, void const *coeff,
-                     void const *sorted, double *target, cudaStream_t s )
+                     void const *sorted, double *target, cudaStream_t s, uint32_t const *order )
 {
     switch ( L )
     {
-    case 1: k_apply_pos<1, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, pos, coeff, sorted, target ); break;
-    case 2: k_apply_pos<2, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, pos, coeff, sorted, target ); break;
-    case 4: k_apply_pos<4, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, pos, coeff, sorted, target ); break;
-    case 8: k_apply_pos<8, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, pos, coeff, sorted, target ); break;
-    case 16: k_apply_pos<16, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, pos, coeff, sorted, target ); break;
-    default: k_apply_pos<32, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, pos, coeff, sorted, target ); break;
+    case 1: k_apply_pos<1, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, pos, coeff, sorted, target, order ); break;
+    case 2: k_apply_pos<2, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, pos, coeff, sorted, target, order ); break;
+    case 4: k_apply_pos<4, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, pos, coeff, sorted, target, order ); break;
+    case 8: k_apply_pos<8, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, pos, coeff, sorted, target, order ); break;
+    case 16: k_apply_pos<16, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, pos, coeff, sorted, target, order ); break;
+    default: k_apply_pos<32, EPL, F32><<<blocks, 256, 0, s>>>( n_tgt, pos, coeff, sorted, target, order ); break;
     }
 }
 
@@ -325,7 +329,7 @@ SortedValues permute_values( int64_t n_src, uint32_t const *perm, double const *
 }
 
 void apply_pos( int64_t n_rows, int uniform_row, int32_t const *pos, double const *coeff64, float const *coeff32,
-                SortedValues const &v, double *target, cudaStream_t s )
+                SortedValues const &v, double *target, cudaStream_t s, uint32_t const *order )
 {
     if ( n_rows == 0 )
         return;
@@ -336,27 +340,27 @@ void apply_pos( int64_t n_rows, int uniform_row, int32_t const *pos, double cons
         int const L = R / epl;
         unsigned const blocks = (unsigned)( ( n_rows * L + 255 ) / 256 );
         if ( epl == 8 )
-            launch_pos_epl<8, true>( L, blocks, n_rows, pos, coeff32, v.v32.get(), target, s );
+            launch_pos_epl<8, true>( L, blocks, n_rows, pos, coeff32, v.v32.get(), target, s, order );
         else
-            launch_pos_epl<4, true>( L, blocks, n_rows, pos, coeff32, v.v32.get(), target, s );
+            launch_pos_epl<4, true>( L, blocks, n_rows, pos, coeff32, v.v32.get(), target, s, order );
     }
     else
     {
         int const L = R / 4;
         unsigned const blocks = (unsigned)( ( n_rows * L + 255 ) / 256 );
-        launch_pos_epl<4, false>( L, blocks, n_rows, pos, coeff64, v.v64.get(), target, s );
+        launch_pos_epl<4, false>( L, blocks, n_rows, pos, coeff64, v.v64.get(), target, s, order );
     }
     check_launch( "k_apply_pos" );
 }
 
 void apply_sorted( int64_t n_tgt, int uniform_row, int32_t const *pos, double const *coeff64,
                    float const *coeff32, int64_t n_src, uint32_t const *perm, double const *values,
-                   double *target, cudaStream_t s )
+                   double *target, cudaStream_t s, uint32_t const *order )
 {
     if ( n_tgt == 0 )
         return;
     SortedValues const v = permute_values( n_src, perm, values, coeff32 != nullptr, s );
-    apply_pos( n_tgt, uniform_row, pos, coeff64, coeff32, v, target, s );
+    apply_pos( n_tgt, uniform_row, pos, coeff64, coeff32, v, target, s, order );
 }
 
 // uniform_row > 0: every row has that length (offset[i] = i * uniform_row);

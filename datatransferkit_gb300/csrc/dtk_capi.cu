@@ -424,7 +424,7 @@ dtk_status dtk_mls_apply( dtk_mls_handle h, const double *source_values, int64_t
         if ( apply_sorted_supported( h->uniform_row ) && ( by_pos || h->coeff32.get() ) )
             apply_sorted( h->n_tgt, h->uniform_row, by_pos ? h->pos.get() : h->idx.get(), h->coeff64.get(),
                           h->coeff32.get(), h->n_src, by_pos ? h->perm.get() : nullptr, source_values,
-                          target_values, s );
+                          target_values, s, by_pos ? h->order.get() : nullptr );
         else
             apply_csr( h->n_tgt, h->offset.get(), h->idx.get(), h->coeff64.get(), h->coeff32.get(),
                        h->uniform_row, h->mean_row, source_values, target_values, s );

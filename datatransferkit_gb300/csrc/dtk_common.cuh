@@ -586,12 +586,14 @@ struct SortedValues
 // (perm null: the values in their own order, for entries that hold indices)
 SortedValues permute_values( int64_t n_src, uint32_t const *perm, double const *values, bool f32,
                              cudaStream_t s );
-// n_rows uniform rows starting at pos / coeff (a slice of the operator's)
+// n_rows uniform rows starting at pos / coeff (a slice of the operator's),
+// taken in the given order (the targets' Morton order: consecutive rows then
+// share most of their neighbours' values in L1) or in row order
 void apply_pos( int64_t n_rows, int uniform_row, int32_t const *pos, double const *coeff64, float const *coeff32,
-                SortedValues const &v, double *target, cudaStream_t s );
+                SortedValues const &v, double *target, cudaStream_t s, uint32_t const *order = nullptr );
 void apply_sorted( int64_t n_tgt, int uniform_row, int32_t const *pos, double const *coeff64,
                    float const *coeff32, int64_t n_src, uint32_t const *perm, double const *values,
-                   double *target, cudaStream_t s );
+                   double *target, cudaStream_t s, uint32_t const *order = nullptr );
 
 // Adjoint kernels.
 struct AdjointArgs
