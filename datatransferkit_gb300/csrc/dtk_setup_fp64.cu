@@ -41,7 +41,8 @@ namespace dtk
 namespace
 {
 
-constexpr int SETUP_BLOCK = 32;
+constexpr int SETUP_BLOCK = 32;   // threads per block of the split Jacobi (E, U, V(:, 0) in shared memory)
+constexpr int FP64_THREADS = 256; // threads per block of the fused FP64 setup (E, V(:, 0) in shared memory)
 constexpr unsigned FULL = 0xffffffffu;
 
 // cos and sin of phi = atan2(y, x) / 2, phi in (-pi/2, pi/2], from the
@@ -119,11 +120,14 @@ __device__ __forceinline__ long long abs_bits( double x )
 template <int M>
 struct Smem
 {
+    // E and V(:, 0) in shared memory, interleaved by thread (stride es, the
+    // thread's column t); U in shared or global memory (stride us, column ut)
     double *E, *U, *V0;
-    int t;
-    __device__ double &e( int i, int j ) const { return E[( i * M + j ) * SETUP_BLOCK + t]; }
-    __device__ double &u( int i, int j ) const { return U[( i * M + j ) * SETUP_BLOCK + t]; }
-    __device__ double &v( int i ) const { return V0[i * SETUP_BLOCK + t]; }
+    int t, es;
+    int64_t ut, us;
+    __device__ double &e( int i, int j ) const { return E[( i * M + j ) * es + t]; }
+    __device__ double &u( int i, int j ) const { return U[( i * M + j ) * us + ut]; }
+    __device__ double &v( int i ) const { return V0[i * es + t]; }
 };
 
 // Runs DTK's Jacobi on the thread's E; on return row0 holds row 0 of the
@@ -199,6 +203,16 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
             p = q;
             q = tmp;
         }
+        // U's columns p and q are read before the 2x2 SVD and the E updates,
+        // so that their loads (L2, when U is in global memory) are in flight
+        // during the FP64 work
+        double up[M], uq[M];
+#pragma unroll
+        for ( int j = 0; j < M; ++j )
+        {
+            up[j] = s.u( j, p );
+            uq[j] = s.u( j, q );
+        }
         double cl, sl, cr, sr;
         svd_2x2( s.e( p, p ), s.e( p, q ), s.e( q, p ), s.e( q, q ), cl, sl, cr, sr );
         // givens_left(E, cl, sl, p, q)
@@ -221,7 +235,7 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
 #pragma unroll
         for ( int j = 0; j < M; ++j )
         {
-            double const a = s.u( j, p ), b = s.u( j, q );
+            double const a = up[j], b = uq[j];
             s.u( j, p ) = cl * a - sl * b;
             s.u( j, q ) = sl * a + cl * b;
         }
@@ -260,17 +274,28 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
     return dropped;
 }
 
+// Persistent blocks of FP64_THREADS threads: a thread takes targets g,
+// g + T, g + 2T, ... (T threads in the grid, g in the targets' Morton order).
+// U lives in u_work, a global work area of M^2 doubles per resident thread
+// (31 MB at M = 10 on 152 SMs, held in L2), so that E and V(:, 0), 880 B a
+// thread in shared memory, let an SM hold 8 warps instead of 4: the FP64
+// pipe then has a second warp per sub-partition to interleave with the
+// argmax scans and the 2x2 SVD's dependency chain.
 template <int M>
-__global__ void __launch_bounds__( SETUP_BLOCK )
+__global__ void __launch_bounds__( FP64_THREADS, 1 )
     k_setup_fp64( Neighbours nb, PointsView tgt, int32_t const *offset,
                   uint32_t const *order, int64_t n_tgt, int rbf, bool rows_sorted,
                   double *coeff, unsigned long long *under_count,
-                  unsigned long long *rot_count, unsigned *status, unsigned jcap )
+                  unsigned long long *rot_count, unsigned *status, unsigned jcap, double *u_work )
 {
     extern __shared__ double smem[];
-    Smem<M> s{smem, smem + M * M * SETUP_BLOCK, smem + 2 * M * M * SETUP_BLOCK, (int)threadIdx.x};
-    int64_t const g = blockIdx.x * (int64_t)SETUP_BLOCK + threadIdx.x;
+    int64_t const T = (int64_t)gridDim.x * FP64_THREADS;
+    int64_t const tid = blockIdx.x * (int64_t)FP64_THREADS + threadIdx.x;
+    Smem<M> s{smem, u_work, smem + M * M * FP64_THREADS, (int)threadIdx.x, FP64_THREADS, tid, T};
     unsigned iters = 0;
+    int dropped_all = 0;
+    for ( int64_t g = tid; g - threadIdx.x < n_tgt; g += T ) // block-uniform trip count
+    {
     int dropped = 0;
     if ( g < n_tgt )
     {
@@ -366,14 +391,16 @@ __global__ void __launch_bounds__( SETUP_BLOCK )
             coeff[b + j] = acc * phi;
         }
     }
+    dropped_all += dropped;
+    }
     // warp totals -> one atomic each
-    unsigned long long it64 = iters, dr64 = dropped;
+    unsigned long long it64 = iters, dr64 = dropped_all;
     for ( int o = 16; o; o >>= 1 )
     {
         it64 += __shfl_xor_sync( FULL, it64, o );
         dr64 += __shfl_xor_sync( FULL, dr64, o );
     }
-    if ( threadIdx.x == 0 )
+    if ( ( threadIdx.x & 31 ) == 0 )
     {
         if ( it64 )
             atomicAdd( rot_count, it64 );
@@ -584,7 +611,8 @@ __global__ void __launch_bounds__( SETUP_BLOCK )
     constexpr int NU = M * ( M + 1 ) / 2;
     constexpr int STRIDE = NU + 1 + M;
     extern __shared__ double smem[];
-    Smem<M> s{smem, smem + M * M * SETUP_BLOCK, smem + 2 * M * M * SETUP_BLOCK, (int)threadIdx.x};
+    Smem<M> s{smem, smem + M * M * SETUP_BLOCK, smem + 2 * M * M * SETUP_BLOCK, (int)threadIdx.x,
+              SETUP_BLOCK, (int64_t)threadIdx.x, SETUP_BLOCK};
     int64_t const g = blockIdx.x * (int64_t)SETUP_BLOCK + threadIdx.x;
     unsigned iters = 0;
     int dropped = 0;
@@ -708,14 +736,16 @@ void launch_split_basis( SetupArgs const &a, int32_t const *targets, int64_t n, 
 template <int M>
 void launch_fp64( SetupArgs const &a, cudaStream_t s )
 {
-    size_t const smem = ( 2 * M * M + M ) * SETUP_BLOCK * sizeof( double );
+    size_t const smem = ( M * M + M ) * FP64_THREADS * sizeof( double );
     ensure_dynamic_smem( k_setup_fp64<M>, smem );
-    unsigned const blocks = (unsigned)( ( a.n_tgt + SETUP_BLOCK - 1 ) / SETUP_BLOCK );
+    int64_t const want = ( a.n_tgt + FP64_THREADS - 1 ) / FP64_THREADS;
+    unsigned const blocks = (unsigned)std::max<int64_t>( 1, std::min<int64_t>( want, num_sms() ) );
+    DeviceBuffer<double> u_work( (size_t)M * M * FP64_THREADS * blocks, s );
     Neighbours const nb{a.src, a.idx, a.pos, a.s2};
-    k_setup_fp64<M><<<blocks, SETUP_BLOCK, smem, s>>>( nb, a.tgt, a.offset, a.order,
-                                                        a.n_tgt, a.rbf, a.rows_sorted, a.coeff64,
-                                                        a.underdetermined, a.rotations, a.status,
-                                                        (unsigned)jacobi_cap( M ) );
+    k_setup_fp64<M><<<blocks, FP64_THREADS, smem, s>>>( nb, a.tgt, a.offset, a.order,
+                                                         a.n_tgt, a.rbf, a.rows_sorted, a.coeff64,
+                                                         a.underdetermined, a.rotations, a.status,
+                                                         (unsigned)jacobi_cap( M ), u_work.get() );
     check_launch( "k_setup_fp64" );
 }
 
