@@ -26,8 +26,13 @@
 // instruction per 64 cycles per SM sub-partition, so every FP64 instruction
 // must carry 32 useful lanes; the 2x2 SVD is scalar work.  Iteration counts
 // are tight (about 114 +- 13 for the quadratic basis), so divergence costs
-// little.  E (m x m), U (m x m) and column 0 of V live in shared memory,
-// interleaved by thread so that dynamic (p, q) accesses are conflict-free.
+// little.  E (m x m) and column 0 of V live in shared memory, interleaved
+// by thread so that dynamic (p, q) accesses are conflict-free; U (m x m) in
+// a global work area per resident thread (L2-resident), interleaved the same
+// way, with its two columns read ahead of each rotation's FP64 work.  That
+// leaves 880 B of shared memory a thread at m = 10: 8 warps an SM, two per
+// FP64 pipe, against 4 with U in shared memory (8M targets: 729 -> 493 ms).
+// The kernels are persistent: a thread takes targets g, g + T, ...
 // The argmax runs on the integer pipe over the IEEE bits of |E_ij|; the stop
 // test too, from exponent bounds, except within a factor of four of the
 // threshold where it sums the squares in FP64; the 2x2 rotation angles use
@@ -41,8 +46,7 @@ namespace dtk
 namespace
 {
 
-constexpr int SETUP_BLOCK = 32;   // threads per block of the split Jacobi (E, U, V(:, 0) in shared memory)
-constexpr int FP64_THREADS = 256; // threads per block of the fused FP64 setup (E, V(:, 0) in shared memory)
+constexpr int FP64_THREADS = 256; // threads per block of the Jacobi kernels (E, V(:, 0) in shared memory)
 constexpr unsigned FULL = 0xffffffffu;
 
 // cos and sin of phi = atan2(y, x) / 2, phi in (-pi/2, pi/2], from the
@@ -129,6 +133,26 @@ struct Smem
     __device__ double &u( int i, int j ) const { return U[( i * M + j ) * us + ut]; }
     __device__ double &v( int i ) const { return V0[i * es + t]; }
 };
+
+// Grid of the persistent Jacobi kernels: blocks of FP64_THREADS (8 warps an
+// SM, one block each) when the targets fill the GPU; otherwise blocks of one
+// warp, one target a thread, spread over as many SMs as there are warps.
+struct JacobiGrid
+{
+    unsigned blocks;
+    int threads;
+    size_t smem;
+};
+template <int M>
+JacobiGrid jacobi_grid( int64_t n )
+{
+    int64_t const sms = num_sms();
+    int const threads = n >= sms * FP64_THREADS ? FP64_THREADS : 32;
+    int64_t const want = ( n + threads - 1 ) / threads;
+    int64_t const cap = threads == FP64_THREADS ? sms : want;
+    return JacobiGrid{(unsigned)std::max<int64_t>( 1, std::min( want, cap ) ), threads,
+                      ( M * M + M ) * threads * sizeof( double )};
+}
 
 // Runs DTK's Jacobi on the thread's E; on return row0 holds row 0 of the
 // pseudo-inverse.  Returns 1 if a singular value was truncated.
@@ -289,9 +313,10 @@ __global__ void __launch_bounds__( FP64_THREADS, 1 )
                   unsigned long long *rot_count, unsigned *status, unsigned jcap, double *u_work )
 {
     extern __shared__ double smem[];
-    int64_t const T = (int64_t)gridDim.x * FP64_THREADS;
-    int64_t const tid = blockIdx.x * (int64_t)FP64_THREADS + threadIdx.x;
-    Smem<M> s{smem, u_work, smem + M * M * FP64_THREADS, (int)threadIdx.x, FP64_THREADS, tid, T};
+    int const nt = blockDim.x; // FP64_THREADS, or 32 when the targets are few
+    int64_t const T = (int64_t)gridDim.x * nt;
+    int64_t const tid = blockIdx.x * (int64_t)nt + threadIdx.x;
+    Smem<M> s{smem, u_work, smem + M * M * nt, (int)threadIdx.x, nt, tid, T};
     unsigned iters = 0;
     int dropped_all = 0;
     for ( int64_t g = tid; g - threadIdx.x < n_tgt; g += T ) // block-uniform trip count
@@ -604,18 +629,20 @@ __global__ void __launch_bounds__( 128 )
 }
 
 template <int M>
-__global__ void __launch_bounds__( SETUP_BLOCK )
+__global__ void __launch_bounds__( FP64_THREADS, 1 )
     k_split_jacobi( int64_t n, double *work, unsigned long long *under_count,
-                    unsigned long long *rot_count, unsigned *status, unsigned jcap )
+                    unsigned long long *rot_count, unsigned *status, unsigned jcap, double *u_work )
 {
     constexpr int NU = M * ( M + 1 ) / 2;
     constexpr int STRIDE = NU + 1 + M;
     extern __shared__ double smem[];
-    Smem<M> s{smem, smem + M * M * SETUP_BLOCK, smem + 2 * M * M * SETUP_BLOCK, (int)threadIdx.x,
-              SETUP_BLOCK, (int64_t)threadIdx.x, SETUP_BLOCK};
-    int64_t const g = blockIdx.x * (int64_t)SETUP_BLOCK + threadIdx.x;
+    int const nt = blockDim.x;
+    int64_t const T = (int64_t)gridDim.x * nt;
+    int64_t const tid = blockIdx.x * (int64_t)nt + threadIdx.x;
+    Smem<M> s{smem, u_work, smem + M * M * nt, (int)threadIdx.x, nt, tid, T};
     unsigned iters = 0;
     int dropped = 0;
+    for ( int64_t g = tid; g - threadIdx.x < n; g += T ) // block-uniform trip count
     if ( g < n )
     {
         double *rec = work + g * STRIDE;
@@ -633,7 +660,7 @@ __global__ void __launch_bounds__( SETUP_BLOCK )
             s.v( a ) = a == 0 ? 1.0 : 0.0;
         }
         double row0[M];
-        dropped = jacobi_row0<M>( s, row0, iters, jcap, status );
+        dropped += jacobi_row0<M>( s, row0, iters, jcap, status );
         for ( int a = 0; a < M; ++a )
             rec[NU + 1 + a] = row0[a];
     }
@@ -643,7 +670,7 @@ __global__ void __launch_bounds__( SETUP_BLOCK )
         it64 += __shfl_xor_sync( FULL, it64, o );
         dr64 += __shfl_xor_sync( FULL, dr64, o );
     }
-    if ( threadIdx.x == 0 )
+    if ( ( threadIdx.x & 31 ) == 0 )
     {
         if ( it64 )
             atomicAdd( rot_count, it64 );
@@ -706,10 +733,11 @@ void launch_split( SetupArgs const &a, int32_t const *targets, int64_t n, cudaSt
     k_split_moments<M, G><<<gblocks, 128, 0, s>>>( a.src, a.tgt, a.offset, a.idx, targets, n, a.rbf,
                                                     work.get(), a.status );
     check_launch( "k_split_moments" );
-    size_t const smem = ( 2 * M * M + M ) * SETUP_BLOCK * sizeof( double );
-    ensure_dynamic_smem( k_split_jacobi<M>, smem );
-    k_split_jacobi<M><<<(unsigned)( ( n + SETUP_BLOCK - 1 ) / SETUP_BLOCK ), SETUP_BLOCK, smem, s>>>(
-        n, work.get(), a.underdetermined, a.rotations, a.status, (unsigned)jacobi_cap( M ) );
+    JacobiGrid const jg = jacobi_grid<M>( n );
+    ensure_dynamic_smem( k_split_jacobi<M>, jg.smem );
+    DeviceBuffer<double> u_work( (size_t)M * M * jg.threads * jg.blocks, s );
+    k_split_jacobi<M><<<jg.blocks, jg.threads, jg.smem, s>>>( n, work.get(), a.underdetermined, a.rotations,
+                                                             a.status, (unsigned)jacobi_cap( M ), u_work.get() );
     check_launch( "k_split_jacobi" );
     k_split_coeffs<M, G><<<gblocks, 128, 0, s>>>( a.src, a.tgt, a.offset, a.idx, targets, n, a.rbf,
                                                    work.get(), a.coeff64, a.coeff32 );
@@ -736,13 +764,11 @@ void launch_split_basis( SetupArgs const &a, int32_t const *targets, int64_t n, 
 template <int M>
 void launch_fp64( SetupArgs const &a, cudaStream_t s )
 {
-    size_t const smem = ( M * M + M ) * FP64_THREADS * sizeof( double );
-    ensure_dynamic_smem( k_setup_fp64<M>, smem );
-    int64_t const want = ( a.n_tgt + FP64_THREADS - 1 ) / FP64_THREADS;
-    unsigned const blocks = (unsigned)std::max<int64_t>( 1, std::min<int64_t>( want, num_sms() ) );
-    DeviceBuffer<double> u_work( (size_t)M * M * FP64_THREADS * blocks, s );
+    JacobiGrid const jg = jacobi_grid<M>( a.n_tgt );
+    ensure_dynamic_smem( k_setup_fp64<M>, jg.smem );
+    DeviceBuffer<double> u_work( (size_t)M * M * jg.threads * jg.blocks, s );
     Neighbours const nb{a.src, a.idx, a.pos, a.s2};
-    k_setup_fp64<M><<<blocks, FP64_THREADS, smem, s>>>( nb, a.tgt, a.offset, a.order,
+    k_setup_fp64<M><<<jg.blocks, jg.threads, jg.smem, s>>>( nb, a.tgt, a.offset, a.order,
                                                          a.n_tgt, a.rbf, a.rows_sorted, a.coeff64,
                                                          a.underdetermined, a.rotations, a.status,
                                                          (unsigned)jacobi_cap( M ), u_work.get() );
