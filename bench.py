@@ -666,9 +666,10 @@ def run_ours(args, rank, world, local_rank):
     traffic_pt = read_profile_traffic("setup_mixed_traffic.txt", "bytes_per_target")
     traffic_q = read_profile_traffic("knn_traffic.txt", "bytes_per_query")
     instr_q = read_profile_traffic("knn_traffic.txt", "warp_instructions_per_query")
-    # kNN query launch, algorithmic bytes: per query the FP64 point, k indices
-    # out and the offset; per source its FP64 + FP32 sorted copies and its index
-    q_bytes = n_tgt * (24 + 4 * k + 4) + len(src) * (24 + 12 + 4)
+    # kNN query launch, algorithmic bytes: per query its 64-byte record, k
+    # indices and k sorted positions out and the offset; per source its FP64 +
+    # FP32 sorted copies and its index
+    q_bytes = n_tgt * (64 + 8 * k + 4) + len(src) * (24 + 12 + 4)
     q_gbs = q_bytes / (query_ms / 1e3) / 1e9
     # the issue ruler: warp instructions (ncu count per query) over the SMs'
     # issue rate, one warp instruction per cycle per scheduler at the sampled clock
@@ -720,7 +721,7 @@ def run_ours(args, rank, world, local_rank):
     detail.update({
         "roofline_detail": {
             "peak_source": hbm_src, "algorithmic_bytes": q_bytes,
-            "note": ("the dominant kernel of a mixed step; algorithmic bytes = N_t (24 + 4k + 4) "
+            "note": ("the dominant kernel of a mixed step; algorithmic bytes = N_t (64 + 8k + 4) "
                      "+ N_s (24 + 12 + 4); traffic = the ncu DRAM bytes per query of profiles/knn_traffic.txt "
                      "x N_t; issue_frac = ncu warp instructions per query x N_t / launch time / "
                      "(SMs x 4 schedulers x sampled SM clock)")},
@@ -731,7 +732,7 @@ def run_ours(args, rank, world, local_rank):
                       "peak": peak, "unit": "T FP32 ops/s (FMA = 1)", "frac": achieved / peak, "ms": setup_ms,
                       "peak_source": "measured cuBLAS SGEMM 8192^3 (no TF32) in this run, FMA/s",
                       "traffic": (traffic_pt * n_tgt) if traffic_pt else None},
-            "apply": {"bound": "hbm", "kernel": "k_apply_vec", "achieved": a_gbs, "peak": hbm,
+            "apply": {"bound": "hbm", "kernel": "k_apply_pos (+ k_permute_values)", "achieved": a_gbs, "peak": hbm,
                       "unit": "GB/s", "frac": a_gbs / hbm, "ms": apply_ms},
             "time_weighted_frac": combined},
         "fp64_form_detail": {"setup_ms": setup64_ms,
