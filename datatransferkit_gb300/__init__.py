@@ -9,7 +9,9 @@ from .operators import (FP64, MIXED, Buhmann, Constant, Linear, MovingLeastSquar
                         MultivariatePolynomialBasis, PointCloudOperator, Quadratic, Wendland, Wu,
                         kernel_launch_count, knn_search, release_cached_memory, svd_pinv)
 from ._capi import DTKError, InvalidArgument, Unsupported
+from .distributed import DistributedMovingLeastSquaresOperator, DistributedNearestNeighborOperator, fetch
 
 __all__ = ["MovingLeastSquaresOperator", "MovingLeastSquaresBatch", "NearestNeighborOperator", "PointCloudOperator", "MultivariatePolynomialBasis",
            "Constant", "Linear", "Quadratic", "Wendland", "Wu", "Buhmann", "FP64", "MIXED",
-           "knn_search", "svd_pinv", "kernel_launch_count", "release_cached_memory", "DTKError", "InvalidArgument", "Unsupported"]
+           "knn_search", "svd_pinv", "DistributedMovingLeastSquaresOperator",
+           "DistributedNearestNeighborOperator", "fetch", "kernel_launch_count", "release_cached_memory", "DTKError", "InvalidArgument", "Unsupported"]

@@ -27,7 +27,7 @@ EXPORTED = [
     "dtk_kernel_launch_count", "dtk_svd_pinv_noalloc", "dtk_mls_apply_multi", "dtk_nn_create",
     "dtk_nn_apply", "dtk_nn_apply_multi", "dtk_nn_get_indices", "dtk_nn_destroy",
     "dtk_mls_export_size", "dtk_mls_export", "dtk_mls_import", "dtk_release_cached_memory",
-    "dtk_mls_transfer_host", "dtk_set_loop_caps", "dtk_stream_synchronize",
+    "dtk_mls_transfer_host", "dtk_set_loop_caps", "dtk_stream_synchronize", "dtk_mls_create_from_neighbors",
 ]
 
 
@@ -99,6 +99,8 @@ def _declare(L):
                                                 C.POINTER(C.c_float)]
     L.dtk_set_loop_caps.argtypes = [_i64, _i64]
     L.dtk_stream_synchronize.argtypes = [_vp]
+    L.dtk_mls_create_from_neighbors.argtypes = [C.POINTER(Options), _vp, _i64, _i64, _i64, C.c_int32, _vp, _vp,
+                                                _i64, _vp, C.POINTER(_vp)]
     L.dtk_last_error.restype = C.c_char_p
     L.dtk_last_error.argtypes = []
     L.dtk_status_string.restype = C.c_char_p

@@ -123,6 +123,21 @@ __global__ void k_fill_uniform_offsets( int32_t *offset, int64_t n_tgt, int row 
         offset[i] = (int32_t)( i * row );
 }
 
+__global__ void k_iota32( int32_t *out, int64_t n )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i < n )
+        out[i] = (int32_t)i;
+}
+
+// DEV_BAD_INDEX for an index outside [0, n)
+__global__ void k_check_indices( int32_t const *idx, int64_t nnz, int64_t n, unsigned *status )
+{
+    int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( i < nnz && ( idx[i] < 0 || idx[i] >= n ) )
+        atomicOr( status, DEV_BAD_INDEX );
+}
+
 __global__ void k_narrow_offsets( int64_t const *in, int32_t *out, int64_t n )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -399,6 +414,106 @@ dtk_status dtk_mls_create( const dtk_mls_options *opts, const double *src, int64
         PointsView const sv{src, n_src, src_pt_stride, src_dim_stride};
         PointsView const tv{tgt, n_tgt, tgt_pt_stride, tgt_dim_stride};
         *out = create_impl( g, opts, sv, tv, s, nullptr ).release();
+    } );
+}
+
+dtk_status dtk_mls_create_from_neighbors( const dtk_mls_options *opts, const double *tgt, int64_t n_tgt,
+                                          int64_t tgt_pt_stride, int64_t tgt_dim_stride, int32_t row,
+                                          const double *nb_points, const int32_t *indices, int64_t n_src,
+                                          dtk_stream_t stream_, dtk_mls_handle *out )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( out != nullptr, "output handle pointer is null" );
+        *out = nullptr;
+        Geometry const g = check_options( opts );
+        if ( g.radius_mode )
+            throw Error{DTK_ERR_UNSUPPORTED, "neighbour rows are kNN rows (radius must be 0)"};
+        if ( g.opts.keep_points )
+            throw Error{DTK_ERR_UNSUPPORTED, "a handle from neighbour rows keeps no points"};
+        validate_points( tgt, n_tgt, tgt_pt_stride, tgt_dim_stride, "target points" );
+        DTK_REQUIRE_OR_THROW( row >= 1 && row <= FUSED_MAX_ROW, "row length must be in [1, 32]" );
+        int64_t const nnz = n_tgt * (int64_t)row;
+        DTK_REQUIRE_OR_THROW( n_src >= ( nnz ? 1 : 0 ) && n_src <= INT32_MAX,
+                              "n_src must be in [1, 2^31) (0 only without targets)" );
+        DTK_REQUIRE_OR_THROW( nnz <= INT32_MAX, "n_targets * row exceeds int32 CSR offsets" );
+        DTK_REQUIRE_OR_THROW( nnz == 0 || ( nb_points && indices ), "null neighbour arrays" );
+        require_device_memory( n_tgt ? tgt : nullptr, "target points" );
+        require_device_memory( nnz ? nb_points : nullptr, "neighbour points" );
+        require_device_memory( nnz ? indices : nullptr, "indices" );
+        cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        auto h = std::make_unique<dtk_mls_s>( s );
+        TouchOnExit const touch{&h->life, s};
+        h->opts = *opts;
+        h->n_src = n_src;
+        h->n_tgt = n_tgt;
+        h->m = g.m;
+        h->nnz = nnz;
+        h->uniform_row = row;
+        h->mean_row = row;
+        h->offset.allocate( n_tgt + 1, s );
+        k_fill_uniform_offsets<<<(unsigned)( ( n_tgt + 256 ) / 256 ), 256, 0, s>>>( h->offset.get(), n_tgt, row );
+        check_launch( "k_fill_uniform_offsets" );
+        h->idx.allocate( std::max<int64_t>( 1, nnz ), s );
+        DeviceBuffer<unsigned> status( 1, s );
+        DeviceBuffer<unsigned long long> counters( 3, s );
+        DTK_CUDA_OR_THROW( cudaMemsetAsync( status.get(), 0, sizeof( unsigned ), s ) );
+        DTK_CUDA_OR_THROW( cudaMemsetAsync( counters.get(), 0, 3 * sizeof( unsigned long long ), s ) );
+        if ( nnz )
+        {
+            DTK_CUDA_OR_THROW( cudaMemcpyAsync( h->idx.get(), indices, nnz * sizeof( int32_t ),
+                                                cudaMemcpyDeviceToDevice, s ) );
+            k_check_indices<<<(unsigned)( ( nnz + 255 ) / 256 ), 256, 0, s>>>( h->idx.get(), nnz, n_src,
+                                                                              status.get() );
+            check_launch( "k_check_indices" );
+        }
+        // the setup reads entry e's neighbour at nb_points[e]: an identity
+        // index over the entries in place of the search's rows
+        DeviceBuffer<int32_t> entry( std::max<int64_t>( 1, nnz ), s );
+        k_iota32<<<(unsigned)( ( nnz + 256 ) / 256 ), 256, 0, s>>>( entry.get(), nnz );
+        check_launch( "k_iota32" );
+        SetupArgs a{};
+        a.src = PointsView{nb_points, std::max<int64_t>( 1, nnz ), 3, 1};
+        a.tgt = PointsView{tgt, n_tgt, tgt_pt_stride, tgt_dim_stride};
+        a.offset = h->offset.get();
+        a.idx = entry.get();
+        a.order = nullptr;
+        a.n_tgt = n_tgt;
+        a.rbf = g.opts.rbf;
+        a.basis = g.opts.basis;
+        a.rows_sorted = false; // the radius is the row's farthest, in any order
+        a.underdetermined = counters.get();
+        a.rotations = counters.get() + 1;
+        a.rotations32 = counters.get() + 2;
+        a.status = status.get();
+        if ( g.opts.precision == DTK_FP64 )
+        {
+            h->coeff64.allocate( std::max<int64_t>( 1, nnz ), s );
+            a.coeff64 = h->coeff64.get();
+            if ( nnz )
+                setup_fp64( a, s );
+        }
+        else
+        {
+            h->coeff32.allocate( std::max<int64_t>( 1, nnz ), s );
+            a.coeff32 = h->coeff32.get();
+            if ( nnz )
+                setup_mixed( a, s );
+        }
+        unsigned st = 0;
+        unsigned long long cnt[3] = {0, 0, 0};
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, status.get(), sizeof( unsigned ), cudaMemcpyDeviceToHost, s ) );
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( cnt, counters.get(), sizeof( cnt ), cudaMemcpyDeviceToHost, s ) );
+        DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+        if ( st & DEV_BAD_INDEX )
+            throw Error{DTK_ERR_INVALID_ARG, "DTK_REQUIRE: indices must lie in [0, n_src)"};
+        if ( st & DEV_TIMEOUT )
+            throw Error{DTK_ERR_TIMEOUT, "a bounded device loop (Jacobi rotations) hit its cap"};
+        if ( st )
+            throw Error{DTK_ERR_INTERNAL, "the setup reported an internal error"};
+        h->underdetermined = (int64_t)cnt[0];
+        h->rotations = (int64_t)cnt[1];
+        h->rotations32 = (int64_t)cnt[2];
+        *out = h.release();
     } );
 }
 

@@ -115,6 +115,13 @@ def _check_points(p: torch.Tensor, what: str) -> torch.Tensor:
     return p
 
 
+def _multi_rank(comm) -> bool:
+    """True for a torch.distributed process group of more than one rank."""
+    import torch.distributed as dist
+    return (dist.is_available() and isinstance(comm, dist.ProcessGroup) and dist.is_initialized()
+            and dist.get_world_size(comm) > 1)
+
+
 def _comm_size(comm) -> int:
     if comm is None:
         return 1
@@ -146,6 +153,17 @@ class MovingLeastSquaresOperator(PointCloudOperator):
     ``precision`` ("fp64" = the reference algorithm, "mixed") and
     ``keep_points`` (keep copies of the points for the coordinate adjoint).
     """
+
+    def __new__(cls, comm=None, *args, **kwargs):
+        # a torch.distributed group of several ranks: the distributed operator
+        # (search and value fetch across the ranks)
+        if cls is MovingLeastSquaresOperator and _multi_rank(comm):
+            from .distributed import DistributedMovingLeastSquaresOperator
+            for key in ("radius", "keep_points"):
+                if kwargs.pop(key, None) not in (None, False):
+                    raise _capi.Unsupported(2, f"{key} is single-rank only")
+            return DistributedMovingLeastSquaresOperator(comm, *args, **kwargs)
+        return super().__new__(cls)
 
     def __init__(self, comm, source_points, target_points, rbf=None, basis=None, *,
                  k: int | None = None, radius: float | None = None, precision="fp64",
@@ -220,6 +238,43 @@ class MovingLeastSquaresOperator(PointCloudOperator):
         op.options, op._h, op._stream = o, h, stream
         op.n_source_points = int(source_points.shape[0])
         op.n_target_points = int(target_points.shape[0])
+        return op
+
+    @classmethod
+    def from_neighbors(cls, target_points, row: int, neighbor_points, indices, n_sources: int,
+                       rbf=None, basis=None, *, precision="fp64", stream=None):
+        """The operator for given kNN rows (the constructor after its search and
+        coordinate fetch, DTK_MovingLeastSquaresOperator_def.hpp:64-118): row i
+        of ``row`` entries has its neighbours' coordinates in
+        ``neighbor_points[i*row:(i+1)*row]`` ((n_tgt*row, 3) float64 CUDA) and
+        the positions of their values in the source-value array ``apply`` takes
+        in ``indices`` (int32 CUDA, in [0, n_sources))."""
+        basis = basis or MultivariatePolynomialBasis(Linear, 3)
+        rbf = rbf or Wendland(0)
+        tgt = _check_points(target_points, "target_points")
+        nb = neighbor_points
+        if (not isinstance(nb, torch.Tensor) or not nb.is_cuda or nb.dtype != torch.float64
+                or nb.dim() != 2 or nb.shape[1] != 3 or not nb.is_contiguous()):
+            raise _capi.InvalidArgument(1, "neighbor_points must be a contiguous (n, 3) float64 CUDA tensor")
+        if (not isinstance(indices, torch.Tensor) or not indices.is_cuda or indices.dtype != torch.int32
+                or indices.dim() != 1 or not indices.is_contiguous()):
+            raise _capi.InvalidArgument(1, "indices must be a contiguous int32 CUDA tensor")
+        if tgt.shape[1] != 3 or basis.dim != 3:
+            raise _capi.InvalidArgument(1, "target_points.extent(1) == 3")
+        if nb.shape[0] != tgt.shape[0] * row or indices.shape[0] != tgt.shape[0] * row:
+            raise _capi.InvalidArgument(1, "neighbour arrays must hold n_targets * row entries")
+        o = Options()
+        lib().dtk_mls_default_options(C.byref(o))
+        o.rbf, o.basis, o.precision = rbf.id, basis.id, _PRECISIONS[precision]
+        h = C.c_void_p()
+        check(lib().dtk_mls_create_from_neighbors(C.byref(o), tgt.data_ptr(), tgt.shape[0], tgt.stride(0),
+                                                  tgt.stride(1), int(row), nb.data_ptr(), indices.data_ptr(),
+                                                  int(n_sources), _stream(stream), C.byref(h)))
+        op = cls.__new__(cls)
+        op.polynomial_basis, op.radial_basis_function = basis, rbf
+        op.options, op._h, op._stream = o, h, stream
+        op.n_source_points = int(n_sources)
+        op.n_target_points = int(tgt.shape[0])
         return op
 
     # -- reference API ------------------------------------------------------
@@ -471,6 +526,12 @@ class NearestNeighborOperator(PointCloudOperator):
     source value (rank-1 or rank-2 fields).
     Mirrors DTK_NearestNeighborOperator_decl.hpp:27-49.
     """
+
+    def __new__(cls, comm=None, *args, **kwargs):
+        if cls is NearestNeighborOperator and _multi_rank(comm):
+            from .distributed import DistributedNearestNeighborOperator
+            return DistributedNearestNeighborOperator(comm, *args, **kwargs)
+        return super().__new__(cls)
 
     def __init__(self, comm, source_points, target_points, *, stream=None):
         src = _check_points(source_points, "source_points")

@@ -108,6 +108,29 @@ dtk_status dtk_mls_create(const dtk_mls_options *opts, const double *src,
                           int64_t tgt_dim_stride, dtk_stream_t stream,
                           dtk_mls_handle *out);
 
+/* Setup from given neighbour rows (the distributed operator's setup, after
+ * its neighbours have been found across ranks and fetched; the constructor's
+ * stages after the search and the fetch of the coordinates,
+ * DTK_MovingLeastSquaresOperator_def.hpp:64-118).  Row i holds `row` entries
+ * (1..32): entry e = i*row + j has its neighbour's coordinates at
+ * nb_points[3e .. 3e+2] (row-major, n_tgt*row x 3) and the index of its value
+ * in the source-value array the handle's apply takes (indices[e] in
+ * [0, n_src)).  The support radius is the row's farthest neighbour, so the
+ * order of a row only orders its sums; rows ascending by (d2, global index)
+ * give the coefficients a single-rank dtk_mls_create computes for the same
+ * rows.  The handle applies like one from dtk_mls_create over n_src
+ * sources (no coordinate adjoint: it keeps no points, and keep_points != 0
+ * is DTK_ERR_UNSUPPORTED).  kNN rows only
+ * (opts->radius > 0 -> DTK_ERR_UNSUPPORTED); opts->comm_size must be 1 (the
+ * handle is this rank's part); indices out of range -> DTK_ERR_INVALID_ARG.
+ * Synchronous. */
+dtk_status dtk_mls_create_from_neighbors(const dtk_mls_options *opts, const double *tgt,
+                                         int64_t n_tgt, int64_t tgt_pt_stride,
+                                         int64_t tgt_dim_stride, int32_t row,
+                                         const double *nb_points, const int32_t *indices,
+                                         int64_t n_src, dtk_stream_t stream,
+                                         dtk_mls_handle *out);
+
 /* apply: target_values[i] = sum_j coeff_j * source_values[idx_j].
  * Replaces MovingLeastSquaresOperator::apply, DTK_MovingLeastSquaresOperator_def.hpp:121-141,
  * with its preconditions n_source_values == n_src and n_target_values ==

@@ -86,7 +86,7 @@ HANDLE_ENTRIES = ("dtk_mls_apply", "dtk_mls_apply_adjoint", "dtk_mls_apply_multi
                   "dtk_mls_export", "dtk_nn_apply", "dtk_nn_apply_multi", "dtk_nn_get_indices",
                   "dtk_mls_batch_apply", "dtk_mls_batch_get_csr", "dtk_mls_batch_get_stage_times")
 CREATE_ENTRIES = ("dtk_mls_import", "dtk_mls_transfer_host", "dtk_nn_create", "dtk_knn_search",
-                  "dtk_mls_batch_create", "dtk_svd_pinv_noalloc")
+                  "dtk_mls_batch_create", "dtk_svd_pinv_noalloc", "dtk_mls_create_from_neighbors")
 
 
 def _null_args(fn):
@@ -102,6 +102,34 @@ def test_every_entry_rejects_null_arguments(dtk_lib):
         assert dtk_lib.dtk_last_error().startswith(b"DTK_REQUIRE"), name
     for name in ("dtk_mls_destroy", "dtk_nn_destroy", "dtk_mls_batch_destroy"):
         assert getattr(dtk_lib, name)(None) == 0, name
+
+
+def test_create_from_neighbors_rejects_bad_arguments_before_device_work(dtk_lib):
+    from datatransferkit_gb300._capi import Options
+    o = Options()
+
+    def create(row=4, n_src=10, nb=1, idx=1, n_tgt=2):
+        h = C.c_void_p()
+        st = dtk_lib.dtk_mls_create_from_neighbors(C.byref(o), 1, n_tgt, 3, 1, row, nb, idx, n_src, None,
+                                                   C.byref(h))
+        assert not h.value
+        return st
+
+    dtk_lib.dtk_mls_default_options(C.byref(o))
+    o.radius = 0.5
+    assert create() == 2  # kNN rows only
+    dtk_lib.dtk_mls_default_options(C.byref(o))
+    o.keep_points = 1
+    assert create() == 2  # no points are kept for the coordinate adjoint
+    dtk_lib.dtk_mls_default_options(C.byref(o))
+    o.comm_size = 2
+    assert create() == 2  # the handle is one rank's part
+    dtk_lib.dtk_mls_default_options(C.byref(o))
+    assert create(row=0) == 1 and create(row=33) == 1
+    assert create(n_src=0) == 1 and create(n_src=1 << 31) == 1
+    assert create(nb=None) == 1 and create(idx=None) == 1
+    assert create(n_tgt=(1 << 31) // 4) == 1  # n_targets * row beyond int32 offsets
+    assert b"DTK_REQUIRE" in dtk_lib.dtk_last_error()
 
 
 def test_svd_rejects_bad_sizes(dtk_lib):
