@@ -192,33 +192,47 @@ def distributed_knn(comm: _Comm, src: torch.Tensor, tgt: torch.Tensor, k: int, s
     answers = comm.exchange(answer, back_send, back_recv)
     answer_gid = comm.exchange(a_gid, back_send, back_recv)
 
-    # 5. merge by (d2, global index) and keep the first `row` of each target
-    t_parts = [torch.arange(n_tgt, device=dev).repeat_interleave(row_l)]
-    d2_parts, gid_parts, pts_parts = [d2.reshape(-1)], [gid.reshape(-1)], [pts.reshape(-1, 3)]
-    at = 0
+    # 5. merge by (d2, global index) and keep the first `row` of each target;
+    #    a target that asked no other rank keeps its local row (then full)
+    asked_any = torch.zeros(n_tgt, dtype=torch.bool, device=dev)
     for q in range(comm.size):
-        rq = min(row, int(counts[q]))
-        n = send_counts[q] * rq
-        if n == 0:
-            continue
-        t_parts.append(sel[q].repeat_interleave(rq))
-        d2_parts.append(answers[at:at + n, 0])
-        pts_parts.append(answers[at:at + n, 1:4])
-        gid_parts.append(answer_gid[at:at + n])
-        at += n
-    t_all, d2_all = torch.cat(t_parts), torch.cat(d2_parts)
-    gid_all, pts_all = torch.cat(gid_parts), torch.cat(pts_parts)
-    order = torch.sort(gid_all, stable=True).indices
-    order = order[torch.sort(d2_all[order], stable=True).indices]
-    order = order[torch.sort(t_all[order], stable=True).indices]
-    per = torch.bincount(t_all, minlength=n_tgt)
-    start = torch.cumsum(per, 0) - per
-    t_sorted = t_all[order]
-    keep = order[(torch.arange(order.numel(), device=dev) - start[t_sorted]) < row]
-    if keep.numel() != n_tgt * row:
-        raise _capi.DTKError(6, "distributed search: a row came back short")
-    return _Rows(gid_all[keep].view(n_tgt, row), pts_all[keep].view(n_tgt, row, 3), counts, first, row,
-                 send_counts)
+        asked_any[sel[q]] = True
+    touched = torch.nonzero(asked_any).view(-1)
+    out_gid = torch.empty((n_tgt, row), dtype=torch.int64, device=dev)
+    out_pts = torch.empty((n_tgt, row, 3), dtype=torch.float64, device=dev)
+    if row_l == row:
+        out_gid.copy_(gid)
+        out_pts.copy_(pts)
+    elif touched.numel() != n_tgt:
+        raise _capi.DTKError(6, "distributed search: a short row asked no other rank")
+    if touched.numel():
+        t_parts = [touched.repeat_interleave(row_l)]
+        d2_parts, gid_parts = [d2[touched].reshape(-1)], [gid[touched].reshape(-1)]
+        pts_parts = [pts[touched].reshape(-1, 3)]
+        at = 0
+        for q in range(comm.size):
+            rq = min(row, int(counts[q]))
+            n = send_counts[q] * rq
+            if n == 0:
+                continue
+            t_parts.append(sel[q].repeat_interleave(rq))
+            d2_parts.append(answers[at:at + n, 0])
+            pts_parts.append(answers[at:at + n, 1:4])
+            gid_parts.append(answer_gid[at:at + n])
+            at += n
+        t_all, d2_all = torch.cat(t_parts), torch.cat(d2_parts)
+        gid_all, pts_all = torch.cat(gid_parts), torch.cat(pts_parts)
+        order = torch.sort(gid_all, stable=True).indices
+        order = order[torch.sort(d2_all[order], stable=True).indices]
+        order = order[torch.sort(t_all[order], stable=True).indices]
+        per = torch.bincount(t_all, minlength=n_tgt)
+        begin = torch.cumsum(per, 0) - per
+        keep = order[(torch.arange(order.numel(), device=dev) - begin[t_all[order]]) < row]
+        if keep.numel() != touched.numel() * row:
+            raise _capi.DTKError(6, "distributed search: a row came back short")
+        out_gid[touched] = gid_all[keep].view(-1, row)
+        out_pts[touched] = pts_all[keep].view(-1, row, 3)
+    return _Rows(out_gid, out_pts, counts, first, row, send_counts)
 
 
 class _FetchPlan:
@@ -235,15 +249,28 @@ class _FetchPlan:
         ends = torch.cumsum(counts, 0).to(dev)
         owner = torch.searchsorted(ends, wanted, right=True)
         local = wanted - first.to(dev)[owner]
-        self.recv_counts = [int(x) for x in torch.bincount(owner, minlength=comm.size).cpu()]
+        per_owner = [int(x) for x in torch.bincount(owner, minlength=comm.size).cpu()]
+        # this rank's own values are gathered on the device (a contiguous run
+        # of the fetched array, the owners being in rank order); only the
+        # others' go through the collective
+        a = sum(per_owner[:comm.rank])
+        self.own = (a, a + per_owner[comm.rank])
+        self.own_index = local[a:a + per_owner[comm.rank]]
+        self.remote = torch.cat([torch.arange(0, a, device=dev),
+                                 torch.arange(self.own[1], int(wanted.numel()), device=dev)])
+        self.recv_counts = list(per_owner)
+        self.recv_counts[comm.rank] = 0
         self.send_counts = comm.counts(self.recv_counts)
         # the owners learn which of their values to send, in the order asked
-        self.send_index = comm.exchange(local, self.recv_counts, self.send_counts)
+        self.send_index = comm.exchange(local[self.remote], self.recv_counts, self.send_counts)
         self.n_fetched = int(wanted.numel())
 
     def __call__(self, values: torch.Tensor) -> torch.Tensor:
-        out = values[self.send_index] if self.send_index.numel() else values[:0]
-        return self.comm.exchange(out, self.send_counts, self.recv_counts)
+        out = torch.empty((self.n_fetched,) + tuple(values.shape[1:]), dtype=values.dtype, device=values.device)
+        out[self.own[0]:self.own[1]] = values[self.own_index]
+        got = self.comm.exchange(values[self.send_index], self.send_counts, self.recv_counts)
+        out[self.remote] = got
+        return out
 
 
 def fetch(group, ranks: torch.Tensor, indices: torch.Tensor, values: torch.Tensor) -> torch.Tensor:
