@@ -409,7 +409,8 @@ def row_batch(torch, dtk, syn, dev, stream, n_problems=256, profile_only=False):
     """Batched uneven transfers: 256 problems (fewer for profiler captures), sizes log-uniform 1e3..1e5,
     Gaussian-mixture sources (8 clusters, sigma 0.02..0.2), U[0,1]^3 targets,
     radius 0.05, linear/quadratic alternating, Wendland<2>, FP64.  One step =
-    batch setup (one search, one bucketed setup) + one graph-replayed apply."""
+    batch setup (one search, one persistent setup launch) + one graph-replayed
+    apply; beside it, a re-setup on the kept rows + apply, both graph replays."""
     from oracle import cpu as ocpu
     probs = syn.batched_problems(n_problems, 5)
     W2 = dtk.Wendland(2)
@@ -434,7 +435,18 @@ def row_batch(torch, dtk, syn, dev, stream, n_problems=256, profile_only=False):
     b = holder["b"]
     ms_graph = _event_time(torch, stream, lambda: b.apply(v_d, out, graph=True), 20, 3)
     ms_direct = _event_time(torch, stream, lambda: b.apply(v_d, out, graph=False), 20, 3)
+    # re-setup on the same coordinates with the create's rows, replayed from
+    # its CUDA graph (one persistent launch), then the graph-replayed apply;
+    # the coefficients must come out bit for bit as the create's
+    _, _, c0 = b.csr()
+
+    def resetup_step():
+        b.resetup()
+        b.apply(v_d, out, graph=True)
+
+    ms_resetup = _event_time(torch, stream, resetup_step, 5, 3)
     off, idx, coeff = b.csr()
+    resetup_bitwise = bool(torch.equal(coeff, c0))
     off = off.cpu().numpy()
     rows = np.diff(off)
     y = out.cpu().numpy()
@@ -457,6 +469,8 @@ def row_batch(torch, dtk, syn, dev, stream, n_problems=256, profile_only=False):
     return {"value": n_tgt / (ms / 1e3), "ms": ms, "n_targets": int(n_tgt), "nnz": int(off[-1]),
             "stages_ms": dict(zip(("search", "setup", "host"), b.stage_times_ms)),
             "apply_ms": {"graph": ms_graph, "direct": ms_direct},
+            "resetup_apply_ms": ms_resetup, "resetup_bitwise": resetup_bitwise,
+            "tuned": b.config,
             "rel_l2_vs_oracle": errs,
             "detail": {"row_length": {"mean": float(rows.mean()), "p50": float(np.percentile(rows, 50)),
                                       "p99": float(np.percentile(rows, 99)), "max": int(rows.max())},

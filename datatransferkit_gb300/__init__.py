@@ -7,11 +7,12 @@ DataTransferKit's operator API.  There is no CPU fallback.
 from .operators import (FP64, MIXED, Buhmann, Constant, Linear, MovingLeastSquaresBatch,
                         MovingLeastSquaresOperator, NearestNeighborOperator,
                         MultivariatePolynomialBasis, PointCloudOperator, Quadratic, Wendland, Wu,
-                        kernel_launch_count, knn_search, release_cached_memory, svd_pinv)
+                        kernel_launch_count, knn_search, release_cached_memory, set_setup_lanes,
+                        svd_pinv)
 from ._capi import DTKError, InvalidArgument, Unsupported
 from .distributed import DistributedMovingLeastSquaresOperator, DistributedNearestNeighborOperator, fetch
 
 __all__ = ["MovingLeastSquaresOperator", "MovingLeastSquaresBatch", "NearestNeighborOperator", "PointCloudOperator", "MultivariatePolynomialBasis",
            "Constant", "Linear", "Quadratic", "Wendland", "Wu", "Buhmann", "FP64", "MIXED",
            "knn_search", "svd_pinv", "DistributedMovingLeastSquaresOperator",
-           "DistributedNearestNeighborOperator", "fetch", "kernel_launch_count", "release_cached_memory", "DTKError", "InvalidArgument", "Unsupported"]
+           "DistributedNearestNeighborOperator", "fetch", "kernel_launch_count", "release_cached_memory", "set_setup_lanes", "DTKError", "InvalidArgument", "Unsupported"]

@@ -38,8 +38,9 @@ namespace dtk
 namespace
 {
 
-constexpr int N_BASIS = 3, N_RBF = 9, N_PATH = 3;
-constexpr int N_KEYS = N_BASIS * N_RBF * N_PATH;
+constexpr int N_BASIS = 3, N_RBF = SETUP_RBFS, N_PATH = SETUP_PATHS;
+constexpr int N_KEYS = SETUP_KEYS;
+static_assert( N_KEYS == N_BASIS * N_RBF * N_PATH, "bucket keys" );
 
 // Bucket key of every target in processing order, the targets themselves as
 // sort values, and a histogram of the keys.
@@ -72,50 +73,293 @@ __global__ void k_plan_keys( int64_t n, uint32_t const *order, int32_t const *of
             atomicAdd( &hist[k], h[k] );
 }
 
+// Task layout from the bucket histogram (one block): buckets of path 2 (the
+// longest rows) first, then path 1, then path 0 (path 0 left out when
+// `with_path0` is false), each bucket cut into tasks of 32 targets.  Writes
+// the task count, the first task of each path and, per bucket, its first
+// target in the bucketed list and its first task.
+__global__ void k_task_layout( unsigned const *hist, bool with_path0, int64_t *n_tasks, int64_t *path_first,
+                               int64_t *bucket_start, int64_t *bucket_task )
+{
+    if ( threadIdx.x != 0 )
+        return;
+    int64_t at = 0;
+    for ( int k = 0; k < N_KEYS; ++k )
+    {
+        bucket_start[k] = at;
+        at += hist[k];
+    }
+    int64_t t = 0;
+    for ( int path = N_PATH - 1; path >= 0; --path )
+    {
+        path_first[path] = t;
+        for ( int k = path; k < N_KEYS; k += N_PATH )
+        {
+            bucket_task[k] = t;
+            if ( path > 0 || with_path0 )
+                t += ( hist[k] + 31 ) / 32;
+        }
+    }
+    path_first[N_PATH] = t;
+    *n_tasks = t;
+}
+
+// The tasks (a grid over the largest possible count; the excess exits).
+__global__ void k_fill_tasks( unsigned const *hist, int64_t const *n_tasks, int64_t const *bucket_start,
+                              int64_t const *bucket_task, bool with_path0, int lanes0, int lanes1, int lanes2,
+                              SetupTask *tasks )
+{
+    int64_t const t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if ( t >= *n_tasks )
+        return;
+    // the bucket whose task range holds t (non-empty buckets are disjoint)
+    int key = -1;
+    for ( int k = 0; k < N_KEYS; ++k )
+    {
+        int const path = k % N_PATH;
+        if ( hist[k] == 0 || ( path == 0 && !with_path0 ) )
+            continue;
+        int64_t const n_t = ( hist[k] + 31 ) / 32;
+        if ( t >= bucket_task[k] && t < bucket_task[k] + n_t )
+            key = k;
+    }
+    if ( key < 0 )
+        return;
+    int64_t const j = t - bucket_task[key];
+    int const path = key % N_PATH;
+    SetupTask x;
+    x.first = (int32_t)( bucket_start[key] + 32 * j );
+    int64_t const left = (int64_t)hist[key] - 32 * j;
+    x.count = (uint8_t)( left < 32 ? left : 32 );
+    x.key = (uint8_t)key;
+    x.lanes = (uint8_t)( path == 2 ? lanes2 : path == 1 ? lanes1 : lanes0 );
+    x.pad = 0;
+    tasks[t] = x;
+}
+
+// Setup tuning: lanes a target for the gather phases of each path.  Path 0
+// (kNN rows) keeps one lane a target, the arithmetic of the single
+// operator's kernel; paths 1 and 2 are timed on a sample of their tasks.
+std::mutex g_setup_tune_mutex;
+std::map<std::tuple<int, int, int>, int> g_setup_tune_cache; // (path, precision, log2 tasks) -> lanes
+
+} // namespace
+
+SetupPlan::~SetupPlan() = default;
+
+void plan_setup( SetupArgs const &a, int precision, uint8_t const *basis_of_group, uint8_t const *rbf_of_group,
+                 uint32_t const *tgt_group, bool split_all, SetupPlan &plan, cudaStream_t s )
+{
+    int64_t const n = a.n_tgt;
+    plan.n = n;
+    plan.precision = precision;
+    // mixed kNN rows (path 0 of the mixed form) run the fused mixed kernel
+    // per bucket, the rest the persistent FP64 kernel
+    plan.with_path0 = !( precision == DTK_MIXED && !split_all );
+    plan.list.allocate( std::max<int64_t>( 1, n ), s );
+    plan.hist.allocate( N_KEYS, s );
+    plan.n_tasks.allocate( 1, s );
+    plan.path_first.allocate( N_PATH + 1, s );
+    plan.bucket_start.allocate( N_KEYS, s );
+    plan.bucket_task.allocate( N_KEYS, s );
+    plan.tasks.allocate( ( n + 31 ) / 32 + N_KEYS, s );
+    plan.counter.allocate( 1, s );
+    DTK_CUDA_OR_THROW( cudaMemsetAsync( plan.hist.get(), 0, N_KEYS * sizeof( unsigned ), s ) );
+    if ( n )
+    {
+        DeviceBuffer<uint32_t> keys( n, s );
+        k_plan_keys<<<(unsigned)( ( n + 255 ) / 256 ), 256, 0, s>>>( n, a.order, a.offset, tgt_group,
+                                                                      basis_of_group, rbf_of_group, a.basis,
+                                                                      a.rbf, split_all, keys.get(),
+                                                                      plan.list.get(), plan.hist.get() );
+        check_launch( "k_plan_keys" );
+        // stable: each bucket keeps the processing order
+        radix_sort_pairs( keys.get(), plan.list.get(), n, 8, s );
+    }
+    k_task_layout<<<1, 32, 0, s>>>( plan.hist.get(), plan.with_path0, plan.n_tasks.get(), plan.path_first.get(),
+                                    plan.bucket_start.get(), plan.bucket_task.get() );
+    check_launch( "k_task_layout" );
+}
+
+void fill_setup_tasks( SetupPlan &plan, cudaStream_t s )
+{
+    int64_t const most = ( plan.n + 31 ) / 32 + N_KEYS;
+    k_fill_tasks<<<(unsigned)( ( most + 255 ) / 256 ), 256, 0, s>>>(
+        plan.hist.get(), plan.n_tasks.get(), plan.bucket_start.get(), plan.bucket_task.get(), plan.with_path0,
+        plan.lanes[0], plan.lanes[1], plan.lanes[2], plan.tasks.get() );
+    check_launch( "k_fill_tasks" );
+}
+
+namespace
+{
+
+BatchSetupArgs batch_args( SetupArgs const &a, SetupPlan &plan, double *u_work )
+{
+    BatchSetupArgs b;
+    b.nb = Neighbours{a.src, a.idx, a.pos, a.s2};
+    b.tgt = a.tgt;
+    b.offset = a.offset;
+    b.list = plan.list.get();
+    b.tasks = plan.tasks.get();
+    b.n_tasks = plan.n_tasks.get();
+    b.rows_sorted = a.rows_sorted;
+    b.coeff64 = a.coeff64;
+    b.coeff32 = a.coeff32;
+    b.underdetermined = a.underdetermined;
+    b.rotations = a.rotations;
+    b.status = a.status;
+    b.counter = plan.counter.get();
+    b.u_work = u_work;
+    return b;
+}
+
+// Times the lane counts of paths 1 and 2 on a sample of their tasks (the
+// first few waves of each), keeps the fastest per path, and caches it by
+// (path, precision, size class).  One synchronisation reads the task layout.
+void tune_setup( SetupArgs const &a, SetupPlan &plan, double *u_work, cudaStream_t s )
+{
+    int fixed[N_PATH] = {0, 0, 0};
+    fixed_setup_lanes( fixed[1], fixed[2] );
+    if ( fixed[1] && fixed[2] )
+    {
+        plan.lanes[1] = fixed[1];
+        plan.lanes[2] = fixed[2];
+        return;
+    }
+    int64_t pf[N_PATH + 1];
+    DTK_CUDA_OR_THROW( cudaMemcpyAsync( pf, plan.path_first.get(), sizeof( pf ), cudaMemcpyDeviceToHost, s ) );
+    DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+    int64_t const wave = batch_setup_threads() / 32; // resident warps
+    cudaEvent_t e0, e1;
+    DTK_CUDA_OR_THROW( cudaEventCreate( &e0 ) );
+    DTK_CUDA_OR_THROW( cudaEventCreate( &e1 ) );
+    struct EvGuard
+    {
+        cudaEvent_t a, b;
+        ~EvGuard()
+        {
+            cudaEventDestroy( a );
+            cudaEventDestroy( b );
+        }
+    } guard{e0, e1};
+    for ( int path = 1; path < N_PATH; ++path )
+    {
+        // tasks of this path: [pf[path], next path's first) (paths run 2, 1, 0)
+        if ( fixed[path] )
+        {
+            plan.lanes[path] = fixed[path];
+            continue;
+        }
+        int64_t const t0 = pf[path], t1 = path == 2 ? pf[1] : pf[0];
+        int64_t const count = t1 - t0;
+        if ( count <= 0 )
+            continue;
+        int size_class = 0;
+        while ( ( int64_t( 1 ) << size_class ) < count )
+            ++size_class;
+        auto const key = std::make_tuple( path, plan.precision, size_class );
+        {
+            std::lock_guard<std::mutex> lock( g_setup_tune_mutex );
+            auto const it = g_setup_tune_cache.find( key );
+            if ( it != g_setup_tune_cache.end() )
+            {
+                plan.lanes[path] = it->second;
+                plan.tuned[path] = true;
+                continue;
+            }
+        }
+        int64_t const sample = std::min<int64_t>( count, 2 * wave );
+        int const cands[2][3] = {{2, 4, 8}, {8, 16, 32}};
+        float best = 3.4e38f;
+        int best_lanes = plan.lanes[path];
+        for ( int G : cands[path - 1] )
+        {
+            BatchSetupArgs b = batch_args( a, plan, u_work );
+            b.t_begin = t0;
+            b.t_end = t0 + sample;
+            b.force_lanes = G;
+            float ms[3];
+            for ( int rep = 0; rep < 3; ++rep )
+            {
+                DTK_CUDA_OR_THROW( cudaEventRecord( e0, s ) );
+                batch_setup( b, s );
+                DTK_CUDA_OR_THROW( cudaEventRecord( e1, s ) );
+                DTK_CUDA_OR_THROW( cudaEventSynchronize( e1 ) );
+                DTK_CUDA_OR_THROW( cudaEventElapsedTime( &ms[rep], e0, e1 ) );
+            }
+            std::sort( ms, ms + 3 );
+            if ( ms[1] < best )
+            {
+                best = ms[1];
+                best_lanes = G;
+            }
+        }
+        plan.lanes[path] = best_lanes;
+        plan.tuned[path] = true;
+        std::lock_guard<std::mutex> lock( g_setup_tune_mutex );
+        g_setup_tune_cache[key] = best_lanes;
+    }
+}
+
 } // namespace
 
 void run_setup_plan( SetupArgs const &a, int precision, uint8_t const *basis_of_group,
                      uint8_t const *rbf_of_group, uint32_t const *tgt_group, bool split_all,
-                     cudaStream_t s )
+                     cudaStream_t s, SetupPlan *keep, bool tune )
 {
-    int64_t const n = a.n_tgt;
-    if ( n == 0 )
+    SetupPlan local;
+    SetupPlan &plan = keep ? *keep : local;
+    plan_setup( a, precision, basis_of_group, rbf_of_group, tgt_group, split_all, plan, s );
+    if ( a.n_tgt == 0 )
         return;
-    DeviceBuffer<uint32_t> keys( n, s ), vals( n, s );
-    DeviceBuffer<unsigned> hist( N_KEYS, s );
-    DTK_CUDA_OR_THROW( cudaMemsetAsync( hist.get(), 0, N_KEYS * sizeof( unsigned ), s ) );
-    k_plan_keys<<<(unsigned)( ( n + 255 ) / 256 ), 256, 0, s>>>( n, a.order, a.offset, tgt_group, basis_of_group,
-                                                                  rbf_of_group, a.basis, a.rbf, split_all,
-                                                                  keys.get(), vals.get(), hist.get() );
-    check_launch( "k_plan_keys" );
-    // stable: each bucket keeps the processing order
-    radix_sort_pairs( keys.get(), vals.get(), n, 8, s );
-    unsigned h[N_KEYS];
-    DTK_CUDA_OR_THROW( cudaMemcpyAsync( h, hist.get(), sizeof( h ), cudaMemcpyDeviceToHost, s ) );
-    DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
-    int64_t start = 0;
-    for ( int key = 0; key < N_KEYS; ++key )
+    if ( !plan.u_work.get() )
+        plan.u_work.allocate( (size_t)BS_MAX_M_SQ * batch_setup_threads(), s );
+    // the statistics counters collect the sample runs too: zeroed after them
+    if ( tune )
     {
-        int64_t const cnt = h[key];
-        if ( cnt == 0 )
-            continue;
-        uint32_t const *list = vals.get() + start;
-        start += cnt;
-        SetupArgs b = a;
-        int const path = key % N_PATH;
-        b.basis = key / N_PATH / N_RBF;
-        b.rbf = key / N_PATH % N_RBF;
-        b.n_tgt = cnt;
-        b.order = list;
-        if ( path == 0 )
+        tune_setup( a, plan, plan.u_work.get(), s );
+        DTK_CUDA_OR_THROW( cudaMemsetAsync( a.underdetermined, 0, sizeof( unsigned long long ), s ) );
+        DTK_CUDA_OR_THROW( cudaMemsetAsync( a.rotations, 0, sizeof( unsigned long long ), s ) );
+    }
+    fill_setup_tasks( plan, s );
+    run_planned_setup( a, plan, s );
+}
+
+void run_planned_setup( SetupArgs const &a, SetupPlan &plan, cudaStream_t s )
+{
+    if ( plan.n == 0 )
+        return;
+    BatchSetupArgs const b = batch_args( a, plan, plan.u_work.get() );
+    batch_setup( b, s );
+    if ( plan.with_path0 )
+        return;
+    // mixed-form kNN rows: the fused mixed kernel per (basis, rbf) bucket;
+    // the bucket sizes come to the host once and are kept
+    if ( plan.mixed_buckets.empty() )
+    {
+        unsigned h[N_KEYS];
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( h, plan.hist.get(), sizeof( h ), cudaMemcpyDeviceToHost, s ) );
+        DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+        int64_t start = 0;
+        for ( int key = 0; key < N_KEYS; ++key )
         {
-            if ( precision == DTK_FP64 )
-                setup_fp64( b, s );
-            else
-                setup_mixed( b, s );
+            if ( h[key] && key % N_PATH == 0 )
+                plan.mixed_buckets.push_back( {key, start, (int64_t)h[key]} );
+            start += h[key];
         }
-        else
-            setup_split( b, reinterpret_cast<int32_t const *>( list ), cnt, path == 1 ? 8 : 32, s );
+        if ( plan.mixed_buckets.empty() )
+            plan.mixed_buckets.push_back( {-1, 0, 0} ); // none: do not ask again
+    }
+    for ( auto const &bk : plan.mixed_buckets )
+    {
+        if ( bk.key < 0 )
+            continue;
+        SetupArgs b = a;
+        b.basis = bk.key / N_PATH / N_RBF;
+        b.rbf = bk.key / N_PATH % N_RBF;
+        b.n_tgt = bk.count;
+        b.order = plan.list.get() + bk.start;
+        setup_mixed( b, s );
     }
 }
 
@@ -263,14 +507,30 @@ struct dtk_mls_batch_s
     double *g_tgt = nullptr;
     int64_t underdetermined = 0, rotations = 0;
     float search_ms = 0.f, setup_ms = 0.f, host_ms = 0.f;
+    // the setup's plan (bucketed targets, tasks, lane counts), kept for
+    // re-setups on new coordinates with the same rows, and their graph
+    SetupPlan plan;
+    bool radius_mode = false;
+    DeviceBuffer<unsigned> status;
+    DeviceBuffer<unsigned long long> counters;
+    cudaGraph_t setup_graph = nullptr;
+    cudaGraphExec_t setup_exec = nullptr;
+    double const *gs_src = nullptr, *gs_tgt = nullptr;
+    int64_t setup_replays = 0;
 
     ~dtk_mls_batch_s()
     {
-        life.retire( offset, idx, coeff64, coeff32, rows, tasks );
+        life.retire( offset, idx, coeff64, coeff32, rows, tasks, status, counters, plan.list, plan.hist,
+                     plan.n_tasks, plan.path_first, plan.bucket_start, plan.bucket_task, plan.tasks, plan.counter,
+                     plan.u_work );
         if ( exec )
             cudaGraphExecDestroy( exec );
         if ( graph )
             cudaGraphDestroy( graph );
+        if ( setup_exec )
+            cudaGraphExecDestroy( setup_exec );
+        if ( setup_graph )
+            cudaGraphDestroy( setup_graph );
         if ( capture )
             cudaStreamDestroy( capture );
     }
@@ -563,7 +823,9 @@ dtk_status dtk_mls_batch_create( int32_t n_problems, const dtk_mls_options *opts
             a.coeff32 = h->coeff32.get();
         }
         auto const t1 = std::chrono::steady_clock::now();
-        run_setup_plan( a, precision, basis_g.get(), rbf_g.get(), tgt_grp.get(), radius_mode, s );
+        h->radius_mode = radius_mode;
+        run_setup_plan( a, precision, basis_g.get(), rbf_g.get(), tgt_grp.get(), radius_mode, s, &h->plan,
+                        true );
         host_ms += ms_since( t1 );
         DTK_CUDA_OR_THROW( cudaEventRecord( ev[2], s ) );
 
@@ -647,6 +909,109 @@ dtk_status dtk_mls_batch_apply( dtk_mls_batch_handle h, const double *src_values
             h->g_tgt = tgt_values;
         }
         DTK_CUDA_OR_THROW( cudaGraphLaunch( h->exec, s ) );
+    } );
+}
+
+dtk_status dtk_mls_batch_resetup( dtk_mls_batch_handle h, const double *src, const double *tgt,
+                                  dtk_stream_t stream_ )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
+        DTK_REQUIRE_OR_THROW( src != nullptr && ( h->n_tgt == 0 || tgt != nullptr ), "null points" );
+        require_device_memory( src, "source points" );
+        require_device_memory( h->n_tgt ? tgt : nullptr, "target points" );
+        cudaStream_t s = reinterpret_cast<cudaStream_t>( stream_ );
+        TouchOnExit const touch{&h->life, s};
+        if ( h->n_tgt == 0 )
+            return;
+        if ( !h->status.get() )
+        {
+            h->status.allocate( 1, s );
+            h->counters.allocate( 3, s );
+        }
+        SetupArgs a{};
+        a.src = PointsView{src, h->n_src, 3, 1};
+        a.tgt = PointsView{tgt, h->n_tgt, 3, 1};
+        a.offset = h->offset.get();
+        a.idx = h->idx.get();
+        a.order = nullptr;
+        a.n_tgt = h->n_tgt;
+        a.rows_sorted = false; // rows kept from other coordinates need not be sorted any more
+        a.coeff64 = h->coeff64.get();
+        a.coeff32 = h->coeff32.get();
+        a.underdetermined = h->counters.get();
+        a.rotations = h->counters.get() + 1;
+        a.rotations32 = h->counters.get() + 2;
+        a.status = h->status.get();
+        auto enqueue = [&]( cudaStream_t q ) {
+            DTK_CUDA_OR_THROW( cudaMemsetAsync( h->status.get(), 0, sizeof( unsigned ), q ) );
+            DTK_CUDA_OR_THROW( cudaMemsetAsync( h->counters.get(), 0, 3 * sizeof( unsigned long long ), q ) );
+            run_planned_setup( a, h->plan, q );
+        };
+        // one graph: the statistics reset and the persistent setup launch (and
+        // the fused mixed kernel per mixed kNN bucket), captured once per pair
+        // of point arrays and replayed
+        if ( !h->setup_exec || h->gs_src != src || h->gs_tgt != tgt )
+        {
+            if ( h->setup_exec )
+            {
+                cudaGraphExecDestroy( h->setup_exec );
+                h->setup_exec = nullptr;
+            }
+            if ( h->setup_graph )
+            {
+                cudaGraphDestroy( h->setup_graph );
+                h->setup_graph = nullptr;
+            }
+            if ( !h->capture )
+                DTK_CUDA_OR_THROW( cudaStreamCreateWithFlags( &h->capture, cudaStreamNonBlocking ) );
+            DTK_CUDA_OR_THROW( cudaStreamBeginCapture( h->capture, cudaStreamCaptureModeThreadLocal ) );
+            try
+            {
+                enqueue( h->capture );
+            }
+            catch ( ... )
+            {
+                cudaGraph_t g = nullptr;
+                cudaStreamEndCapture( h->capture, &g );
+                if ( g )
+                    cudaGraphDestroy( g );
+                throw;
+            }
+            DTK_CUDA_OR_THROW( cudaStreamEndCapture( h->capture, &h->setup_graph ) );
+            DTK_CUDA_OR_THROW( cudaGraphInstantiate( &h->setup_exec, h->setup_graph, 0 ) );
+            h->gs_src = src;
+            h->gs_tgt = tgt;
+        }
+        DTK_CUDA_OR_THROW( cudaGraphLaunch( h->setup_exec, s ) );
+        ++h->setup_replays;
+        unsigned st = 0;
+        unsigned long long cnt[3] = {0, 0, 0};
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( &st, h->status.get(), sizeof( st ), cudaMemcpyDeviceToHost, s ) );
+        DTK_CUDA_OR_THROW( cudaMemcpyAsync( cnt, h->counters.get(), sizeof( cnt ), cudaMemcpyDeviceToHost, s ) );
+        DTK_CUDA_OR_THROW( cudaStreamSynchronize( s ) );
+        if ( st & DEV_TIMEOUT )
+            throw Error{DTK_ERR_TIMEOUT, "a bounded device loop hit its cap"};
+        if ( st )
+            throw Error{DTK_ERR_INTERNAL, "the setup reported an internal error"};
+        h->underdetermined = (int64_t)cnt[0];
+        h->rotations = (int64_t)cnt[1];
+    } );
+}
+
+dtk_status dtk_mls_batch_get_config( dtk_mls_batch_handle h, int32_t *setup_lanes, int32_t *apply_lanes,
+                                     int64_t *setup_graph_replays )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
+        if ( setup_lanes )
+            for ( int p = 0; p < 3; ++p )
+                setup_lanes[p] = h->plan.lanes[p];
+        if ( apply_lanes )
+            for ( int b = 0; b < dtk_mls_batch_s::NBINS; ++b )
+                apply_lanes[b] = h->tuned && h->bin_start[b + 1] > h->bin_start[b] ? h->lanes[b] : 0;
+        if ( setup_graph_replays )
+            *setup_graph_replays = h->setup_replays;
     } );
 }
 

@@ -74,12 +74,19 @@ std::vector<int> g_sms;                                    // per device, 0 = no
 namespace
 {
 std::atomic<int64_t> g_jacobi_cap{0}, g_traversal_cap{0};
+std::atomic<int> g_setup_lanes1{0}, g_setup_lanes2{0};
 }
 
 unsigned long long jacobi_cap( int m )
 {
     int64_t const c = g_jacobi_cap.load( std::memory_order_relaxed );
     return c > 0 ? (unsigned long long)c : 200ull * m * m + 2000ull;
+}
+
+void fixed_setup_lanes( int &lanes1, int &lanes2 )
+{
+    lanes1 = g_setup_lanes1.load( std::memory_order_relaxed );
+    lanes2 = g_setup_lanes2.load( std::memory_order_relaxed );
 }
 
 int64_t traversal_cap( int64_t wide_nodes )
@@ -375,6 +382,17 @@ dtk_status dtk_set_loop_caps( int64_t jacobi_rotations, int64_t traversal_steps 
         DTK_REQUIRE_OR_THROW( jacobi_rotations <= UINT32_MAX, "Jacobi cap exceeds 2^32 - 1" );
         g_jacobi_cap.store( jacobi_rotations, std::memory_order_relaxed );
         g_traversal_cap.store( traversal_steps, std::memory_order_relaxed );
+    } );
+}
+
+dtk_status dtk_set_setup_lanes( int32_t lanes_short, int32_t lanes_long )
+{
+    return guarded( [&] {
+        auto ok = []( int v ) { return v == 0 || ( v >= 1 && v <= 32 && ( v & ( v - 1 ) ) == 0 ); };
+        DTK_REQUIRE_OR_THROW( ok( lanes_short ) && ok( lanes_long ),
+                              "lanes must be 0 (tuned) or a power of two in [1, 32]" );
+        g_setup_lanes1.store( lanes_short, std::memory_order_relaxed );
+        g_setup_lanes2.store( lanes_long, std::memory_order_relaxed );
     } );
 }
 

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include <cfloat>
 #include <climits>
 #include <cstdint>
@@ -548,16 +550,87 @@ void setup_mixed( SetupArgs const &a, cudaStream_t s );
 void setup_split( SetupArgs const &a, int32_t const *targets, int64_t n, int lanes, cudaStream_t s );
 constexpr int FUSED_MAX_ROW = 32; // longest row the fused one-thread-per-target kernels take
 
+// Persistent batched setup (FP64 Jacobi): the targets of a bucketed list in
+// tasks of up to 32 targets of one bucket, taken by warps from a counter.
+constexpr int SETUP_RBFS = 9, SETUP_PATHS = 3, SETUP_KEYS = 3 * SETUP_RBFS * SETUP_PATHS;
+constexpr int BS_WARPS = 8; // warps a block of the persistent setup (one block an SM)
+struct SetupTask
+{
+    int32_t first; // the task's first target in the bucketed list
+    uint8_t count; // targets (1 .. 32)
+    uint8_t key;   // bucket: (basis * SETUP_RBFS + rbf) * SETUP_PATHS + path
+    uint8_t lanes; // lanes a target in the gather phases (a power of two, 1 .. 32)
+    uint8_t pad;
+};
+struct BatchSetupArgs
+{
+    Neighbours nb;
+    PointsView tgt;
+    int32_t const *offset;
+    uint32_t const *list; // targets in bucket order
+    SetupTask const *tasks;
+    int64_t const *n_tasks; // task count (device), read when t_end < 0
+    int64_t t_begin = 0, t_end = -1;
+    int force_lanes = 0; // > 0: every task with this many lanes (the tuner's samples)
+    bool rows_sorted = false;
+    double *coeff64 = nullptr;
+    float *coeff32 = nullptr;
+    unsigned long long *underdetermined, *rotations;
+    unsigned *status;
+    unsigned *counter; // zeroed by batch_setup before the launch
+    double *u_work;    // 100 doubles per thread of the grid (batch_setup_threads)
+    unsigned jcap[3] = {0, 0, 0};
+};
+void batch_setup( BatchSetupArgs const &a, cudaStream_t s );
+int64_t batch_setup_threads();
+constexpr int BS_MAX_M_SQ = 100; // U's doubles a thread in the persistent setup's work area
+
+// The device plan of a setup over targets of mixed classes (kept by a batch
+// handle for its re-setups): the targets in bucket order, the bucket sizes,
+// the task list and the persistent kernel's work area.
+struct SetupPlan
+{
+    int64_t n = 0;
+    int precision = 0;
+    bool with_path0 = true;            // path 0 rows in the persistent kernel
+    int lanes[3] = {1, 8, 32};         // lanes a target per path (paths 1 and 2 tunable)
+    bool tuned[3] = {false, false, false};
+    DeviceBuffer<uint32_t> list;       // targets, bucket order
+    DeviceBuffer<unsigned> hist;       // targets per bucket
+    DeviceBuffer<int64_t> n_tasks, path_first, bucket_start, bucket_task;
+    DeviceBuffer<SetupTask> tasks;
+    DeviceBuffer<unsigned> counter;
+    DeviceBuffer<double> u_work;
+    struct Bucket
+    {
+        int key;
+        int64_t start, count;
+    };
+    std::vector<Bucket> mixed_buckets; // mixed-form kNN buckets (fused mixed kernel), once known
+    ~SetupPlan();
+};
+// plan_setup: bucket sort and task layout (no synchronisation); fill_setup_tasks:
+// the task list with the plan's lane counts; run_planned_setup: the persistent
+// launch (plus the fused mixed kernel per mixed kNN bucket).
+void plan_setup( SetupArgs const &a, int precision, uint8_t const *basis_of_group, uint8_t const *rbf_of_group,
+                 uint32_t const *tgt_group, bool split_all, SetupPlan &plan, cudaStream_t s );
+void fill_setup_tasks( SetupPlan &plan, cudaStream_t s );
+void run_planned_setup( SetupArgs const &a, SetupPlan &plan, cudaStream_t s );
+// Lane counts fixed by the caller for paths 1 and 2 (0: tuned by timing).
+void fixed_setup_lanes( int &lanes1, int &lanes2 );
+
 // Setup over targets of mixed classes, planned on the device: a stable key
 // sort of the processing order `a.order` partitions the targets into buckets
-// (basis, rbf, path), path 0 = the fused kernel of the requested precision
-// (rows up to FUSED_MAX_ROW, unless split_all), 1 = split with 8 lanes per
-// target (rows up to 32), 2 = split with 32 lanes.  The class of a target
+// (basis, rbf, path), path 0 = rows up to FUSED_MAX_ROW (unless split_all),
+// 1 = split rows up to 32, 2 = longer rows; every bucket runs in one
+// persistent launch (FP64 Jacobi), except mixed-form kNN rows (path 0 of the
+// mixed form), which run the fused mixed kernel.  The class of a target
 // comes from its group (basis_of_group / rbf_of_group indexed by
-// tgt_group[target]; null: the uniform a.basis / a.rbf).
+// tgt_group[target]; null: the uniform a.basis / a.rbf).  `keep` keeps the
+// plan (for re-setups); `tune` times the lane counts of paths 1 and 2.
 void run_setup_plan( SetupArgs const &a, int precision, uint8_t const *basis_of_group,
                      uint8_t const *rbf_of_group, uint32_t const *tgt_group, bool split_all,
-                     cudaStream_t s );
+                     cudaStream_t s, SetupPlan *keep = nullptr, bool tune = false );
 
 // Batched SVD pseudo-inverse (general n <= 64), DTK SVDFunctor semantics.
 void svd_pinv_batched( int n, int64_t count, double const *a, double *pinv,

@@ -724,6 +724,219 @@ __global__ void __launch_bounds__( 128 )
     }
 }
 
+// ---------------------------------------------------------------------------
+// Persistent batched setup: every FP64-Jacobi target of a batch, of any
+// (basis, rbf) and row length, in one launch.  A warp takes tasks from a
+// counter; a task is up to 32 targets of one bucket (same basis and rbf) and
+// a lane count G: G lanes per target gather the neighbours for the radius and
+// the moments (sums combined by shuffles in the group), the moments go to the
+// owning lane's column of the warp's shared-memory E, every lane runs the
+// reference Jacobi on its own target, and G lanes per target write the
+// coefficients.  With G = 1 a lane walks its target's row alone, in entry
+// order: the same arithmetic as k_setup_fp64, so the coefficients equal the
+// single operator's bit for bit.
+// ---------------------------------------------------------------------------
+constexpr int BS_MAX_M = 10;
+constexpr int BS_SLOT = ( BS_MAX_M * BS_MAX_M + BS_MAX_M ) * 32; // doubles a warp: E and V(:, 0), by lane
+
+template <int M>
+__device__ void setup_task( BatchSetupArgs const &a, SetupTask const &t, int rbf, int G, double *wsm,
+                            int64_t ut, int64_t us, unsigned jcap, unsigned &iters, int &dropped, int lane )
+{
+    constexpr int NU = M * ( M + 1 ) / 2;
+    int const per = 32 / G, sub = lane & ( G - 1 ), cnt = t.count;
+    double my_radius = 0.0;
+    // the moments, G lanes a target, into column ti of E
+    for ( int r = 0; r * per < cnt; ++r ) // warp-uniform
+    {
+        int const ti = r * per + lane / G;
+        bool const active = ti < cnt;
+        int64_t const i = active ? (int64_t)a.list[t.first + ti] : 0;
+        int64_t const b = active ? a.offset[i] : 0;
+        int len = active ? a.offset[i + 1] - (int)b : 0;
+        double const tx = active ? a.tgt( i, 0 ) : 0.0, ty = active ? a.tgt( i, 1 ) : 0.0,
+                     tz = active ? a.tgt( i, 2 ) : 0.0;
+        bool bad = false;
+        for ( int j = sub; j < len; j += G )
+            bad |= (uint32_t)a.nb.ref( b + j ) >= (uint64_t)a.nb.src.n;
+        for ( int o = G >> 1; o; o >>= 1 )
+            bad |= __shfl_xor_sync( FULL, (int)bad, o ) != 0;
+        if ( bad )
+        {
+            if ( sub == 0 )
+                atomicOr( a.status, DEV_BAD_INDEX );
+            len = 0;
+        }
+        // computeRadius: the farthest neighbour (the last of a row sorted by
+        // distance)
+        double d2max = 0.0;
+        for ( int j = a.rows_sorted ? ( sub == 0 ? max( 0, len - 1 ) : len ) : sub; j < len; j += G )
+        {
+            double sx, sy, sz;
+            a.nb.xyz( b + j, sx, sy, sz );
+            d2max = fmax( d2max, dist2_rn( sx, sy, sz, tx, ty, tz ) );
+        }
+        for ( int o = G >> 1; o; o >>= 1 )
+            d2max = fmax( d2max, __shfl_xor_sync( FULL, d2max, o ) );
+        double distance = 10. * DBL_EPSILON;
+        double const dmax = __dsqrt_rn( d2max );
+        if ( dmax > distance )
+            distance = dmax;
+        double const radius = 1.1 * distance;
+        double A[NU];
+#pragma unroll
+        for ( int u = 0; u < NU; ++u )
+            A[u] = 0.0;
+        for ( int j = sub; j < len; j += G )
+        {
+            double sx, sy, sz;
+            a.nb.xyz( b + j, sx, sy, sz );
+            double const x = __dsub_rn( sx, tx ), y = __dsub_rn( sy, ty ), z = __dsub_rn( sz, tz );
+            double P[M];
+            basis_eval<M>( x, y, z, P );
+            double const dist =
+                __dsqrt_rn( __dadd_rn( __dadd_rn( __dmul_rn( x, x ), __dmul_rn( y, y ) ), __dmul_rn( z, z ) ) );
+            double const phi = rbf_eval<double>( rbf, dist / radius );
+            int o = 0;
+#pragma unroll
+            for ( int p = 0; p < M; ++p )
+            {
+                double const pa = P[p] * phi;
+#pragma unroll
+                for ( int c = p; c < M; ++c, ++o )
+                    A[o] = fma( pa, P[c], A[o] );
+            }
+        }
+        if ( G > 1 )
+        {
+#pragma unroll
+            for ( int u = 0; u < NU; ++u )
+                for ( int o = G >> 1; o; o >>= 1 )
+                    A[u] += __shfl_xor_sync( FULL, A[u], o );
+        }
+        if ( active )
+        {
+            int o = 0;
+#pragma unroll
+            for ( int p = 0; p < M; ++p )
+#pragma unroll
+                for ( int c = p; c < M; ++c, ++o )
+                    if ( ( o & ( G - 1 ) ) == sub )
+                    {
+                        wsm[( p * M + c ) * 32 + ti] = A[o];
+                        wsm[( c * M + p ) * 32 + ti] = A[o];
+                    }
+        }
+        // the radius to the target's own lane
+        double const rv = __shfl_sync( FULL, radius, ( lane % per ) * G );
+        if ( lane / per == r )
+            my_radius = rv;
+    }
+    __syncwarp();
+    // the reference Jacobi, a target a lane; row 0 of the pseudo-inverse
+    // replaces V(:, 0) in the lane's column
+    Smem<M> sm{wsm, a.u_work, wsm + M * M * 32, lane, 32, ut, us};
+    if ( lane < cnt )
+    {
+#pragma unroll
+        for ( int p = 0; p < M; ++p )
+        {
+#pragma unroll
+            for ( int c = 0; c < M; ++c )
+                sm.u( p, c ) = ( p == c ) ? 1.0 : 0.0;
+            sm.v( p ) = p == 0 ? 1.0 : 0.0;
+        }
+        double row0[M];
+        dropped += jacobi_row0<M>( sm, row0, iters, jcap, a.status );
+#pragma unroll
+        for ( int p = 0; p < M; ++p )
+            sm.v( p ) = row0[p];
+    }
+    __syncwarp();
+    // computePolynomialCoefficients, G lanes a target
+    for ( int r = 0; r * per < cnt; ++r )
+    {
+        int const ti = r * per + lane / G;
+        double const radius = __shfl_sync( FULL, my_radius, ti & 31 );
+        if ( ti >= cnt )
+            continue;
+        int64_t const i = a.list[t.first + ti];
+        int64_t const b = a.offset[i];
+        int const len = a.offset[i + 1] - (int)b;
+        double const tx = a.tgt( i, 0 ), ty = a.tgt( i, 1 ), tz = a.tgt( i, 2 );
+        double row0[M];
+#pragma unroll
+        for ( int p = 0; p < M; ++p )
+            row0[p] = wsm[M * M * 32 + p * 32 + ti];
+        for ( int j = sub; j < len; j += G )
+        {
+            if ( (uint32_t)a.nb.ref( b + j ) >= (uint64_t)a.nb.src.n )
+                continue; // reported above
+            double sx, sy, sz;
+            a.nb.xyz( b + j, sx, sy, sz );
+            double const x = __dsub_rn( sx, tx ), y = __dsub_rn( sy, ty ), z = __dsub_rn( sz, tz );
+            double P[M];
+            basis_eval<M>( x, y, z, P );
+            double const dist =
+                __dsqrt_rn( __dadd_rn( __dadd_rn( __dmul_rn( x, x ), __dmul_rn( y, y ) ), __dmul_rn( z, z ) ) );
+            double const phi = rbf_eval<double>( rbf, dist / radius );
+            double acc = 0.0;
+#pragma unroll
+            for ( int p = 0; p < M; ++p )
+                acc = fma( row0[p], P[p], acc );
+            if ( a.coeff32 )
+                a.coeff32[b + j] = (float)( acc * phi );
+            else
+                a.coeff64[b + j] = acc * phi;
+        }
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__( BS_WARPS * 32, 1 ) k_batch_setup( BatchSetupArgs a )
+{
+    extern __shared__ double smem[];
+    int const lane = threadIdx.x & 31;
+    double *const wsm = smem + (size_t)( threadIdx.x >> 5 ) * BS_SLOT;
+    int64_t const ut = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t const us = (int64_t)gridDim.x * blockDim.x;
+    int64_t const t_end = a.t_end >= 0 ? a.t_end : *a.n_tasks;
+    unsigned iters = 0;
+    int dropped = 0;
+    for ( ;; )
+    {
+        unsigned c = 0;
+        if ( lane == 0 )
+            c = atomicAdd( a.counter, 1u );
+        int64_t const ti = a.t_begin + __shfl_sync( FULL, c, 0 );
+        if ( ti >= t_end )
+            break;
+        SetupTask const t = a.tasks[ti];
+        int const key = t.key;
+        int const basis = key / SETUP_PATHS / SETUP_RBFS, rbf = key / SETUP_PATHS % SETUP_RBFS;
+        int const G = a.force_lanes ? a.force_lanes : t.lanes;
+        if ( basis == DTK_CONSTANT3 )
+            setup_task<1>( a, t, rbf, G, wsm, ut, us, a.jcap[0], iters, dropped, lane );
+        else if ( basis == DTK_LINEAR3 )
+            setup_task<4>( a, t, rbf, G, wsm, ut, us, a.jcap[1], iters, dropped, lane );
+        else
+            setup_task<10>( a, t, rbf, G, wsm, ut, us, a.jcap[2], iters, dropped, lane );
+    }
+    unsigned long long it64 = iters, dr64 = dropped;
+    for ( int o = 16; o; o >>= 1 )
+    {
+        it64 += __shfl_xor_sync( FULL, it64, o );
+        dr64 += __shfl_xor_sync( FULL, dr64, o );
+    }
+    if ( lane == 0 )
+    {
+        if ( it64 )
+            atomicAdd( a.rotations, it64 );
+        if ( dr64 )
+            atomicAdd( a.underdetermined, dr64 );
+    }
+}
+
 template <int M, int G>
 void launch_split( SetupArgs const &a, int32_t const *targets, int64_t n, cudaStream_t s )
 {
@@ -803,6 +1016,28 @@ void setup_split( SetupArgs const &a, int32_t const *targets, int64_t n, int lan
         launch_split_basis<32>( a, targets, n, s );
     else
         launch_split_basis<8>( a, targets, n, s );
+}
+
+size_t batch_setup_smem()
+{
+    return (size_t)BS_WARPS * BS_SLOT * sizeof( double );
+}
+
+int64_t batch_setup_threads()
+{
+    return (int64_t)num_sms() * BS_WARPS * 32;
+}
+
+void batch_setup( BatchSetupArgs const &args, cudaStream_t s )
+{
+    BatchSetupArgs a = args;
+    a.jcap[0] = (unsigned)jacobi_cap( 1 );
+    a.jcap[1] = (unsigned)jacobi_cap( 4 );
+    a.jcap[2] = (unsigned)jacobi_cap( 10 );
+    ensure_dynamic_smem( k_batch_setup, batch_setup_smem() );
+    DTK_CUDA_OR_THROW( cudaMemsetAsync( a.counter, 0, sizeof( unsigned ), s ) );
+    k_batch_setup<<<(unsigned)num_sms(), BS_WARPS * 32, batch_setup_smem(), s>>>( a );
+    check_launch( "k_batch_setup" );
 }
 
 void svd_pinv_batched_work( int n, int64_t count, double const *a, double *pinv, double *work,

@@ -465,6 +465,34 @@ class MovingLeastSquaresBatch:
                                         1 if graph else 0,
                                         _stream(stream if stream is not None else self._stream)))
 
+    def resetup(self, source_points: torch.Tensor | None = None, target_points: torch.Tensor | None = None,
+                stream=None) -> None:
+        """Recompute the coefficients for new coordinates (packed like the
+        create's, same counts), keeping the create's neighbour rows; replays a
+        captured CUDA graph of the persistent setup when the point arrays are
+        the ones of the previous call.  None keeps the current points."""
+        src = self.source_points if source_points is None else source_points
+        tgt = self.target_points if target_points is None else target_points
+        for t, ref, what in ((src, self.source_points, "source_points"), (tgt, self.target_points, "target_points")):
+            _check_points(t, what)
+            if t.shape != ref.shape or not t.is_contiguous():
+                raise _capi.InvalidArgument(1, f"{what} must be contiguous of shape {tuple(ref.shape)}")
+        self.source_points, self.target_points = src, tgt
+        check(lib().dtk_mls_batch_resetup(self._h, src.data_ptr(), tgt.data_ptr(),
+                                          _stream(stream if stream is not None else self._stream)))
+
+    @property
+    def config(self) -> dict:
+        """The tuned configuration: lanes a target of the setup per row class,
+        lanes a row of the apply per length bin (non-empty bins), setup graph replays."""
+        sl = (C.c_int32 * 3)()
+        al = (C.c_int32 * 32)()
+        n = C.c_int64()
+        check(lib().dtk_mls_batch_get_config(self._h, sl, al, C.byref(n)))
+        return {"setup_lanes": {"knn_rows": sl[0], "rows_le_32": sl[1], "rows_gt_32": sl[2]},
+                "apply_lanes_by_bin": {f"<={1 << b}": al[b] for b in range(32) if al[b]},
+                "setup_graph_replays": n.value}
+
     def csr(self):
         """(offset, indices, coefficients) over all problems; indices are packed source indices."""
         off, idx, coeff = C.c_void_p(), C.c_void_p(), C.c_void_p()
@@ -600,6 +628,12 @@ def release_cached_memory() -> None:
     to 1/8 of a device's memory, so that repeated setups need not map memory
     again."""
     check(lib().dtk_release_cached_memory())
+
+
+def set_setup_lanes(rows_le_32: int = 0, rows_gt_32: int = 0) -> None:
+    """Fix the lanes a target of the batched setup's gather phases (powers of
+    two in [1, 32]) for the batches created afterwards; 0 = tuned by timing."""
+    check(lib().dtk_set_setup_lanes(int(rows_le_32), int(rows_gt_32)))
 
 
 def knn_search(source_points: torch.Tensor, target_points: torch.Tensor, k: int, stream=None):

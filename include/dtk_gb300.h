@@ -326,7 +326,11 @@ dtk_status dtk_svd_pinv_noalloc(int32_t n, int64_t count, const double *a,
  * [tgt_offsets[p], tgt_offsets[p+1]) of the packed row-major n x 3 arrays,
  * and options opts[p] (HOST arrays: src_offsets, tgt_offsets, opts).
  * The batch's CSR product is one global CSR over all targets with global
- * source indices. */
+ * source indices.  One search serves all problems; the setup is one
+ * persistent launch over tasks of 32 targets of one (basis, rbf) bucket
+ * (FP64 Jacobi rows; mixed-form kNN rows run the fused mixed kernel per
+ * bucket), with the lanes a target of its gather phases tuned by timing on a
+ * sample of the tasks at create (dtk_set_setup_lanes fixes them). */
 typedef struct dtk_mls_batch_s *dtk_mls_batch_handle;
 dtk_status dtk_mls_batch_create(int32_t n_problems, const dtk_mls_options *opts,
                                 const int64_t *src_offsets, const double *src,
@@ -338,6 +342,21 @@ dtk_status dtk_mls_batch_create(int32_t n_problems, const dtk_mls_options *opts,
 dtk_status dtk_mls_batch_apply(dtk_mls_batch_handle h, const double *src_values,
                                double *tgt_values, int32_t use_graph,
                                dtk_stream_t stream);
+/* Re-setup on new coordinates (same packed layout and counts), keeping the
+ * neighbour rows of the create: the coefficients are recomputed for the new
+ * points (the support radius from the row's farthest entry).  The statistics
+ * reset and the persistent setup launch are captured into a CUDA graph on the
+ * first call for a pair of point arrays and replayed on later calls with the
+ * same arrays.  Synchronous (reads the status).  With the create's points it
+ * reproduces the create's coefficients bit for bit. */
+dtk_status dtk_mls_batch_resetup(dtk_mls_batch_handle h, const double *src,
+                                 const double *tgt, dtk_stream_t stream);
+/* The chosen configuration: setup_lanes[3] = lanes a target per row class
+ * (kNN rows, rows up to 32, longer rows), apply_lanes[32] = lanes a row per
+ * length bin (0 for empty bins or before the first apply), and the number of
+ * setup graph replays so far.  Any pointer may be NULL. */
+dtk_status dtk_mls_batch_get_config(dtk_mls_batch_handle h, int32_t *setup_lanes,
+                                    int32_t *apply_lanes, int64_t *setup_graph_replays);
 dtk_status dtk_mls_batch_get_csr(dtk_mls_batch_handle h, const int32_t **offset,
                                  const int32_t **indices, const void **coeff,
                                  int64_t *nnz, int32_t *coeff_is_fp32);
@@ -357,6 +376,14 @@ dtk_status dtk_mls_batch_get_stage_times(dtk_mls_batch_handle h, float *search_m
  * caps: 200 m^2 + 2000 rotations, and the tree's node count in steps (more
  * than a search takes).  Negative values -> DTK_ERR_INVALID_ARG. */
 dtk_status dtk_set_loop_caps(int64_t jacobi_rotations, int64_t traversal_steps);
+
+/* Lanes a target in the gather phases of the persistent setup, for rows of
+ * up to 32 entries and for longer rows (powers of two in [1, 32]; 0 = tuned
+ * by timing, the default), for the batches created after it in this
+ * process.  The lane count sets the order of the moment sums, so fixing it
+ * makes the coefficients reproducible across processes.  Other values ->
+ * DTK_ERR_INVALID_ARG. */
+dtk_status dtk_set_setup_lanes(int32_t lanes_short, int32_t lanes_long);
 
 /* Last error message of the calling host thread (never NULL). */
 const char *dtk_last_error(void);

@@ -84,7 +84,8 @@ HANDLE_ENTRIES = ("dtk_mls_apply", "dtk_mls_apply_adjoint", "dtk_mls_apply_multi
                   "dtk_mls_get_sizes", "dtk_mls_underdetermined_count", "dtk_mls_get_stage_times",
                   "dtk_mls_get_search_times", "dtk_mls_get_rotation_count", "dtk_mls_export_size",
                   "dtk_mls_export", "dtk_nn_apply", "dtk_nn_apply_multi", "dtk_nn_get_indices",
-                  "dtk_mls_batch_apply", "dtk_mls_batch_get_csr", "dtk_mls_batch_get_stage_times")
+                  "dtk_mls_batch_apply", "dtk_mls_batch_get_csr", "dtk_mls_batch_get_stage_times",
+                  "dtk_mls_batch_resetup", "dtk_mls_batch_get_config")
 CREATE_ENTRIES = ("dtk_mls_import", "dtk_mls_transfer_host", "dtk_nn_create", "dtk_knn_search",
                   "dtk_mls_batch_create", "dtk_svd_pinv_noalloc", "dtk_mls_create_from_neighbors")
 
@@ -130,6 +131,13 @@ def test_create_from_neighbors_rejects_bad_arguments_before_device_work(dtk_lib)
     assert create(nb=None) == 1 and create(idx=None) == 1
     assert create(n_tgt=(1 << 31) // 4) == 1  # n_targets * row beyond int32 offsets
     assert b"DTK_REQUIRE" in dtk_lib.dtk_last_error()
+
+
+def test_setup_lanes_accept_powers_of_two_only(dtk_lib):
+    for bad in ((3, 8), (8, 64), (-1, 0), (0, 48)):
+        assert dtk_lib.dtk_set_setup_lanes(*bad) == 1
+    assert dtk_lib.dtk_set_setup_lanes(4, 16) == 0
+    assert dtk_lib.dtk_set_setup_lanes(0, 0) == 0  # back to tuning
 
 
 def test_svd_rejects_bad_sizes(dtk_lib):

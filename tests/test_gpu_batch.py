@@ -101,7 +101,10 @@ def radius_problems(n_problems=16, seed=5):
 
 def test_radius_batch_against_oracle_per_problem():
     problems = radius_problems()
-    b, vals, out, off, idx, coeff = run_batch(problems)
+    check_radius_batch(problems, *run_batch(problems))
+
+
+def check_radius_batch(problems, b, vals, out, off, idx, coeff):
     so, to = b.source_offsets, b.target_offsets
     lens = []
     for p, pr in enumerate(problems):
@@ -142,3 +145,71 @@ def test_batch_preconditions():
     with pytest.raises(dtk.InvalidArgument):
         b.apply(torch.zeros(49, dtype=torch.float64, device="cuda"),
                 torch.zeros(10, dtype=torch.float64, device="cuda"))
+
+
+def _per_problem_rows(off, idx, so, to, p):
+    """Problem p's rows in its own numbering: (offset from 0, local indices)."""
+    o = off[to[p]:to[p + 1] + 1]
+    return o - o[0], idx[o[0]:o[-1]] - so[p]
+
+
+@pytest.mark.parametrize("kind", ["radius", "knn", "knn_mixed"])
+def test_resetup_with_the_same_points_is_bitwise_and_replays_a_graph(kind):
+    problems = radius_problems(8) if kind == "radius" else knn_problems(seed=31)
+    b, vals, out, off, idx, coeff = run_batch(problems, precision="mixed" if kind == "knn_mixed" else "fp64")
+    for replay in range(3):  # capture, then replays
+        b.resetup()
+        _, idx2, c2 = b.csr()
+        assert np.array_equal(idx2.cpu().numpy(), idx)
+        assert np.array_equal(c2.double().cpu().numpy(), coeff), replay
+    assert b.config["setup_graph_replays"] == 3
+    y = torch.empty(b.target_offsets[-1], dtype=torch.float64, device="cuda")
+    b.apply(dev(vals), y)
+    assert np.array_equal(y.cpu().numpy(), out)
+
+
+def test_resetup_on_moved_points_matches_the_oracle_on_the_kept_rows():
+    problems = radius_problems(8, seed=9)
+    b, vals, out, off, idx, coeff = run_batch(problems)
+    so, to = b.source_offsets, b.target_offsets
+    rng = np.random.default_rng(4)
+    moved = [dict(pr, src=pr["src"] + rng.normal(0, 2e-3, pr["src"].shape),
+                  tgt=pr["tgt"] + rng.normal(0, 2e-3, pr["tgt"].shape)) for pr in problems]
+    b.resetup(dev(np.concatenate([m["src"] for m in moved])), dev(np.concatenate([m["tgt"] for m in moved])))
+    _, idx2, c2 = b.csr()
+    assert np.array_equal(idx2.cpu().numpy(), idx)  # the rows are kept
+    c2 = c2.cpu().numpy()
+    y = torch.empty(to[-1], dtype=torch.float64, device="cuda")
+    b.apply(dev(vals), y)
+    y = y.cpu().numpy()
+    for p, m in enumerate(moved):
+        o, li = _per_problem_rows(off, idx, so, to, p)
+        if o[-1] == 0:
+            continue
+        ref, _, _, _ = cpu.mls_coefficients(m["src"], m["tgt"], o, li, 1, m["basis"])
+        tc, tt = tolerances(m["src"], m["tgt"], o, li, 1, m["basis"], vals[so[p]:so[p + 1]], ref)
+        mine = c2[off[to[p]]:off[to[p + 1]]]
+        for i in range(len(o) - 1):
+            r_ = slice(o[i], o[i + 1])
+            if o[i + 1] > o[i]:
+                assert np.abs(mine[r_] - ref[r_]).max() <= tc * max(np.abs(ref[r_]).max(), 1e-300), (p, i)
+        want = cpu.apply(o, li, ref, vals[so[p]:so[p + 1]])
+        assert rel_l2(y[to[p]:to[p + 1]], want) <= tt, p
+
+
+def test_fixed_setup_lanes_agree_with_the_tuned_ones():
+    problems = radius_problems(8, seed=13)
+    try:
+        for lanes in ((1, 1), (2, 8), (8, 32)):
+            dtk.set_setup_lanes(*lanes)
+            b, vals, out, off, idx, coeff = run_batch(problems)
+            cfg = b.config["setup_lanes"]
+            assert (cfg["rows_le_32"], cfg["rows_gt_32"]) == lanes
+            check_radius_batch(problems, b, vals, out, off, idx, coeff)
+    finally:
+        dtk.set_setup_lanes(0, 0)
+    b, *_ = run_batch(problems)
+    cfg = b.config
+    assert cfg["setup_lanes"]["knn_rows"] == 1
+    assert cfg["setup_lanes"]["rows_le_32"] in (2, 4, 8) and cfg["setup_lanes"]["rows_gt_32"] in (8, 16, 32)
+    assert cfg["apply_lanes_by_bin"]  # tuned at the first apply
