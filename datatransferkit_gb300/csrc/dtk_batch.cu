@@ -200,6 +200,7 @@ BatchSetupArgs batch_args( SetupArgs const &a, SetupPlan &plan, double *u_work )
     b.tgt = a.tgt;
     b.offset = a.offset;
     b.list = plan.list.get();
+    b.n_list = plan.n;
     b.tasks = plan.tasks.get();
     b.n_tasks = plan.n_tasks.get();
     b.rows_sorted = a.rows_sorted;
@@ -314,14 +315,17 @@ void run_setup_plan( SetupArgs const &a, int precision, uint8_t const *basis_of_
         return;
     if ( !plan.u_work.get() )
         plan.u_work.allocate( (size_t)BS_MAX_M_SQ * batch_setup_threads(), s );
-    // the statistics counters collect the sample runs too: zeroed after them
+    // the tasks exist before any launch reads them (the tuner's samples
+    // too); refilled with the tuned lane counts.  The statistics counters
+    // collect the sample runs as well: zeroed after them
+    fill_setup_tasks( plan, s );
     if ( tune )
     {
         tune_setup( a, plan, plan.u_work.get(), s );
         DTK_CUDA_OR_THROW( cudaMemsetAsync( a.underdetermined, 0, sizeof( unsigned long long ), s ) );
         DTK_CUDA_OR_THROW( cudaMemsetAsync( a.rotations, 0, sizeof( unsigned long long ), s ) );
+        fill_setup_tasks( plan, s );
     }
-    fill_setup_tasks( plan, s );
     run_planned_setup( a, plan, s );
 }
 

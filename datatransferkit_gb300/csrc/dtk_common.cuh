@@ -250,7 +250,8 @@ enum : unsigned
     DEV_STACK_OVERFLOW = 2u,
     DEV_BAD_INDEX = 4u,
     DEV_NONFINITE_SOURCE = 8u, // a source coordinate is NaN or infinite
-    DEV_NONFINITE_TARGET = 16u // a target coordinate is NaN or infinite
+    DEV_NONFINITE_TARGET = 16u, // a target coordinate is NaN or infinite
+    DEV_BAD_TASK = 32u          // a task of the persistent setup out of range (skipped)
 };
 
 // NaN or infinite: all exponent bits set (integer pipe).
@@ -568,6 +569,7 @@ struct BatchSetupArgs
     PointsView tgt;
     int32_t const *offset;
     uint32_t const *list; // targets in bucket order
+    int64_t n_list;       // its length (the tasks are checked against it)
     SetupTask const *tasks;
     int64_t const *n_tasks; // task count (device), read when t_end < 0
     int64_t t_begin = 0, t_end = -1;

@@ -87,24 +87,42 @@ __device__ __forceinline__ void half_angle( double y, double x, double &c, doubl
     }
 }
 
+// The rotation pair (c a - s b, s a + c b) with the multiply-adds spelled
+// out, so that every kernel that runs the Jacobi rounds alike (the compiler
+// is free to contract a*b - c*d either way, and may choose differently in
+// different kernels).
+__device__ __forceinline__ double rot_minus( double c, double s, double a, double b )
+{
+    return __fma_rn( c, a, -__dmul_rn( s, b ) );
+}
+__device__ __forceinline__ double rot_plus( double c, double s, double a, double b )
+{
+    return __fma_rn( s, a, __dmul_rn( c, b ) );
+}
+// x0 y0 + x1 y1 with the same spelled-out rounding
+__device__ __forceinline__ double dot2( double x0, double y0, double x1, double y1 )
+{
+    return __fma_rn( x0, y0, __dmul_rn( x1, y1 ) );
+}
+
 // 2x2 SVD rotations of DTK_DetailsSVDImpl.hpp:119-162 and the sr sign rule
 // of :260-263.
 __device__ __forceinline__ void svd_2x2( double a, double b, double c, double d, double &cl,
                                          double &sl, double &cr, double &sr )
 {
     // A A^T and A^T A in the element order of SVDImpl.hpp:109-117,123-126
-    double const p00 = a * a + b * b, p01 = a * c + b * d, p10 = c * a + d * b,
-                 p11 = c * c + d * d;
-    double const q00 = a * a + c * c, q01 = a * b + c * d, q10 = b * a + d * c,
-                 q11 = b * b + d * d;
+    double const p00 = dot2( a, a, b, b ), p01 = dot2( a, c, b, d ), p10 = dot2( c, a, d, b ),
+                 p11 = dot2( c, c, d, d );
+    double const q00 = dot2( a, a, c, c ), q01 = dot2( a, b, c, d ), q10 = dot2( b, a, d, c ),
+                 q11 = dot2( b, b, d, d );
     double sphi, cphi, sth, cth;
     half_angle( p01 + p10, p00 - p11, cphi, sphi );
     half_angle( q01 + q10, q00 - q11, cth, sth );
     // S = U^T A W diagonal signs (SVDImpl.hpp:149-159)
-    double const aw00 = a * cth + b * sth, aw01 = a * -sth + b * cth;
-    double const aw10 = c * cth + d * sth, aw11 = c * -sth + d * cth;
-    double const s00 = cphi * aw00 + sphi * aw10;
-    double const s11 = -sphi * aw01 + cphi * aw11;
+    double const aw00 = dot2( a, cth, b, sth ), aw01 = dot2( a, -sth, b, cth );
+    double const aw10 = dot2( c, cth, d, sth ), aw11 = dot2( c, -sth, d, cth );
+    double const s00 = dot2( cphi, aw00, sphi, aw10 );
+    double const s11 = dot2( -sphi, aw01, cphi, aw11 );
     double const c0 = copysign( 1.0, s00 ), c1 = copysign( 1.0, s11 );
     // V = W diag(c0, c1)
     double const v00 = cth * c0, v01 = -sth * c1, v10 = sth * c0;
@@ -244,30 +262,30 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
         for ( int j = 0; j < M; ++j )
         {
             double const a = s.e( p, j ), b = s.e( q, j );
-            s.e( p, j ) = cl * a - sl * b;
-            s.e( q, j ) = sl * a + cl * b;
+            s.e( p, j ) = rot_minus( cl, sl, a, b );
+            s.e( q, j ) = rot_plus( cl, sl, a, b );
         }
         // givens_right(E, cr, sr, p, q)
 #pragma unroll
         for ( int j = 0; j < M; ++j )
         {
             double const a = s.e( j, p ), b = s.e( j, q );
-            s.e( j, p ) = cr * a - sr * b;
-            s.e( j, q ) = sr * a + cr * b;
+            s.e( j, p ) = rot_minus( cr, sr, a, b );
+            s.e( j, q ) = rot_plus( cr, sr, a, b );
         }
         // givens_right(U, cl, sl, p, q)
 #pragma unroll
         for ( int j = 0; j < M; ++j )
         {
             double const a = up[j], b = uq[j];
-            s.u( j, p ) = cl * a - sl * b;
-            s.u( j, q ) = sl * a + cl * b;
+            s.u( j, p ) = rot_minus( cl, sl, a, b );
+            s.u( j, q ) = rot_plus( cl, sl, a, b );
         }
         // givens_left(V, cr, sr, p, q), column 0 only
         {
             double const a = s.v( p ), b = s.v( q );
-            s.v( p ) = cr * a - sr * b;
-            s.v( q ) = sr * a + cr * b;
+            s.v( p ) = rot_minus( cr, sr, a, b );
+            s.v( q ) = rot_plus( cr, sr, a, b );
         }
     }
     iters += it;
@@ -494,26 +512,26 @@ __global__ void k_svd_general( int n, int64_t count, double const *a, double *pi
         for ( int j = 0; j < n; ++j )
         {
             double const x = E[p * n + j], y = E[q * n + j];
-            E[p * n + j] = cl * x - sl * y;
-            E[q * n + j] = sl * x + cl * y;
+            E[p * n + j] = rot_minus( cl, sl, x, y );
+            E[q * n + j] = rot_plus( cl, sl, x, y );
         }
         for ( int j = 0; j < n; ++j )
         {
             double const x = E[j * n + p], y = E[j * n + q];
-            E[j * n + p] = cr * x - sr * y;
-            E[j * n + q] = sr * x + cr * y;
+            E[j * n + p] = rot_minus( cr, sr, x, y );
+            E[j * n + q] = rot_plus( cr, sr, x, y );
         }
         for ( int j = 0; j < n; ++j )
         {
             double const x = U[j * n + p], y = U[j * n + q];
-            U[j * n + p] = cl * x - sl * y;
-            U[j * n + q] = sl * x + cl * y;
+            U[j * n + p] = rot_minus( cl, sl, x, y );
+            U[j * n + q] = rot_plus( cl, sl, x, y );
         }
         for ( int j = 0; j < n; ++j )
         {
             double const x = V[p * n + j], y = V[q * n + j];
-            V[p * n + j] = cr * x - sr * y;
-            V[q * n + j] = sr * x + cr * y;
+            V[p * n + j] = rot_minus( cr, sr, x, y );
+            V[q * n + j] = rot_plus( cr, sr, x, y );
         }
     }
     int dropped = 0;
@@ -915,6 +933,14 @@ __global__ void __launch_bounds__( BS_WARPS * 32, 1 ) k_batch_setup( BatchSetupA
         int const key = t.key;
         int const basis = key / SETUP_PATHS / SETUP_RBFS, rbf = key / SETUP_PATHS % SETUP_RBFS;
         int const G = a.force_lanes ? a.force_lanes : t.lanes;
+        // a task out of range is reported and skipped, never followed
+        if ( key >= SETUP_KEYS || t.count < 1 || t.count > 32 || G < 1 || G > 32 || ( G & ( G - 1 ) ) ||
+             t.first < 0 || (int64_t)t.first + t.count > a.n_list )
+        {
+            if ( lane == 0 )
+                atomicOr( a.status, DEV_BAD_TASK );
+            continue;
+        }
         if ( basis == DTK_CONSTANT3 )
             setup_task<1>( a, t, rbf, G, wsm, ut, us, a.jcap[0], iters, dropped, lane );
         else if ( basis == DTK_LINEAR3 )
