@@ -7,10 +7,15 @@
 // a query only enters nodes and points of its own problem.  Targets are
 // processed in problem-major Morton order.  The setup is planned on the
 // device: a stable key sort splits the processing order into buckets of
-// (basis, rbf, path).  kNN rows run the fused one-thread-per-target kernel of
-// the requested precision; radius rows (0 to thousands of entries) run the
-// split FP64 path, with 8 lanes per target for rows of up to 32 entries and
-// 32 lanes beyond, so that no thread walks a long row alone.
+// (basis, rbf, path), and a layout kernel cuts the buckets into tasks of 32
+// targets (longest rows first).  One persistent launch runs every task: a
+// warp gathers its targets' rows with G lanes a target (1 for kNN rows, the
+// single operator's arithmetic; for radius rows, 0 to thousands of entries,
+// G is tuned by timing candidates on a sample of the tasks at create), then
+// runs the reference Jacobi one target a lane.  Mixed-form kNN rows run the
+// fused mixed kernel per bucket instead.  The plan is kept: a re-setup on
+// new coordinates with the same rows is the persistent launch alone,
+// captured into a CUDA graph and replayed.
 //
 // Apply is one persistent launch over a schedule of warp tasks.  Rows are
 // binned by length (bin b holds rows of at most 2^b entries); a task is up to
@@ -215,8 +220,9 @@ BatchSetupArgs batch_args( SetupArgs const &a, SetupPlan &plan, double *u_work )
 }
 
 // Times the lane counts of paths 1 and 2 on a sample of their tasks (the
-// first few waves of each), keeps the fastest per path, and caches it by
-// (path, precision, size class).  One synchronisation reads the task layout.
+// first wave of each: one task a resident warp; the faster of two runs per
+// candidate), keeps the fastest per path, and caches it by (path,
+// precision, size class).  One synchronisation reads the task layout.
 void tune_setup( SetupArgs const &a, SetupPlan &plan, double *u_work, cudaStream_t s )
 {
     int fixed[N_PATH] = {0, 0, 0};
@@ -269,7 +275,7 @@ void tune_setup( SetupArgs const &a, SetupPlan &plan, double *u_work, cudaStream
                 continue;
             }
         }
-        int64_t const sample = std::min<int64_t>( count, 2 * wave );
+        int64_t const sample = std::min<int64_t>( count, wave ); // one task a resident warp
         int const cands[2][3] = {{2, 4, 8}, {8, 16, 32}};
         float best = 3.4e38f;
         int best_lanes = plan.lanes[path];
@@ -279,8 +285,8 @@ void tune_setup( SetupArgs const &a, SetupPlan &plan, double *u_work, cudaStream
             b.t_begin = t0;
             b.t_end = t0 + sample;
             b.force_lanes = G;
-            float ms[3];
-            for ( int rep = 0; rep < 3; ++rep )
+            float ms[2];
+            for ( int rep = 0; rep < 2; ++rep )
             {
                 DTK_CUDA_OR_THROW( cudaEventRecord( e0, s ) );
                 batch_setup( b, s );
@@ -288,10 +294,10 @@ void tune_setup( SetupArgs const &a, SetupPlan &plan, double *u_work, cudaStream
                 DTK_CUDA_OR_THROW( cudaEventSynchronize( e1 ) );
                 DTK_CUDA_OR_THROW( cudaEventElapsedTime( &ms[rep], e0, e1 ) );
             }
-            std::sort( ms, ms + 3 );
-            if ( ms[1] < best )
+            float const t = std::min( ms[0], ms[1] );
+            if ( t < best )
             {
-                best = ms[1];
+                best = t;
                 best_lanes = G;
             }
         }

@@ -324,8 +324,8 @@ std::unique_ptr<dtk_mls_s> create_impl( Geometry const &g, dtk_mls_options const
         a.coeff32 = h->coeff32.get();
     }
     if ( g.radius_mode )
-        // radius rows are uneven (0 to thousands of entries): the split
-        // setup with 8 or 32 lanes per target by row length
+        // radius rows are uneven (0 to thousands of entries): the persistent
+        // setup with 8 or 32 lanes a target for the gathers, by row length
         run_setup_plan( a, g.opts.precision, nullptr, nullptr, nullptr, true, s );
     else if ( g.opts.precision == DTK_FP64 )
         setup_fp64( a, s );

@@ -544,11 +544,6 @@ struct SetupArgs
 };
 void setup_fp64( SetupArgs const &a, cudaStream_t s );
 void setup_mixed( SetupArgs const &a, cudaStream_t s );
-// Split setup for uneven rows: FP64 moments and coefficients with `lanes`
-// (8 or 32) lanes per target around one thread per target for the reference
-// Jacobi, for the n targets listed in `targets`; writes coeff64 or (rounded)
-// coeff32.
-void setup_split( SetupArgs const &a, int32_t const *targets, int64_t n, int lanes, cudaStream_t s );
 constexpr int FUSED_MAX_ROW = 32; // longest row the fused one-thread-per-target kernels take
 
 // Persistent batched setup (FP64 Jacobi): the targets of a bucketed list in

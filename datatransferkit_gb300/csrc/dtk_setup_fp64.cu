@@ -555,194 +555,6 @@ __global__ void k_svd_general( int n, int64_t count, double const *a, double *pi
 }
 
 // ---------------------------------------------------------------------------
-// Split setup for uneven rows (radius neighbourhoods of 0 to tens of
-// thousands of sources): the same FP64 stages in three kernels so that no
-// single thread walks a long row.  G lanes per target assemble the moments
-// (the lanes split the neighbours; the NU sums are combined by shuffles
-// within the group) and later the coefficients; one thread per target runs
-// the reference Jacobi in between.  Work area per target: NU moments +
-// radius + M row-0 values (doubles).
-// ---------------------------------------------------------------------------
-template <int M, int G>
-__global__ void __launch_bounds__( 128 )
-    k_split_moments( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
-                     int32_t const *targets, int64_t n, int rbf, double *work, unsigned *status )
-{
-    constexpr int NU = M * ( M + 1 ) / 2;
-    constexpr int STRIDE = NU + 1 + M;
-    int const sub = threadIdx.x & ( G - 1 );
-    int64_t const w = ( blockIdx.x * (int64_t)blockDim.x + threadIdx.x ) / G;
-    bool const active = w < n;
-    int64_t const i = active ? targets[w] : 0;
-    int64_t const b = active ? offset[i] : 0;
-    int len = active ? offset[i + 1] - (int)b : 0;
-    double const tx = active ? tgt( i, 0 ) : 0.0, ty = active ? tgt( i, 1 ) : 0.0,
-                 tz = active ? tgt( i, 2 ) : 0.0;
-    double d2max = 0.0;
-    bool bad = false;
-    for ( int j = sub; j < len; j += G )
-    {
-        int64_t const sj = idx[b + j];
-        if ( (uint64_t)sj >= (uint64_t)src.n )
-        {
-            bad = true;
-            continue;
-        }
-        d2max = fmax( d2max, dist2_rn( src( sj, 0 ), src( sj, 1 ), src( sj, 2 ), tx, ty, tz ) );
-    }
-#pragma unroll
-    for ( int o = G / 2; o; o >>= 1 )
-    {
-        d2max = fmax( d2max, __shfl_xor_sync( FULL, d2max, o ) );
-        bad |= __shfl_xor_sync( FULL, (int)bad, o ) != 0;
-    }
-    if ( bad )
-    {
-        if ( sub == 0 )
-            atomicOr( status, DEV_BAD_INDEX );
-        len = 0; // the row is not read again
-    }
-    double distance = 10. * DBL_EPSILON;
-    double const dmax = __dsqrt_rn( d2max );
-    if ( dmax > distance )
-        distance = dmax;
-    double const radius = 1.1 * distance;
-    double A[NU];
-#pragma unroll
-    for ( int u = 0; u < NU; ++u )
-        A[u] = 0.0;
-    for ( int j = sub; j < len; j += G )
-    {
-        int64_t const sj = idx[b + j];
-        double const x = __dsub_rn( src( sj, 0 ), tx ), y = __dsub_rn( src( sj, 1 ), ty ),
-                     z = __dsub_rn( src( sj, 2 ), tz );
-        double P[M];
-        basis_eval<M>( x, y, z, P );
-        double const dist =
-            __dsqrt_rn( __dadd_rn( __dadd_rn( __dmul_rn( x, x ), __dmul_rn( y, y ) ), __dmul_rn( z, z ) ) );
-        double const phi = rbf_eval<double>( rbf, dist / radius );
-        int o = 0;
-#pragma unroll
-        for ( int a = 0; a < M; ++a )
-        {
-            double const pa = P[a] * phi;
-#pragma unroll
-            for ( int c = a; c < M; ++c, ++o )
-                A[o] = fma( pa, P[c], A[o] );
-        }
-    }
-#pragma unroll
-    for ( int u = 0; u < NU; ++u )
-#pragma unroll
-        for ( int o = G / 2; o; o >>= 1 )
-            A[u] += __shfl_xor_sync( FULL, A[u], o );
-    if ( active && sub == 0 )
-    {
-        double *out = work + w * STRIDE;
-#pragma unroll
-        for ( int u = 0; u < NU; ++u )
-            out[u] = A[u];
-        out[NU] = radius;
-    }
-}
-
-template <int M>
-__global__ void __launch_bounds__( FP64_THREADS, 1 )
-    k_split_jacobi( int64_t n, double *work, unsigned long long *under_count,
-                    unsigned long long *rot_count, unsigned *status, unsigned jcap, double *u_work )
-{
-    constexpr int NU = M * ( M + 1 ) / 2;
-    constexpr int STRIDE = NU + 1 + M;
-    extern __shared__ double smem[];
-    int const nt = blockDim.x;
-    int64_t const T = (int64_t)gridDim.x * nt;
-    int64_t const tid = blockIdx.x * (int64_t)nt + threadIdx.x;
-    Smem<M> s{smem, u_work, smem + M * M * nt, (int)threadIdx.x, nt, tid, T};
-    unsigned iters = 0;
-    int dropped = 0;
-    for ( int64_t g = tid; g - threadIdx.x < n; g += T ) // block-uniform trip count
-    if ( g < n )
-    {
-        double *rec = work + g * STRIDE;
-        int o = 0;
-        for ( int a = 0; a < M; ++a )
-            for ( int c = a; c < M; ++c, ++o )
-            {
-                s.e( a, c ) = rec[o];
-                s.e( c, a ) = rec[o];
-            }
-        for ( int a = 0; a < M; ++a )
-        {
-            for ( int c = 0; c < M; ++c )
-                s.u( a, c ) = ( a == c ) ? 1.0 : 0.0;
-            s.v( a ) = a == 0 ? 1.0 : 0.0;
-        }
-        double row0[M];
-        dropped += jacobi_row0<M>( s, row0, iters, jcap, status );
-        for ( int a = 0; a < M; ++a )
-            rec[NU + 1 + a] = row0[a];
-    }
-    unsigned long long it64 = iters, dr64 = dropped;
-    for ( int o = 16; o; o >>= 1 )
-    {
-        it64 += __shfl_xor_sync( FULL, it64, o );
-        dr64 += __shfl_xor_sync( FULL, dr64, o );
-    }
-    if ( ( threadIdx.x & 31 ) == 0 )
-    {
-        if ( it64 )
-            atomicAdd( rot_count, it64 );
-        if ( dr64 )
-            atomicAdd( under_count, dr64 );
-    }
-}
-
-template <int M, int G>
-__global__ void __launch_bounds__( 128 )
-    k_split_coeffs( PointsView src, PointsView tgt, int32_t const *offset, int32_t const *idx,
-                    int32_t const *targets, int64_t n, int rbf, double const *work, double *coeff64,
-                    float *coeff32 )
-{
-    constexpr int NU = M * ( M + 1 ) / 2;
-    constexpr int STRIDE = NU + 1 + M;
-    int const sub = threadIdx.x & ( G - 1 );
-    int64_t const w = ( blockIdx.x * (int64_t)blockDim.x + threadIdx.x ) / G;
-    if ( w >= n )
-        return; // no shuffles below
-    int64_t const i = targets[w];
-    int64_t const b = offset[i];
-    int const len = offset[i + 1] - (int)b;
-    double const tx = tgt( i, 0 ), ty = tgt( i, 1 ), tz = tgt( i, 2 );
-    double const *rec = work + w * STRIDE;
-    double const radius = rec[NU];
-    double row0[M];
-#pragma unroll
-    for ( int a = 0; a < M; ++a )
-        row0[a] = rec[NU + 1 + a];
-    for ( int j = sub; j < len; j += G )
-    {
-        int64_t const sj = idx[b + j];
-        if ( (uint64_t)sj >= (uint64_t)src.n )
-            continue; // reported by the moments kernel
-        double const x = __dsub_rn( src( sj, 0 ), tx ), y = __dsub_rn( src( sj, 1 ), ty ),
-                     z = __dsub_rn( src( sj, 2 ), tz );
-        double P[M];
-        basis_eval<M>( x, y, z, P );
-        double const dist =
-            __dsqrt_rn( __dadd_rn( __dadd_rn( __dmul_rn( x, x ), __dmul_rn( y, y ) ), __dmul_rn( z, z ) ) );
-        double const phi = rbf_eval<double>( rbf, dist / radius );
-        double acc = 0.0;
-#pragma unroll
-        for ( int a = 0; a < M; ++a )
-            acc = fma( row0[a], P[a], acc );
-        if ( coeff32 )
-            coeff32[b + j] = (float)( acc * phi );
-        else
-            coeff64[b + j] = acc * phi;
-    }
-}
-
-// ---------------------------------------------------------------------------
 // Persistent batched setup: every FP64-Jacobi target of a batch, of any
 // (basis, rbf) and row length, in one launch.  A warp takes tasks from a
 // counter; a task is up to 32 targets of one bucket (same basis and rbf) and
@@ -963,43 +775,6 @@ __global__ void __launch_bounds__( BS_WARPS * 32, 1 ) k_batch_setup( BatchSetupA
     }
 }
 
-template <int M, int G>
-void launch_split( SetupArgs const &a, int32_t const *targets, int64_t n, cudaStream_t s )
-{
-    constexpr int NU = M * ( M + 1 ) / 2;
-    DeviceBuffer<double> work( n * ( NU + 1 + M ), s );
-    unsigned const gblocks = (unsigned)( ( n * G + 127 ) / 128 );
-    k_split_moments<M, G><<<gblocks, 128, 0, s>>>( a.src, a.tgt, a.offset, a.idx, targets, n, a.rbf,
-                                                    work.get(), a.status );
-    check_launch( "k_split_moments" );
-    JacobiGrid const jg = jacobi_grid<M>( n );
-    ensure_dynamic_smem( k_split_jacobi<M>, jg.smem );
-    DeviceBuffer<double> u_work( (size_t)M * M * jg.threads * jg.blocks, s );
-    k_split_jacobi<M><<<jg.blocks, jg.threads, jg.smem, s>>>( n, work.get(), a.underdetermined, a.rotations,
-                                                             a.status, (unsigned)jacobi_cap( M ), u_work.get() );
-    check_launch( "k_split_jacobi" );
-    k_split_coeffs<M, G><<<gblocks, 128, 0, s>>>( a.src, a.tgt, a.offset, a.idx, targets, n, a.rbf,
-                                                   work.get(), a.coeff64, a.coeff32 );
-    check_launch( "k_split_coeffs" );
-}
-
-template <int G>
-void launch_split_basis( SetupArgs const &a, int32_t const *targets, int64_t n, cudaStream_t s )
-{
-    switch ( a.basis )
-    {
-    case DTK_CONSTANT3:
-        launch_split<1, G>( a, targets, n, s );
-        break;
-    case DTK_LINEAR3:
-        launch_split<4, G>( a, targets, n, s );
-        break;
-    default:
-        launch_split<10, G>( a, targets, n, s );
-        break;
-    }
-}
-
 template <int M>
 void launch_fp64( SetupArgs const &a, cudaStream_t s )
 {
@@ -1032,16 +807,6 @@ void setup_fp64( SetupArgs const &a, cudaStream_t s )
         launch_fp64<10>( a, s );
         break;
     }
-}
-
-void setup_split( SetupArgs const &a, int32_t const *targets, int64_t n, int lanes, cudaStream_t s )
-{
-    if ( n == 0 )
-        return;
-    if ( lanes >= 32 )
-        launch_split_basis<32>( a, targets, n, s );
-    else
-        launch_split_basis<8>( a, targets, n, s );
 }
 
 size_t batch_setup_smem()
