@@ -133,6 +133,29 @@ __device__ __forceinline__ void svd_2x2( double a, double b, double c, double d,
     sr = ( g01 == g10 ) ? -v01 : v01;
 }
 
+// svd_2x2 of a symmetric block [[a, b], [b, d]]: A A^T and A^T A are then
+// formed by the same operations, so the two half-angles are one, and the
+// rotations come out bit for bit as svd_2x2( a, b, b, d ) gives them.
+__device__ __forceinline__ void svd_2x2_sym( double a, double b, double d, double &cl, double &sl,
+                                             double &cr, double &sr )
+{
+    double const q00 = dot2( a, a, b, b ), q01 = dot2( a, b, b, d ), q10 = dot2( b, a, d, b ),
+                 q11 = dot2( b, b, d, d );
+    double sth, cth;
+    half_angle( q01 + q10, q00 - q11, cth, sth );
+    double const aw00 = dot2( a, cth, b, sth ), aw01 = dot2( a, -sth, b, cth );
+    double const aw10 = dot2( b, cth, d, sth ), aw11 = dot2( b, -sth, d, cth );
+    double const s00 = dot2( cth, aw00, sth, aw10 );
+    double const s11 = dot2( -sth, aw01, cth, aw11 );
+    double const c0 = copysign( 1.0, s00 ), c1 = copysign( 1.0, s11 );
+    double const v00 = cth * c0, v01 = -sth * c1, v10 = sth * c0;
+    cl = cth;
+    sl = -sth;
+    cr = v00;
+    int const g01 = ( v01 > 0 ) - ( v01 < 0 ), g10 = ( v10 > 0 ) - ( v10 < 0 );
+    sr = ( g01 == g10 ) ? -v01 : v01;
+}
+
 // |x| as an ordered integer (non-negative doubles order like their bits).
 __device__ __forceinline__ long long abs_bits( double x )
 {
@@ -174,18 +197,43 @@ JacobiGrid jacobi_grid( int64_t n )
 
 // Runs DTK's Jacobi on the thread's E; on return row0 holds row 0 of the
 // pseudo-inverse.  Returns 1 if a singular value was truncated.
+//
+// E enters exactly symmetric (the moments fill both triangles from one sum).
+// For a non-degenerate E (no zero on the diagonal), while the rotations keep
+// it so -- the pivot block is then symmetric, the
+// left and right rotations of its 2x2 SVD come out equal (a positive
+// semi-definite block), and the right rotation of the off-block entries of
+// columns p and q computes the left rotation's values of rows p and q --
+// the columns are copied from the rows instead of recomputed, the 2x2 SVD
+// solves one half-angle instead of two (their inputs are equal), the scan
+// reads the upper triangle (the first largest |E_ij| in row-major order is
+// there), and the block's off-diagonal pair, which the two rotations leave
+// as two different residuals of the same zero, takes the upper one's value.
+// That last step is the only departure from the reference's arithmetic (a
+// rounding residual); at the first rotation whose left and right parts
+// differ (an indefinite block, as negative Buhmann weights give) the loop
+// falls back to the reference's full row and column updates.
 template <int M>
 __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, unsigned cap,
                             unsigned *status )
 {
     double const tol = DBL_EPSILON;
     unsigned it = 0;
+    // a basis function that vanishes on every neighbour (collinear or
+    // coplanar rows) leaves a zero on the diagonal: such degenerate systems
+    // keep the reference's updates throughout, since their truncation
+    // decisions rest on rounding residuals
+    bool sym = true;
+#pragma unroll
+    for ( int k = 0; k < M; ++k )
+        sym = sym && s.e( k, k ) != 0.0;
     while ( true )
     {
         // Fused scan: first largest |E_ij| (integer compare of |bits|) and
         // FP32 bounds on the off-diagonal sum of squares from the exponents
         // alone: 4^e <= x^2 < 4^(e+1) for x in [2^e, 2^(e+1)).  Rows loop
-        // (not unrolled) to keep the kernel's code small.
+        // (not unrolled) to keep the kernel's code small.  A symmetric E
+        // counts its upper triangle twice.
         float lower = 0.f, upper = 0.f;
         bool huge = false, special = false;
         long long best = -1;
@@ -196,7 +244,8 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
 #pragma unroll
             for ( int j = 0; j < M; ++j )
             {
-                long long const ab = j == i ? -2 : abs_bits( s.e( i, j ) );
+                bool const skip = j == i || ( sym && j < i );
+                long long const ab = skip ? -2 : abs_bits( s.e( i, j ) );
                 if ( ab > best )
                 {
                     best = ab;
@@ -209,12 +258,18 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
                 bool const mid = e >= -62 && e <= 62;
                 lower += mid ? __int_as_float( ( 2 * e + 127 ) << 23 ) : 0.f;
                 upper += mid ? __int_as_float( ( 2 * e + 129 ) << 23 )
-                             : ( e < -62 && j != i ? 4.70197740328915e-38f : 0.f ); // 2^-124
+                             : ( e < -62 && !skip ? 4.70197740328915e-38f : 0.f ); // 2^-124
             }
+        }
+        if ( sym )
+        {
+            lower *= 2.f;
+            upper *= 2.f;
         }
         // Stop test of the reference, sqrt(sum) > DBL_EPSILON, decided by the
         // bounds unless they straddle DBL_EPSILON^2 = 2^-104; then the FP64
-        // row-major sum of squares as the reference forms it.
+        // row-major sum of squares as the reference forms it (twice the upper
+        // triangle's for a symmetric E).
         constexpr float tol2 = 4.930380657631324e-32f; // 2^-104 exactly
         bool go;
         if ( !special && ( huge || lower > tol2 * 1.0009765625f ) )
@@ -228,8 +283,10 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
             for ( int i = 0; i < M; ++i )
 #pragma unroll
                 for ( int j = 0; j < M; ++j )
-                    if ( i != j )
+                    if ( i != j && !( sym && j < i ) )
                         acc = fma( s.e( i, j ), s.e( i, j ), acc );
+            if ( sym )
+                acc *= 2.0;
             go = sqrt( acc ) > tol;
         }
         if ( !go )
@@ -256,22 +313,54 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
             uq[j] = s.u( j, q );
         }
         double cl, sl, cr, sr;
-        svd_2x2( s.e( p, p ), s.e( p, q ), s.e( q, p ), s.e( q, q ), cl, sl, cr, sr );
-        // givens_left(E, cl, sl, p, q)
-#pragma unroll
-        for ( int j = 0; j < M; ++j )
+        double const bpp = s.e( p, p ), bpq = s.e( p, q ), bqp = s.e( q, p ), bqq = s.e( q, q );
+        if ( sym )
+            svd_2x2_sym( bpp, bpq, bqq, cl, sl, cr, sr );
+        else
+            svd_2x2( bpp, bpq, bqp, bqq, cl, sl, cr, sr );
+        sym = sym && cr == cl && sr == sl;
+        if ( sym )
         {
-            double const a = s.e( p, j ), b = s.e( q, j );
-            s.e( p, j ) = rot_minus( cl, sl, a, b );
-            s.e( q, j ) = rot_plus( cl, sl, a, b );
+            // rows p and q by the left rotation, columns p and q off the
+            // block copied from them, the block by the right rotation
+#pragma unroll
+            for ( int j = 0; j < M; ++j )
+            {
+                if ( j == p || j == q )
+                    continue;
+                double const a = s.e( p, j ), b = s.e( q, j );
+                double const x = rot_minus( cl, sl, a, b ), y = rot_plus( cl, sl, a, b );
+                s.e( p, j ) = x;
+                s.e( q, j ) = y;
+                s.e( j, p ) = x;
+                s.e( j, q ) = y;
+            }
+            double const lpp = rot_minus( cl, sl, bpp, bqp ), lpq = rot_minus( cl, sl, bpq, bqq );
+            double const lqp = rot_plus( cl, sl, bpp, bqp ), lqq = rot_plus( cl, sl, bpq, bqq );
+            double const opq = rot_plus( cr, sr, lpp, lpq );
+            s.e( p, p ) = rot_minus( cr, sr, lpp, lpq );
+            s.e( p, q ) = opq;
+            s.e( q, p ) = opq;
+            s.e( q, q ) = rot_plus( cr, sr, lqp, lqq );
         }
-        // givens_right(E, cr, sr, p, q)
-#pragma unroll
-        for ( int j = 0; j < M; ++j )
+        else
         {
-            double const a = s.e( j, p ), b = s.e( j, q );
-            s.e( j, p ) = rot_minus( cr, sr, a, b );
-            s.e( j, q ) = rot_plus( cr, sr, a, b );
+            // givens_left(E, cl, sl, p, q)
+#pragma unroll
+            for ( int j = 0; j < M; ++j )
+            {
+                double const a = s.e( p, j ), b = s.e( q, j );
+                s.e( p, j ) = rot_minus( cl, sl, a, b );
+                s.e( q, j ) = rot_plus( cl, sl, a, b );
+            }
+            // givens_right(E, cr, sr, p, q)
+#pragma unroll
+            for ( int j = 0; j < M; ++j )
+            {
+                double const a = s.e( j, p ), b = s.e( j, q );
+                s.e( j, p ) = rot_minus( cr, sr, a, b );
+                s.e( j, q ) = rot_plus( cr, sr, a, b );
+            }
         }
         // givens_right(U, cl, sl, p, q)
 #pragma unroll
