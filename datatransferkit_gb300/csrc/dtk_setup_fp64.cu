@@ -238,33 +238,43 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
         bool huge = false, special = false;
         long long best = -1;
         int p = 0, q = 1;
-#pragma unroll 1
-        for ( int i = 0; i < M; ++i )
-        {
-#pragma unroll
-            for ( int j = 0; j < M; ++j )
+        auto visit = [&]( int i, int j ) {
+            long long const ab = abs_bits( s.e( i, j ) );
+            if ( ab > best )
             {
-                bool const skip = j == i || ( sym && j < i );
-                long long const ab = skip ? -2 : abs_bits( s.e( i, j ) );
-                if ( ab > best )
-                {
-                    best = ab;
-                    p = i;
-                    q = j;
-                }
-                int const e = (int)( ab >> 52 ) - 1023; // -1023 for zero/subnormal
-                special |= e == 1024;                   // Inf/NaN: decide exactly
-                huge |= e > 62 && e < 1024;
-                bool const mid = e >= -62 && e <= 62;
-                lower += mid ? __int_as_float( ( 2 * e + 127 ) << 23 ) : 0.f;
-                upper += mid ? __int_as_float( ( 2 * e + 129 ) << 23 )
-                             : ( e < -62 && !skip ? 4.70197740328915e-38f : 0.f ); // 2^-124
+                best = ab;
+                p = i;
+                q = j;
             }
-        }
+            int const e = (int)( ab >> 52 ) - 1023; // -1023 for zero/subnormal
+            special |= e == 1024;                   // Inf/NaN: decide exactly
+            huge |= e > 62 && e < 1024;
+            bool const mid = e >= -62 && e <= 62;
+            lower += mid ? __int_as_float( ( 2 * e + 127 ) << 23 ) : 0.f;
+            upper += mid ? __int_as_float( ( 2 * e + 129 ) << 23 )
+                         : ( e < -62 ? 4.70197740328915e-38f : 0.f ); // 2^-124
+        };
         if ( sym )
         {
+            // the upper triangle in row-major order, unrolled
+#pragma unroll
+            for ( int i = 0; i < M; ++i )
+#pragma unroll
+                for ( int j = i + 1; j < M; ++j )
+                    visit( i, j );
             lower *= 2.f;
             upper *= 2.f;
+        }
+        else
+        {
+#pragma unroll 1
+            for ( int i = 0; i < M; ++i )
+            {
+#pragma unroll
+                for ( int j = 0; j < M; ++j )
+                    if ( j != i )
+                        visit( i, j );
+            }
         }
         // Stop test of the reference, sqrt(sum) > DBL_EPSILON, decided by the
         // bounds unless they straddle DBL_EPSILON^2 = 2^-104; then the FP64
