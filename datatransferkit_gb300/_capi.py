@@ -29,6 +29,7 @@ EXPORTED = [
     "dtk_mls_export_size", "dtk_mls_export", "dtk_mls_import", "dtk_release_cached_memory",
     "dtk_mls_transfer_host", "dtk_set_loop_caps", "dtk_stream_synchronize", "dtk_mls_create_from_neighbors",
     "dtk_mls_batch_resetup", "dtk_mls_batch_get_config", "dtk_set_setup_lanes",
+    "dtk_knn_search_d2", "dtk_points_bounds", "dtk_points_pack", "dtk_gather_points", "dtk_gather_values",
 ]
 
 
@@ -101,6 +102,11 @@ def _declare(L):
     L.dtk_set_loop_caps.argtypes = [_i64, _i64]
     L.dtk_stream_synchronize.argtypes = [_vp]
     L.dtk_mls_batch_resetup.argtypes = [_vp, _vp, _vp, _vp]
+    L.dtk_knn_search_d2.argtypes = [_vp, _i64, _i64, _i64, _vp, _i64, _i64, _i64, C.c_int32, _vp, _vp, _vp]
+    L.dtk_points_bounds.argtypes = [_vp, _i64, _i64, _i64, _vp, _vp]
+    L.dtk_points_pack.argtypes = [_vp, _i64, _i64, _i64, _vp, _vp]
+    L.dtk_gather_points.argtypes = [_vp, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _vp]
+    L.dtk_gather_values.argtypes = [_vp, _i64, _vp, _i64, _vp, _vp]
     L.dtk_mls_batch_get_config.argtypes = [_vp, _vp, _vp, _vp]
     L.dtk_set_setup_lanes.argtypes = [C.c_int32, C.c_int32]
     L.dtk_mls_create_from_neighbors.argtypes = [C.POINTER(Options), _vp, _i64, _i64, _i64, C.c_int32, _vp, _vp,

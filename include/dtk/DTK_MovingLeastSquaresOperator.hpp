@@ -25,16 +25,21 @@
  * apply returns after the target values are written, like the reference's
  * apply, which ends in Kokkos::deep_copy (DTK_MovingLeastSquaresOperator_def.hpp:140);
  * MlsOptions::asynchronous leaves it queued on the operator's stream instead.
- * The communicator must have one rank (MPI_COMM_SELF): with <mpi.h>
- * included first its size is checked, otherwise any communicator value is
- * taken as one rank.
+ * Communicators: MPI_Comm (with <mpi.h> included first) or any type with
+ * rank(), size(), allgather() and alltoallv() (DTK_DistributedSearch.hpp);
+ * with more than one rank the constructor and apply are collective and run
+ * the distributed search and value fetch (kNN rows only).  Any other
+ * communicator value is taken as one rank.  The header needs the CUDA
+ * runtime's headers (cuda_runtime.h) for the multi-rank path.
  */
 #ifndef DTK_GB300_MOVING_LEAST_SQUARES_OPERATOR_HPP
 #define DTK_GB300_MOVING_LEAST_SQUARES_OPERATOR_HPP
 
 #include "../dtk_gb300.h"
+#include "DTK_DistributedSearch.hpp"
 
 #include <cmath>
+#include <functional>
 #include <cstddef>
 #include <cstdint>
 #include <memory>
@@ -313,18 +318,10 @@ struct MlsOptions
 
 namespace Details
 {
-#ifdef MPI_VERSION
-inline int comm_size( MPI_Comm comm )
-{
-    int s = 1;
-    MPI_Comm_size( comm, &s );
-    return s;
-}
-#endif
 template <typename Comm>
-int comm_size( Comm const & )
+int comm_size( Comm const &comm )
 {
-    return 1;
+    return CommTraits<Comm>::size( comm );
 }
 } // namespace Details
 
@@ -370,6 +367,39 @@ class MovingLeastSquaresOperator : public PointCloudOperator<DeviceType>
         o.radius = ext.radius;
         o.precision = ext.precision;
         o.comm_size = Details::comm_size( comm );
+        if constexpr ( Details::CommTraits<Comm>::exchange )
+            if ( o.comm_size > 1 )
+            {
+                // the distributed search and fetch of the reference's MPI
+                // operator (DTK_MovingLeastSquaresOperator_def.hpp:47-67)
+                if ( ext.radius > 0.0 )
+                    throw DataTransferKitException( "DTK_ERR_UNSUPPORTED: the distributed operator takes kNN rows" );
+                int const k = ext.k ? ext.k : PolynomialBasis::size;
+                if ( k > 32 )
+                    throw DataTransferKitException( "DTK_ERR_UNSUPPORTED: kNN search supports k <= 32" );
+                std::shared_ptr<Details::DistributedOperator> d;
+                try
+                {
+                    d = Details::distributed_setup(
+                        comm, o,
+                        Details::PointsArg{reinterpret_cast<double const *>( source_points.data() ),
+                                           (int64_t)source_points.extent( 0 ), (int64_t)source_points.stride( 0 ),
+                                           (int64_t)source_points.stride( 1 )},
+                        Details::PointsArg{reinterpret_cast<double const *>( target_points.data() ),
+                                           (int64_t)target_points.extent( 0 ), (int64_t)target_points.stride( 0 ),
+                                           (int64_t)target_points.stride( 1 )},
+                        k, reinterpret_cast<cudaStream_t>( _stream ) );
+                }
+                catch ( std::exception const &e )
+                {
+                    throw DataTransferKitException( e.what() );
+                }
+                _handle = d->handle;
+                _dist_apply = [comm, d]( double const *sv, double *tv ) {
+                    Details::distributed_apply( comm, *d, sv, tv );
+                };
+                return;
+            }
         dtk_mls_handle h = nullptr;
         Details::check( dtk_mls_create(
             &o, reinterpret_cast<double const *>( source_points.data() ),
@@ -390,6 +420,21 @@ class MovingLeastSquaresOperator : public PointCloudOperator<DeviceType>
         if ( (std::size_t)target_values.extent( 0 ) != _n_target_points )
             throw DataTransferKitException(
                 "DTK_REQUIRE( target_values.extent( 0 ) == _offset.extent( 0 ) - 1 )" );
+        if ( _dist_apply )
+        {
+            try
+            {
+                _dist_apply( reinterpret_cast<double const *>( source_values.data() ),
+                             const_cast<double *>( reinterpret_cast<double const *>( target_values.data() ) ) );
+            }
+            catch ( std::exception const &e )
+            {
+                throw DataTransferKitException( e.what() );
+            }
+            if ( !_asynchronous )
+                Details::check( dtk_stream_synchronize( _stream ) );
+            return;
+        }
         Details::check( dtk_mls_apply( _handle.get(),
                                        reinterpret_cast<double const *>( source_values.data() ),
                                        (int64_t)source_values.extent( 0 ),
@@ -419,6 +464,8 @@ class MovingLeastSquaresOperator : public PointCloudOperator<DeviceType>
     template <typename SourceValues, typename TargetValues>
     void apply_fields( SourceValues const &source_values, TargetValues const &target_values ) const
     {
+        if ( _dist_apply )
+            throw DataTransferKitException( "DTK_ERR_UNSUPPORTED: rank-2 fields on one rank only" );
         if ( source_values.extent( 1 ) != target_values.extent( 1 ) )
             throw DataTransferKitException(
                 "DTK_REQUIRE( source_values.extent( 1 ) == target_values.extent( 1 ) )" );
@@ -445,6 +492,7 @@ class MovingLeastSquaresOperator : public PointCloudOperator<DeviceType>
     dtk_stream_t _stream;
     bool _asynchronous;
     std::shared_ptr<struct dtk_mls_s> _handle;
+    std::function<void( double const *, double * )> _dist_apply; // set with more than one rank
 };
 
 } // namespace DataTransferKit

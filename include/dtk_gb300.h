@@ -237,6 +237,38 @@ dtk_status dtk_knn_search(const double *src, int64_t n_src,
                           int32_t k, int32_t *offset, int32_t *indices,
                           dtk_stream_t stream);
 
+/* ---- device steps of a distributed operator (the exchange is the caller's) ----
+ * A multi-rank host side (the C++ drop-in over an MPI-like communicator, the
+ * Python operator over torch.distributed) runs the reference's distributed
+ * search and fetch (DTK_MovingLeastSquaresOperator_def.hpp:47-67,133-134;
+ * DTK_DetailsNearestNeighborOperatorImpl.hpp:47-192) with these and
+ * dtk_mls_create_from_neighbors; all arrays are device arrays unless named
+ * _host.
+ * dtk_knn_search_d2: the rows of dtk_knn_search (min(k, n_src) entries a
+ *   target, ascending by (d2, index)) and each entry's d2, (dx*dx + dy*dy)
+ *   + dz*dz in FP64 with separately rounded operations.  Synchronous.
+ * dtk_points_bounds: the box of a cloud, box_host = (min x, y, z, max x, y, z);
+ *   (+inf, -inf) for an empty cloud.  Synchronous.
+ * dtk_points_pack: a strided cloud copied to a row-major n x 3 array.
+ * dtk_gather_points: out[e] = the point indices[e] names: source indices[e]
+ *   when below n_src, else row indices[e] - n_src of `extra` (row-major); an
+ *   index outside both -> DTK_ERR_INVALID_ARG.  Synchronous.
+ * dtk_gather_values: out[i] = values[indices[i]]; an index outside [0, n) ->
+ *   DTK_ERR_INVALID_ARG.  Synchronous. */
+dtk_status dtk_knn_search_d2(const double *src, int64_t n_src, int64_t src_pt_stride,
+                             int64_t src_dim_stride, const double *tgt, int64_t n_tgt,
+                             int64_t tgt_pt_stride, int64_t tgt_dim_stride, int32_t k,
+                             int32_t *indices, double *d2, dtk_stream_t stream);
+dtk_status dtk_points_bounds(const double *pts, int64_t n, int64_t pt_stride, int64_t dim_stride,
+                             double *box_host, dtk_stream_t stream);
+dtk_status dtk_points_pack(const double *pts, int64_t n, int64_t pt_stride, int64_t dim_stride,
+                           double *out, dtk_stream_t stream);
+dtk_status dtk_gather_points(const double *src, int64_t n_src, int64_t src_pt_stride,
+                             int64_t src_dim_stride, const double *extra, int64_t n_extra,
+                             const int32_t *indices, int64_t nnz, double *out, dtk_stream_t stream);
+dtk_status dtk_gather_values(const double *values, int64_t n, const int32_t *indices, int64_t m,
+                             double *out, dtk_stream_t stream);
+
 /* ---- the operator product on disk and on the wire (extension) ----
  * The CSR that create produces (offset, source indices, coefficients, the
  * members of DTK_MovingLeastSquaresOperator_decl.hpp:56-62) as a flat

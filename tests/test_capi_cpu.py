@@ -87,7 +87,8 @@ HANDLE_ENTRIES = ("dtk_mls_apply", "dtk_mls_apply_adjoint", "dtk_mls_apply_multi
                   "dtk_mls_batch_apply", "dtk_mls_batch_get_csr", "dtk_mls_batch_get_stage_times",
                   "dtk_mls_batch_resetup", "dtk_mls_batch_get_config")
 CREATE_ENTRIES = ("dtk_mls_import", "dtk_mls_transfer_host", "dtk_nn_create", "dtk_knn_search",
-                  "dtk_mls_batch_create", "dtk_svd_pinv_noalloc", "dtk_mls_create_from_neighbors")
+                  "dtk_mls_batch_create", "dtk_svd_pinv_noalloc", "dtk_mls_create_from_neighbors",
+                  "dtk_knn_search_d2", "dtk_points_bounds")
 
 
 def _null_args(fn):
