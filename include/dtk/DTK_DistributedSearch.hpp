@@ -215,13 +215,16 @@ struct DistributedOperator
     DevArray<double> fetched, send_values;         // [own | remote] values; the values sent
     std::vector<double> send_host, recv_host;
     std::vector<int64_t> global_rows;              // (n_tgt x row) global source index of every entry
+    DevArray<int32_t> slots;                       // the entries' positions in `fetched` (nearest neighbour)
     int64_t queries_sent = 0;
 };
 
 // The distributed setup (collective).  k: neighbours per target (<= 32).
+// With `mls`, the MLS operator of the rows; without, only the rows' positions
+// in the fetched values (the nearest-neighbour operator, k = 1).
 template <typename Comm>
 std::unique_ptr<DistributedOperator> distributed_setup( Comm const &comm, dtk_mls_options opts, PointsArg src,
-                                                        PointsArg tgt, int k, cudaStream_t stream )
+                                                        PointsArg tgt, int k, cudaStream_t stream, bool mls = true )
 {
     using T = CommTraits<Comm>;
     int const world = T::size( comm ), rank = T::rank( comm );
@@ -468,17 +471,20 @@ std::unique_ptr<DistributedOperator> distributed_setup( Comm const &comm, dtk_ml
 
     // 6. the operator of the rows
     int64_t const nnz = (int64_t)slots.size();
-    DevArray<int32_t> slots_d( nnz, stream );
-    DevArray<double> extra_d( remote_xyz.size(), stream ), nb_d( 3 * nnz, stream );
-    slots_d.upload( slots.data(), slots.size() );
-    extra_d.upload( remote_xyz.data(), remote_xyz.size() );
-    dtk_check( dtk_gather_points( src.data, n_loc, src.ps, src.ds, extra_d.get(), op->n_remote, slots_d.get(), nnz,
-                                  nb_d.get(), ds ) );
-    opts.comm_size = 1;
-    dtk_mls_handle h = nullptr;
-    dtk_check( dtk_mls_create_from_neighbors( &opts, tgt.data, n_tgt, tgt.ps, tgt.ds, row, nb_d.get(), slots_d.get(),
-                                              n_loc + op->n_remote, ds, &h ) );
-    op->handle.reset( h, []( dtk_mls_handle p ) { dtk_mls_destroy( p ); } );
+    op->slots.resize( nnz, stream );
+    op->slots.upload( slots.data(), slots.size() );
+    if ( mls )
+    {
+        DevArray<double> extra_d( remote_xyz.size(), stream ), nb_d( 3 * nnz, stream );
+        extra_d.upload( remote_xyz.data(), remote_xyz.size() );
+        dtk_check( dtk_gather_points( src.data, n_loc, src.ps, src.ds, extra_d.get(), op->n_remote,
+                                      op->slots.get(), nnz, nb_d.get(), ds ) );
+        opts.comm_size = 1;
+        dtk_mls_handle h = nullptr;
+        dtk_check( dtk_mls_create_from_neighbors( &opts, tgt.data, n_tgt, tgt.ps, tgt.ds, row, nb_d.get(),
+                                                  op->slots.get(), n_loc + op->n_remote, ds, &h ) );
+        op->handle.reset( h, []( dtk_mls_handle p ) { dtk_mls_destroy( p ); } );
+    }
 
     // 7. the fetch plan: each owner learns which of its values to send, in
     //    the order asked (remote is ascending, so grouped by owner)
@@ -515,11 +521,10 @@ std::unique_ptr<DistributedOperator> distributed_setup( Comm const &comm, dtk_ml
     return op;
 }
 
-// The distributed apply (collective): target_values = the rows' transfer of
-// all ranks' source values; this rank's values stay on the device.
+// The value fetch (collective): op.fetched = [this rank's values | the
+// remote values its rows use]; this rank's values stay on the device.
 template <typename Comm>
-void distributed_apply( Comm const &comm, DistributedOperator &op, double const *source_values,
-                        double *target_values )
+void distributed_fetch( Comm const &comm, DistributedOperator &op, double const *source_values )
 {
     using T = CommTraits<Comm>;
     int const world = T::size( comm );
@@ -543,8 +548,28 @@ void distributed_apply( Comm const &comm, DistributedOperator &op, double const 
     }
     T::alltoallv( comm, op.send_host.data(), sb, op.recv_host.data(), rb );
     op.fetched.upload( op.recv_host.data(), op.recv_host.size(), op.n_loc );
+}
+
+// The distributed MLS apply (collective): target_values = the rows'
+// transfer of all ranks' source values.
+template <typename Comm>
+void distributed_apply( Comm const &comm, DistributedOperator &op, double const *source_values,
+                        double *target_values )
+{
+    distributed_fetch( comm, op, source_values );
     dtk_check( dtk_mls_apply( op.handle.get(), op.fetched.get(), op.n_loc + op.n_remote, target_values, op.n_tgt,
-                              ds ) );
+                              reinterpret_cast<dtk_stream_t>( op.stream ) ) );
+}
+
+// The distributed nearest-neighbour apply (collective): every target takes
+// the value of its nearest source on any rank.
+template <typename Comm>
+void distributed_apply_nearest( Comm const &comm, DistributedOperator &op, double const *source_values,
+                                double *target_values )
+{
+    distributed_fetch( comm, op, source_values );
+    dtk_check( dtk_gather_values( op.fetched.get(), op.n_loc + op.n_remote, op.slots.get(), op.n_tgt,
+                                  target_values, reinterpret_cast<dtk_stream_t>( op.stream ) ) );
 }
 
 } // namespace Details

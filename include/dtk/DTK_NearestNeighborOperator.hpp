@@ -9,7 +9,9 @@
  *
  * Views, communicator, exceptions and the synchronous apply (the reference's
  * ends in Kokkos::deep_copy, DTK_NearestNeighborOperator_def.hpp:85) as in
- * DTK_MovingLeastSquaresOperator.hpp.
+ * DTK_MovingLeastSquaresOperator.hpp; with a communicator of several ranks
+ * the nearest source is searched on every rank and its value fetched
+ * (rank-1 values), DTK_DistributedSearch.hpp.
  * The nearest source of a target is the smallest (d^2, source index): ties
  * go to the smaller source index.
  */
@@ -36,6 +38,35 @@ class NearestNeighborOperator : public PointCloudOperator<DeviceType>
         , _stream( stream )
         , _asynchronous( asynchronous )
     {
+        if constexpr ( Details::CommTraits<Comm>::exchange )
+            if ( Details::comm_size( comm ) > 1 )
+            {
+                if ( source_points.extent( 1 ) != 3 || target_points.extent( 1 ) != 3 )
+                    throw DataTransferKitException( "DTK_REQUIRE( source_points.extent_int( 1 ) == 3 )" );
+                dtk_mls_options o;
+                dtk_mls_default_options( &o );
+                std::shared_ptr<Details::DistributedOperator> d;
+                try
+                {
+                    d = Details::distributed_setup(
+                        comm, o,
+                        Details::PointsArg{reinterpret_cast<double const *>( source_points.data() ),
+                                           (int64_t)source_points.extent( 0 ), (int64_t)source_points.stride( 0 ),
+                                           (int64_t)source_points.stride( 1 )},
+                        Details::PointsArg{reinterpret_cast<double const *>( target_points.data() ),
+                                           (int64_t)target_points.extent( 0 ), (int64_t)target_points.stride( 0 ),
+                                           (int64_t)target_points.stride( 1 )},
+                        1, reinterpret_cast<cudaStream_t>( _stream ), false );
+                }
+                catch ( std::exception const &e )
+                {
+                    throw DataTransferKitException( e.what() );
+                }
+                _dist_apply = [comm, d]( double const *sv, double *tv ) {
+                    Details::distributed_apply_nearest( comm, *d, sv, tv );
+                };
+                return;
+            }
         dtk_nn_handle h = nullptr;
         Details::check( dtk_nn_create(
             reinterpret_cast<double const *>( source_points.data() ), (int64_t)source_points.extent( 0 ),
@@ -54,6 +85,23 @@ class NearestNeighborOperator : public PointCloudOperator<DeviceType>
             throw DataTransferKitException( "DTK_REQUIRE( _indices.extent( 0 ) == target_values.extent( 0 ) )" );
         if ( (std::size_t)source_values.extent( 0 ) != _size )
             throw DataTransferKitException( "DTK_REQUIRE( _size == source_values.extent_int( 0 ) )" );
+        if ( _dist_apply )
+        {
+            if ( source_values.extent( 1 ) != 1 || target_values.extent( 1 ) != 1 )
+                throw DataTransferKitException( "DTK_ERR_UNSUPPORTED: rank-2 values on one rank only" );
+            try
+            {
+                _dist_apply( reinterpret_cast<double const *>( source_values.data() ),
+                             const_cast<double *>( reinterpret_cast<double const *>( target_values.data() ) ) );
+            }
+            catch ( std::exception const &e )
+            {
+                throw DataTransferKitException( e.what() );
+            }
+            if ( !_asynchronous )
+                Details::check( dtk_stream_synchronize( _stream ) );
+            return;
+        }
         Details::check( dtk_nn_apply_multi(
             _handle.get(), reinterpret_cast<double const *>( source_values.data() ),
             (int64_t)source_values.extent( 0 ), (int64_t)source_values.extent( 1 ),
@@ -80,13 +128,14 @@ class NearestNeighborOperator : public PointCloudOperator<DeviceType>
         apply_values( source_values, target_values );
     }
 
-    dtk_nn_handle handle() const { return _handle.get(); }
+    dtk_nn_handle handle() const { return _handle.get(); } // null with more than one rank
 
   private:
     std::size_t _size, _n_target_points;
     dtk_stream_t _stream;
     bool _asynchronous;
     std::shared_ptr<struct dtk_nn_s> _handle;
+    std::function<void( double const *, double * )> _dist_apply; // set with more than one rank
 };
 
 } // namespace DataTransferKit

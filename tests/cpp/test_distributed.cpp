@@ -5,10 +5,13 @@
 // own sources and targets; its results must equal the one-rank operator over
 // the union of the clouds in rank order, and the reference's grid case
 // (tstMeshfreeOperators.cpp:226-300: 40x40 sources at z = rank, the target on
-// a source) must reproduce its polynomial to 1e-14.  No kernel of one rank
-// waits on the other's: the exchange runs on the host between the steps.
+// a source) must reproduce its polynomial to 1e-14.  NearestNeighborOperator
+// over both ranks must copy the one-rank operator's nearest values exactly.
+// No kernel of one rank waits on the other's: the exchange runs on the host
+// between the steps.
 // Prints "PASS <n>" on success; exits non-zero on the first failure.
 #include <dtk/DTK_MovingLeastSquaresOperator.hpp>
+#include <dtk/DTK_NearestNeighborOperator.hpp>
 
 #include <cuda_runtime.h>
 
@@ -238,6 +241,32 @@ void rank_main( Shared *sh, int r )
         MlsOptions ext;
         ext.k = 10;
         compare_with_union<Quad>( comm, stream, srcs, tgt, ext, 1e-13 );
+    }
+    {
+        // nearest neighbour over both ranks: exactly the one-rank operator's values
+        std::vector<std::vector<Pt>> srcs = {cloud( 5000, 61, 0.5, 0.0 ), cloud( 3000, 62, 0.5, 0.5 )};
+        std::vector<Pt> tgt = cloud( 2000, 70 + r, 1.0, 0.0 );
+        std::vector<Pt> const &src = srcs[r];
+        Buf bs( 3 * src.size() ), bt( 3 * tgt.size() ), bv( src.size() ), bo( tgt.size() );
+        std::vector<double> sv;
+        for ( auto &p : src )
+            sv.push_back( field( p ) );
+        NearestNeighborOperator<CudaDevice> nn( comm, points( bs, src ), points( bt, tgt ),
+                                                reinterpret_cast<dtk_stream_t>( stream ) );
+        nn.apply( values( bv, sv ), out( bo ) );
+        std::vector<Pt> uni;
+        std::vector<double> uv;
+        for ( auto const &c : srcs )
+            for ( auto &p : c )
+            {
+                uni.push_back( p );
+                uv.push_back( field( p ) );
+            }
+        Buf us( 3 * uni.size() ), ub( uni.size() ), uo( tgt.size() );
+        NearestNeighborOperator<CudaDevice> one( 0, points( us, uni ), points( bt, tgt ),
+                                                 reinterpret_cast<dtk_stream_t>( stream ) );
+        one.apply( values( ub, uv ), out( uo ) );
+        CHECK( host( bo ) == host( uo ) );
     }
     {
         // the reference's grid case across the ranks (ties at the k-th neighbour)
