@@ -15,9 +15,9 @@ Mirrors (paths inside the DataTransferKit project):
 Each rank holds its own sources and targets (CUDA tensors).  A source's
 global index is its rank's offset (the sources of the lower ranks) plus its
 local index, so a row ordered by (d2, global index) is the row a one-rank
-operator gives over the rank-ordered union of the clouds; d2 is
-(dx*dx + dy*dy) + dz*dz in FP64 with separately rounded operations, as the
-library's search computes it.
+operator gives over the rank-ordered union of the clouds; every d2 is the
+one the library's search computes ((dx*dx + dy*dy) + dz*dz in FP64 with
+separately rounded operations, dtk_knn_search_d2).
 
 The search (ArborX's DistributedTree is a third-party dependency, not in the
 reference's tree; this restates its contract, exact kNN over all ranks):
@@ -47,8 +47,9 @@ import torch
 import torch.distributed as dist
 
 from . import _capi
+from ._capi import check, lib
 from .operators import (Linear, MovingLeastSquaresOperator, MultivariatePolynomialBasis, PointCloudOperator,
-                        Wendland, _check_points, _multi_rank, knn_search)
+                        Wendland, _check_points, _multi_rank, _stream)
 
 __all__ = ["DistributedMovingLeastSquaresOperator", "DistributedNearestNeighborOperator", "fetch",
            "is_multi_rank", "distributed_knn"]
@@ -93,31 +94,29 @@ class _Comm:
         return r.to(home)
 
 
-def _d2(points: torch.Tensor, tgt: torch.Tensor) -> torch.Tensor:
-    """(dx*dx + dy*dy) + dz*dz of points (n, r, 3) to their targets (n, 3), each
-    operation rounded on its own."""
-    d = torch.sub(points, tgt.unsqueeze(1))
-    dx, dy, dz = d[..., 0], d[..., 1], d[..., 2]
-    return torch.add(torch.add(torch.mul(dx, dx), torch.mul(dy, dy)), torch.mul(dz, dz))
-
-
 def _box_d2(tgt: torch.Tensor, lo: torch.Tensor, hi: torch.Tensor) -> torch.Tensor:
-    """Rounded squared distance of each target to the box [lo, hi], never above
-    the rounded d2 of a point in the box."""
+    """Squared distance of each target to the box [lo, hi], less a relative
+    2^-40: never above the d2 the search computes for a point in the box."""
     g = torch.clamp(torch.maximum(torch.sub(lo, tgt), torch.sub(tgt, hi)), min=0.0)
     gx, gy, gz = g[:, 0], g[:, 1], g[:, 2]
-    return torch.add(torch.add(torch.mul(gx, gx), torch.mul(gy, gy)), torch.mul(gz, gz))
+    d2 = torch.add(torch.add(torch.mul(gx, gx), torch.mul(gy, gy)), torch.mul(gz, gz))
+    return d2 * (1.0 - 2.0 ** -40)
 
 
 class _LibrarySearch:
-    """The library's kNN (rows ascending by (d2, index))."""
+    """The library's kNN: (indices, d2) of rows ascending by (d2, index)."""
 
-    def knn(self, src: torch.Tensor, tgt: torch.Tensor, k: int) -> torch.Tensor:
+    def knn(self, src: torch.Tensor, tgt: torch.Tensor, k: int):
         row = min(int(k), src.shape[0])
-        if tgt.shape[0] == 0 or row == 0:
-            return torch.empty((tgt.shape[0], row), dtype=torch.int64, device=tgt.device)
-        _, idx = knn_search(src, tgt, row)
-        return idx.view(tgt.shape[0], row).to(torch.int64)
+        n = tgt.shape[0]
+        idx = torch.empty((n, row), dtype=torch.int32, device=tgt.device)
+        d2 = torch.empty((n, row), dtype=torch.float64, device=tgt.device)
+        if n and row:
+            tgt = tgt.contiguous()
+            check(lib().dtk_knn_search_d2(src.data_ptr(), src.shape[0], src.stride(0), src.stride(1),
+                                          tgt.data_ptr(), n, tgt.stride(0), tgt.stride(1), row,
+                                          idx.data_ptr(), d2.data_ptr(), _stream(None)))
+        return idx.to(torch.int64), d2
 
 
 class _Rows:
@@ -154,10 +153,14 @@ def distributed_knn(comm: _Comm, src: torch.Tensor, tgt: torch.Tensor, k: int, s
     boxes = comm.all_gather(box.to(torch.float64))
 
     # 2. the local rows and their bounds
-    idx = search.knn(src, tgt, row) if n_loc else torch.empty((n_tgt, 0), dtype=torch.int64, device=dev)
+    if n_loc:
+        idx, d2 = search.knn(src, tgt, row)
+        pts = src[idx]
+    else:
+        idx = torch.empty((n_tgt, 0), dtype=torch.int64, device=dev)
+        d2 = torch.empty((n_tgt, 0), dtype=torch.float64, device=dev)
+        pts = torch.empty((n_tgt, 0, 3), dtype=torch.float64, device=dev)
     row_l = idx.shape[1]
-    pts = src[idx] if n_loc else torch.empty((n_tgt, 0, 3), dtype=torch.float64, device=dev)
-    d2 = _d2(pts, tgt)
     gid = idx + int(first[comm.rank])
     if row_l == row and row_l > 0:
         bound = d2[:, -1]
@@ -180,9 +183,9 @@ def distributed_knn(comm: _Comm, src: torch.Tensor, tgt: torch.Tensor, k: int, s
     # 4. this rank's answers: (d2, x, y, z) and the global index per entry
     row_o = min(row, n_loc)
     if asked.shape[0] and row_o:
-        a_idx = search.knn(src, asked, row)
+        a_idx, a_d2 = search.knn(src, asked, row)
         a_pts = src[a_idx]
-        answer = torch.cat([_d2(a_pts, asked).unsqueeze(2), a_pts], 2).reshape(-1, 4)
+        answer = torch.cat([a_d2.unsqueeze(2), a_pts], 2).reshape(-1, 4)
         a_gid = (a_idx + int(first[comm.rank])).reshape(-1)
     else:
         answer = torch.empty((0, 4), dtype=torch.float64, device=dev)

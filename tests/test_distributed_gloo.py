@@ -37,15 +37,17 @@ def _free_port():
 
 
 class _OracleSearch:
-    """kNN rows by (d2, index) from the oracle."""
+    """kNN rows by (d2, index) and their d2, from the oracle."""
 
     def knn(self, src, tgt, k):
         from oracle import cpu
         row = min(int(k), src.shape[0])
         if tgt.shape[0] == 0 or row == 0:
-            return torch.empty((tgt.shape[0], row), dtype=torch.int64)
-        _, idx, _ = cpu.knn(src.numpy(), tgt.numpy(), k)
-        return torch.from_numpy(idx.astype(np.int64)).view(tgt.shape[0], row)
+            return (torch.empty((tgt.shape[0], row), dtype=torch.int64),
+                    torch.empty((tgt.shape[0], row), dtype=torch.float64))
+        _, idx, d2 = cpu.knn(src.numpy(), tgt.numpy(), k)
+        return (torch.from_numpy(idx.astype(np.int64)).view(tgt.shape[0], row),
+                torch.from_numpy(d2).view(tgt.shape[0], row))
 
 
 class _OracleRows:
