@@ -35,6 +35,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -101,22 +102,30 @@ struct CommTraits<MPI_Comm, void>
         MPI_Comm_size( c, &s );
         return s;
     }
+    // MPI counts and displacements are int: larger exchanges are refused
+    static int count( int64_t v )
+    {
+        if ( v < 0 || v > INT_MAX )
+            throw std::length_error( "DTK distributed: an exchange exceeds MPI's int byte counts" );
+        return (int)v;
+    }
     static void allgather( MPI_Comm c, void const *send, int64_t bytes, void *recv )
     {
-        MPI_Allgather( const_cast<void *>( send ), (int)bytes, MPI_BYTE, recv, (int)bytes, MPI_BYTE, c );
+        MPI_Allgather( const_cast<void *>( send ), count( bytes ), MPI_BYTE, recv, count( bytes ), MPI_BYTE, c );
     }
     static void alltoallv( MPI_Comm c, void const *send, std::vector<int64_t> const &send_bytes, void *recv,
                            std::vector<int64_t> const &recv_bytes )
     {
         int const n = (int)send_bytes.size();
         std::vector<int> sc( n ), sd( n ), rc( n ), rd( n );
-        for ( int r = 0, s = 0, t = 0; r < n; ++r )
+        int64_t s = 0, t = 0;
+        for ( int r = 0; r < n; ++r )
         {
-            sc[r] = (int)send_bytes[r];
-            sd[r] = s;
+            sc[r] = count( send_bytes[r] );
+            sd[r] = count( s );
             s += sc[r];
-            rc[r] = (int)recv_bytes[r];
-            rd[r] = t;
+            rc[r] = count( recv_bytes[r] );
+            rd[r] = count( t );
             t += rc[r];
         }
         MPI_Alltoallv( const_cast<void *>( send ), sc.data(), sd.data(), MPI_BYTE, recv, rc.data(), rd.data(),

@@ -1,6 +1,7 @@
 """The C++ drop-in headers compile on the host without a GPU: with and
 without the Kokkos stand-in (where PointCloudOperator<DeviceType>::apply
-takes the reference's Kokkos::View value types)."""
+takes the reference's Kokkos::View value types), and the multi-rank test
+program with its shared-memory communicator."""
 import os
 import shutil
 import subprocess
@@ -21,5 +22,19 @@ def test_dropin_test_program_compiles(kokkos):
         pytest.skip("no CUDA headers")
     cmd = [gxx, "-std=c++17", "-fsyntax-only", "-Wall", str(ROOT / "tests" / "cpp" / "test_dropin.cpp"),
            "-I", str(ROOT / "include"), "-I", str(cuda / "include")] + (["-DDTK_FAKE_KOKKOS"] if kokkos else [])
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+
+
+def test_distributed_test_program_compiles():
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    cuda = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+    if not (cuda / "include" / "cuda_runtime.h").exists():
+        pytest.skip("no CUDA headers")
+    cmd = [gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-pthread",
+           str(ROOT / "tests" / "cpp" / "test_distributed.cpp"), "-I", str(ROOT / "include"),
+           "-I", str(cuda / "include")]
     res = subprocess.run(cmd, capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
