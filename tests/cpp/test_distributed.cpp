@@ -9,7 +9,14 @@
 // over both ranks must copy the one-rank operator's nearest values exactly.
 // No kernel of one rank waits on the other's: the exchange runs on the host
 // between the steps.
+// Built twice: with the shared-memory communicator below, and with
+// -DDTK_FAKE_MPI, where the communicator is MPI_COMM_WORLD of a test
+// stand-in for MPI (tests/cpp/fake_mpi.hpp) and the drop-in takes its
+// MPI_Comm path.
 // Prints "PASS <n>" on success; exits non-zero on the first failure.
+#ifdef DTK_FAKE_MPI
+#include "fake_mpi.hpp"
+#endif
 #include <dtk/DTK_MovingLeastSquaresOperator.hpp>
 #include <dtk/DTK_NearestNeighborOperator.hpp>
 
@@ -114,6 +121,20 @@ struct ThreadComm
     }
 };
 
+#ifdef DTK_FAKE_MPI
+using CommT = MPI_Comm;
+CommT make_comm( Shared *, int r )
+{
+    fake_mpi::thread_rank() = r;
+    return MPI_COMM_WORLD;
+}
+MPI_Comm const ONE_RANK = MPI_COMM_SELF;
+#else
+using CommT = ThreadComm;
+CommT make_comm( Shared *sh, int r ) { return ThreadComm{sh, r}; }
+int const ONE_RANK = 0; // not a communicator type: one rank
+#endif
+
 struct Buf
 {
     double *d = nullptr;
@@ -175,10 +196,9 @@ std::vector<Pt> cloud( int n, unsigned seed, double scale, double shift )
 double field( Pt const &p ) { return std::sin( 3 * p[0] ) + p[1] * p[2] + 0.5 * p[2]; }
 
 template <typename Op>
-void compare_with_union( ThreadComm const &comm, cudaStream_t stream, std::vector<std::vector<Pt>> const &srcs,
+void compare_with_union( CommT const &comm, int r, cudaStream_t stream, std::vector<std::vector<Pt>> const &srcs,
                          std::vector<Pt> const &tgt, MlsOptions ext, double tol )
 {
-    int const r = comm.rank();
     std::vector<Pt> const &src = srcs[r];
     Buf bs( 3 * src.size() ), bt( 3 * tgt.size() ), bv( src.size() ), bo( tgt.size() );
     std::vector<double> sv;
@@ -198,7 +218,7 @@ void compare_with_union( ThreadComm const &comm, cudaStream_t stream, std::vecto
             uv.push_back( field( p ) );
         }
     Buf us( 3 * uni.size() ), uvb( uni.size() ), uo( tgt.size() );
-    Op one( 0, points( us, uni ), points( bt, tgt ), ext );
+    Op one( ONE_RANK, points( us, uni ), points( bt, tgt ), ext );
     one.apply( values( uvb, uv ), out( uo ) );
     auto z = host( uo );
     double num = 0.0, den = 0.0;
@@ -215,7 +235,7 @@ void rank_main( Shared *sh, int r )
     cudaSetDevice( 0 );
     cudaStream_t stream;
     cudaStreamCreateWithFlags( &stream, cudaStreamNonBlocking );
-    ThreadComm comm{sh, r};
+    CommT const comm = make_comm( sh, r );
     using Quad = MovingLeastSquaresOperator<CudaDevice, Wendland<2>, MultivariatePolynomialBasis<Quadratic, 3>>;
     using Lin = MovingLeastSquaresOperator<CudaDevice, Wendland<0>, MultivariatePolynomialBasis<Linear, 3>>;
     {
@@ -224,15 +244,15 @@ void rank_main( Shared *sh, int r )
         std::vector<Pt> tgt = cloud( r == 0 ? 1500 : 900, 20 + r, 1.0, 0.0 );
         MlsOptions ext;
         ext.k = 20;
-        compare_with_union<Quad>( comm, stream, srcs, tgt, ext, 1e-13 );
+        compare_with_union<Quad>( comm, r, stream, srcs, tgt, ext, 1e-13 );
         ext.precision = DTK_MIXED;
-        compare_with_union<Quad>( comm, stream, srcs, tgt, ext, 1e-12 );
+        compare_with_union<Quad>( comm, r, stream, srcs, tgt, ext, 1e-12 );
     }
     {
         // side-by-side slabs; the reference's default k (basis size)
         std::vector<std::vector<Pt>> srcs = {cloud( 5000, 31, 0.5, 0.0 ), cloud( 5000, 32, 0.5, 0.5 )};
         std::vector<Pt> tgt = cloud( 1000, 40 + r, 0.5, 0.5 * r );
-        compare_with_union<Lin>( comm, stream, srcs, tgt, MlsOptions{}, 1e-13 );
+        compare_with_union<Lin>( comm, r, stream, srcs, tgt, MlsOptions{}, 1e-13 );
     }
     {
         // one rank without sources, one without targets
@@ -240,7 +260,7 @@ void rank_main( Shared *sh, int r )
         std::vector<Pt> tgt = r == 0 ? std::vector<Pt>{} : cloud( 700, 52, 1.0, 0.0 );
         MlsOptions ext;
         ext.k = 10;
-        compare_with_union<Quad>( comm, stream, srcs, tgt, ext, 1e-13 );
+        compare_with_union<Quad>( comm, r, stream, srcs, tgt, ext, 1e-13 );
     }
     {
         // nearest neighbour over both ranks: exactly the one-rank operator's values
@@ -263,7 +283,7 @@ void rank_main( Shared *sh, int r )
                 uv.push_back( field( p ) );
             }
         Buf us( 3 * uni.size() ), ub( uni.size() ), uo( tgt.size() );
-        NearestNeighborOperator<CudaDevice> one( 0, points( us, uni ), points( bt, tgt ),
+        NearestNeighborOperator<CudaDevice> one( ONE_RANK, points( us, uni ), points( bt, tgt ),
                                                  reinterpret_cast<dtk_stream_t>( stream ) );
         one.apply( values( ub, uv ), out( uo ) );
         CHECK( host( bo ) == host( uo ) );
@@ -308,6 +328,9 @@ void rank_main( Shared *sh, int r )
 
 int main()
 {
+#ifdef DTK_FAKE_MPI
+    fake_mpi::init( 2 );
+#endif
     Shared sh( 2 );
     std::thread a( rank_main, &sh, 0 ), b( rank_main, &sh, 1 );
     a.join();

@@ -26,7 +26,8 @@ def test_dropin_test_program_compiles(kokkos):
     assert res.returncode == 0, res.stderr
 
 
-def test_distributed_test_program_compiles():
+@pytest.mark.parametrize("mpi", [False, True])
+def test_distributed_test_program_compiles(mpi):
     gxx = shutil.which("g++")
     if gxx is None:
         pytest.skip("no g++")
@@ -35,6 +36,6 @@ def test_distributed_test_program_compiles():
         pytest.skip("no CUDA headers")
     cmd = [gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-pthread",
            str(ROOT / "tests" / "cpp" / "test_distributed.cpp"), "-I", str(ROOT / "include"),
-           "-I", str(cuda / "include")]
+           "-I", str(cuda / "include")] + (["-DDTK_FAKE_MPI"] if mpi else [])
     res = subprocess.run(cmd, capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
