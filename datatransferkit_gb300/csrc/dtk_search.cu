@@ -628,17 +628,28 @@ __device__ __forceinline__ uint32_t compact10( uint32_t v )
 // last leaves' first codes (the leaves are cells).  The box is inset by a
 // margin of 2^-18 (|c| + S + extent), which covers the FP32 rounding of the
 // Morton quantization; a side at the end of the quantized range is open (no
-// source lies beyond the scene box).  wide_cell[2 w] = (lo, parent),
-// wide_cell[2 w + 1] = (hi, -).
-__global__ void k_wide_cells( int64_t ni, int64_t const *flag, int64_t const *widx, int const *parent_node,
-                              int const *range_lo, int const *range_hi, int32_t const *leaf_start,
-                              uint32_t const *codes, double const *scene, float4 *wide_cell )
+// source lies beyond the scene box).  A cell that also holds points outside
+// the node (a run of equal codes split between leaves by position: the
+// point just before or just after the node's range shares the prefix) holds
+// no ball: its box is left empty, so a search never starts there.
+// wide_cell[2 w] = (lo, parent), wide_cell[2 w + 1] = (hi, -).
+__global__ void k_wide_cells( int64_t ni, int64_t n, int64_t const *flag, int64_t const *widx,
+                              int const *parent_node, int const *range_lo, int const *range_hi,
+                              int32_t const *leaf_start, uint32_t const *codes, double const *scene,
+                              float4 *wide_cell )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i >= ni || !flag[i] )
         return;
     uint32_t const c1 = codes[leaf_start[range_lo[i]]], c2 = codes[leaf_start[range_hi[i]]];
     int const len = c1 == c2 ? 30 : __clz( c1 ^ c2 ) - 2;
+    int64_t const p0 = leaf_start[range_lo[i]], p1 = leaf_start[range_hi[i] + 1];
+    bool shared = false;
+    if ( len > 0 )
+    {
+        auto same = [&]( uint32_t c ) { return ( c >> ( 30 - len ) ) == ( c1 >> ( 30 - len ) ); };
+        shared = ( p0 > 0 && same( codes[p0 - 1] ) ) || ( p1 < n && same( codes[p1] ) );
+    }
     double const ext = fmax( scene[6] - scene[0], fmax( scene[7] - scene[1], scene[8] - scene[2] ) );
     double const cmax = fmax( fabs( scene[9] ), fmax( fabs( scene[10] ), fabs( scene[11] ) ) );
     double const mg = ldexp( cmax + scene[12] + ext, -18 );
@@ -656,6 +667,13 @@ __global__ void k_wide_cells( int64_t ni, int64_t const *flag, int64_t const *wi
         lo[a] = __double2float_ru( dlo );
         hi[a] = __double2float_rd( dhi );
     }
+    if ( shared )
+#pragma unroll
+        for ( int a = 0; a < 3; ++a )
+        {
+            lo[a] = __int_as_float( 0x7f800000 );  // +inf
+            hi[a] = -__int_as_float( 0x7f800000 ); // -inf
+        }
     int p = (int)i;
     for ( int t = 0; t < 3 && p != 0; ++t )
         p = parent_node[p];
@@ -1290,15 +1308,19 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
             // Start node: every point within the speculative bound lies in the
             // subtree of a wide node whose Morton cell holds the ball of that
             // radius (the cell's points are the subtree's), so the search may
-            // start there; the proof after the search covers the bound, and a
-            // second pass starts from the root.  The previous query's start
-            // node is the first guess: up while its cell misses the ball, then
-            // down while one internal child's cell holds it.  (Ungrouped trees:
-            // the keys of a batch tree carry the problem above the code.)
+            // start there; the proof after the search covers the bound.  A
+            // second pass (the bound not proven) starts from the cell that
+            // holds the ball of the list's own k-th distance, which bounds
+            // every point that can still enter (from the root while the list
+            // is not full).  The previous start node is the first guess: up
+            // while its cell misses the ball, then down while one internal
+            // child's cell holds it.  (Ungrouped trees: the keys of a batch
+            // tree carry the problem above the code.)
             int start = 0;
-            if ( !GROUPED && spec < __int_as_float( 0x7f800000 ) )
+            float const ball = spec < __int_as_float( 0x7f800000 ) ? spec : bound_f;
+            if ( !GROUPED && ball < __int_as_float( 0x7f800000 ) )
             {
-                float const R = __fadd_ru( __fsqrt_ru( spec ), q.err );
+                float const R = __fadd_ru( __fsqrt_ru( ball ), q.err );
                 auto holds = [&]( int w ) {
                     float4 const lo = __ldg( tr.wide_cell + 2 * (int64_t)w ),
                                  hi = __ldg( tr.wide_cell + 2 * (int64_t)w + 1 );
@@ -1676,7 +1698,7 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
                                                            tree.wide_range.get() );
         check_launch( "k_collapse" );
         tree.wide_cell.allocate( 2 * std::max<int64_t>( 1, nw ), s );
-        k_wide_cells<<<blocks_for( ni, 256 ), 256, 0, s>>>( ni, flag.get(), widx.get(), parent_node.get(),
+        k_wide_cells<<<blocks_for( ni, 256 ), 256, 0, s>>>( ni, n, flag.get(), widx.get(), parent_node.get(),
                                                               range_lo.get(), range_hi.get(), tree.leaf_start.get(),
                                                               tree.codes.get(), tree.scene.get(),
                                                               tree.wide_cell.get() );

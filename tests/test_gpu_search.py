@@ -139,3 +139,17 @@ def test_radius_sets_bit_exact():
     assert np.array_equal(off, o2)
     for i in range(len(tgt)):
         assert np.array_equal(np.sort(idx[off[i]:off[i + 1]]), np.sort(i2[o2[i]:o2[i + 1]])), i
+
+
+def test_knn_in_a_cluster_sharing_one_morton_code():
+    # 400 sources inside a cube of side 1e-9 (one 30-bit Morton code: the
+    # run is split between leaves by position) in a unit cloud, and targets
+    # inside the cube, off the sources: a search may only start in a subtree
+    # whose cell holds no point outside it, else it would miss the sibling
+    # leaves of the same code
+    rng = np.random.default_rng(21)
+    cube = 0.5 + 1e-9 * rng.random((400, 3))
+    src = np.concatenate([rng.random((5000, 3)), cube, rng.random((3000, 3))])
+    tgt = np.concatenate([0.5 + 1e-9 * rng.random((300, 3)), rng.random((200, 3))])
+    for k in (1, 4, 32):
+        assert np.array_equal(gpu_knn(src, tgt, k)[1], cpu.knn(src, tgt, k)[1]), k
