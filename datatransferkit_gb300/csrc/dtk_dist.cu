@@ -100,27 +100,37 @@ __global__ void k_gather_values( double const *values, int64_t n, int32_t const 
     out[i] = values[j];
 }
 
-// the box of a point cloud as ordered bits (min and -max), one atomic a block
+// order-preserving bits of a double (larger values, larger bits)
+__device__ __forceinline__ unsigned long long ordered_bits( double v )
+{
+    long long const b = __double_as_longlong( v );
+    return b < 0 ? ~(unsigned long long)b : (unsigned long long)b | ( 1ull << 63 );
+}
+
+// the box of a point cloud as ordered bits of (min, -max): a thread's own
+// minima, then the warp's, then one atomic a warp and value
 __global__ void k_box_bits( PointsView p, unsigned long long *box )
 {
-    __shared__ unsigned long long s[6];
-    if ( threadIdx.x < 6 )
-        s[threadIdx.x] = ~0ull;
-    __syncthreads();
+    unsigned long long m[6];
+#pragma unroll
+    for ( int d = 0; d < 6; ++d )
+        m[d] = ~0ull;
     for ( int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < p.n; i += (int64_t)gridDim.x * blockDim.x )
+#pragma unroll
         for ( int d = 0; d < 3; ++d )
         {
             double const v = p( i, d );
-            // order-preserving bits of v and of -v (the max as a min)
-            long long const b = __double_as_longlong( v ), nb = __double_as_longlong( -v );
-            unsigned long long const o = b < 0 ? ~(unsigned long long)b : (unsigned long long)b | ( 1ull << 63 );
-            unsigned long long const no = nb < 0 ? ~(unsigned long long)nb : (unsigned long long)nb | ( 1ull << 63 );
-            atomicMin( &s[d], o );
-            atomicMin( &s[3 + d], no );
+            m[d] = min( m[d], ordered_bits( v ) );
+            m[3 + d] = min( m[3 + d], ordered_bits( -v ) );
         }
-    __syncthreads();
-    if ( threadIdx.x < 6 )
-        atomicMin( &box[threadIdx.x], s[threadIdx.x] );
+#pragma unroll
+    for ( int d = 0; d < 6; ++d )
+    {
+        for ( int o = 16; o; o >>= 1 )
+            m[d] = min( m[d], __shfl_xor_sync( 0xffffffffu, m[d], o ) );
+        if ( ( threadIdx.x & 31 ) == 0 && m[d] != ~0ull )
+            atomicMin( &box[d], m[d] );
+    }
 }
 
 double from_ordered( unsigned long long o )
