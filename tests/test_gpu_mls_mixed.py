@@ -184,3 +184,20 @@ def test_jacobi_path_error_on_thin_slabs():
               f"(oracle {ref['underdetermined']})")
         assert np.all(np.isfinite(y))
         assert err <= 1e-3
+
+
+@pytest.mark.parametrize("offset", [1e3, 1e5, -2.5e6])
+def test_far_from_the_origin(offset):
+    # a cloud of unit extent whose coordinates carry a large common offset
+    # (an engineering mesh in its site frame): the FP64 form within the
+    # FP64 bar of the oracle, the mixed form within 1e-6 of it, rows bit-exact
+    src = offset + syn.uniform_points(20_000, 31)
+    tgt = offset + 0.1 + 0.8 * syn.uniform_points(2_000, 32)
+    vals = syn.smooth_field(src - offset)
+    ref = cpu.mls_transfer(src, tgt, vals, 2, 2, k=32)
+    for precision, tol in (("fp64", 1e-10), ("mixed", MIXED_TOL)):
+        y, op = transfer(src, tgt, vals, RBF[2], Q, k=32, precision=precision)
+        _, idx, _ = op.csr()
+        assert np.array_equal(idx.cpu().numpy(), ref["idx"]), precision
+        err = rel_l2(y, ref["target"])
+        assert err <= tol, (precision, offset, err)
