@@ -55,3 +55,39 @@ def test_svd_entry_points_refuse_pageable_host_matrices():
         assert b"a is host memory" in L.dtk_last_error(), fn
         assert f(4, 1, dev.data_ptr(), out.ctypes.data, None, None) == INVALID_ARG, fn
         assert b"pinv is host memory" in L.dtk_last_error(), fn
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_create_from_neighbors_reproduces_create(precision):
+    # the rows of a one-rank operator handed back to dtk_mls_create_from_neighbors:
+    # in their order the coefficients are the create's bit for bit; with every
+    # row reversed, the same coefficients up to the order of the moment sums
+    from oracle import cpu
+    src, tgt = syn.uniform_points(20_000, 83), syn.uniform_points(3_000, 84)
+    s, t = torch.from_numpy(src).cuda(), torch.from_numpy(tgt).cuda()
+    Q = dtk.MultivariatePolynomialBasis(dtk.Quadratic, 3)
+    op = dtk.MovingLeastSquaresOperator(None, s, t, dtk.Wendland(4), Q, k=32, precision=precision)
+    _, idx, coeff = op.csr()
+    idx = idx.long()
+    nb = s[idx].contiguous()
+    local = torch.arange(idx.numel(), dtype=torch.int32, device="cuda")
+    again = dtk.MovingLeastSquaresOperator.from_neighbors(t, 32, nb, local, idx.numel(), dtk.Wendland(4), Q,
+                                                          precision=precision)
+    assert torch.equal(again.csr()[2], coeff)
+    rev = idx.view(-1, 32).flip(1).reshape(-1)
+    other = dtk.MovingLeastSquaresOperator.from_neighbors(t, 32, s[rev].contiguous(), local, idx.numel(),
+                                                          dtk.Wendland(4), Q, precision=precision)
+    c2 = other.csr()[2].view(-1, 32).flip(1).reshape(-1)
+    scale = coeff.abs().view(-1, 32).amax(1, keepdim=True)
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    assert ((c2 - coeff).abs().view(-1, 32) <= tol * scale).all()
+    # values through the fetched layout: this rank's values in entry order
+    vals = syn.smooth_field(src)
+    y = torch.empty(len(tgt), dtype=torch.float64, device="cuda")
+    again.apply(torch.from_numpy(vals).cuda()[idx].contiguous(), y)
+    ref = cpu.mls_transfer(src, tgt, vals, 2, 2, k=32)["target"]
+    err = np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref)
+    assert err <= (1e-13 if precision == "fp64" else 1e-6), err
+    # rows must hold 1..32 entries; indices in range
+    with pytest.raises(dtk.InvalidArgument):
+        dtk.MovingLeastSquaresOperator.from_neighbors(t, 32, nb, local, idx.numel() - 1, dtk.Wendland(4), Q)
