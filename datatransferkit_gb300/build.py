@@ -67,7 +67,8 @@ def build(force: bool = False, jobs: int | None = None) -> Path:
             o.unlink()
     if force or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
         tmp = LIB.with_suffix(".so.tmp")
-        cmd = [nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs)]
+        # -ldl: the NVTX ranges find a profiling tool with dlopen when one is attached
+        cmd = [nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-ldl"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

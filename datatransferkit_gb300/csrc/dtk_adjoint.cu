@@ -622,6 +622,7 @@ extern "C" dtk_status dtk_mls_apply_adjoint( dtk_mls_handle h, const double *cot
 {
     try
     {
+        NvtxRange const nvtx_range( "DTK_apply_adjoint" );
         DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
         DTK_REQUIRE_OR_THROW( n_cot == h->n_tgt, "cot.extent(0) == n_target_points" );
         DTK_REQUIRE_OR_THROW( h->n_tgt == 0 || cot != nullptr, "cot is null" );

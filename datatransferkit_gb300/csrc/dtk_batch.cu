@@ -883,6 +883,7 @@ dtk_status dtk_mls_batch_apply( dtk_mls_batch_handle h, const double *src_values
                                 int32_t use_graph, dtk_stream_t stream_ )
 {
     return guarded( [&] {
+        NvtxRange const nvtx_range( "DTK_compute_values" );
         DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
         DTK_REQUIRE_OR_THROW( src_values != nullptr && ( h->n_tgt == 0 || tgt_values != nullptr ),
                               "null values" );

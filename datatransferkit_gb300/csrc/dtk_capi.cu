@@ -539,6 +539,7 @@ dtk_status dtk_mls_apply( dtk_mls_handle h, const double *source_values, int64_t
                           double *target_values, int64_t n_target_values, dtk_stream_t stream_ )
 {
     return guarded( [&] {
+        NvtxRange const nvtx_range( "DTK_compute_values" );
         DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
         // DTK_REQUIRE at DTK_MovingLeastSquaresOperator_def.hpp:129-130
         DTK_REQUIRE_OR_THROW( n_source_values == h->n_src,

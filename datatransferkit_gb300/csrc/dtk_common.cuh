@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <vector>
 
@@ -204,6 +205,17 @@ struct TouchOnExit
         if ( life )
             life->touch( s );
     }
+};
+
+// A named NVTX range over the host code that enqueues a stage (the labels
+// of the reference's DTK_MARK_REGION, "DTK_" + name, where a stage has one;
+// no-ops unless a profiling tool is attached).
+struct NvtxRange
+{
+    explicit NvtxRange( char const *name ) { nvtxRangePushA( name ); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange( NvtxRange const & ) = delete;
+    NvtxRange &operator=( NvtxRange const & ) = delete;
 };
 
 // Running count of this library's kernel launches (diagnostics).

@@ -258,6 +258,7 @@ dtk_status dtk_gather_points( const double *src, int64_t n_src, int64_t src_pt_s
                               double *out, dtk_stream_t stream_ )
 {
     return guarded( [&] {
+        NvtxRange const nvtx_range( "DTK_get_source_values" );
         validate_points( src, n_src, src_pt_stride, src_dim_stride, "source points" );
         DTK_REQUIRE_OR_THROW( n_extra >= 0 && nnz >= 0, "negative count" );
         DTK_REQUIRE_OR_THROW( n_extra == 0 || extra != nullptr, "extra points are null" );
@@ -282,6 +283,7 @@ dtk_status dtk_gather_values( const double *values, int64_t n, const int32_t *in
                               dtk_stream_t stream_ )
 {
     return guarded( [&] {
+        NvtxRange const nvtx_range( "DTK_get_source_values" );
         DTK_REQUIRE_OR_THROW( n >= 0 && m >= 0, "negative count" );
         DTK_REQUIRE_OR_THROW( m == 0 || ( values && indices && out ), "null values, indices or output" );
         require_device_memory( m ? values : nullptr, "values" );

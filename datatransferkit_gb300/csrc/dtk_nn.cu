@@ -130,6 +130,7 @@ dtk_status dtk_nn_apply_multi( dtk_nn_handle h, const double *source_values, int
                                int64_t tgt_comp_stride, dtk_stream_t stream_ )
 {
     return guarded( [&] {
+        NvtxRange const nvtx_range( "DTK_set_target_values" );
         DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
         // DTK_REQUIRE at DTK_NearestNeighborOperator_def.hpp:79-80
         DTK_REQUIRE_OR_THROW( n_target_values == h->n_tgt, "_indices.extent(0) == target_values.extent(0)" );
@@ -171,6 +172,7 @@ dtk_status dtk_mls_apply_multi( dtk_mls_handle h, const double *source_values, i
                                 int64_t tgt_comp_stride, dtk_stream_t stream_ )
 {
     return guarded( [&] {
+        NvtxRange const nvtx_range( "DTK_compute_values" );
         DTK_REQUIRE_OR_THROW( h != nullptr, "handle is null" );
         // DTK_REQUIRE at DTK_MovingLeastSquaresOperator_def.hpp:129-130, per component
         DTK_REQUIRE_OR_THROW( n_source_values == h->n_src, "source_values.extent(0) == n_source_points" );

@@ -1737,6 +1737,7 @@ void build_tree_and_order( PointsView src, PointsView tgt, Lbvh &tree, DeviceBuf
                            unsigned *status, cudaStream_t s, uint32_t const *src_group,
                            uint32_t const *tgt_group, int64_t n_groups, cudaEvent_t tgt_ready )
 {
+    NvtxRange const nvtx_range( "DTK_build_tree" );
     struct Side
     {
         cudaStream_t s2 = nullptr;
@@ -1780,6 +1781,7 @@ void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
                 GroupArgs const &groups, int32_t const *offset, int32_t *idx, unsigned *status,
                 cudaStream_t s, int32_t *pos )
 {
+    NvtxRange const nvtx_range( "DTK_knn_query" );
     if ( tgt.n == 0 || tree.n == 0 || ( k == 0 && !groups.k ) )
         return;
     GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
@@ -1814,6 +1816,7 @@ void knn_query( Lbvh const &tree, PointsView tgt, uint32_t const *order, int k,
 void radius_count( Lbvh const &tree, PointsView tgt, uint32_t const *order, double r,
                    GroupArgs const &groups, int64_t *counts, unsigned *status, cudaStream_t s )
 {
+    NvtxRange const nvtx_range( "DTK_radius_query" );
     if ( tgt.n == 0 )
         return;
     GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};
@@ -1830,6 +1833,7 @@ void radius_fill( Lbvh const &tree, PointsView tgt, uint32_t const *order, doubl
                   GroupArgs const &groups, int32_t const *offset, int32_t *idx, unsigned *status,
                   cudaStream_t s )
 {
+    NvtxRange const nvtx_range( "DTK_radius_query" );
     if ( tgt.n == 0 )
         return;
     GroupView const gv{groups.src_off, groups.tgt_grp, groups.k, groups.r};

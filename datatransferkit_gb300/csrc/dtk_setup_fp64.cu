@@ -892,6 +892,7 @@ void launch_fp64( SetupArgs const &a, cudaStream_t s )
 
 void setup_fp64( SetupArgs const &a, cudaStream_t s )
 {
+    NvtxRange const nvtx_range( "DTK_compute_polynomial_coeffs" );
     if ( a.n_tgt == 0 )
         return;
     switch ( a.basis )
@@ -920,6 +921,7 @@ int64_t batch_setup_threads()
 
 void batch_setup( BatchSetupArgs const &args, cudaStream_t s )
 {
+    NvtxRange const nvtx_range( "DTK_compute_polynomial_coeffs" );
     BatchSetupArgs a = args;
     a.jcap[0] = (unsigned)jacobi_cap( 1 );
     a.jcap[1] = (unsigned)jacobi_cap( 4 );

@@ -717,6 +717,7 @@ void launch_mixed( SetupArgs const &a, cudaStream_t s )
 
 void setup_mixed( SetupArgs const &a, cudaStream_t s )
 {
+    NvtxRange const nvtx_range( "DTK_compute_polynomial_coeffs" );
     if ( a.n_tgt == 0 )
         return;
     switch ( a.basis )
