@@ -28,7 +28,7 @@ EXPORTED = [
     "dtk_nn_apply", "dtk_nn_apply_multi", "dtk_nn_get_indices", "dtk_nn_destroy",
     "dtk_mls_export_size", "dtk_mls_export", "dtk_mls_import", "dtk_release_cached_memory",
     "dtk_mls_transfer_host", "dtk_set_loop_caps", "dtk_stream_synchronize", "dtk_mls_create_from_neighbors",
-    "dtk_mls_batch_resetup", "dtk_mls_batch_get_config", "dtk_set_setup_lanes",
+    "dtk_mls_batch_resetup", "dtk_mls_batch_get_config", "dtk_set_setup_lanes", "dtk_set_rotation_log",
     "dtk_knn_search_d2", "dtk_points_bounds", "dtk_points_pack", "dtk_gather_points", "dtk_gather_values",
 ]
 
@@ -109,6 +109,7 @@ def _declare(L):
     L.dtk_gather_values.argtypes = [_vp, _i64, _vp, _i64, _vp, _vp]
     L.dtk_mls_batch_get_config.argtypes = [_vp, _vp, _vp, _vp]
     L.dtk_set_setup_lanes.argtypes = [C.c_int32, C.c_int32]
+    L.dtk_set_rotation_log.argtypes = [C.c_int32]
     L.dtk_mls_create_from_neighbors.argtypes = [C.POINTER(Options), _vp, _i64, _i64, _i64, C.c_int32, _vp, _vp,
                                                 _i64, _vp, C.POINTER(_vp)]
     L.dtk_last_error.restype = C.c_char_p

@@ -320,7 +320,7 @@ void run_setup_plan( SetupArgs const &a, int precision, uint8_t const *basis_of_
     if ( a.n_tgt == 0 )
         return;
     if ( !plan.u_work.get() )
-        plan.u_work.allocate( (size_t)BS_MAX_M_SQ * batch_setup_threads(), s );
+        plan.u_work.allocate( (size_t)jacobi_work_doubles( BS_MAX_M ) * batch_setup_threads(), s );
     // the tasks exist before any launch reads them (the tuner's samples
     // too); refilled with the tuned lane counts.  The statistics counters
     // collect the sample runs as well: zeroed after them

@@ -74,6 +74,7 @@ std::vector<int> g_sms;                                    // per device, 0 = no
 namespace
 {
 std::atomic<int64_t> g_jacobi_cap{0}, g_traversal_cap{0};
+std::atomic<int> g_jacobi_log{JACOBI_LOG};
 std::atomic<int> g_setup_lanes1{0}, g_setup_lanes2{0};
 }
 
@@ -81,6 +82,11 @@ unsigned long long jacobi_cap( int m )
 {
     int64_t const c = g_jacobi_cap.load( std::memory_order_relaxed );
     return c > 0 ? (unsigned long long)c : 200ull * m * m + 2000ull;
+}
+
+int jacobi_log_cap()
+{
+    return g_jacobi_log.load( std::memory_order_relaxed );
 }
 
 void fixed_setup_lanes( int &lanes1, int &lanes2 )
@@ -382,6 +388,14 @@ dtk_status dtk_set_loop_caps( int64_t jacobi_rotations, int64_t traversal_steps 
         DTK_REQUIRE_OR_THROW( jacobi_rotations <= UINT32_MAX, "Jacobi cap exceeds 2^32 - 1" );
         g_jacobi_cap.store( jacobi_rotations, std::memory_order_relaxed );
         g_traversal_cap.store( traversal_steps, std::memory_order_relaxed );
+    } );
+}
+
+dtk_status dtk_set_rotation_log( int32_t rotations )
+{
+    return guarded( [&] {
+        DTK_REQUIRE_OR_THROW( rotations >= 0 && rotations <= JACOBI_LOG, "rotations must be in [0, 160]" );
+        g_jacobi_log.store( rotations, std::memory_order_relaxed );
     } );
 }
 

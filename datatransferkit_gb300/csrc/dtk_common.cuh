@@ -248,6 +248,7 @@ inline void ensure_dynamic_smem( K *kernel, size_t bytes )
 // and tree-traversal steps per query (built in: the tree's wide-node count,
 // which a search never exceeds).
 unsigned long long jacobi_cap( int m );
+int jacobi_log_cap(); // rotations logged before U is formed (JACOBI_LOG unless lowered for a test)
 int64_t traversal_cap( int64_t wide_nodes );
 
 inline int basis_size( int basis )
@@ -570,6 +571,17 @@ struct SetupTask
     uint8_t lanes; // lanes a target in the gather phases (a power of two, 1 .. 32)
     uint8_t pad;
 };
+// A Jacobi thread's global work area, interleaved by thread: the rotation
+// log, JACOBI_LOG (cos, sin) pairs and JACOBI_LOG pivot bytes (p * 16 + q),
+// then U (M x M, formed only for targets whose rotations outrun the log) from
+// JACOBI_U0 doubles on.
+constexpr int JACOBI_LOG = 160;
+constexpr int JACOBI_U0 = 2 * JACOBI_LOG + JACOBI_LOG / 8;
+constexpr int BS_MAX_M = 10;
+__host__ __device__ constexpr int jacobi_work_doubles( int m )
+{
+    return JACOBI_U0 + m * m;
+}
 struct BatchSetupArgs
 {
     Neighbours nb;
@@ -587,12 +599,12 @@ struct BatchSetupArgs
     unsigned long long *underdetermined, *rotations;
     unsigned *status;
     unsigned *counter; // zeroed by batch_setup before the launch
-    double *u_work;    // 100 doubles per thread of the grid (batch_setup_threads)
+    double *u_work;    // jacobi_work_doubles( BS_MAX_M ) doubles per thread of the grid (batch_setup_threads)
     unsigned jcap[3] = {0, 0, 0};
+    int jlog = JACOBI_LOG;
 };
 void batch_setup( BatchSetupArgs const &a, cudaStream_t s );
 int64_t batch_setup_threads();
-constexpr int BS_MAX_M_SQ = 100; // U's doubles a thread in the persistent setup's work area
 
 // The device plan of a setup over targets of mixed classes (kept by a batch
 // handle for its re-setups): the targets in bucket order, the bucket sizes,

@@ -27,11 +27,12 @@
 // must carry 32 useful lanes; the 2x2 SVD is scalar work.  Iteration counts
 // are tight (about 114 +- 13 for the quadratic basis), so divergence costs
 // little.  E (m x m) and column 0 of V live in shared memory, interleaved
-// by thread so that dynamic (p, q) accesses are conflict-free; U (m x m) in
-// a global work area per resident thread (L2-resident), interleaved the same
-// way, with its two columns read ahead of each rotation's FP64 work.  That
-// leaves 880 B of shared memory a thread at m = 10: 8 warps an SM, two per
-// FP64 pipe, against 4 with U in shared memory (8M targets: 729 -> 493 ms).
+// by thread so that dynamic (p, q) accesses are conflict-free: 880 B a
+// thread at m = 10, 8 warps an SM, two per FP64 pipe.  U is never updated
+// rotation by rotation: the rotations go to a log in a global work area per
+// resident thread (L2-resident, interleaved the same way), and row 0 of the
+// pseudo-inverse is the log applied in reverse to one vector (8M targets:
+// 432 -> 366 ms against U's explicit updates).
 // The kernels are persistent: a thread takes targets g, g + T, ...
 // The argmax runs on the integer pipe over the IEEE bits of |E_ij|; the stop
 // test too, from exponent bounds, except within a factor of four of the
@@ -166,14 +167,48 @@ template <int M>
 struct Smem
 {
     // E and V(:, 0) in shared memory, interleaved by thread (stride es, the
-    // thread's column t); U in shared or global memory (stride us, column ut)
-    double *E, *U, *V0;
+    // thread's column t); the global work area W (the rotation log, then U)
+    // interleaved by thread too (stride us, column ut).  Every part starts
+    // at an offset that does not depend on M, so that threads working on
+    // different M at once (the batched setup) never share a slot.
+    double *E, *W, *V0;
     int t, es;
     int64_t ut, us;
     __device__ double &e( int i, int j ) const { return E[( i * M + j ) * es + t]; }
-    __device__ double &u( int i, int j ) const { return U[( i * M + j ) * us + ut]; }
+    __device__ double &u( int i, int j ) const { return W[( JACOBI_U0 + i * M + j ) * us + ut]; }
     __device__ double &v( int i ) const { return V0[i * es + t]; }
+    // rotation r of the log: (cos, sin) of U's right rotation and p * 16 + q
+    __device__ double2 &rot( int r ) const { return reinterpret_cast<double2 *>( W )[r * us + ut]; }
+    __device__ uint8_t &pivot( int r ) const
+    {
+        return reinterpret_cast<uint8_t *>( W + 2 * JACOBI_LOG * us )[r * us + ut];
+    }
 };
+
+// U = G_0 G_1 ... G_{n-1} formed explicitly from the first n logged
+// rotations (the updates the reference makes, in its order): for a target
+// whose rotations outrun the log, which then updates U as it goes.
+template <int M>
+__device__ __noinline__ void form_u( Smem<M> const &s, int n )
+{
+#pragma unroll
+    for ( int i = 0; i < M; ++i )
+#pragma unroll
+        for ( int j = 0; j < M; ++j )
+            s.u( i, j ) = i == j ? 1.0 : 0.0;
+    for ( int r = 0; r < n; ++r )
+    {
+        double2 const cs = s.rot( r );
+        int const pq = s.pivot( r ), p = pq >> 4, q = pq & 15;
+#pragma unroll
+        for ( int j = 0; j < M; ++j )
+        {
+            double const a = s.u( j, p ), b = s.u( j, q );
+            s.u( j, p ) = rot_minus( cs.x, cs.y, a, b );
+            s.u( j, q ) = rot_plus( cs.x, cs.y, a, b );
+        }
+    }
+}
 
 // Grid of the persistent Jacobi kernels: blocks of FP64_THREADS (8 warps an
 // SM, one block each) when the targets fill the GPU; otherwise blocks of one
@@ -198,6 +233,15 @@ JacobiGrid jacobi_grid( int64_t n )
 // Runs DTK's Jacobi on the thread's E; on return row0 holds row 0 of the
 // pseudo-inverse.  Returns 1 if a singular value was truncated.
 //
+// U is not updated as the reference does (40 FP64 operations and 20 loads
+// and stores a rotation at M = 10): the rotations go to a log, and row 0 of
+// the pseudo-inverse, U w with w_k = V(0, k) / E(k, k) (0 where truncated),
+// is G_0 (G_1 (... (G_{n-1} w))), the logged rotations applied to w in
+// reverse, 4 operations each.  The pivots, rotations and stop are the
+// reference's; only the final product is associated differently (a
+// rounding-level difference).  A target whose rotations outrun the log forms
+// U from it and continues with the reference's updates.
+//
 // E enters exactly symmetric (the moments fill both triangles from one sum).
 // For a non-degenerate E (no zero on the diagonal), while the rotations keep
 // it so -- the pivot block is then symmetric, the
@@ -214,11 +258,13 @@ JacobiGrid jacobi_grid( int64_t n )
 // differ (an indefinite block, as negative Buhmann weights give) the loop
 // falls back to the reference's full row and column updates.
 template <int M>
-__device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, unsigned cap,
+__device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, unsigned cap, int log_cap,
                             unsigned *status )
 {
     double const tol = DBL_EPSILON;
     unsigned it = 0;
+    int nlog = 0;        // rotations in the log
+    bool formed = false; // U formed: updated explicitly from here on
     // a basis function that vanishes on every neighbour (collinear or
     // coplanar rows) leaves a zero on the diagonal: such degenerate systems
     // keep the reference's updates throughout, since their truncation
@@ -312,15 +358,22 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
             p = q;
             q = tmp;
         }
-        // U's columns p and q are read before the 2x2 SVD and the E updates,
-        // so that their loads (L2, when U is in global memory) are in flight
-        // during the FP64 work
-        double up[M], uq[M];
-#pragma unroll
-        for ( int j = 0; j < M; ++j )
+        if ( !formed && nlog == log_cap )
         {
-            up[j] = s.u( j, p );
-            uq[j] = s.u( j, q );
+            form_u<M>( s, nlog );
+            formed = true;
+        }
+        // a formed U's columns p and q are read before the 2x2 SVD and the E
+        // updates, so that their loads (L2) are in flight during the FP64 work
+        double up[M], uq[M];
+        if ( formed )
+        {
+#pragma unroll
+            for ( int j = 0; j < M; ++j )
+            {
+                up[j] = s.u( j, p );
+                uq[j] = s.u( j, q );
+            }
         }
         double cl, sl, cr, sr;
         double const bpp = s.e( p, p ), bpq = s.e( p, q ), bqp = s.e( q, p ), bqq = s.e( q, q );
@@ -372,13 +425,22 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
                 s.e( j, q ) = rot_plus( cr, sr, a, b );
             }
         }
-        // givens_right(U, cl, sl, p, q)
-#pragma unroll
-        for ( int j = 0; j < M; ++j )
+        // givens_right(U, cl, sl, p, q): logged, or applied to a formed U
+        if ( formed )
         {
-            double const a = up[j], b = uq[j];
-            s.u( j, p ) = rot_minus( cl, sl, a, b );
-            s.u( j, q ) = rot_plus( cl, sl, a, b );
+#pragma unroll
+            for ( int j = 0; j < M; ++j )
+            {
+                double const a = up[j], b = uq[j];
+                s.u( j, p ) = rot_minus( cl, sl, a, b );
+                s.u( j, q ) = rot_plus( cl, sl, a, b );
+            }
+        }
+        else
+        {
+            s.rot( nlog ) = make_double2( cl, sl );
+            s.pivot( nlog ) = (uint8_t)( p * 16 + q );
+            ++nlog;
         }
         // givens_left(V, cr, sr, p, q), column 0 only
         {
@@ -403,22 +465,59 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
             dropped = 1;
         }
     }
+    if ( formed )
+    {
+#pragma unroll
+        for ( int j = 0; j < M; ++j )
+        {
+            double v = 0.0;
+#pragma unroll
+            for ( int k = 0; k < M; ++k )
+                v = fma( s.u( j, k ), w[k], v );
+            row0[j] = v;
+        }
+        return dropped;
+    }
+    // U w = G_0 (G_1 (... (G_{n-1} w))) in V(:, 0)'s place: G = the right
+    // rotation (c, s) of columns p and q, so (G z)_p = c z_p + s z_q and
+    // (G z)_q = c z_q - s z_p; the log read four entries ahead
+#pragma unroll
+    for ( int k = 0; k < M; ++k )
+        s.v( k ) = w[k];
+    auto turn = [&]( double2 cs, int pq ) {
+        int const p = pq >> 4, q = pq & 15;
+        double const zp = s.v( p ), zq = s.v( q );
+        s.v( p ) = rot_plus( cs.x, cs.y, zq, zp );
+        s.v( q ) = rot_minus( cs.x, cs.y, zq, zp );
+    };
+    int r = nlog;
+    for ( ; r >= 4; r -= 4 )
+    {
+        double2 cs[4];
+        int pq[4];
+#pragma unroll
+        for ( int u = 0; u < 4; ++u )
+        {
+            cs[u] = s.rot( r - 1 - u );
+            pq[u] = s.pivot( r - 1 - u );
+        }
+#pragma unroll
+        for ( int u = 0; u < 4; ++u )
+            turn( cs[u], pq[u] );
+    }
+    for ( ; r > 0; --r )
+        turn( s.rot( r - 1 ), s.pivot( r - 1 ) );
 #pragma unroll
     for ( int j = 0; j < M; ++j )
-    {
-        double v = 0.0;
-#pragma unroll
-        for ( int k = 0; k < M; ++k )
-            v = fma( s.u( j, k ), w[k], v );
-        row0[j] = v;
-    }
+        row0[j] = s.v( j );
     return dropped;
 }
 
 // Persistent blocks of FP64_THREADS threads: a thread takes targets g,
 // g + T, g + 2T, ... (T threads in the grid, g in the targets' Morton order).
-// U lives in u_work, a global work area of M^2 doubles per resident thread
-// (31 MB at M = 10 on 152 SMs, held in L2), so that E and V(:, 0), 880 B a
+// The rotation log (and U, for a target that outruns it) lives in u_work,
+// jacobi_work_doubles( M ) doubles per resident thread (about 1.9 KB a
+// target touched at M = 10, held in L2), so that E and V(:, 0), 880 B a
 // thread in shared memory, let an SM hold 8 warps instead of 4: the FP64
 // pipe then has a second warp per sub-partition to interleave with the
 // argmax scans and the 2x2 SVD's dependency chain.
@@ -427,7 +526,7 @@ __global__ void __launch_bounds__( FP64_THREADS, 1 )
     k_setup_fp64( Neighbours nb, PointsView tgt, int32_t const *offset,
                   uint32_t const *order, int64_t n_tgt, int rbf, bool rows_sorted,
                   double *coeff, unsigned long long *under_count,
-                  unsigned long long *rot_count, unsigned *status, unsigned jcap, double *u_work )
+                  unsigned long long *rot_count, unsigned *status, unsigned jcap, int jlog, double *u_work )
 {
     extern __shared__ double smem[];
     int const nt = blockDim.x; // FP64_THREADS, or 32 when the targets are few
@@ -505,15 +604,10 @@ __global__ void __launch_bounds__( FP64_THREADS, 1 )
                 }
 #pragma unroll
             for ( int a = 0; a < M; ++a )
-            {
-#pragma unroll
-                for ( int c = 0; c < M; ++c )
-                    s.u( a, c ) = ( a == c ) ? 1.0 : 0.0;
                 s.v( a ) = a == 0 ? 1.0 : 0.0;
-            }
         }
         double row0[M];
-        dropped = jacobi_row0<M>( s, row0, iters, jcap, status );
+        dropped = jacobi_row0<M>( s, row0, iters, jcap, jlog, status );
 
         // computePolynomialCoefficients: c_k = phi_k * (row0 . P_k)
         for ( int j = 0; j < len; ++j )
@@ -665,7 +759,6 @@ __global__ void k_svd_general( int n, int64_t count, double const *a, double *pi
 // order: the same arithmetic as k_setup_fp64, so the coefficients equal the
 // single operator's bit for bit.
 // ---------------------------------------------------------------------------
-constexpr int BS_MAX_M = 10;
 constexpr int BS_SLOT = ( BS_MAX_M * BS_MAX_M + BS_MAX_M ) * 32; // doubles a warp: E and V(:, 0), by lane
 
 template <int M>
@@ -769,14 +862,9 @@ __device__ void setup_task( BatchSetupArgs const &a, SetupTask const &t, int rbf
     {
 #pragma unroll
         for ( int p = 0; p < M; ++p )
-        {
-#pragma unroll
-            for ( int c = 0; c < M; ++c )
-                sm.u( p, c ) = ( p == c ) ? 1.0 : 0.0;
             sm.v( p ) = p == 0 ? 1.0 : 0.0;
-        }
         double row0[M];
-        dropped += jacobi_row0<M>( sm, row0, iters, jcap, a.status );
+        dropped += jacobi_row0<M>( sm, row0, iters, jcap, a.jlog, a.status );
 #pragma unroll
         for ( int p = 0; p < M; ++p )
             sm.v( p ) = row0[p];
@@ -879,12 +967,13 @@ void launch_fp64( SetupArgs const &a, cudaStream_t s )
 {
     JacobiGrid const jg = jacobi_grid<M>( a.n_tgt );
     ensure_dynamic_smem( k_setup_fp64<M>, jg.smem );
-    DeviceBuffer<double> u_work( (size_t)M * M * jg.threads * jg.blocks, s );
+    DeviceBuffer<double> u_work( (size_t)jacobi_work_doubles( M ) * jg.threads * jg.blocks, s );
     Neighbours const nb{a.src, a.idx, a.pos, a.s2};
     k_setup_fp64<M><<<jg.blocks, jg.threads, jg.smem, s>>>( nb, a.tgt, a.offset, a.order,
                                                          a.n_tgt, a.rbf, a.rows_sorted, a.coeff64,
                                                          a.underdetermined, a.rotations, a.status,
-                                                         (unsigned)jacobi_cap( M ), u_work.get() );
+                                                         (unsigned)jacobi_cap( M ), jacobi_log_cap(),
+                                                         u_work.get() );
     check_launch( "k_setup_fp64" );
 }
 
@@ -926,6 +1015,7 @@ void batch_setup( BatchSetupArgs const &args, cudaStream_t s )
     a.jcap[0] = (unsigned)jacobi_cap( 1 );
     a.jcap[1] = (unsigned)jacobi_cap( 4 );
     a.jcap[2] = (unsigned)jacobi_cap( 10 );
+    a.jlog = jacobi_log_cap();
     ensure_dynamic_smem( k_batch_setup, batch_setup_smem() );
     DTK_CUDA_OR_THROW( cudaMemsetAsync( a.counter, 0, sizeof( unsigned ), s ) );
     k_batch_setup<<<(unsigned)num_sms(), BS_WARPS * 32, batch_setup_smem(), s>>>( a );

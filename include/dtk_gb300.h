@@ -409,6 +409,17 @@ dtk_status dtk_mls_batch_get_stage_times(dtk_mls_batch_handle h, float *search_m
  * than a search takes).  Negative values -> DTK_ERR_INVALID_ARG. */
 dtk_status dtk_set_loop_caps(int64_t jacobi_rotations, int64_t traversal_steps);
 
+/* Rotations the FP64 Jacobi (FP64-form setup, persistent batched setup) logs
+ * per moment matrix before it forms U explicitly, for tests (no counterpart
+ * in the reference), for the calls made after it in this process.  Row 0 of
+ * the pseudo-inverse is the logged rotations applied in reverse to one
+ * vector; a matrix that takes more rotations forms U from the log and then
+ * updates it rotation by rotation as the reference does.  0 forms U for
+ * every matrix (the reference's product order); 160, the most, is the
+ * default.  The two orders differ at rounding level.  Values outside
+ * [0, 160] -> DTK_ERR_INVALID_ARG. */
+dtk_status dtk_set_rotation_log(int32_t rotations);
+
 /* Lanes a target in the gather phases of the persistent setup, for rows of
  * up to 32 entries and for longer rows (powers of two in [1, 32]; 0 = tuned
  * by timing, the default), for the batches created after it in this

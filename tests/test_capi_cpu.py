@@ -141,6 +141,13 @@ def test_setup_lanes_accept_powers_of_two_only(dtk_lib):
     assert dtk_lib.dtk_set_setup_lanes(0, 0) == 0  # back to tuning
 
 
+def test_rotation_log_range(dtk_lib):
+    for bad in (-1, 161):
+        assert dtk_lib.dtk_set_rotation_log(bad) == 1
+    assert dtk_lib.dtk_set_rotation_log(0) == 0
+    assert dtk_lib.dtk_set_rotation_log(160) == 0  # the default
+
+
 def test_svd_rejects_bad_sizes(dtk_lib):
     assert dtk_lib.dtk_svd_pinv(0, 1, 1, 1, None, None) == 1
     assert dtk_lib.dtk_svd_pinv(65, 1, 1, 1, None, None) == 1

@@ -15,6 +15,7 @@ import pytest
 import torch
 
 import datatransferkit_gb300 as dtk
+from datatransferkit_gb300 import _capi
 from datatransferkit_gb300 import synthetic as syn
 from oracle import cpu
 from tests.test_gpu_mls_fp64 import BASIS, RBF, dev, rel_l2, tolerances
@@ -54,7 +55,19 @@ def knn_problems(seed=11):
     return out
 
 
-def test_knn_batch_matches_single_operators_bitwise():
+@pytest.fixture
+def rotation_log(request):
+    """The FP64 Jacobi's rotation log length for the test (160 restored)."""
+    L = _capi.lib()
+    assert L.dtk_set_rotation_log(request.param) == 0
+    yield request.param
+    assert L.dtk_set_rotation_log(160) == 0
+
+
+# 160: every matrix from its rotation log; 40: the quadratic ones form U after
+# 40 rotations and update it from there, the others stay within the log
+@pytest.mark.parametrize("rotation_log", [160, 40], indirect=True)
+def test_knn_batch_matches_single_operators_bitwise(rotation_log):
     problems = knn_problems()
     b, vals, out, off, idx, coeff = run_batch(problems)
     so, to = b.source_offsets, b.target_offsets
@@ -72,6 +85,24 @@ def test_knn_batch_matches_single_operators_bitwise():
         f = vals[so[p]:so[p + 1]]
         op.apply(dev(f), y)
         assert_apply_close(out[to[p]:to[p + 1]], y.cpu().numpy(), o1, i1, c1, f)
+
+
+@pytest.mark.parametrize("rotation_log", [160, 40], indirect=True)
+def test_large_mixed_basis_batch_matches_single_operators_bitwise(rotation_log):
+    """Constant, linear and quadratic problems of 20k targets each in one
+    batch: warps run matrices of different sizes side by side (at every
+    bucket boundary of the persistent setup), each thread on its own part of
+    the shared work area; every coefficient as the single operator's."""
+    problems = [dict(src=syn.uniform_points(30_000, 300 + p), tgt=syn.uniform_points(20_000, 400 + p),
+                     rbf=(2, 5, 7)[p % 3], basis=(2, 1, 0, 1, 2, 2)[p], k=(20, 16, 8, 32, 12, 32)[p])
+                for p in range(6)]
+    b, vals, out, off, idx, coeff = run_batch(problems)
+    to = b.target_offsets
+    for p, pr in enumerate(problems):
+        op = dtk.MovingLeastSquaresOperator(None, dev(pr["src"]), dev(pr["tgt"]), RBF[pr["rbf"]],
+                                            BASIS[pr["basis"]], k=pr["k"])
+        _, _, c1 = (t.cpu().numpy() for t in op.csr())
+        assert np.array_equal(coeff[off[to[p]]:off[to[p + 1]]], c1), p
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])

@@ -18,6 +18,7 @@ import pytest
 import torch
 
 import datatransferkit_gb300 as dtk
+from datatransferkit_gb300 import _capi
 from datatransferkit_gb300 import synthetic as syn
 from oracle import cpu
 
@@ -137,6 +138,32 @@ def test_benchmark_density_against_oracle(k):
     assert rel_l2(r["target"], ref["target"]) <= tt
     if k >= 20:  # the benchmark neighbourhoods: the plain 1e-12 bound holds
         assert rel_l2(r["target"], ref["target"]) <= TOL
+
+
+@pytest.mark.parametrize("log", [0, 40])
+def test_rotation_log_and_formed_u_agree(log):
+    """Row 0 of the pseudo-inverse from the rotation log (the default) against
+    U formed for every matrix (log 0: the reference's product order) and U
+    formed after 40 logged rotations (every quadratic matrix here outruns
+    that): each within the FP64 bound of the oracle, and of one another at
+    rounding level."""
+    src = syn.uniform_points(6000, 90)
+    tgt = syn.uniform_points(1500, 91)
+    vals = syn.smooth_field(src)
+    ref = cpu.mls_transfer(src, tgt, vals, 2, 2, k=32)
+    base = run_gpu(src, tgt, vals, 2, 2, k=32)
+    L = _capi.lib()
+    assert L.dtk_set_rotation_log(log) == 0
+    try:
+        r = run_gpu(src, tgt, vals, 2, 2, k=32)
+    finally:
+        assert L.dtk_set_rotation_log(160) == 0
+    for x in (base, r):
+        assert np.array_equal(x["idx"], ref["idx"])
+        assert_coeff_close(x["coeff"], ref["coeff"], ref["offset"], TOL)
+        assert rel_l2(x["target"], ref["target"]) <= TOL
+    assert_coeff_close(r["coeff"], base["coeff"], ref["offset"], 1e-13)
+    assert not np.array_equal(r["coeff"], base["coeff"])  # the other product order ran
 
 
 def test_radius_mode_against_oracle():
