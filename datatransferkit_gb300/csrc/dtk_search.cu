@@ -1049,6 +1049,12 @@ __device__ __forceinline__ float screen_threshold( float b, float err )
 
 constexpr int QUEUE = 64;
 constexpr float SPEC_GROWTH = 1.25f; // speculative k-th squared distance over the previous query's
+// A chunk's leaf list: after the chunk's first query, the leaves within
+// LIST_GROWTH x its k-th squared distance of the box of the chunk's other
+// queries (at most LIST_CAP, else none), which those queries scan instead of
+// traversing the tree.
+constexpr int LIST_CAP = 128;
+constexpr float LIST_GROWTH = 1.5f;
 
 // Queries go to warps in chunks of Morton-consecutive queries (each query
 // seeds the next): n_big chunks of seq queries, then chunks of seq / 2 up to
@@ -1076,6 +1082,97 @@ __device__ __forceinline__ void chunk_range( KnnChunks const &ch, unsigned c, in
     }
 }
 
+// The leaf list of a kNN chunk: every leaf whose box lies within r2 =
+// LIST_GROWTH x kth (the chunk's first query's k-th key, rounded up) of the
+// box of queries [x0, x1) (the union of their FP32 intervals), collected by
+// one traversal into list; a query of the chunk whose k-th key is proven
+// below r2 then lost nothing to the leaves left out.  Too many leaves: no
+// list (*n_list = -1).  Out of line: it runs once a chunk, and its
+// registers stay out of the query loop's.
+__device__ __noinline__ void chunk_leaf_list( float4 const *wide, int64_t step_cap, int levels,
+                                              Query const *qrec, int64_t x0, int64_t x1, float kth,
+                                              int *stack, int *list, int *n_list, float *list_r2 )
+{
+    int const lane = threadIdx.x & 31;
+    unsigned const lt_mask = ( 1u << lane ) - 1u;
+    float const r2 = __fmul_ru( kth, LIST_GROWTH );
+    float blo[3], bhi[3];
+#pragma unroll
+    for ( int d = 0; d < 3; ++d )
+    {
+        blo[d] = __int_as_float( 0x7f800000 );
+        bhi[d] = -__int_as_float( 0x7f800000 );
+    }
+    for ( int64_t x = x0 + lane; x < x1; x += 32 )
+    {
+#pragma unroll
+        for ( int d = 0; d < 3; ++d )
+        {
+            blo[d] = fminf( blo[d], __ldg( qrec[x].qlo + d ) );
+            bhi[d] = fmaxf( bhi[d], __ldg( qrec[x].qhi + d ) );
+        }
+    }
+#pragma unroll
+    for ( int o = 16; o; o >>= 1 )
+#pragma unroll
+        for ( int d = 0; d < 3; ++d )
+        {
+            blo[d] = fminf( blo[d], __shfl_xor_sync( FULL, blo[d], o ) );
+            bhi[d] = fmaxf( bhi[d], __shfl_xor_sync( FULL, bhi[d], o ) );
+        }
+    int n = 0, sp = 0;
+    bool over = !( r2 < __int_as_float( 0x7f800000 ) );
+    int const grp = lane >> 3, slot = lane & 7;
+    int node = grp == 0 ? 0 : -1;
+    for ( int64_t guard = 0; !over; ++guard )
+    {
+        if ( guard >= step_cap )
+        {
+            over = true;
+            break;
+        }
+        float lb = __int_as_float( 0x7f800000 );
+        int ref = WIDE_EMPTY, lend = 0;
+        if ( node >= 0 )
+        {
+            float lo[3], hi[3];
+            int rlo = 0, rhi = 0;
+            load_wide<false>( wide, nullptr, node, slot, lo, hi, ref, lend, rlo, rhi );
+            lb = box_lb( lo, hi, blo, bhi );
+        }
+        bool const cand = ref != WIDE_EMPTY && lb <= r2;
+        unsigned const ml = __ballot_sync( FULL, cand && ref < 0 );
+        unsigned const mi = __ballot_sync( FULL, cand && ref >= 0 );
+        int const n_int = __popc( mi ), n_leaf = __popc( ml );
+        if ( sp + n_int > STACK || n + n_leaf > LIST_CAP )
+        {
+            over = true;
+            break;
+        }
+        if ( cand && ref >= 0 )
+            stack[sp + __popc( mi & lt_mask )] = ref;
+        if ( cand && ref < 0 )
+            list[n + __popc( ml & lt_mask )] = node * WIDE + slot;
+        sp += n_int;
+        n += n_leaf;
+        __syncwarp();
+        // as the query traversal: four nodes a step while a descent fits
+        int const P = sp + ( NODE_GROUPS + levels ) * ( WIDE - 1 ) <= STACK ? NODE_GROUPS : 1;
+        int const taken = sp < P ? sp : P;
+        if ( taken == 0 )
+            break;
+        node = grp < taken ? stack[sp - 1 - grp] : -1;
+        sp -= taken;
+        __syncwarp();
+    }
+    if ( lane == 0 )
+    {
+        *n_list = over ? -1 : n;
+        *list_r2 = r2;
+    }
+    __syncwarp();
+}
+
 template <bool GROUPED>
 __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     k_knn( TreeView tr, PointsView tgt, uint32_t const *order, Query const *qrec, int k_all, KnnChunks ch,
@@ -1088,6 +1185,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     __shared__ int s_queue[Q_WARPS][QUEUE];
     __shared__ Query s_query[Q_WARPS];
     __shared__ int s_entry[Q_WARPS]; // the wide node the previous query started from
+    __shared__ int s_list[Q_WARPS][LIST_CAP]; // the chunk's leaf list (wide node * WIDE + child slot)
+    __shared__ int s_nlist[Q_WARPS];          // its length, -1 while there is none
+    __shared__ float s_list_r2[Q_WARPS];      // every leaf within this of the chunk's box is listed
     int const lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     unsigned const lt_mask = ( 1u << lane ) - 1u;
     if ( lane == 0 )
@@ -1102,6 +1202,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     chunk_range( ch, c, w0, len );
     if ( w0 >= tgt.n )
         return;
+    if ( lane == 0 )
+        s_nlist[wib] = -1;
+    __syncwarp();
     // the list of the previous query (its sorted positions kp and indices ki)
     // seeds the next one: Morton-consecutive queries share most neighbours
     int prev_g = -1, prev_row = 0;
@@ -1182,8 +1285,13 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     int seed_leaf = kp >= 0 ? leaf_first( tr, kp ) : -1;
     unsigned seed_bit = kp >= 0 ? 1u << ( kp - seed_leaf ) : 0u;
     // speculative bound (seeded queries with full rows): boxes and points
-    // beyond it are skipped as if the list were already that tight
+    // beyond it are skipped as if the list were already that tight.  A query
+    // that scans its chunk's leaf list skips every leaf beyond the list's
+    // bound as well.
     float spec = seeded && row == k ? next_spec : __int_as_float( 0x7f800000 );
+    bool list_pass = !GROUPED && w > w0 && row == k && s_nlist[wib] >= 0;
+    if ( list_pass )
+        spec = fminf( spec, s_list_r2[wib] );
     float bound_f = fminf( prune_threshold( __shfl_sync( FULL, kd, k - 1 ) ), spec );
     float screen_f = screen_threshold( bound_f, q.err ); // the leaf screen's bound
     int qn = 0; // queued survivors (warp-uniform)
@@ -1293,6 +1401,35 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         if ( tr.nl == 1 )
         {
             process_leaf( 0, (int)tr.n );
+        }
+        else if ( list_pass )
+        {
+            // the chunk's leaf list, 32 leaves a round: lane j tests leaf j's
+            // box, the leaves that pass are screened in list order
+            int const n_list = s_nlist[wib];
+            for ( int b = 0; b < n_list; b += 32 )
+            {
+                int const e = b + lane < n_list ? s_list[wib][b + lane] : -1;
+                float lb = __int_as_float( 0x7f800000 );
+                int ref = WIDE_EMPTY, lend = 0;
+                if ( e >= 0 )
+                {
+                    float lo[3], hi[3];
+                    int rlo = 0, rhi = 0;
+                    load_wide<false>( tr.wide, tr.wide_range, e / WIDE, e % WIDE, lo, hi, ref, lend, rlo, rhi );
+                    lb = box_lb( lo, hi, q.qlo, q.qhi );
+                }
+                unsigned const ml = __ballot_sync( FULL, e >= 0 && lb <= bound_f );
+                for ( unsigned m = ml; m; m &= m - 1 )
+                {
+                    int const from = __ffs( m ) - 1;
+                    float const lbr = __shfl_sync( FULL, lb, from );
+                    int const lref = __shfl_sync( FULL, ref, from );
+                    int const le = __shfl_sync( FULL, lend, from );
+                    if ( lbr <= bound_f )
+                        process_leaf( ~lref, le );
+                }
+            }
         }
         else
         {
@@ -1425,6 +1562,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         seed_leaf = kp >= 0 ? leaf_first( tr, kp ) : -1;
         seed_bit = kp >= 0 ? 1u << ( kp - seed_leaf ) : 0u;
         spec = __int_as_float( 0x7f800000 );
+        list_pass = false;
         bound_f = prune_threshold( bd );
         screen_f = screen_threshold( bound_f, q.err );
     }
@@ -1439,6 +1577,9 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     prev_row = row;
     next_spec = __fmul_ru( __fmul_ru( kth_ru, 1.0f + 9.5367431640625e-07f ), SPEC_GROWTH ); // prune_threshold
     __syncwarp();
+    if ( !GROUPED && w == w0 && len > 1 && row == k && tr.nl > 1 )
+        chunk_leaf_list( tr.wide, tr.step_cap, tr.levels, qrec, w0 + 1, min( w0 + len, tgt.n ), kth_ru,
+                         s_stack[wib], s_list[wib], s_nlist + wib, s_list_r2 + wib );
     }
     }
 }

@@ -126,6 +126,26 @@ def test_knn_deep_and_degenerate_trees():
         assert np.array_equal(gpu_knn(src, tgt, k)[1], cpu.knn(src, tgt, k)[1]), k
 
 
+@pytest.mark.parametrize("kind", ["uniform", "clustered", "duplicates"])
+def test_knn_chunked_queries_bit_exact(kind):
+    """300k targets: warps take chunks of Morton-consecutive queries, and each
+    chunk's later queries scan the leaf list collected after its first query
+    (they traverse the tree when the list overflowed, and search again when
+    the list's bound is not proven): clustered sources leave uniform targets
+    far from most leaves, duplicates give zero k-th distances."""
+    rng = np.random.default_rng(21)
+    n = 300_000
+    if kind == "uniform":
+        src, tgt = syn.uniform_points(400_000, 22), syn.uniform_points(n, 23)
+    elif kind == "clustered":
+        src, tgt = syn.gaussian_mixture(400_000, 24), syn.uniform_points(n, 25)
+    else:
+        spots = rng.random((40, 3))
+        src = np.concatenate([syn.uniform_points(200_000, 26), np.repeat(spots, 100, axis=0)])
+        tgt = np.concatenate([syn.uniform_points(n - 4000, 27), np.repeat(spots, 100, axis=0)])
+    assert np.array_equal(gpu_knn(src, tgt, 32)[1], cpu.knn(src, tgt, 32)[1])
+
+
 def test_radius_sets_bit_exact():
     src = syn.gaussian_mixture(20000, 11)
     tgt = syn.uniform_points(3000, 12)
