@@ -19,12 +19,14 @@
 // keys sit one per lane, sorted across lanes.
 // The first target of a chunk starts from the 32 Morton-sorted sources around
 // its code, every later one from the previous target's final list re-keyed
-// for it (neighbouring targets share most neighbours).  The starting members
-// are screened out of their leaves (a warp OR-reduction of a per-leaf lane
-// mask), so no source enters the list twice.  A seeded target also prunes
-// with a speculative bound, 1.25 times the previous target's k-th squared
-// distance, and starts at the deepest wide node whose cell holds the ball of
-// that radius; when the search ends with a k-th key above the bound, a
+// for it (neighbouring targets share most neighbours).  The list's members
+// are screened out of a leaf (a warp OR-reduction of the lanes whose
+// position lies in the leaf), so no source enters the list twice.  A seeded
+// target also prunes with a speculative bound, 1.25 times the previous
+// target's k-th squared distance, and starts at the deepest wide node whose
+// cell holds the ball of that radius, or scans its chunk's leaf list (the
+// leaves near the chunk's targets, collected after the chunk's first
+// search); when the search ends with a k-th key above the bound, a
 // second pass (from the root, with the whole list screened out and the
 // list's own bound) finds what it skipped.  A box is pruned only when its
 // FP32 round-down lower bound exceeds the round-up bound with a 2^-20
@@ -240,8 +242,8 @@ __global__ void k_morton_of( PointsView p, uint32_t const *perm, double const *s
     }
 }
 
-__global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double const *scene,
-                                 int32_t const *leaf_of, int32_t const *leaf_start, double2 *s2, float4 *f4 )
+__global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double const *scene, double2 *s2,
+                                 float4 *f4 )
 {
     int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if ( i < p.n )
@@ -250,8 +252,7 @@ __global__ void k_gather_sorted( PointsView p, uint32_t const *perm, double cons
         double const x = p( o, 0 ), y = p( o, 1 ), z = p( o, 2 );
         s2[2 * i] = make_double2( x, y );
         s2[2 * i + 1] = make_double2( z, __longlong_as_double( o ) );
-        f4[i] = make_float4( (float)( x - scene[9] ), (float)( y - scene[10] ), (float)( z - scene[11] ),
-                             __int_as_float( leaf_start[leaf_of[i]] ) );
+        f4[i] = make_float4( (float)( x - scene[9] ), (float)( y - scene[10] ), (float)( z - scene[11] ), 0.f );
     }
 }
 
@@ -780,7 +781,7 @@ struct GroupView
 struct TreeView
 {
     double2 const *s2; // Morton-sorted FP64 points: (x, y), (z, original index bits)
-    float4 const *f4; // centred FP32 coordinates (x, y, z) and the first position of the point's leaf
+    float4 const *f4; // centred FP32 coordinates (x, y, z; w unused: one 16-byte load a point)
     uint32_t const *codes, *perm;
     int32_t const *leaf_start, *leaf_of;
     float4 const *wide; // 8-wide nodes (16 float4 each)
@@ -1000,12 +1001,6 @@ __global__ void k_query_frame( PointsView tgt, uint32_t const *order, double con
     qrec[w] = make_query( scene, tgt, order ? (int64_t)order[w] : w );
 }
 
-// First sorted position of the leaf of sorted source p.
-__device__ __forceinline__ int leaf_first( TreeView const &tr, int64_t p )
-{
-    return __float_as_int( __ldg( reinterpret_cast<float const *>( tr.f4 + p ) + 3 ) );
-}
-
 // Sorted source p: the FP64 squared distance to the query (the exact key)
 // and the source's original index (its bits in .y); two 16-byte loads.
 __device__ __forceinline__ double2 sorted_dist2( TreeView const &tr, int64_t p, Query const &q )
@@ -1213,9 +1208,11 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     float next_spec = __int_as_float( 0x7f800000 );
     unsigned long long kd = KEY_INF;
     int ki = 0x7fffffff, kp = -1;
-    for ( int64_t w = w0; w < w0 + len && w < tgt.n; ++w )
+    // positions and targets are below 2^31 (int32 offsets): 32-bit loop state
+    int const wb = (int)w0, we = (int)( w0 + len < tgt.n ? w0 + len : tgt.n );
+    for ( int w = wb; w < we; ++w )
     {
-    int64_t const qi = order ? (int64_t)order[w] : w;
+    int const qi = order ? (int)order[w] : w;
     Range const rg = query_range<GROUPED>( tr, gv, qi );
     int64_t const ng = rg.pe - rg.ps;
     int const k = GROUPED ? gv.k[rg.g] : k_all;
@@ -1280,16 +1277,12 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         ki = 0x7fffffff;
         kp = -1;
     }
-    // the list's starting members by leaf and lane: a leaf screens them out
-    // (a leaf is named by its first position)
-    int seed_leaf = kp >= 0 ? leaf_first( tr, kp ) : -1;
-    unsigned seed_bit = kp >= 0 ? 1u << ( kp - seed_leaf ) : 0u;
     // speculative bound (seeded queries with full rows): boxes and points
     // beyond it are skipped as if the list were already that tight.  A query
     // that scans its chunk's leaf list skips every leaf beyond the list's
     // bound as well.
     float spec = seeded && row == k ? next_spec : __int_as_float( 0x7f800000 );
-    bool list_pass = !GROUPED && w > w0 && row == k && s_nlist[wib] >= 0;
+    bool list_pass = !GROUPED && w > wb && row == k && s_nlist[wib] >= 0;
     if ( list_pass )
         spec = fminf( spec, s_list_r2[wib] );
     float bound_f = fminf( prune_threshold( __shfl_sync( FULL, kd, k - 1 ) ), spec );
@@ -1301,7 +1294,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     // batch: the candidates below the bound are sorted (bitonic) and merged
     // with the list (elementwise minimum against the reversed candidates, then
     // a bitonic clean), keeping the k smallest (d2, index).  No candidate is
-    // in the list already: the list's starting members are screened out.
+    // in the list already: the list's members are screened out of a leaf.
     auto flush = [&]( int count, bool last ) {
         int const p = lane < count ? s_queue[wib][lane] : -1;
         __syncwarp();
@@ -1372,9 +1365,12 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     // bound cannot beat or tie it (screen_threshold keeps all the others);
     // the survivors queue for exact keys.
     auto process_leaf = [&]( int start, int end ) {
-        int64_t const p = (int64_t)start + lane;
+        int const p = start + lane;
         bool surv = false;
-        unsigned const seen = __reduce_or_sync( FULL, seed_leaf == start ? seed_bit : 0u );
+        // the list's members in this leaf are screened out: a leaf is
+        // screened once a pass, so they are members it started with
+        unsigned const seen =
+            __reduce_or_sync( FULL, (unsigned)( kp - start ) < (unsigned)( end - start ) ? 1u << ( kp - start ) : 0u );
         if ( ( GROUPED ? p >= rg.ps && p < rg.pe : true ) && p < end && !( ( seen >> lane ) & 1u ) )
         {
             float4 const f = __ldg( tr.f4 + p );
@@ -1385,7 +1381,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         }
         unsigned const m = __ballot_sync( FULL, surv );
         if ( surv )
-            s_queue[wib][qn + __popc( m & lt_mask )] = (int)p;
+            s_queue[wib][qn + __popc( m & lt_mask )] = p;
         __syncwarp();
         qn += __popc( m );
         if ( qn >= 32 )
@@ -1487,7 +1483,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
             int node = grp == 0 ? start : -1;
             // every step enters at least one wide node, and every wide node is
             // entered at most once
-            for ( int64_t guard = 0;; ++guard )
+            for ( int guard = 0;; ++guard )
             {
                 if ( guard >= tr.step_cap )
                 {
@@ -1559,8 +1555,6 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
         kth_ru = ru_float_of( bd );
         if ( !( spec < __int_as_float( 0x7f800000 ) ) || kth_ru <= __fmul_rd( spec, 1.0f - 9.5367431640625e-07f ) )
             break;
-        seed_leaf = kp >= 0 ? leaf_first( tr, kp ) : -1;
-        seed_bit = kp >= 0 ? 1u << ( kp - seed_leaf ) : 0u;
         spec = __int_as_float( 0x7f800000 );
         list_pass = false;
         bound_f = prune_threshold( bd );
@@ -1577,8 +1571,8 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     prev_row = row;
     next_spec = __fmul_ru( __fmul_ru( kth_ru, 1.0f + 9.5367431640625e-07f ), SPEC_GROWTH ); // prune_threshold
     __syncwarp();
-    if ( !GROUPED && w == w0 && len > 1 && row == k && tr.nl > 1 )
-        chunk_leaf_list( tr.wide, tr.step_cap, tr.levels, qrec, w0 + 1, min( w0 + len, tgt.n ), kth_ru,
+    if ( !GROUPED && w == wb && we - wb > 1 && row == k && tr.nl > 1 )
+        chunk_leaf_list( tr.wide, tr.step_cap, tr.levels, qrec, wb + 1, we, kth_ru,
                          s_stack[wib], s_list[wib], s_nlist + wib, s_list_r2 + wib );
     }
     }
@@ -1612,7 +1606,7 @@ __global__ void __launch_bounds__( R_WARPS * 32 )
     int64_t const out_end = FILL ? offset[qi + 1] : 0;
 
     auto process_leaf = [&]( int start, int end ) {
-        int64_t const p = (int64_t)start + lane;
+        int const p = start + lane;
         bool hit = false, unsure = false;
         if ( ( GROUPED ? p >= rg.ps && p < rg.pe : true ) && p < end )
         {
@@ -1786,7 +1780,6 @@ void build_lbvh( PointsView src, Lbvh &tree, unsigned *status, cudaStream_t s,
     tree.s2.allocate( 2 * n, s );
     tree.f4.allocate( n, s );
     k_gather_sorted<<<blocks_for( n, 256 ), 256, 0, s>>>( src, tree.perm.get(), tree.scene.get(),
-                                                            tree.leaf_of.get(), tree.leaf_start.get(),
                                                             tree.s2.get(), tree.f4.get() );
     check_launch( "k_gather_sorted" );
 
