@@ -1210,16 +1210,17 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     int ki = 0x7fffffff, kp = -1;
     // positions and targets are below 2^31 (int32 offsets): 32-bit loop state
     int const wb = (int)w0, we = (int)( w0 + len < tgt.n ? w0 + len : tgt.n );
+    bool head = true; // the chunk's first query
     for ( int w = wb; w < we; ++w )
     {
-    int const qi = order ? (int)order[w] : w;
-    Range const rg = query_range<GROUPED>( tr, gv, qi );
+    Range const rg = query_range<GROUPED>( tr, gv, order ? (int)order[w] : w );
     int64_t const ng = rg.pe - rg.ps;
     int const k = GROUPED ? gv.k[rg.g] : k_all;
     int const row = (int)( k < ng ? k : ng );
     if ( row <= 0 )
     {
         prev_row = 0;
+        head = false;
         continue;
     }
     // the query waits in shared memory: registers limit how many warps an
@@ -1282,7 +1283,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     // that scans its chunk's leaf list skips every leaf beyond the list's
     // bound as well.
     float spec = seeded && row == k ? next_spec : __int_as_float( 0x7f800000 );
-    bool list_pass = !GROUPED && w > wb && row == k && s_nlist[wib] >= 0;
+    bool list_pass = !GROUPED && !head && row == k && s_nlist[wib] >= 0;
     if ( list_pass )
         spec = fminf( spec, s_list_r2[wib] );
     float bound_f = fminf( prune_threshold( __shfl_sync( FULL, kd, k - 1 ) ), spec );
@@ -1562,6 +1563,7 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     }
     if ( lane < row )
     {
+        int const qi = order ? (int)__ldg( order + w ) : w; // reloaded: not kept across the search
         int64_t const o = offset[qi] + lane;
         idx_out[o] = ki;
         if ( pos_out )
@@ -1571,9 +1573,10 @@ __global__ void __launch_bounds__( Q_WARPS * 32, KNN_BLOCKS_PER_SM )
     prev_row = row;
     next_spec = __fmul_ru( __fmul_ru( kth_ru, 1.0f + 9.5367431640625e-07f ), SPEC_GROWTH ); // prune_threshold
     __syncwarp();
-    if ( !GROUPED && w == wb && we - wb > 1 && row == k && tr.nl > 1 )
-        chunk_leaf_list( tr.wide, tr.step_cap, tr.levels, qrec, wb + 1, we, kth_ru,
+    if ( !GROUPED && head && w + 1 < we && row == k && tr.nl > 1 )
+        chunk_leaf_list( tr.wide, tr.step_cap, tr.levels, qrec, w + 1, we, kth_ru,
                          s_stack[wib], s_list[wib], s_nlist + wib, s_list_r2 + wib );
+    head = false;
     }
     }
 }

@@ -50,24 +50,79 @@ namespace
 constexpr int FP64_THREADS = 256; // threads per block of the Jacobi kernels (E, V(:, 0) in shared memory)
 constexpr unsigned FULL = 0xffffffffu;
 
+// Comparisons and sign operations of the Jacobi on the IEEE bits, on the
+// integer pipe: GB300's FP64 pipe issues one warp instruction per 64 cycles
+// per SM sub-partition and its compares would take those slots.  Each gives
+// exactly the IEEE result (signed zeros and NaN included; a NaN keeps its
+// payload where the FP64 instruction would not).
+constexpr unsigned long long SIGN_BIT = 0x8000000000000000ull, ABS_BITS = 0x7fffffffffffffffull,
+                             INF_BITS = 0x7ff0000000000000ull;
+__device__ __forceinline__ unsigned long long bits_of( double x )
+{
+    return (unsigned long long)__double_as_longlong( x );
+}
+__device__ __forceinline__ double of_bits( unsigned long long b )
+{
+    return __longlong_as_double( (long long)b );
+}
+__device__ __forceinline__ bool nan_bits( unsigned long long b )
+{
+    return ( b & ABS_BITS ) > INF_BITS;
+}
+__device__ __forceinline__ bool zero_bits( unsigned long long b )
+{
+    return ( b & ABS_BITS ) == 0;
+}
+// x == y
+__device__ __forceinline__ bool ieee_eq( double x, double y )
+{
+    unsigned long long const a = bits_of( x ), b = bits_of( y );
+    return ( a == b && !nan_bits( a ) ) || ( zero_bits( a ) && zero_bits( b ) );
+}
+// x >= 0 (true for -0, false for NaN)
+__device__ __forceinline__ bool ieee_nonneg( double x )
+{
+    unsigned long long const a = bits_of( x );
+    return zero_bits( a ) || ( !( a & SIGN_BIT ) && !nan_bits( a ) );
+}
+// (x > 0) - (x < 0)
+__device__ __forceinline__ int ieee_sign( double x )
+{
+    unsigned long long const a = bits_of( x );
+    return zero_bits( a ) || nan_bits( a ) ? 0 : ( a & SIGN_BIT ? -1 : 1 );
+}
+// -x, and x * copysign(1, s): a sign-bit flip, exactly the product
+__device__ __forceinline__ double ieee_neg( double x )
+{
+    return of_bits( bits_of( x ) ^ SIGN_BIT );
+}
+__device__ __forceinline__ double times_sign_of( double x, double s )
+{
+    return of_bits( bits_of( x ) ^ ( bits_of( s ) & SIGN_BIT ) );
+}
+
 // cos and sin of phi = atan2(y, x) / 2, phi in (-pi/2, pi/2], from the
 // half-angle identities (cos phi >= 0, sin phi has the sign of y):
 //   x >= 0: cos = (r + x) / sqrt(2r(r + x)),  sin = y / sqrt(2r(r + x))
 //   x <  0: |sin| = (r - x) / sqrt(2r(r - x)), cos = |y| / sqrt(2r(r - x))
 // with r = |(x, y)|: one sqrt and one reciprocal square root instead of
 // atan2 and sincos.  (x, y) is rescaled by a power of two when r^2 would
-// leave the normal range (atan2 is scale-invariant).
+// leave [1e-280, 1e280] (atan2 is scale-invariant); r^2 >= 0 or NaN, whose
+// bits order like its values.
 __device__ __forceinline__ void half_angle( double y, double x, double &c, double &s )
 {
+    constexpr unsigned long long R2_LO = 0x05cd0b15a491eb84ull, R2_HI = 0x7a11a0fc668aac70ull; // 1e-280, 1e280
     double r2 = fma( x, x, y * y );
-    if ( !( r2 > 1e-280 && r2 < 1e280 ) && ( x != 0.0 || y != 0.0 ) )
+    unsigned long long b2 = bits_of( r2 );
+    if ( !( b2 > R2_LO && b2 < R2_HI ) && !( zero_bits( bits_of( x ) ) && zero_bits( bits_of( y ) ) ) )
     {
         int const e = ilogb( fmax( fabs( x ), fabs( y ) ) );
         x = scalbn( x, -e );
         y = scalbn( y, -e );
         r2 = fma( x, x, y * y );
+        b2 = bits_of( r2 );
     }
-    if ( r2 == 0.0 )
+    if ( zero_bits( b2 ) )
     {
         c = 1.0;
         s = y; // atan2(+-0, +0) = +-0
@@ -75,8 +130,12 @@ __device__ __forceinline__ void half_angle( double y, double x, double &c, doubl
     }
     double const r = sqrt( r2 );
     double const w = r + fabs( x );
-    double const t = rsqrt( 2.0 * r * w );
-    if ( x >= 0.0 )
+    // 2 r by its exponent, exactly the product: a finite r is normal here (r^2
+    // lies in [1e-280, 1e280], or in [1, 8) after the rescaling); inf and NaN
+    // stay as they are
+    unsigned long long const br = bits_of( r );
+    double const t = rsqrt( of_bits( br < INF_BITS ? br + ( 1ull << 52 ) : br ) * w );
+    if ( ieee_nonneg( x ) )
     {
         c = w * t;
         s = y * t;
@@ -124,14 +183,13 @@ __device__ __forceinline__ void svd_2x2( double a, double b, double c, double d,
     double const aw10 = dot2( c, cth, d, sth ), aw11 = dot2( c, -sth, d, cth );
     double const s00 = dot2( cphi, aw00, sphi, aw10 );
     double const s11 = dot2( -sphi, aw01, cphi, aw11 );
-    double const c0 = copysign( 1.0, s00 ), c1 = copysign( 1.0, s11 );
-    // V = W diag(c0, c1)
-    double const v00 = cth * c0, v01 = -sth * c1, v10 = sth * c0;
+    // V = W diag(c0, c1), c0 = copysign(1, s00), c1 = copysign(1, s11)
+    double const v00 = times_sign_of( cth, s00 ), v01 = times_sign_of( ieee_neg( sth ), s11 ),
+                 v10 = times_sign_of( sth, s00 );
     cl = cphi;
-    sl = -sphi;
+    sl = ieee_neg( sphi );
     cr = v00;
-    int const g01 = ( v01 > 0 ) - ( v01 < 0 ), g10 = ( v10 > 0 ) - ( v10 < 0 );
-    sr = ( g01 == g10 ) ? -v01 : v01;
+    sr = ieee_sign( v01 ) == ieee_sign( v10 ) ? ieee_neg( v01 ) : v01;
 }
 
 // svd_2x2 of a symmetric block [[a, b], [b, d]]: A A^T and A^T A are then
@@ -140,21 +198,20 @@ __device__ __forceinline__ void svd_2x2( double a, double b, double c, double d,
 __device__ __forceinline__ void svd_2x2_sym( double a, double b, double d, double &cl, double &sl,
                                              double &cr, double &sr )
 {
-    double const q00 = dot2( a, a, b, b ), q01 = dot2( a, b, b, d ), q10 = dot2( b, a, d, b ),
-                 q11 = dot2( b, b, d, d );
+    // q10 = dot2( b, a, d, b ) is q01 bit for bit (IEEE products commute)
+    double const q00 = dot2( a, a, b, b ), q01 = dot2( a, b, b, d ), q11 = dot2( b, b, d, d );
     double sth, cth;
-    half_angle( q01 + q10, q00 - q11, cth, sth );
+    half_angle( q01 + q01, q00 - q11, cth, sth );
     double const aw00 = dot2( a, cth, b, sth ), aw01 = dot2( a, -sth, b, cth );
     double const aw10 = dot2( b, cth, d, sth ), aw11 = dot2( b, -sth, d, cth );
     double const s00 = dot2( cth, aw00, sth, aw10 );
     double const s11 = dot2( -sth, aw01, cth, aw11 );
-    double const c0 = copysign( 1.0, s00 ), c1 = copysign( 1.0, s11 );
-    double const v00 = cth * c0, v01 = -sth * c1, v10 = sth * c0;
+    double const v00 = times_sign_of( cth, s00 ), v01 = times_sign_of( ieee_neg( sth ), s11 ),
+                 v10 = times_sign_of( sth, s00 );
     cl = cth;
-    sl = -sth;
+    sl = ieee_neg( sth );
     cr = v00;
-    int const g01 = ( v01 > 0 ) - ( v01 < 0 ), g10 = ( v10 > 0 ) - ( v10 < 0 );
-    sr = ( g01 == g10 ) ? -v01 : v01;
+    sr = ieee_sign( v01 ) == ieee_sign( v10 ) ? ieee_neg( v01 ) : v01;
 }
 
 // |x| as an ordered integer (non-negative doubles order like their bits).
@@ -381,7 +438,7 @@ __device__ int jacobi_row0( Smem<M> const &s, double *row0, unsigned &iters, uns
             svd_2x2_sym( bpp, bpq, bqq, cl, sl, cr, sr );
         else
             svd_2x2( bpp, bpq, bqp, bqq, cl, sl, cr, sr );
-        sym = sym && cr == cl && sr == sl;
+        sym = sym && ieee_eq( cr, cl ) && ieee_eq( sr, sl );
         if ( sym )
         {
             // rows p and q by the left rotation, columns p and q off the
