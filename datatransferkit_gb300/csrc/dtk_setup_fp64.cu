@@ -39,6 +39,7 @@
 // threshold where it sums the squares in FP64; the 2x2 rotation angles use
 // half-angle identities rather than atan2 and sincos.
 #include "dtk_common.cuh"
+#include "dtk_ieee.cuh"
 
 #include <algorithm>
 
@@ -50,57 +51,6 @@ namespace
 constexpr int FP64_THREADS = 256; // threads per block of the Jacobi kernels (E, V(:, 0) in shared memory)
 constexpr unsigned FULL = 0xffffffffu;
 
-// Comparisons and sign operations of the Jacobi on the IEEE bits, on the
-// integer pipe: GB300's FP64 pipe issues one warp instruction per 64 cycles
-// per SM sub-partition and its compares would take those slots.  Each gives
-// exactly the IEEE result (signed zeros and NaN included; a NaN keeps its
-// payload where the FP64 instruction would not).
-constexpr unsigned long long SIGN_BIT = 0x8000000000000000ull, ABS_BITS = 0x7fffffffffffffffull,
-                             INF_BITS = 0x7ff0000000000000ull;
-__device__ __forceinline__ unsigned long long bits_of( double x )
-{
-    return (unsigned long long)__double_as_longlong( x );
-}
-__device__ __forceinline__ double of_bits( unsigned long long b )
-{
-    return __longlong_as_double( (long long)b );
-}
-__device__ __forceinline__ bool nan_bits( unsigned long long b )
-{
-    return ( b & ABS_BITS ) > INF_BITS;
-}
-__device__ __forceinline__ bool zero_bits( unsigned long long b )
-{
-    return ( b & ABS_BITS ) == 0;
-}
-// x == y
-__device__ __forceinline__ bool ieee_eq( double x, double y )
-{
-    unsigned long long const a = bits_of( x ), b = bits_of( y );
-    return ( a == b && !nan_bits( a ) ) || ( zero_bits( a ) && zero_bits( b ) );
-}
-// x >= 0 (true for -0, false for NaN)
-__device__ __forceinline__ bool ieee_nonneg( double x )
-{
-    unsigned long long const a = bits_of( x );
-    return zero_bits( a ) || ( !( a & SIGN_BIT ) && !nan_bits( a ) );
-}
-// (x > 0) - (x < 0)
-__device__ __forceinline__ int ieee_sign( double x )
-{
-    unsigned long long const a = bits_of( x );
-    return zero_bits( a ) || nan_bits( a ) ? 0 : ( a & SIGN_BIT ? -1 : 1 );
-}
-// -x, and x * copysign(1, s): a sign-bit flip, exactly the product
-__device__ __forceinline__ double ieee_neg( double x )
-{
-    return of_bits( bits_of( x ) ^ SIGN_BIT );
-}
-__device__ __forceinline__ double times_sign_of( double x, double s )
-{
-    return of_bits( bits_of( x ) ^ ( bits_of( s ) & SIGN_BIT ) );
-}
-
 // cos and sin of phi = atan2(y, x) / 2, phi in (-pi/2, pi/2], from the
 // half-angle identities (cos phi >= 0, sin phi has the sign of y):
 //   x >= 0: cos = (r + x) / sqrt(2r(r + x)),  sin = y / sqrt(2r(r + x))
@@ -111,10 +61,9 @@ __device__ __forceinline__ double times_sign_of( double x, double s )
 // bits order like its values.
 __device__ __forceinline__ void half_angle( double y, double x, double &c, double &s )
 {
-    constexpr unsigned long long R2_LO = 0x05cd0b15a491eb84ull, R2_HI = 0x7a11a0fc668aac70ull; // 1e-280, 1e280
     double r2 = fma( x, x, y * y );
     unsigned long long b2 = bits_of( r2 );
-    if ( !( b2 > R2_LO && b2 < R2_HI ) && !( zero_bits( bits_of( x ) ) && zero_bits( bits_of( y ) ) ) )
+    if ( !r2_in_range( b2 ) && !( zero_bits( bits_of( x ) ) && zero_bits( bits_of( y ) ) ) )
     {
         int const e = ilogb( fmax( fabs( x ), fabs( y ) ) );
         x = scalbn( x, -e );
@@ -130,11 +79,9 @@ __device__ __forceinline__ void half_angle( double y, double x, double &c, doubl
     }
     double const r = sqrt( r2 );
     double const w = r + fabs( x );
-    // 2 r by its exponent, exactly the product: a finite r is normal here (r^2
-    // lies in [1e-280, 1e280], or in [1, 8) after the rescaling); inf and NaN
-    // stay as they are
-    unsigned long long const br = bits_of( r );
-    double const t = rsqrt( of_bits( br < INF_BITS ? br + ( 1ull << 52 ) : br ) * w );
+    // 2 r by its exponent: a finite r is normal here (r^2 lies in
+    // [1e-280, 1e280], or in [1, 8) after the rescaling)
+    double const t = rsqrt( twice_normal( r ) * w );
     if ( ieee_nonneg( x ) )
     {
         c = w * t;
