@@ -110,12 +110,15 @@ def config_of(name, n_src, n_tgt_per_rank):
 # clocks during the timed region
 # ---------------------------------------------------------------------------
 class ClockSampler:
+    """nvidia-smi samples every 200 ms, each stamped with the host clock when
+    it arrives; the summary keeps the samples of a window (the timed region),
+    all samples when none fell inside it."""
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device_index: int):
-        self.rows = []
+        self.rows = []  # (host time, fields)
         self.proc = None
         self.device_index = device_index
 
@@ -135,7 +138,13 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) == 8:
-                self.rows.append(parts)
+                self.rows.append((time.monotonic(), parts))
+
+    def wait_first(self, timeout: float = 3.0):
+        """Until the first sample arrives (nvidia-smi starting up), at most timeout seconds."""
+        end = time.monotonic() + timeout
+        while self.proc is not None and not self.rows and time.monotonic() < end and self.proc.poll() is None:
+            time.sleep(0.02)
 
     def __exit__(self, *a):
         if self.proc:
@@ -145,20 +154,30 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self):
-        if not self.rows:
+    def summary(self, t0: float | None = None, t1: float | None = None):
+        rows = list(self.rows)
+        window = "timed region"
+        if t0 is not None and t1 is not None:
+            # a sample arrives up to one period after it was taken
+            inside = [r for r in rows if t0 <= r[0] <= t1 + 0.25]
+            if inside:
+                rows = inside
+            else:
+                window = "sampler run (no sample inside the timed region)"
+        rows = [r[1] for r in rows]
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
-        smax = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        smax = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         reasons = set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
+        for r in rows:
             for name, v in zip(names, r[4:8]):
                 if v.lower() in ("active", "1"):
                     reasons.add(name)
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
-                "samples": len(self.rows)}
+                "samples": len(rows), "window": window}
 
 
 # ---------------------------------------------------------------------------
@@ -586,21 +605,26 @@ def run_ours(args, rank, world, local_rank):
         return op
 
     def timed(precision, steps, warmup):
-        for _ in range(warmup):
-            step(precision, None)
-        rec = []
-        barrier()
-        launches0 = dtk.kernel_launch_count()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        # the sampler starts before the warm-up, so that its first samples
+        # are in by the time the timed region starts
         with ClockSampler(dev.index) as clk:
+            clk.wait_first()
+            for _ in range(warmup):
+                step(precision, None)
+            rec = []
+            barrier()
+            launches0 = dtk.kernel_launch_count()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0 = time.monotonic()
             e0.record(stream)
             for _ in range(steps):
                 step(precision, rec)
             e1.record(stream)
             barrier()
+            t1 = time.monotonic()
         launches = (dtk.kernel_launch_count() - launches0) // steps
         ms = max_over_ranks(e0.elapsed_time(e1) / steps)
-        return ms, rec, clk.summary(), launches
+        return ms, rec, clk.summary(t0, t1), launches
 
     # -- headline: mixed form, inputs resident ---------------------------------
     ms_mixed, rec_mixed, clocks, launches = timed("mixed", args.steps, args.warmup)
