@@ -37,7 +37,9 @@
 // The argmax runs on the integer pipe over the IEEE bits of |E_ij|; the stop
 // test too, from exponent bounds, except within a factor of four of the
 // threshold where it sums the squares in FP64; the 2x2 rotation angles use
-// half-angle identities rather than atan2 and sincos.
+// half-angle identities rather than atan2 and sincos, and the 2x2 SVD's
+// compares and sign logic run on the integer pipe too (dtk_ieee.cuh, exactly
+// the IEEE results; 8M targets: 366 -> 343 ms).
 #include "dtk_common.cuh"
 #include "dtk_ieee.cuh"
 
